@@ -1,0 +1,118 @@
+// cfd_common.cuh — shared definitions of the cfd_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "../../include/cfd_gpu.h"
+
+namespace cfd {
+
+// ------------------------------------------------------------------ error plumbing
+extern std::atomic<long long> g_launches;
+
+#define CFD_CUDA(call)                                                          \
+    do {                                                                        \
+        cudaError_t e_ = (call);                                                \
+        if (e_ != cudaSuccess) {                                                \
+            cfd::set_last_cuda_error(e_, #call, __FILE__, __LINE__);            \
+            return e_ == cudaErrorMemoryAllocation ? CFD_ERR_NOMEM : CFD_ERR_CUDA; \
+        }                                                                       \
+    } while (0)
+
+// launch + count + check the launch error
+#define CFD_LAUNCH(kernel, grid, block, smem, stream, ...)                      \
+    do {                                                                        \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);             \
+        cfd::g_launches.fetch_add(1, std::memory_order_relaxed);                \
+        CFD_CUDA(cudaGetLastError());                                           \
+    } while (0)
+
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+
+inline unsigned blocks_for(long n, int threads) {
+    long b = (n + threads - 1) / threads;
+    return (unsigned)(b > 0 ? b : 1);
+}
+
+// ------------------------------------------------------------------ fixed-order sums
+// The dot-product order every FP64 reduction of this library takes (and the oracle's
+// or_vecdot restates): chunks of 1024 terms, lane t of a 256-thread block sums terms
+// t, t+256, t+512, t+768 in that order; a shuffle-down tree over each warp's 32 lanes;
+// an 8-way shuffle-down tree over the warps.  Chunk partials are folded by 256 lanes
+// with stride 256, then the same 256-lane tree.
+constexpr int kChunk = 1024;
+constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ double warp_tree32(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = v + __shfl_down_sync(0xffffffffu, v, off);
+    return v;  // lane 0
+}
+
+// 256-lane tree; every thread of the block gets the result.  `red` holds >= 9 doubles.
+__device__ __forceinline__ double block_tree256(double v, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = warp_tree32(v);
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double w = lane < 8 ? red[lane] : 0.0;
+#pragma unroll
+        for (int off = 4; off > 0; off >>= 1) w = w + __shfl_down_sync(0xffffffffu, w, off);
+        if (lane == 0) red[8] = w;
+    }
+    __syncthreads();
+    double r = red[8];
+    __syncthreads();
+    return r;
+}
+
+// Final fold of nc chunk partials (blockDim.x == 256); every thread gets the sum.
+__device__ __forceinline__ double fold_partials(const double* part, long nc, double* red) {
+    const int t = threadIdx.x;
+    double acc = (t < nc) ? part[t] : 0.0;
+    for (long c = t + 256; c < nc; c += 256) acc = acc + part[c];
+    return block_tree256(acc, red);
+}
+
+// ------------------------------------------------------------------ bounded grid barrier
+// Sense-free generation barrier for cooperative launches.  Every wait is bounded: after
+// kSpinLimit polls the block sets *err = CFD_ERR_BARRIER and leaves; callers check err.
+constexpr long long kSpinLimit = 1LL << 24;
+
+struct GridBar {
+    unsigned int arrive;
+    unsigned int gen;
+    int err;
+    int pad;
+};
+
+__device__ __forceinline__ void grid_barrier(GridBar* gb, unsigned nblocks) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = &gb->gen;
+        unsigned int g = *vgen;
+        __threadfence();
+        unsigned int prev = atomicAdd(&gb->arrive, 1u);
+        if (prev == nblocks - 1) {
+            atomicExch(&gb->arrive, 0u);
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (++spins > kSpinLimit) {
+                    atomicExch(&gb->err, (int)CFD_ERR_BARRIER);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+}  // namespace cfd

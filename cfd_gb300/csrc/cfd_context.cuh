@@ -1,0 +1,95 @@
+// cfd_context.cuh — the resident context (one mesh, its state and every work array in HBM).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "cfd_kernels.cuh"
+#include "host_prep.h"
+
+namespace cfd {
+
+enum { TM_DELTAT, TM_ESTAB, TM_CALCRHS, TM_FUENTE, TM_UPDATE, TM_FORCES, TM_TRANSF, TM_GRAD,
+       TM_NORMALES, TM_DERIV, TM_MASAS, TM_LAPLACE, TM_N };
+
+void set_last_message(const std::string& m);
+std::string last_message();
+
+struct Ctx {
+    int npoin = 0, nelem = 0, prec = 0;
+    cfd_params prm{};
+    Adjacency adj;
+    BcTables bc;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_scal = nullptr;
+    StepScal* h_scal = nullptr;  // pinned
+    std::vector<void*> allocs;
+    // time-loop scalars kept on the host
+    int iter = 0;
+    int bandera_host = 1;
+    double time = 0.0, last_dtmin = 0.0;
+    double disn[2] = {0.0, 0.0};
+    // sizes
+    int nwn = 0, nnmove = 0, nufix = 0, pcg_grid = 1;
+    // mesh
+    int4* d_elem = nullptr;
+    double *d_X = nullptr, *d_Y = nullptr;
+    int *d_esup_ptr = nullptr, *d_esup_slot = nullptr;
+    uchar4* d_lap_pos = nullptr;
+    int *d_rowptr = nullptr, *d_col = nullptr;
+    double *d_val = nullptr, *d_diag = nullptr;
+    // BC
+    unsigned char* d_bcflag = nullptr;
+    double* d_bcval = nullptr;
+    double2* d_nrm = nullptr;
+    int *d_wnode = nullptr, *d_wptr = nullptr;
+    int2 *d_wedge = nullptr, *d_walls = nullptr;
+    int* d_set_ptr = nullptr;
+    int2* d_set_edges = nullptr;
+    double *d_xref = nullptr, *d_yref = nullptr;
+    int *d_fix_node = nullptr, *d_fix_set = nullptr, *d_ufix_node = nullptr, *d_ufix_src = nullptr;
+    unsigned char* d_isfix = nullptr;
+    // state
+    double *d_U = nullptr, *d_U1 = nullptr, *d_T = nullptr, *d_VX = nullptr, *d_VY = nullptr;
+    double *d_RHO = nullptr, *d_E = nullptr, *d_P = nullptr, *d_RMACH = nullptr;
+    double *d_WX = nullptr, *d_WY = nullptr, *d_M = nullptr, *d_Wxo = nullptr, *d_Wyo = nullptr;
+    double *d_area = nullptr, *d_area_old = nullptr, *d_geo = nullptr, *d_DT = nullptr,
+           *d_DTL = nullptr;
+    double *d_SHOC = nullptr, *d_TS1 = nullptr, *d_TS2 = nullptr, *d_TS3 = nullptr;
+    double *d_contrib = nullptr, *d_contribF = nullptr;
+    // mesh motion
+    double* d_pos[2] = {nullptr, nullptr};  // xpos, ypos (guess in, solution out)
+    double* d_xfix[2] = {nullptr, nullptr};
+    double *d_r[2] = {}, *d_z[2] = {}, *d_y[2] = {};
+    double* d_p[2][2] = {};
+    double* d_part = nullptr;
+    GridBar* d_bar = nullptr;
+    int *d_pcg_iters = nullptr, *d_pcg_conv = nullptr;
+    double* d_pcg_rz = nullptr;
+    StepScal* d_scal = nullptr;
+    // timers
+    bool timers_on = false;
+    cudaEvent_t ev[TM_N][2] = {};
+    cudaEvent_t mark[8] = {};  // caller-requested events (cfd_ctx_mark)
+    bool used[TM_N] = {};
+    double seconds[TM_N] = {};
+
+    ~Ctx();
+    int create(const cfd_mesh* m, const cfd_params* p, int precision_mode);
+    int geometry(bool masas, bool with_laplace);
+    int run_pcg(int nsolve);
+    int step_once();
+    int step(int nsteps, cfd_step_report* rep);
+    int tstart(int slot);
+    int tstop(int slot);
+    int tcollect();
+    template <class T>
+    int dalloc(T** p, size_t n);
+    template <class T>
+    int upload(T** p, const T* h, size_t n);
+};
+
+}  // namespace cfd
+
+struct cfd_ctx {
+    cfd::Ctx impl;
+};

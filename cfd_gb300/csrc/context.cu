@@ -1,0 +1,443 @@
+// context.cu — the resident context: device buffers, setup and the time-step loop body
+// of ns2DComp.ALE.f90:140-280 as a sequence of sm_103a kernels on one stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "cfd_context.cuh"
+
+namespace cfd {
+
+std::atomic<long long> g_launches{0};
+static std::mutex g_err_mu;
+static std::string g_last_err;
+
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    g_last_err = buf;
+}
+
+void set_last_message(const std::string& m) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_last_err = m;
+}
+
+std::string last_message() {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    return g_last_err;
+}
+
+static const char* kTimerNames[TM_N] = {"deltat_t", "estab_t",  "calcrhs_t", "fuente_t",
+                                        "update_t", "forces_t", "transf_t",  "grad_t",
+                                        "normales_t", "deriv_t", "masas_t",  "laplace_t"};
+
+// ------------------------------------------------------------------ timers
+int Ctx::tstart(int slot) {
+    if (!timers_on) return CFD_OK;
+    CFD_CUDA(cudaEventRecord(ev[slot][0], stream));
+    return CFD_OK;
+}
+int Ctx::tstop(int slot) {
+    if (!timers_on) return CFD_OK;
+    CFD_CUDA(cudaEventRecord(ev[slot][1], stream));
+    used[slot] = true;
+    return CFD_OK;
+}
+int Ctx::tcollect() {
+    if (!timers_on) return CFD_OK;
+    CFD_CUDA(cudaStreamSynchronize(stream));
+    for (int i = 0; i < TM_N; ++i)
+        if (used[i]) {
+            float ms = 0.f;
+            CFD_CUDA(cudaEventElapsedTime(&ms, ev[i][0], ev[i][1]));
+            seconds[i] += ms * 1e-3;
+            used[i] = false;
+        }
+    return CFD_OK;
+}
+
+Ctx::~Ctx() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : allocs) cudaFree(p);
+    if (h_scal) cudaFreeHost(h_scal);
+    if (ev_scal) cudaEventDestroy(ev_scal);
+    for (int i = 0; i < TM_N; ++i)
+        for (int j = 0; j < 2; ++j)
+            if (ev[i][j]) cudaEventDestroy(ev[i][j]);
+    for (auto& m : mark)
+        if (m) cudaEventDestroy(m);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+// ------------------------------------------------------------------ geometry of the mesh
+int Ctx::geometry(bool masas, bool with_laplace) {
+    const int N = npoin, E = nelem;
+    const int TB = 256;
+    tstart(TM_NORMALES);
+    if (nwn > 0)
+        CFD_LAUNCH(k_normales, blocks_for(nwn, TB), TB, 0, stream, nwn, d_wnode, d_wptr,
+                   d_wedge, d_walls, d_X, d_Y, d_bcflag, d_nrm);
+    tstop(TM_NORMALES);
+    tstart(TM_DERIV);
+    CFD_LAUNCH(k_deriv, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_X, d_Y, d_area, d_geo,
+               (double*)nullptr, (double*)nullptr, (double*)nullptr);
+    tstop(TM_DERIV);
+    if (masas) {
+        tstart(TM_MASAS);
+        CFD_LAUNCH(k_mass, blocks_for(N, TB), TB, 0, stream, N, d_esup_ptr, d_esup_slot, d_area, d_M);
+        tstop(TM_MASAS);
+    }
+    if (with_laplace) {
+        tstart(TM_LAPLACE);
+        CFD_LAUNCH(k_laplace, blocks_for(N, 128), 128, 0, stream, N, E, d_elem, d_esup_ptr,
+                   d_esup_slot, d_lap_pos, d_geo, d_X, d_Y, d_rowptr, d_val, d_diag);
+        tstop(TM_LAPLACE);
+    }
+    return CFD_OK;
+}
+
+// ------------------------------------------------------------------ PCG launch
+int Ctx::run_pcg(int nsolve) {
+    PcgArgs a{};
+    a.n = npoin;
+    a.nsolve = nsolve;
+    a.rowptr = d_rowptr;
+    a.col = d_col;
+    a.val = d_val;
+    a.diag = d_diag;
+    a.isfix = d_isfix;
+    a.nfix = nufix;
+    a.fix_node = d_ufix_node;
+    a.fix_src = d_ufix_src;
+    for (int s = 0; s < 2; ++s) {
+        a.fixval[s] = d_xfix[s];
+        a.x[s] = d_pos[s];
+        a.b[s] = nullptr;
+        a.r[s] = d_r[s];
+        a.z[s] = d_z[s];
+        a.y[s] = d_y[s];
+        a.p[s][0] = d_p[s][0];
+        a.p[s][1] = d_p[s][1];
+    }
+    a.part = d_part;
+    a.bar = d_bar;
+    a.tol = prm.bicg_tol;
+    a.maxit = prm.bicg_maxit;
+    a.iters_out = d_pcg_iters;
+    a.rz_out = d_pcg_rz;
+    a.conv_out = d_pcg_conv;
+    CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
+    void* args[] = {&a};
+    CFD_CUDA(cudaLaunchCooperativeKernel((void*)k_pcg_fp64, dim3(pcg_grid), dim3(256), args, 0, stream));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return CFD_OK;
+}
+
+// ------------------------------------------------------------------ one time step
+int Ctx::step_once() {
+    const int N = npoin, E = nelem;
+    const int TB = 256;
+    iter += 1;
+    // DELTAT + hysteresis (ns2DComp.ALE.f90:144-156)
+    tstart(TM_DELTAT);
+    CFD_LAUNCH(k_deltat, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_T, d_VX, d_VY, d_WX, d_WY,
+               d_area, prm.fsafe, prm.t_inf, d_DT, &d_scal->dtmin_bits);
+    CFD_LAUNCH(k_dt_finalize, 1, 1, 0, stream, d_scal);
+    tstop(TM_DELTAT);
+    CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
+    CFD_CUDA(cudaEventRecord(ev_scal, stream));
+    const double* dtl_arr = nullptr;
+    if (prm.itlocal != 0) {  // :159-162
+        double dtfact = 1.0 - std::exp(-(iter * 4.6 / prm.itlocal));
+        CFD_LAUNCH(k_dtl, blocks_for(E, TB), TB, 0, stream, E, d_DT, d_DTL, d_scal, dtfact);
+        dtl_arr = d_DTL;
+    }
+    const double* dtl_scalar = &d_scal->dtmin;
+    // RK (subrutinas.f90:645-849): ESTAB once, then 4 stages of calcRHS+FUENTE and update
+    tstart(TM_ESTAB);
+    CFD_LAUNCH(k_estab, blocks_for(E, 128), 128, 0, stream, E, d_elem, d_U, d_T, prm.gama,
+               (const double*)nullptr, d_VX,
+               d_VY, d_WX, d_WY, d_geo, prm.fr, d_scal, prm.rho_inf, prm.t_inf, d_SHOC, d_TS1,
+               d_TS2, d_TS3);
+    tstop(TM_ESTAB);
+    GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte};
+    const bool viscous = prm.fmu > 2.2250738585072014e-308;
+    const int NRK = 4;
+    for (int irk = 1; irk <= NRK; ++irk) {
+        const double rk_fact = 1.0 / (NRK + 1 - irk);
+        // FUENTE depends on the step-start U and W only: its contributions are formed in
+        // stage 1 and re-read by stages 2-4
+        double* cF = (irk == 1) ? d_contribF : nullptr;
+        tstart(TM_CALCRHS);
+        CFD_CUDA(launch_elem_rhs(viscous, false, stream, E, d_elem, d_U, nullptr, d_T, d_geo, d_area,
+                                 d_SHOC, dtl_arr, dtl_scalar, d_TS1, d_TS2, d_TS3, gc, d_contrib,
+                                 d_WX, d_WY, cF));
+        tstop(TM_CALCRHS);
+        tstart(TM_UPDATE);
+        CFD_LAUNCH(k_node_update, blocks_for(N, TB), TB, 0, stream, N, d_esup_ptr, d_esup_slot,
+                   d_contrib, d_contribF, d_U, d_M, rk_fact, prm.gama, prm.fr, d_bcflag,
+                   (const double*)d_bcval, d_nrm, d_WX, d_WY, d_U1, d_RHO, d_VX, d_VY, d_E,
+                   d_P, d_T, d_RMACH, (const double*)nullptr, (double*)nullptr);
+        tstop(TM_UPDATE);
+    }
+    // fluidStructure (meshMove.f90:28-142) needs TIME: the host reads DTMIN
+    CFD_CUDA(cudaEventSynchronize(ev_scal));
+    const double dtmin = h_scal->dtmin;
+    time = time + dtmin;
+    last_dtmin = dtmin;
+    tstart(TM_FORCES);
+    CFD_LAUNCH(k_forces, 1, 256, 0, stream, bc.nset_numb, d_set_ptr, d_set_edges, d_P, d_X, d_Y,
+               d_xref, d_yref, d_scal);
+    tstop(TM_FORCES);
+    const double PI = std::acos(-1.0);
+    double alphav = disn[1], yposrv = disn[0];
+    if (prm.motion_law == CFD_MOTION_HARMONIC) {
+        double ph = 2.0 * PI * prm.motion_freq * time;
+        disn[0] = prm.heave_amp * std::sin(ph);
+        disn[1] = prm.pitch_amp * std::sin(ph);
+    } else {
+        const double ampli = PI / 8.0;
+        disn[1] = ampli * std::sin(10.0 * time);
+    }
+    const double alpha = disn[1] - alphav, yposr = disn[0] - yposrv;
+    const double ca = std::cos(alpha), sa = std::sin(alpha);
+    tstart(TM_TRANSF);
+    if (nnmove > 0)
+        CFD_LAUNCH(k_transf, blocks_for(nnmove, TB), TB, 0, stream, nnmove, d_fix_node, d_fix_set,
+                   d_X, d_Y, d_xref, d_yref, ca, sa, yposr, d_xfix[0], d_xfix[1]);
+    tstop(TM_TRANSF);
+    if (prm.guess_mode == CFD_GUESS_ZERO) {
+        CFD_CUDA(cudaMemsetAsync(d_pos[0], 0, sizeof(double) * N, stream));
+        CFD_CUDA(cudaMemsetAsync(d_pos[1], 0, sizeof(double) * N, stream));
+    }
+    tstart(TM_GRAD);
+    int st = run_pcg(2);
+    if (st) return st;
+    tstop(TM_GRAD);
+    CFD_LAUNCH(k_motion_update, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1], d_scal,
+               d_X, d_Y, d_WX, d_WY);
+    if (prm.moving == 1) {  // ns2DComp.ALE.f90:259-275
+        st = geometry(prm.mass_mode == CFD_MASS_MASAS, false);
+        if (st) return st;
+        if (prm.mass_mode != CFD_MASS_MASAS) {  // gcl main, then putW/putArea
+            tstart(TM_MASAS);
+            CFD_LAUNCH(k_gcl, blocks_for(N, TB), TB, 0, stream, N, E, d_elem, d_esup_ptr,
+                       d_esup_slot, d_geo, d_area, d_area_old, d_WX, d_WY, d_Wxo, d_Wyo,
+                       &d_scal->dtmin, prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_M);
+            CFD_CUDA(cudaMemcpyAsync(d_Wxo, d_WX, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
+            CFD_CUDA(cudaMemcpyAsync(d_Wyo, d_WY, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
+            CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
+            tstop(TM_MASAS);
+        }
+        tstart(TM_LAPLACE);
+        CFD_LAUNCH(k_laplace, blocks_for(N, 128), 128, 0, stream, N, E, d_elem, d_esup_ptr,
+                   d_esup_slot, d_lap_pos, d_geo, d_X, d_Y, d_rowptr, d_val, d_diag);
+        tstop(TM_LAPLACE);
+    }
+    std::swap(d_U, d_U1);  // U = U1 (:277-281)
+    bandera_host += 1;
+    return tcollect();
+}
+
+int Ctx::step(int nsteps, cfd_step_report* rep) {
+    if (nsteps < 0) return CFD_ERR_ARG;
+    for (int s = 0; s < nsteps; ++s) {
+        int st = step_once();
+        if (st) return st;
+    }
+    CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
+    int it[2] = {0, 0}, cv[2] = {0, 0};
+    double rz[2] = {0, 0};
+    GridBar gb{};
+    CFD_CUDA(cudaMemcpyAsync(it, d_pcg_iters, sizeof(it), cudaMemcpyDeviceToHost, stream));
+    CFD_CUDA(cudaMemcpyAsync(cv, d_pcg_conv, sizeof(cv), cudaMemcpyDeviceToHost, stream));
+    CFD_CUDA(cudaMemcpyAsync(rz, d_pcg_rz, sizeof(rz), cudaMemcpyDeviceToHost, stream));
+    CFD_CUDA(cudaMemcpyAsync(&gb, d_bar, sizeof(gb), cudaMemcpyDeviceToHost, stream));
+    CFD_CUDA(cudaStreamSynchronize(stream));
+    if (gb.err) {
+        set_last_message("a grid barrier of the BiCG kernel gave up waiting");
+        return CFD_ERR_BARRIER;
+    }
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->iter = iter;
+        rep->time = time;
+        rep->dtmin = last_dtmin;
+        for (int s = 0; s < 2; ++s) {
+            rep->bicg_iters[s] = it[s];
+            rep->bicg_rz[s] = rz[s];
+            rep->bicg_converged[s] = cv[s];
+        }
+        rep->nset_numb = bc.nset_numb;
+        for (int i = 0; i < 10; ++i) {
+            rep->fx[i] = h_scal->fx[i];
+            rep->fy[i] = h_scal->fy[i];
+            rep->rm[i] = h_scal->rm[i];
+        }
+    }
+    return CFD_OK;
+}
+
+// ------------------------------------------------------------------ create
+template <class T>
+int Ctx::dalloc(T** p, size_t n) {
+    if (n == 0) n = 1;
+    void* v = nullptr;
+    CFD_CUDA(cudaMalloc(&v, n * sizeof(T)));
+    allocs.push_back(v);
+    *p = (T*)v;
+    return CFD_OK;
+}
+
+template <class T>
+int Ctx::upload(T** p, const T* h, size_t n) {
+    int st = dalloc(p, n);
+    if (st) return st;
+    if (n) CFD_CUDA(cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return CFD_OK;
+}
+
+int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
+    npoin = m->npoin;
+    nelem = m->nelem;
+    prm = *p;
+    prec = precision_mode;
+    if (prm.bicg_maxit <= 0) prm.bicg_maxit = 1000;
+    if (!(prm.bicg_tol > 0.0)) prm.bicg_tol = 1.0e-10;
+    prm.xref[1] = 1.4;  // meshMove.f90:58 (set before every FORCES/TRANSF)
+    prm.yref[1] = 0.0;
+    std::string why;
+    int st = build_adjacency(npoin, nelem, m->inpoel, adj, &why);
+    if (st) { set_last_message(why); return st; }
+    st = build_bc_tables(m, bc, &why);
+    if (st) { set_last_message(why); return st; }
+    const int N = npoin, E = nelem;
+    timers_on = getenv("CFD_TIMERS") && atoi(getenv("CFD_TIMERS")) != 0;
+    CFD_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CFD_CUDA(cudaEventCreateWithFlags(&ev_scal, cudaEventDisableTiming));
+    for (int i = 0; i < TM_N; ++i)
+        for (int j = 0; j < 2; ++j) CFD_CUDA(cudaEventCreate(&ev[i][j]));
+    CFD_CUDA(cudaMallocHost((void**)&h_scal, sizeof(StepScal)));
+    // mesh
+    std::vector<int4> el(E);
+    for (int e = 0; e < E; ++e)
+        el[e] = make_int4(m->inpoel[3 * e] - 1, m->inpoel[3 * e + 1] - 1, m->inpoel[3 * e + 2] - 1, e);
+    if ((st = upload(&d_elem, el.data(), E))) return st;
+    if ((st = upload(&d_X, m->x, N))) return st;
+    if ((st = upload(&d_Y, m->y, N))) return st;
+    if ((st = upload(&d_esup_ptr, adj.esup_ptr.data(), N + 1))) return st;
+    if ((st = upload(&d_esup_slot, adj.esup_slot.data(), 3 * (size_t)E))) return st;
+    if ((st = upload(&d_lap_pos, (const uchar4*)adj.lap_pos.data(), 3 * (size_t)E))) return st;
+    if ((st = upload(&d_rowptr, adj.rowptr.data(), N + 1))) return st;
+    if ((st = upload(&d_col, adj.col.data(), adj.col.size()))) return st;
+    if ((st = dalloc(&d_val, adj.col.size()))) return st;
+    if ((st = dalloc(&d_diag, N))) return st;
+    // BC tables
+    std::vector<uint8_t> fl = bc.flag;
+    for (auto& f : fl) {  // host bits -> device bits (same values, normals set on device)
+        uint8_t d = 0;
+        if (f & 1) d |= BC_FIXV;
+        if (f & 4) d |= BC_FIXRHO;
+        if (f & 8) d |= BC_FIXT;
+        f = d;
+    }
+    if ((st = upload(&d_bcflag, fl.data(), N))) return st;
+    if ((st = upload(&d_bcval, bc.val.data(), 4 * (size_t)N))) return st;
+    if ((st = dalloc(&d_nrm, N))) return st;
+    CFD_CUDA(cudaMemsetAsync(d_nrm, 0, sizeof(double2) * N, stream));
+    nwn = (int)bc.wnode.size();
+    if ((st = upload(&d_wnode, bc.wnode.data(), bc.wnode.size()))) return st;
+    if ((st = upload(&d_wptr, bc.wptr.data(), bc.wptr.size()))) return st;
+    std::vector<int2> wo(bc.wedge.size());
+    for (size_t i = 0; i < wo.size(); ++i) wo[i] = make_int2(bc.wedge[i], 0);
+    if ((st = upload(&d_wedge, wo.data(), wo.size()))) return st;
+    if ((st = upload(&d_walls, (const int2*)bc.walls.data(), bc.walls.size() / 2))) return st;
+    if ((st = upload(&d_set_ptr, bc.set_ptr.data(), bc.set_ptr.size()))) return st;
+    if ((st = upload(&d_set_edges, (const int2*)bc.set_edges.data(), bc.set_edges.size() / 2))) return st;
+    if ((st = upload(&d_xref, prm.xref, 10))) return st;
+    if ((st = upload(&d_yref, prm.yref, 10))) return st;
+    nnmove = (int)bc.fix_node.size();
+    if ((st = upload(&d_fix_node, bc.fix_node.data(), bc.fix_node.size()))) return st;
+    if ((st = upload(&d_fix_set, bc.fix_set.data(), bc.fix_set.size()))) return st;
+    nufix = (int)bc.ufix_node.size();
+    if ((st = upload(&d_ufix_node, bc.ufix_node.data(), bc.ufix_node.size()))) return st;
+    if ((st = upload(&d_ufix_src, bc.ufix_src.data(), bc.ufix_src.size()))) return st;
+    if ((st = upload(&d_isfix, bc.isfix.data(), N))) return st;
+    // state and work arrays
+    for (double** q : {&d_U, &d_U1}) if ((st = dalloc(q, 4 * (size_t)N))) return st;
+    for (double** q : {&d_T, &d_VX, &d_VY, &d_RHO, &d_E, &d_P, &d_RMACH, &d_WX, &d_WY, &d_M,
+                       &d_Wxo, &d_Wyo})
+        if ((st = dalloc(q, N))) return st;
+    for (double** q : {&d_area, &d_area_old, &d_DT, &d_DTL, &d_SHOC, &d_TS1, &d_TS2, &d_TS3})
+        if ((st = dalloc(q, E))) return st;
+    if ((st = dalloc(&d_geo, 6 * (size_t)E))) return st;
+    if ((st = dalloc(&d_contrib, 12 * (size_t)E))) return st;
+    if ((st = dalloc(&d_contribF, 12 * (size_t)E))) return st;
+    for (int s = 0; s < 2; ++s) {
+        for (double** q : {&d_pos[s], &d_r[s], &d_z[s], &d_y[s], &d_p[s][0], &d_p[s][1]})
+            if ((st = dalloc(q, N))) return st;
+        if ((st = dalloc(&d_xfix[s], nnmove))) return st;
+        CFD_CUDA(cudaMemsetAsync(d_pos[s], 0, sizeof(double) * N, stream));
+        CFD_CUDA(cudaMemsetAsync(d_xfix[s], 0, sizeof(double) * (nnmove ? nnmove : 1), stream));
+    }
+    const long nc = ((long)N + kChunk - 1) / kChunk;
+    if ((st = dalloc(&d_part, 4 * (size_t)(nc > 0 ? nc : 1)))) return st;
+    if ((st = dalloc(&d_bar, 1))) return st;
+    if ((st = dalloc(&d_pcg_iters, 2))) return st;
+    if ((st = dalloc(&d_pcg_conv, 2))) return st;
+    if ((st = dalloc(&d_pcg_rz, 2))) return st;
+    CFD_CUDA(cudaMemsetAsync(d_pcg_iters, 0, 2 * sizeof(int), stream));
+    CFD_CUDA(cudaMemsetAsync(d_pcg_conv, 0, 2 * sizeof(int), stream));
+    CFD_CUDA(cudaMemsetAsync(d_pcg_rz, 0, 2 * sizeof(double), stream));
+    if ((st = dalloc(&d_scal, 1))) return st;
+    StepScal sc0{};
+    sc0.dtmin_bits = 0x7ff0000000000000ull;
+    sc0.bandera = 1;
+    std::memcpy(h_scal, &sc0, sizeof(sc0));
+    CFD_CUDA(cudaMemcpyAsync(d_scal, h_scal, sizeof(StepScal), cudaMemcpyHostToDevice, stream));
+    CFD_CUDA(cudaStreamSynchronize(stream));
+    // persistent BiCG grid: co-resident blocks only
+    int dev = 0, nsm = 0, per_sm = 0;
+    CFD_CUDA(cudaGetDevice(&dev));
+    CFD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CFD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_fp64, 256, 0));
+    long g = (long)nsm * (per_sm > 0 ? per_sm : 1);
+    if (g > nc) g = nc;
+    pcg_grid = (int)(g > 0 ? g : 1);
+    // RESTART: freestream (ns2DComp.ALE.f90:59-60, :404-420)
+    std::vector<double> U(4 * (size_t)N), T(N), VX(N), VY(N), zero(N, 0.0);
+    for (int i = 0; i < N; ++i) {
+        const double rhoamb = prm.rho_inf, uamb = prm.u_inf, vamb = prm.v_inf;
+        const double pamb = prm.rho_inf * prm.fr * prm.t_inf;
+        U[4 * i] = rhoamb;
+        U[4 * i + 1] = rhoamb * uamb;
+        U[4 * i + 2] = rhoamb * vamb;
+        double energia = pamb / ((prm.gama - 1.0) * rhoamb) + 0.5 * (uamb * uamb + vamb * vamb);
+        U[4 * i + 3] = energia * rhoamb;
+        VX[i] = uamb;
+        VY[i] = vamb;
+        T[i] = prm.t_inf;
+    }
+    CFD_CUDA(cudaMemcpyAsync(d_U, U.data(), sizeof(double) * 4 * N, cudaMemcpyHostToDevice, stream));
+    CFD_CUDA(cudaMemcpyAsync(d_T, T.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
+    CFD_CUDA(cudaMemcpyAsync(d_VX, VX.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
+    CFD_CUDA(cudaMemcpyAsync(d_VY, VY.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
+    for (double* q : {d_WX, d_WY, d_Wxo, d_Wyo, d_RHO, d_E, d_P, d_RMACH})
+        CFD_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * N, stream));
+    // setup geometry: NORMALES, DERIV, MASAS, laplace (ns2DComp.ALE.f90:88-100)
+    st = geometry(true, true);
+    if (st) return st;
+    CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
+    CFD_CUDA(cudaStreamSynchronize(stream));
+    return tcollect();
+}
+
+}  // namespace cfd

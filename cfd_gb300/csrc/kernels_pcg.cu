@@ -1,0 +1,245 @@
+// kernels_pcg.cu — biCG (biconjGrad.f90:117-171) as one persistent cooperative kernel.
+//
+// The reference's solver is Jacobi-preconditioned CG with Dirichlet rows handled by
+// overwrite and a 1e30 penalty; every vector operation is a separate OpenMP loop and the
+// dots are OpenMP reductions.  Here the whole solve (both mesh-motion right-hand sides at
+// once, sharing the matrix reads) is one launch: each iteration is two grid-wide phases
+// separated by a bounded grid barrier.
+//   phase 1: x += alfa*p (deferred from the previous iteration), r -= alfa*y, z = r/diag,
+//            partial sums of r.z
+//   phase 2: p_new = beta*p + z computed on the fly inside the SpMV row loop
+//            (y_i = sum_j A_ij*(beta*p_j + z_j)), y(fix) = 1e30*p_new(fix), partial p.y
+// Every block folds the chunk partials itself in the fixed order of cfd_common.cuh, so
+// all blocks hold bit-identical scalars and take the same branch.  With --fmad=false the
+// iterates equal the CPU restatement's bit for bit.
+#include "cfd_kernels.cuh"
+
+namespace cfd {
+
+__device__ __forceinline__ double spmv_row(const PcgArgs& a, int i, const double* v) {
+    double dot = 0.0;
+    const int j1 = a.rowptr[i + 1];
+    for (int j = a.rowptr[i]; j < j1; ++j) dot = dot + a.val[j] * v[a.col[j]];
+    return dot;
+}
+
+__device__ __forceinline__ double spmv_row_dir(const PcgArgs& a, int i, const double* p,
+                                               const double* z, double beta) {
+    double dot = 0.0;
+    const int j1 = a.rowptr[i + 1];
+    for (int j = a.rowptr[i]; j < j1; ++j) {
+        const int c = a.col[j];
+        dot = dot + a.val[j] * (beta * p[c] + z[c]);
+    }
+    return dot;
+}
+
+__device__ __forceinline__ bool bar_failed(GridBar* gb) {
+    return *((volatile int*)&gb->err) != 0;
+}
+
+__global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
+    __shared__ double red[9];
+    const int t = threadIdx.x;
+    const int n = a.n;
+    const int ns = a.nsolve;
+    const long nc = ((long)n + kChunk - 1) / kChunk;
+    const unsigned nb = gridDim.x;
+    auto part = [&](int buf, int s) { return a.part + ((long)buf * 2 + s) * nc; };
+
+    // copy1 (biconjGrad.f90:137): x(fix) = x_fix
+    for (int k = blockIdx.x * blockDim.x + t; k < a.nfix; k += gridDim.x * blockDim.x)
+        for (int s = 0; s < ns; ++s) a.x[s][a.fix_node[k]] = 1.0 * a.fixval[s][a.fix_src[k]];
+    grid_barrier(a.bar, nb);
+    if (bar_failed(a.bar)) return;
+
+    // y = A.x; y(fix) = 1e30*x(fix); r = -1*y + b; r(fix) = 0; r.r   (:138-144)
+    for (long c = blockIdx.x; c < nc; c += gridDim.x) {
+        double acc[2] = {0.0, 0.0};
+        for (int k = 0; k < 4; ++k) {
+            const long i = c * kChunk + t + 256L * k;
+            if (i >= n) break;
+            const bool fx = a.isfix[i];
+            for (int s = 0; s < ns; ++s) {
+                double yi = fx ? 1.0e30 * a.x[s][i] : spmv_row(a, (int)i, a.x[s]);
+                a.y[s][i] = yi;
+                double ri = -1.0 * yi + (a.b[s] ? a.b[s][i] : 0.0);
+                if (fx) ri = 0.0;
+                a.r[s][i] = ri;
+                acc[s] = (k == 0) ? ri * ri : acc[s] + ri * ri;
+            }
+        }
+        for (int s = 0; s < ns; ++s) {
+            double v = block_tree256(acc[s], red);
+            if (t == 0) part(0, s)[c] = v;
+        }
+    }
+    grid_barrier(a.bar, nb);
+    if (bar_failed(a.bar)) return;
+    bool done[2] = {true, true};
+    double err_old[2] = {0.0, 0.0}, alfa[2] = {0.0, 0.0};
+    for (int s = 0; s < ns; ++s) {
+        double rr = fold_partials(part(0, s), nc, red);
+        done[s] = rr < a.tol;
+        if (done[s] && blockIdx.x == 0 && t == 0) {
+            a.iters_out[s] = 0;
+            a.rz_out[s] = rr;
+            a.conv_out[s] = 1;
+        }
+    }
+    if (done[0] && (ns < 2 || done[1])) return;
+
+    // p = r/diag; err_new = r.p   (:146-147)
+    for (long c = blockIdx.x; c < nc; c += gridDim.x) {
+        double acc[2] = {0.0, 0.0};
+        for (int k = 0; k < 4; ++k) {
+            const long i = c * kChunk + t + 256L * k;
+            if (i >= n) break;
+            const double d = a.diag[i];
+            for (int s = 0; s < ns; ++s) {
+                if (done[s]) continue;
+                double ri = a.r[s][i];
+                double pi = ri / d;
+                a.p[s][0][i] = pi;
+                acc[s] = (k == 0) ? ri * pi : acc[s] + ri * pi;
+            }
+        }
+        for (int s = 0; s < ns; ++s) {
+            if (done[s]) continue;
+            double v = block_tree256(acc[s], red);
+            if (t == 0) part(1, s)[c] = v;
+        }
+    }
+    grid_barrier(a.bar, nb);
+    if (bar_failed(a.bar)) return;
+    double err_new[2] = {0.0, 0.0};
+    for (int s = 0; s < ns; ++s)
+        if (!done[s]) err_new[s] = fold_partials(part(1, s), nc, red);
+
+    // y = A.p; y(fix) = 1e30*p(fix); py = p.y   (:148-151)
+    for (long c = blockIdx.x; c < nc; c += gridDim.x) {
+        double acc[2] = {0.0, 0.0};
+        for (int k = 0; k < 4; ++k) {
+            const long i = c * kChunk + t + 256L * k;
+            if (i >= n) break;
+            const bool fx = a.isfix[i];
+            for (int s = 0; s < ns; ++s) {
+                if (done[s]) continue;
+                const double* p = a.p[s][0];
+                double yi = fx ? 1.0e30 * p[i] : spmv_row(a, (int)i, p);
+                a.y[s][i] = yi;
+                acc[s] = (k == 0) ? p[i] * yi : acc[s] + p[i] * yi;
+            }
+        }
+        for (int s = 0; s < ns; ++s) {
+            if (done[s]) continue;
+            double v = block_tree256(acc[s], red);
+            if (t == 0) part(0, s)[c] = v;
+        }
+    }
+    grid_barrier(a.bar, nb);
+    if (bar_failed(a.bar)) return;
+    bool pend[2] = {false, false};
+    int cur[2] = {0, 0};
+    for (int s = 0; s < ns; ++s) {
+        if (done[s]) continue;
+        double py = fold_partials(part(0, s), nc, red);
+        alfa[s] = err_new[s] / py;  // :152
+        err_old[s] = err_new[s];
+        pend[s] = true;  // x = alfa*p + x (:153), applied in the next pass
+    }
+
+    int k = 0;
+    int last_iter[2] = {0, 0};
+    while (true) {  // :156-170
+        bool act[2] = {false, false};
+        for (int s = 0; s < ns; ++s)
+            act[s] = !done[s] && fabs(err_old[s]) > a.tol && k < a.maxit;
+        if (!act[0] && !act[1]) break;
+        k = k + 1;
+        // phase 1
+        for (long c = blockIdx.x; c < nc; c += gridDim.x) {
+            double acc[2] = {0.0, 0.0};
+            for (int kk = 0; kk < 4; ++kk) {
+                const long i = c * kChunk + t + 256L * kk;
+                if (i >= n) break;
+                const double d = a.diag[i];
+                for (int s = 0; s < ns; ++s) {
+                    if (pend[s]) a.x[s][i] = alfa[s] * a.p[s][cur[s]][i] + a.x[s][i];
+                    if (!act[s]) continue;
+                    double ri = (-alfa[s]) * a.y[s][i] + a.r[s][i];
+                    double zi = ri / d;
+                    a.r[s][i] = ri;
+                    a.z[s][i] = zi;
+                    acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
+                }
+            }
+            for (int s = 0; s < ns; ++s) {
+                if (!act[s]) continue;
+                double v = block_tree256(acc[s], red);
+                if (t == 0) part(1, s)[c] = v;
+            }
+        }
+        for (int s = 0; s < ns; ++s) pend[s] = false;
+        grid_barrier(a.bar, nb);
+        if (bar_failed(a.bar)) return;
+        double beta[2] = {0.0, 0.0};
+        for (int s = 0; s < ns; ++s) {
+            if (!act[s]) continue;
+            err_new[s] = fold_partials(part(1, s), nc, red);
+            beta[s] = err_new[s] / err_old[s];
+        }
+        // phase 2
+        for (long c = blockIdx.x; c < nc; c += gridDim.x) {
+            double acc[2] = {0.0, 0.0};
+            for (int kk = 0; kk < 4; ++kk) {
+                const long i = c * kChunk + t + 256L * kk;
+                if (i >= n) break;
+                const bool fx = a.isfix[i];
+                for (int s = 0; s < ns; ++s) {
+                    if (!act[s]) continue;
+                    const double* p = a.p[s][cur[s]];
+                    const double* z = a.z[s];
+                    double pn = beta[s] * p[i] + z[i];
+                    double yi = fx ? 1.0e30 * pn : spmv_row_dir(a, (int)i, p, z, beta[s]);
+                    a.p[s][cur[s] ^ 1][i] = pn;
+                    a.y[s][i] = yi;
+                    acc[s] = (kk == 0) ? pn * yi : acc[s] + pn * yi;
+                }
+            }
+            for (int s = 0; s < ns; ++s) {
+                if (!act[s]) continue;
+                double v = block_tree256(acc[s], red);
+                if (t == 0) part(0, s)[c] = v;
+            }
+        }
+        grid_barrier(a.bar, nb);
+        if (bar_failed(a.bar)) return;
+        for (int s = 0; s < ns; ++s) {
+            if (!act[s]) continue;
+            double py = fold_partials(part(0, s), nc, red);
+            alfa[s] = err_new[s] / py;
+            err_old[s] = err_new[s];
+            cur[s] ^= 1;
+            pend[s] = true;
+            last_iter[s] = k;
+        }
+    }
+    // the last deferred x update
+    for (long c = blockIdx.x; c < nc; c += gridDim.x)
+        for (int kk = 0; kk < 4; ++kk) {
+            const long i = c * kChunk + t + 256L * kk;
+            if (i >= n) break;
+            for (int s = 0; s < ns; ++s)
+                if (pend[s]) a.x[s][i] = alfa[s] * a.p[s][cur[s]][i] + a.x[s][i];
+        }
+    if (blockIdx.x == 0 && t == 0)
+        for (int s = 0; s < ns; ++s) {
+            if (done[s]) continue;
+            a.iters_out[s] = last_iter[s];
+            a.rz_out[s] = fabs(err_old[s]);
+            a.conv_out[s] = fabs(err_old[s]) > a.tol ? 0 : 1;
+        }
+}
+
+}  // namespace cfd

@@ -1,0 +1,269 @@
+/*
+ * cfd_gpu.h — C-ABI of the GB300 (sm_103a) implementation of the explicit SUPG
+ * compressible Navier–Stokes step on linear triangles with ALE mesh motion.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and returns an
+ * int status (0 = CFD_OK; see cfd_strerror()).  Two layers:
+ *
+ *  1. Drop-in routines.  Same argument lists, argument meaning and array layout as the
+ *     Fortran routines they replace: column-major arrays (U(4,npoin) is node-major
+ *     interleaved), 1-based node/element indices, scalars passed by pointer (Fortran
+ *     by-reference).  All pointers are HOST memory; each call stages its inputs to the
+ *     GPU, runs the kernels and copies the outputs back.
+ *
+ *  2. Resident context.  Mesh, state and every per-step array live in GPU memory; the
+ *     host uploads once, steps N times and downloads on demand.  This is the timed path.
+ *
+ * Nothing here holds global mutable state except the documented per-device buffers of
+ * the drop-in layer; a context belongs to one host thread at a time.
+ */
+#ifndef CFD_GPU_H
+#define CFD_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+enum {
+    CFD_OK = 0,
+    CFD_ERR_ARG = 1,          /* null pointer, non-positive size, bad enum value      */
+    CFD_ERR_MESH = 2,         /* index out of 1..npoin, degenerate/inverted element   */
+    CFD_ERR_CUDA = 3,         /* a CUDA runtime call failed                           */
+    CFD_ERR_NOMEM = 4,        /* device allocation failed                             */
+    CFD_ERR_NOT_CONVERGED = 5,/* BiCG hit its iteration cap (reference: silent)       */
+    CFD_ERR_NONFINITE = 6,    /* NaN/Inf found in the state (reference: fuse > 1e2)   */
+    CFD_ERR_BARRIER = 7,      /* a device-side bounded wait gave up                   */
+    CFD_ERR_LIMIT = 8,        /* a size above a documented maximum                    */
+    CFD_ERR_STATE = 9         /* call out of order (e.g. step before upload)          */
+};
+
+/* precision_mode for cfd_ctx_create */
+enum {
+    CFD_PREC_FP64 = 0,        /* plain: every operation FP64, reference evaluation order */
+    CFD_PREC_MIXED = 1        /* calcRHS and SpMV in FP32 (compensated node sums);
+                                 state update, gcl, BiCG dots and scalars in FP64        */
+};
+
+/* mass_mode: how the lumped mass follows a moving mesh */
+enum {
+    CFD_MASS_MASAS = 0,       /* recompute M = sum(area/3) (reference, MOVING=1)        */
+    CFD_MASS_GCL_LITERAL = 1, /* gcl.f90 main as written (divW uses dNy*W_x)            */
+    CFD_MASS_GCL_CORRECTED = 2/* gcl.f90 main with divW = dNx.W_x + dNy.W_y             */
+};
+
+/* motion_law: the prescribed body motion (reference hard-codes law 0) */
+enum {
+    CFD_MOTION_REFERENCE = 0, /* pitch pi/8*sin(10 t), no heave (meshMove.f90:55-71)    */
+    CFD_MOTION_HARMONIC = 1   /* heave A_h*sin(2 pi f t), pitch A_p*sin(2 pi f t)       */
+};
+
+/* guess_mode: initial guess of the two mesh-motion solves */
+enum {
+    CFD_GUESS_PREVIOUS = 0,   /* previous step's increment (reference, meshMove.f90:97) */
+    CFD_GUESS_ZERO = 1,
+    CFD_GUESS_LEARNED = 2     /* edge message-passing network (falls back to PREVIOUS)  */
+};
+
+/* ---------------------------------------------------------------- plain structs */
+
+/* InputData (dataLoader.f90:5-15) after readInputData's derivations (:58-64),
+ * plus the options the reference hard-codes. */
+typedef struct cfd_params {
+    int irestart, maxiter, iprint, movie, itlocal, ngas, moving;
+    double fsafe, u_inf, v_inf, mach_inf, t_inf, rho_inf, p_inf, c_inf;
+    double fmu, fgx, fgy, qh, fk, fr, fcv, gama;
+    double cte;               /* as stored by readInputData: 1/CTE of the file (:59)   */
+    double xref[10], yref[10];
+    /* build-side options (reference: hard-coded) */
+    int motion_law;           /* CFD_MOTION_*                                          */
+    double heave_amp, pitch_amp, motion_freq;
+    int mass_mode;            /* CFD_MASS_*                                            */
+    int guess_mode;           /* CFD_GUESS_*                                           */
+    double bicg_tol;          /* 1e-10 in biconjGrad.f90:135 (absolute, on r.z)        */
+    int bicg_maxit;           /* 1000 in biconjGrad.f90:156                            */
+    int reserved[7];
+} cfd_params;
+
+/* MeshData (dataLoader.f90:68-91) as loadMeshData leaves it.  Host pointers, Fortran
+ * layout, 1-based indices.  iset is ISET(3,10,nsets) column-major. */
+typedef struct cfd_mesh {
+    int npoin, nelem;
+    const int* inpoel;        /* 3*nelem                                               */
+    const double* x;          /* npoin                                                 */
+    const double* y;
+    int nfixrho;  const int* ifixrho_node; const double* rfixrho_value;
+    int nfixv;    const int* ifixv_node;   const double* rfixv_valuex; const double* rfixv_valuey;
+    int nfixt;    const int* ifixt_node;   const double* rfixt_value;
+    int nwall;    const int* wall;         /* 2*nwall                                  */
+    int nsets;    int nset_numb;  int ielem_sets[10]; const int* iset; /* 3*10*nsets   */
+    int nmove;    int nfix_move;  const int* ilaux;    /* nmove+nfix_move              */
+} cfd_mesh;
+
+/* Per-call report of cfd_step (the last step of the call). */
+typedef struct cfd_step_report {
+    int iter;                 /* ITER after the call                                   */
+    int status;
+    double time;              /* TIME                                                  */
+    double dtmin;             /* DTMIN used by the step (after hysteresis)             */
+    int bicg_iters[2];        /* x and y solves                                        */
+    double bicg_rz[2];        /* final |r.z|                                           */
+    int bicg_converged[2];
+    double fx[10], fy[10], rm[10]; /* FORCES (pressure) per set, before the mesh moves */
+    int nset_numb;
+    int reserved[5];
+} cfd_step_report;
+
+typedef struct cfd_solve_info {
+    int iters;                /* k of biconjGrad.f90:156                               */
+    int converged;            /* 1 if |r.z| <= tol (or early exit at :144)             */
+    double rz;                /* final |r.z|                                           */
+} cfd_solve_info;
+
+typedef struct cfd_ctx cfd_ctx;
+
+/* ---------------------------------------------------------------- drop-in routines */
+
+/* calcRHS (calcRHS.f90:4-154).  rhs(4,npoin) is ACCUMULATED into (the caller zeroes it,
+ * subrutinas.f90:680-682).  T(npoin) is the module temperature read at calcRHS.f90:6.
+ * gas = {FCV, FK, FMU, GAMA, T_inf, CTE} as calcRHS.f90:5 imports them. */
+int cfd_calcrhs(double* rhs, const double* U, const double* theta,
+                const double* dNx, const double* dNy, const double* area,
+                const double* shoc, const double* dtl, const double* t_sugn1,
+                const double* t_sugn2, const double* t_sugn3, const int* inpoel,
+                const int* nelem, const int* npoin, const double* T, const double* gas6);
+
+/* FUENTE (subrutinas.f90:1036-1094): rhs += ALE source term. */
+int cfd_fuente(double* rhs, const double* U, const double* W_X, const double* W_Y,
+               const double* dNx, const double* dNy, const double* area, const double* dtl,
+               const int* inpoel, const int* nelem, const int* npoin);
+
+/* ESTAB (subrutinas.f90:332-446) -> SHOC, T_SUGN1..3 per element.
+ * scal = {GAMA, FR, DTMIN, RHOINF, TINF} (RMU, UINF, VINF are read but unused). */
+int cfd_estab(const double* U, const double* T, const double* GAMM, const double* VEL_X,
+              const double* VEL_Y, const double* W_X, const double* W_Y,
+              const double* dNx, const double* dNy, const int* inpoel,
+              const int* nelem, const int* npoin, const double* scal5,
+              double* SHOC, double* T_SUGN1, double* T_SUGN2, double* T_SUGN3);
+
+/* deltat (subrutinas.f90:155-218) -> DT(nelem) (clamped at 10*DTMIN) and DTMIN.
+ * scal = {FSAFE, FR, GAMA, T_inf}. */
+int cfd_deltat(const double* T, const double* VEL_X, const double* VEL_Y,
+               const double* W_X, const double* W_Y, const double* area,
+               const int* inpoel, const int* nelem, const int* npoin,
+               const double* scal4, double* DT, double* DTMIN);
+
+/* deriv (subrutinas.f90:88-126) -> area, dNx(3,nelem), dNy, HH, HHX, HHY, hmin. */
+int cfd_deriv(const double* X, const double* Y, const int* inpoel, const int* nelem,
+              const int* npoin, double* area, double* dNx, double* dNy,
+              double* HH, double* HHX, double* HHY, double* hmin);
+
+/* MASAS (subrutinas.f90:128-153) -> lumped mass M(npoin). */
+int cfd_masas(const double* area, const int* inpoel, const int* nelem, const int* npoin,
+              double* M);
+
+/* gcl_mod::main (gcl.f90:8-46) with putW/putArea's saved state passed explicitly:
+ * M += dt*(tot1+tot2)/2.  mode = CFD_MASS_GCL_LITERAL or CFD_MASS_GCL_CORRECTED. */
+int cfd_gcl(double* M, const double* W_x, const double* W_y, const double* W_x_old,
+            const double* W_y_old, const double* dNx, const double* dNy,
+            const double* area, const double* area_old, const int* inpoel,
+            const int* nelem, const int* npoin, const double* dt, int mode);
+
+/* getEsup / getPsup (pointNeighbor.f90:5-91), host-side.  Output arrays are 1-based
+ * like the reference: esup2(npoin+1) offsets, esup1(3*nelem); psup2(npoin+1) offsets,
+ * psup1(*npsup).  Call once with psup1 == NULL to get *npsup. */
+int cfd_get_esup(const int* inpoel, const int* nelem, const int* npoin,
+                 int* esup1, int* esup2);
+int cfd_get_psup(const int* inpoel, const int* nelem, const int* npoin,
+                 int* psup1, int* psup2, int* npsup);
+
+/* Mlaplace::initialize (mLaplace.f90:60-94): lap_rowptr(npoin+1) (0-based offsets),
+ * lap_idx(nnz) (1-based, diagonal first).  Call with lap_idx == NULL to get *nnz. */
+int cfd_laplace_pattern(const int* inpoel, const int* nelem, const int* npoin,
+                        int* lap_rowptr, int* lap_idx, int* nnz);
+
+/* Mlaplace::laplace (mLaplace.f90:7-58): values of the mesh-motion operator on a given
+ * pattern (from cfd_laplace_pattern).  area is accepted and unused, as in the reference. */
+int cfd_laplace(const int* inpoel, const double* area, const double* dNx, const double* dNy,
+                const int* nelem, const int* npoin, const double* X, const double* Y,
+                double* lap_sparse, const int* lap_idx, const int* lap_rowptr,
+                double* lap_diag);
+
+/* biCG (biconjGrad.f90:117-171): Jacobi-preconditioned CG with Dirichlet rows by
+ * overwrite + 1e30 penalty.  x is the initial guess on entry, the solution on exit.
+ * tol/maxit as the reference (1e-10 absolute on |r.z|, 1000) unless overridden by
+ * cfd_bicg_ex.  info may be NULL.  Returns CFD_OK also when the cap is hit (like the
+ * reference); info->converged says which. */
+int cfd_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
+             const double* diagMtx, double* x, const double* b, const double* x_fix,
+             const int* x_fixIdx, const int* npoin, const int* nfix,
+             cfd_solve_info* info);
+int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr,
+                const double* diagMtx, double* x, const double* b, const double* x_fix,
+                const int* x_fixIdx, const int* npoin, const int* nfix,
+                double tol, int maxit, cfd_solve_info* info);
+
+/* ---------------------------------------------------------------- resident context */
+
+/* Builds adjacency, BC tables, the Laplacian pattern and every device buffer.
+ * Runs normales/deriv/MASAS/laplace on the device (ns2DComp.ALE.f90:88-100).
+ * The freestream initial state of RESTART (ns2DComp.ALE.f90:404-420) is loaded. */
+int cfd_ctx_create(cfd_ctx** ctx, const cfd_mesh* mesh, const cfd_params* p,
+                   int precision_mode);
+void cfd_ctx_destroy(cfd_ctx* ctx);
+
+/* Overwrite the flow state.  U(4,npoin), T, VEL_X, VEL_Y may be NULL to keep the
+ * current ones; when VEL_* are NULL they are derived from U. */
+int cfd_ctx_upload_state(cfd_ctx* ctx, const double* U, const double* T,
+                         const double* VEL_X, const double* VEL_Y);
+/* Overwrite the mesh-motion state: X, Y, W_X, W_Y, xpos, ypos (any may be NULL), and
+ * recompute the geometry of the new mesh (normales, deriv, mass, laplace). */
+int cfd_ctx_upload_mesh(cfd_ctx* ctx, const double* X, const double* Y,
+                        const double* W_X, const double* W_Y,
+                        const double* xpos, const double* ypos);
+/* Time-loop scalars: ITER, TIME, DTMIN1 (hysteresis memory), BANDERA, DISN(1:2). */
+int cfd_ctx_set_clock(cfd_ctx* ctx, int iter, double time, double dtmin1, int bandera,
+                      double disn1, double disn2);
+
+/* nsteps iterations of the loop body ns2DComp.ALE.f90:140-280. */
+int cfd_step(cfd_ctx* ctx, int nsteps, cfd_step_report* rep);
+
+/* Any pointer may be NULL.  U(4,npoin) reference layout. */
+int cfd_ctx_download_state(cfd_ctx* ctx, double* U, double* T, double* X, double* Y);
+/* Primitive fields of the last stage: RHO, VEL_X, VEL_Y, E, P, RMACH, W_X, W_Y. */
+int cfd_ctx_download_fields(cfd_ctx* ctx, double* RHO, double* VEL_X, double* VEL_Y,
+                            double* E, double* P, double* RMACH, double* W_X, double* W_Y);
+/* Mesh-motion increments of the last step (guess of the next). */
+int cfd_ctx_download_motion(cfd_ctx* ctx, double* xpos, double* ypos);
+/* Geometry of the current mesh: area(nelem), dNx(3,nelem), dNy(3,nelem), M(npoin). */
+int cfd_ctx_download_geometry(cfd_ctx* ctx, double* area, double* dNx, double* dNy,
+                              double* M);
+
+/* Per-kernel timers (CUDA events) accumulated since create, in seconds; names follow
+ * the reference TIMERS module (commonModules.f90:31-35).  n = slots written. */
+int cfd_ctx_timers(cfd_ctx* ctx, double* seconds, int max, int* n);
+const char* cfd_timer_name(int slot);
+
+/* The cudaStream_t (as void*) every kernel of this context is launched on, so a caller
+ * can record CUDA events around cfd_step on the launching stream. */
+void* cfd_ctx_stream(cfd_ctx* ctx);
+/* CUDA events on the context's stream: mark(slot) records event slot (0..7);
+ * elapsed waits for event b and returns the time from a to b in milliseconds. */
+int cfd_ctx_mark(cfd_ctx* ctx, int slot);
+int cfd_ctx_elapsed(cfd_ctx* ctx, int a, int b, double* ms);
+
+/* Select the device (ordinal) this library's contexts and drop-in calls use on the
+ * calling host thread (one process per GPU sets its local rank). */
+int cfd_set_device(int ordinal);
+
+/* Number of kernels this library launched since process start (all contexts). */
+long long cfd_kernel_launches(void);
+
+const char* cfd_strerror(int status);
+/* 1 if a CUDA device is usable by this library. */
+int cfd_device_available(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFD_GPU_H */
