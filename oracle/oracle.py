@@ -67,6 +67,9 @@ def lib():
             f = getattr(L, k)
             f.restype = r
             f.argtypes = a
+        # one thread by default: the element order of the serial loops (the parity
+        # order); the CPU baseline raises it with set_threads()
+        L.or_set_threads(1)
         _LIB = L
     return _LIB
 
