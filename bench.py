@@ -37,7 +37,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the plain-FP64 timing and the mixed-vs-FP64 error")
     ap.add_argument("--scale", type=int, default=None, help="nr = ntheta (reduced-size runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
@@ -154,10 +156,27 @@ def config_dict(k, args, ws):
             "data": "seeded synthetic O-grid (seed 0)"}
 
 
-# algorithmic bytes per launch of each timed group (FP64 path; the design doc lists them)
-def algorithmic_bytes(k, iters):
+# Algorithmic bytes per launch of each timed group: every array a launch must touch, read
+# or written once (gathers of node data count once per node).  N nodes, E elements, and
+# 3E element-around-point slots (~6 per node).
+def algorithmic_bytes(k, iters, precision):
     N, E = k.npoin, k.nelem
     nnz = 7 * N
+    if precision == "mixed":
+        return {
+            # elem 16 + slot_pos 12 + geo 48 + area 8 + shoc/tau 16 B/E, records 96 B/E;
+            # U 32 + W 16 B/N
+            "calcrhs_t": E * (16 + 12 + 48 + 8 + 16 + 96) + N * (32 + 16),
+            # ptr 4 + slots 12*... : 3E slot ids (4 B) and records (32 B), elem 16 B/E,
+            # T 8, U 32, 1/M 8, flags 1 B/N; writes U1 32 + 6 primitives 48 B/N
+            "update_t": 3 * E * (4 + 32) + E * 16 + N * (4 + 8 + 32 + 8 + 1 + 32 + 48),
+            "estab_t": E * (16 + 48 + 16) + N * (8 + 8 + 32 + 16),
+            "deltat_t": E * (16 + 8) + N * 40,
+            "laplace_t": 3 * E * (4 + 4) + E * (16 + 48) + N * 16 + nnz * 12 + N * 24,
+            "masas_t": E * (16 + 48 + 16 + 16) + N * 32 + 3 * E * 4 + N * 24,
+            "deriv_t": E * (16 + 8 + 48) + N * 16,
+            "grad_t": (nnz * 12 + N * 4) * (2 + iters) + N * 8 * 10 * (2 + iters),
+        }
     return {
         "calcrhs_t": E * (16 + 48 + 8 + 8 + 24 + 96) + N * 40 + (E * 96 + N * 16) / 4.0,
         "update_t": N * (24 + 2 * 6 * 32 + 32 + 8 + 32 + 56),
@@ -212,44 +231,60 @@ def main_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def timed_run(solver_mod, k, prec, W, K, L):
+    """Create a context, W warm-up steps, then K steps between CUDA events on the
+    context's stream.  Returns (solver, ms per step, kernel launches, report)."""
+    S = solver_mod.Solver(k, precision=prec)
+    S.step(W)
+    import torch
+    torch.cuda.synchronize()
+    l0 = L.cfd_kernel_launches()
+    S.mark(0)
+    rep = S.step(K)
+    S.mark(1)
+    ms = S.elapsed_ms(0, 1)
+    return S, ms / K, L.cfd_kernel_launches() - l0, rep
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
 def main_ours(args):
     ws, rank, local = dist_env()
+    import torch
     from cfd_gb300 import abi, build, solver
     build.build()
     L = abi.lib()
     abi.check(L.cfd_set_device(local), "cfd_set_device")
     dist = Dist(use_gpu=True)
     k = workload(args)
-    prec = abi.CFD_PREC_FP64 if args.precision == "fp64" else abi.CFD_PREC_MIXED
-    S = solver.Solver(k, precision=prec)
+    mixed = args.precision == "mixed"
+    prec = abi.CFD_PREC_MIXED if mixed else abi.CFD_PREC_FP64
+    # the mixed form runs the regularized ESTAB (continuous in the state; the reference's
+    # is discontinuous at round-off level); the plain form runs the reference's
+    k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED if mixed else abi.CFD_ESTAB_REFERENCE
     W, K = max(3, args.warmup), args.steps
     if args.profile_steps:
+        S = solver.Solver(k, precision=prec)
         S.step(W)
         S.step(args.profile_steps)
         return
-    S.step(W)
-    # ---- timed region (device time, CUDA events on the launching stream)
-    import torch
+    # ---- headline form: timed region (device time, CUDA events on the launching stream)
     torch.cuda.synchronize()
     dist.barrier()
     clocks = Clocks(local)
     clocks.start()
-    l0 = L.cfd_kernel_launches()
-    S.mark(0)
-    rep = S.step(K)
-    S.mark(1)
-    ms = S.elapsed_ms(0, 1)
-    launches = L.cfd_kernel_launches() - l0
+    S, ms_step, launches, rep = timed_run(solver, k, prec, W, K, L)
     torch.cuda.synchronize()
     dist.barrier()
     clk = clocks.stop()
-    ms_max = dist.max(ms)
-    sec_step = ms_max / 1e3 / K
+    sec_step = dist.max(ms_step) / 1e3
     value = ws * k.npoin / sec_step
-    # ---- e2e through the C-ABI with host buffers (pinned), copies inside the timed region
+    final_U = S.state()["U"]
+    # ---- e2e through the C-ABI with pinned host buffers, copies inside the timed region
     N = k.npoin
-    st = S.state()
-    f = S.fields()
+    st, f = S.state(), S.fields()
     hU = torch.empty((N, 4), dtype=torch.float64, pin_memory=True).numpy()
     hT = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
     hvx = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
@@ -268,7 +303,29 @@ def main_ours(args):
     e2e_sec = dist.max(time.perf_counter() - t0) / KE
     e2e = {"value": ws * N / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(N * (32 + 8 * 3)),
            "d2h_bytes_per_step": int(N * (32 + 8))}
-    # ---- per-kernel breakdown and roofline of the dominant kernel (timers on, separate ctx)
+    S.close()
+    # ---- the other forms: plain FP64 (reference ESTAB) speed; FP64 with the same ESTAB
+    # as the mixed run for its error
+    forms = {}
+    if mixed and not args.no_compare:
+        kp = workload(args)
+        Sp, msp, lp, repp = timed_run(solver, kp, abi.CFD_PREC_FP64, W, min(K, 10), L)
+        forms["fp64_plain"] = {"value": ws * N / (dist.max(msp) / 1e3), "unit": UNIT,
+                               "ms_per_step": msp, "estab_mode": "reference"}
+        Sp.close()
+        kr = workload(args)
+        kr.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
+        Sr = solver.Solver(kr, precision=abi.CFD_PREC_FP64)
+        repr_ = Sr.step(W + K)
+        Ur = Sr.state()["U"]
+        Sr.close()
+        forms["mixed_vs_fp64"] = {
+            "steps": W + K, "estab_mode": "regularized",
+            "rel_l2": [rel_l2(final_U[:, q], Ur[:, q]) for q in range(4)],
+            "force_rel_err": float(np.hypot(rep.fx[0] - repr_.fx[0], rep.fy[0] - repr_.fy[0])
+                                   / np.hypot(repr_.fx[0], repr_.fy[0]))}
+        forms["speedup_vs_fp64_plain"] = value / forms["fp64_plain"]["value"]
+    # ---- per-kernel breakdown and roofline of the dominant kernel (timers on, own ctx)
     os.environ["CFD_TIMERS"] = "1"
     S2 = solver.Solver(k, precision=prec)
     os.environ.pop("CFD_TIMERS")
@@ -277,40 +334,50 @@ def main_ours(args):
     KT = 4
     rep2 = S2.step(KT)
     t_after = S2.timers()
-    per = {n: (t_after[n] - t_before.get(n, 0.0)) / KT for n in t_after}
-    launches_per_step = {"calcrhs_t": 4, "update_t": 4, "estab_t": 1, "deltat_t": 1, "grad_t": 1}
+    S2.close()
+    per_step, per_launch = {}, {}
+    for n_, (sec, calls) in t_after.items():
+        ds, dc = sec - t_before[n_][0], calls - t_before[n_][1]
+        if dc > 0:
+            per_step[n_] = ds / KT
+            per_launch[n_] = ds / dc
     iters = float(np.mean(list(rep2.bicg_iters)))
-    ab = algorithmic_bytes(k, iters)
-    total = sum(per.values())
-    dom = max(per, key=lambda n: per[n])
+    ab = algorithmic_bytes(k, iters, args.precision)
+    total = sum(per_step.values())
+    dom = max(per_step, key=lambda n_: per_step[n_])
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    dom_launch_s = per[dom] / launches_per_step.get(dom, 1)
-    ach = ab.get(dom, 0.0) / dom_launch_s / 1e9 if dom in ab else None
+    ach = ab[dom] / per_launch[dom] / 1e9 if dom in ab else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": (ach / hbm_peak) if ach else None, "traffic": None,
-                "peak_source": "measured" if peaks else "fallback",
-                "share": per[dom] / total if total else None,
-                "launch_ms": dom_launch_s * 1e3}
-    S2.close()
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
+                "share_of_step": per_step[dom] / total if total else None,
+                "launch_ms": per_launch[dom] * 1e3,
+                "algorithmic_bytes_per_launch": ab.get(dom)}
+    kernels = {n_: {"ms_per_launch": per_launch[n_] * 1e3,
+                    "GBps_algorithmic": (ab[n_] / per_launch[n_] / 1e9) if n_ in ab else None}
+               for n_ in per_launch}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sec, _ = run_cpu_reference(k, threads, 1)
+        kc = workload(args)
+        sec, _ = run_cpu_reference(kc, threads, 1)
         cpu = {"value": k.npoin / sec, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"1 full step of the {k.npoin}-node workload (oracle, OpenMP, "
-                         f"{threads} threads), setup excluded"}
+                         f"{threads} threads, reference ESTAB), setup excluded"}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": sec_step * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32+f64 (mixed)" if mixed else "f64", "data": "synthetic",
                 "config": config_dict(k, args, ws), "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
-                "breakdown_ms_per_step": {n: v * 1e3 for n, v in per.items() if v > 0},
-                "bicg_iters": list(rep.bicg_iters), "bicg_converged": list(rep.bicg_converged)}
+                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "forms": forms,
+                "kernels": kernels,
+                "breakdown_ms_per_step": {n_: v * 1e3 for n_, v in per_step.items()},
+                "bicg_iters": list(rep.bicg_iters), "bicg_converged": list(rep.bicg_converged),
+                "state_finite": bool(np.isfinite(final_U).all())}
         print(json.dumps(line), flush=True)
-    S.close()
     dist.close()
 
 

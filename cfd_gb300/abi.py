@@ -22,6 +22,7 @@ CFD_PREC_FP64, CFD_PREC_MIXED = 0, 1
 CFD_MASS_MASAS, CFD_MASS_GCL_LITERAL, CFD_MASS_GCL_CORRECTED = 0, 1, 2
 CFD_MOTION_REFERENCE, CFD_MOTION_HARMONIC = 0, 1
 CFD_GUESS_PREVIOUS, CFD_GUESS_ZERO, CFD_GUESS_LEARNED = 0, 1, 2
+CFD_ESTAB_REFERENCE, CFD_ESTAB_EXACT, CFD_ESTAB_REGULARIZED = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -41,8 +42,8 @@ class CfdParams(C.Structure):
         ("motion_law", C.c_int),
         ("heave_amp", C.c_double), ("pitch_amp", C.c_double), ("motion_freq", C.c_double),
         ("mass_mode", C.c_int), ("guess_mode", C.c_int),
-        ("bicg_tol", C.c_double), ("bicg_maxit", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("bicg_tol", C.c_double), ("bicg_maxit", C.c_int), ("estab_mode", C.c_int),
+        ("reserved", C.c_int * 6),
     ]
 
 
@@ -122,6 +123,7 @@ SIGNATURES = {
     "cfd_ctx_download_motion": (C.c_int, [_P, _dp, _dp]),
     "cfd_ctx_download_geometry": (C.c_int, [_P, _dp, _dp, _dp, _dp]),
     "cfd_ctx_timers": (C.c_int, [_P, _dp, C.c_int, _ip]),
+    "cfd_ctx_timer_calls": (C.c_int, [_P, C.POINTER(C.c_longlong), C.c_int, _ip]),
     "cfd_timer_name": (C.c_char_p, [C.c_int]),
     "cfd_ctx_stream": (C.c_void_p, [_P]),
     "cfd_ctx_mark": (C.c_int, [_P, C.c_int]),

@@ -21,6 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("kernels_fp64.cu", ["--fmad=false"]),
     ("kernels_pcg.cu", ["--fmad=false"]),
+    ("kernels_mixed.cu", []),
+    ("kernels_pcg_mixed.cu", []),
     ("context.cu", ["--fmad=false"]),
     ("abi.cu", ["--fmad=false"]),
     ("host_prep.cpp", []),

@@ -191,10 +191,8 @@ int cfd_ctx_create(cfd_ctx** out, const cfd_mesh* mesh, const cfd_params* p, int
     *out = nullptr;
     if (precision_mode != CFD_PREC_FP64 && precision_mode != CFD_PREC_MIXED)
         return arg_error("precision_mode");
-    if (precision_mode == CFD_PREC_MIXED) {
-        set_last_message("the mixed-precision form is not available in this build");
-        return CFD_ERR_ARG;
-    }
+    if (p->estab_mode < CFD_ESTAB_REFERENCE || p->estab_mode > CFD_ESTAB_REGULARIZED)
+        return arg_error("estab_mode");
     if (p->ngas != 0) {
         set_last_message("only the perfect-gas path (NGAS = 0) is implemented");
         return CFD_ERR_ARG;
@@ -250,7 +248,7 @@ int cfd_ctx_upload_mesh(cfd_ctx* ctx, const double* X, const double* Y, const do
     if (W_Y) CFD_CUDA(cudaMemcpyAsync(c.d_WY, W_Y, n8, cudaMemcpyHostToDevice, c.stream));
     if (xpos) CFD_CUDA(cudaMemcpyAsync(c.d_pos[0], xpos, n8, cudaMemcpyHostToDevice, c.stream));
     if (ypos) CFD_CUDA(cudaMemcpyAsync(c.d_pos[1], ypos, n8, cudaMemcpyHostToDevice, c.stream));
-    if (X || Y) TRY(c.geometry(true, true));
+    if (X || Y) TRY(c.prec == CFD_PREC_MIXED ? c.geometry_mixed(true) : c.geometry(true, true));
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     return c.tcollect();
 }
@@ -338,6 +336,14 @@ int cfd_ctx_timers(cfd_ctx* ctx, double* seconds, int max, int* n) {
     if (!ctx || !seconds) return arg_error("ctx/seconds");
     int k = max < TM_N ? max : TM_N;
     for (int i = 0; i < k; ++i) seconds[i] = ctx->impl.seconds[i];
+    if (n) *n = k;
+    return CFD_OK;
+}
+
+int cfd_ctx_timer_calls(cfd_ctx* ctx, long long* calls, int max, int* n) {
+    if (!ctx || !calls) return arg_error("ctx/calls");
+    int k = max < TM_N ? max : TM_N;
+    for (int i = 0; i < k; ++i) calls[i] = ctx->impl.calls[i];
     if (n) *n = k;
     return CFD_OK;
 }
@@ -500,7 +506,8 @@ int cfd_estab(const double* U, const double* T, const double* GAMM, const double
     sc.dtmin = scal5[2];
     TRY(s.put(&d_sc, &sc, 1));
     CFD_LAUNCH(k_estab, blocks_for(E, 128), 128, 0, s.stream, E, d_el, d_U, d_T, scal5[0], d_G, d_vx,
-               d_vy, d_wx, d_wy, d_geo, scal5[1], d_sc, scal5[3], scal5[4], o[0], o[1], o[2], o[3]);
+               d_vy, d_wx, d_wy, d_geo, scal5[1], d_sc, scal5[3], scal5[4], (int)CFD_ESTAB_REFERENCE,
+               0.0, 1.0, 0.0, o[0], o[1], o[2], o[3]);
     TRY(s.get(SHOC, o[0], E));
     TRY(s.get(T_SUGN1, o[1], E));
     TRY(s.get(T_SUGN2, o[2], E));

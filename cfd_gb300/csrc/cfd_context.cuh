@@ -56,6 +56,18 @@ struct Ctx {
            *d_DTL = nullptr;
     double *d_SHOC = nullptr, *d_TS1 = nullptr, *d_TS2 = nullptr, *d_TS3 = nullptr;
     double *d_contrib = nullptr, *d_contribF = nullptr;
+    // mixed precision
+    double *d_T2 = nullptr, *d_invM = nullptr, *d_invdiag = nullptr;
+    float *d_shocf = nullptr, *d_ts1f = nullptr, *d_ts2f = nullptr, *d_ts3f = nullptr;
+    float* d_valf = nullptr;
+    float* d_pf[2][2] = {};
+    float* d_zf[2] = {};
+    int* d_slot_pos = nullptr;
+    void* d_rec = nullptr;
+    double2* d_gterms = nullptr;
+    double estab_eps = 1.0e-3;  // CFD_ESTAB_REGULARIZED relative gradient scale
+    double dir[2] = {1.0, 0.0};  // CFD_ESTAB_REGULARIZED freestream direction
+    bool laplace_fp64 = false;  // mixed form: Laplacian values in FP64 arithmetic
     // mesh motion
     double* d_pos[2] = {nullptr, nullptr};  // xpos, ypos (guess in, solution out)
     double* d_xfix[2] = {nullptr, nullptr};
@@ -68,16 +80,21 @@ struct Ctx {
     StepScal* d_scal = nullptr;
     // timers
     bool timers_on = false;
-    cudaEvent_t ev[TM_N][2] = {};
+    std::vector<cudaEvent_t> pool;  // event pairs of the timed groups of one step
+    size_t pool_next = 0;
+    int open_pair[TM_N] = {};
+    std::vector<std::pair<int, int>> pending;  // (slot, pair) recorded, not yet read
     cudaEvent_t mark[8] = {};  // caller-requested events (cfd_ctx_mark)
-    bool used[TM_N] = {};
+    long long calls[TM_N] = {};
     double seconds[TM_N] = {};
 
     ~Ctx();
     int create(const cfd_mesh* m, const cfd_params* p, int precision_mode);
     int geometry(bool masas, bool with_laplace);
+    int geometry_mixed(bool setup);
     int run_pcg(int nsolve);
     int step_once();
+    int step_once_mixed();
     int step(int nsteps, cfd_step_report* rep);
     int tstart(int slot);
     int tstop(int slot);

@@ -40,27 +40,38 @@ static const char* kTimerNames[TM_N] = {"deltat_t", "estab_t",  "calcrhs_t", "fu
                                         "normales_t", "deriv_t", "masas_t",  "laplace_t"};
 
 // ------------------------------------------------------------------ timers
+// Every tstart/tstop pair takes a fresh pair of events from a pool, so a group timed
+// several times per step (the 4 RK stages) accumulates every launch.
 int Ctx::tstart(int slot) {
     if (!timers_on) return CFD_OK;
-    CFD_CUDA(cudaEventRecord(ev[slot][0], stream));
+    if (2 * (pool_next + 1) > pool.size()) {
+        for (int j = 0; j < 2; ++j) {
+            cudaEvent_t e;
+            CFD_CUDA(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+    }
+    open_pair[slot] = (int)pool_next++;
+    CFD_CUDA(cudaEventRecord(pool[2 * open_pair[slot]], stream));
     return CFD_OK;
 }
 int Ctx::tstop(int slot) {
     if (!timers_on) return CFD_OK;
-    CFD_CUDA(cudaEventRecord(ev[slot][1], stream));
-    used[slot] = true;
+    CFD_CUDA(cudaEventRecord(pool[2 * open_pair[slot] + 1], stream));
+    pending.push_back(std::make_pair(slot, open_pair[slot]));
+    calls[slot] += 1;
     return CFD_OK;
 }
 int Ctx::tcollect() {
     if (!timers_on) return CFD_OK;
     CFD_CUDA(cudaStreamSynchronize(stream));
-    for (int i = 0; i < TM_N; ++i)
-        if (used[i]) {
-            float ms = 0.f;
-            CFD_CUDA(cudaEventElapsedTime(&ms, ev[i][0], ev[i][1]));
-            seconds[i] += ms * 1e-3;
-            used[i] = false;
-        }
+    for (auto& sp : pending) {
+        float ms = 0.f;
+        CFD_CUDA(cudaEventElapsedTime(&ms, pool[2 * sp.second], pool[2 * sp.second + 1]));
+        seconds[sp.first] += ms * 1e-3;
+    }
+    pending.clear();
+    pool_next = 0;
     return CFD_OK;
 }
 
@@ -69,9 +80,7 @@ Ctx::~Ctx() {
     for (void* p : allocs) cudaFree(p);
     if (h_scal) cudaFreeHost(h_scal);
     if (ev_scal) cudaEventDestroy(ev_scal);
-    for (int i = 0; i < TM_N; ++i)
-        for (int j = 0; j < 2; ++j)
-            if (ev[i][j]) cudaEventDestroy(ev[i][j]);
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (auto& m : mark)
         if (m) cudaEventDestroy(m);
     if (stream) cudaStreamDestroy(stream);
@@ -134,9 +143,20 @@ int Ctx::run_pcg(int nsolve) {
     a.iters_out = d_pcg_iters;
     a.rz_out = d_pcg_rz;
     a.conv_out = d_pcg_conv;
+    const bool mixed = (prec == CFD_PREC_MIXED);
+    if (mixed) {
+        a.valf = d_valf;
+        a.invdiag = d_invdiag;
+        for (int s = 0; s < 2; ++s) {
+            a.pf[s][0] = d_pf[s][0];
+            a.pf[s][1] = d_pf[s][1];
+            a.zf[s] = d_zf[s];
+        }
+    }
     CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
     void* args[] = {&a};
-    CFD_CUDA(cudaLaunchCooperativeKernel((void*)k_pcg_fp64, dim3(pcg_grid), dim3(256), args, 0, stream));
+    CFD_CUDA(cudaLaunchCooperativeKernel(mixed ? (void*)k_pcg_mixed : (void*)k_pcg_fp64, dim3(pcg_grid),
+                                         dim3(256), args, 0, stream));
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return CFD_OK;
 }
@@ -165,10 +185,10 @@ int Ctx::step_once() {
     tstart(TM_ESTAB);
     CFD_LAUNCH(k_estab, blocks_for(E, 128), 128, 0, stream, E, d_elem, d_U, d_T, prm.gama,
                (const double*)nullptr, d_VX,
-               d_VY, d_WX, d_WY, d_geo, prm.fr, d_scal, prm.rho_inf, prm.t_inf, d_SHOC, d_TS1,
-               d_TS2, d_TS3);
+               d_VY, d_WX, d_WY, d_geo, prm.fr, d_scal, prm.rho_inf, prm.t_inf, prm.estab_mode,
+               estab_eps, dir[0], dir[1], d_SHOC, d_TS1, d_TS2, d_TS3);
     tstop(TM_ESTAB);
-    GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte};
+    GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte, prm.fr};
     const bool viscous = prm.fmu > 2.2250738585072014e-308;
     const int NRK = 4;
     for (int irk = 1; irk <= NRK; ++irk) {
@@ -250,7 +270,7 @@ int Ctx::step_once() {
 int Ctx::step(int nsteps, cfd_step_report* rep) {
     if (nsteps < 0) return CFD_ERR_ARG;
     for (int s = 0; s < nsteps; ++s) {
-        int st = step_once();
+        int st = (prec == CFD_PREC_MIXED) ? step_once_mixed() : step_once();
         if (st) return st;
     }
     CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
@@ -321,10 +341,15 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if (st) { set_last_message(why); return st; }
     const int N = npoin, E = nelem;
     timers_on = getenv("CFD_TIMERS") && atoi(getenv("CFD_TIMERS")) != 0;
+    if (getenv("CFD_ESTAB_EPS")) estab_eps = atof(getenv("CFD_ESTAB_EPS"));
+    {  // freestream direction (the oracle's or_set_estab_dir, same operations)
+        const double n = std::sqrt(prm.u_inf * prm.u_inf + prm.v_inf * prm.v_inf);
+        dir[0] = n > 0.0 ? prm.u_inf / n : 1.0;
+        dir[1] = n > 0.0 ? prm.v_inf / n : 0.0;
+    }
+    if (getenv("CFD_MIXED_LAPLACE_FP64")) laplace_fp64 = atoi(getenv("CFD_MIXED_LAPLACE_FP64")) != 0;
     CFD_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CFD_CUDA(cudaEventCreateWithFlags(&ev_scal, cudaEventDisableTiming));
-    for (int i = 0; i < TM_N; ++i)
-        for (int j = 0; j < 2; ++j) CFD_CUDA(cudaEventCreate(&ev[i][j]));
     CFD_CUDA(cudaMallocHost((void**)&h_scal, sizeof(StepScal)));
     // mesh
     std::vector<int4> el(E);
@@ -400,6 +425,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if ((st = dalloc(&d_scal, 1))) return st;
     StepScal sc0{};
     sc0.dtmin_bits = 0x7ff0000000000000ull;
+    sc0.dtmin32_bits = 0x7ff0000000000000ull;
     sc0.bandera = 1;
     std::memcpy(h_scal, &sc0, sizeof(sc0));
     CFD_CUDA(cudaMemcpyAsync(d_scal, h_scal, sizeof(StepScal), cudaMemcpyHostToDevice, stream));
@@ -408,7 +434,8 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     int dev = 0, nsm = 0, per_sm = 0;
     CFD_CUDA(cudaGetDevice(&dev));
     CFD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    CFD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_fp64, 256, 0));
+    CFD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, prec == CFD_PREC_MIXED ? k_pcg_mixed : k_pcg_fp64, 256, 0));
     long g = (long)nsm * (per_sm > 0 ? per_sm : 1);
     if (g > nc) g = nc;
     pcg_grid = (int)(g > 0 ? g : 1);
@@ -432,11 +459,152 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     CFD_CUDA(cudaMemcpyAsync(d_VY, VY.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
     for (double* q : {d_WX, d_WY, d_Wxo, d_Wyo, d_RHO, d_E, d_P, d_RMACH})
         CFD_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * N, stream));
+    if (prec == CFD_PREC_MIXED) {
+        if (prm.itlocal != 0) {
+            set_last_message("the mixed-precision form runs with a global time step (ITLOCAL = 0)");
+            return CFD_ERR_ARG;
+        }
+        for (double** q : {&d_T2, &d_invM, &d_invdiag})
+            if ((st = dalloc(q, N))) return st;
+        for (float** q : {&d_shocf, &d_ts1f, &d_ts2f, &d_ts3f})
+            if ((st = dalloc(q, E))) return st;
+        for (int s = 0; s < 2; ++s)
+            for (float** q : {&d_pf[s][0], &d_pf[s][1], &d_zf[s]})
+                if ((st = dalloc(q, N))) return st;
+        if ((st = dalloc(&d_valf, adj.col.size()))) return st;
+        if ((st = dalloc(&d_gterms, E))) return st;
+        // slot (e, i) -> its position in element-around-point order
+        std::vector<int> pos(3 * (size_t)E);
+        for (size_t s = 0; s < adj.esup_slot.size(); ++s) pos[adj.esup_slot[s]] = (int)s;
+        if ((st = upload(&d_slot_pos, pos.data(), pos.size()))) return st;
+        char* rec = nullptr;
+        if ((st = dalloc(&rec, slot_record_bytes() * 3 * (size_t)E))) return st;
+        d_rec = rec;
+    }
     // setup geometry: NORMALES, DERIV, MASAS, laplace (ns2DComp.ALE.f90:88-100)
-    st = geometry(true, true);
+    st = (prec == CFD_PREC_MIXED) ? geometry_mixed(true) : geometry(true, true);
     if (st) return st;
     CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
     CFD_CUDA(cudaStreamSynchronize(stream));
+    return tcollect();
+}
+
+// ------------------------------------------------------------------ mixed precision
+// Geometry of the current mesh for the mixed form: normales, deriv (FP64 areas), the
+// lumped mass (MASAS at setup; MASAS or gcl per step) with 1/M, FP32 Laplacian values.
+int Ctx::geometry_mixed(bool setup) {
+    const int N = npoin, E = nelem;
+    const int TB = 256;
+    tstart(TM_NORMALES);
+    if (nwn > 0)
+        CFD_LAUNCH(k_normales, blocks_for(nwn, TB), TB, 0, stream, nwn, d_wnode, d_wptr, d_wedge,
+                   d_walls, d_X, d_Y, d_bcflag, d_nrm);
+    tstop(TM_NORMALES);
+    tstart(TM_DERIV);
+    CFD_LAUNCH(k_deriv_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_X, d_Y, d_area, d_geo);
+    tstop(TM_DERIV);
+    tstart(TM_MASAS);
+    const bool gcl = !setup && prm.mass_mode != CFD_MASS_MASAS;
+    if (gcl) {
+        CFD_LAUNCH(k_gcl_elem, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_geo, d_area, d_area_old,
+                   d_WX, d_WY, d_Wxo, d_Wyo, prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_gterms);
+    }
+    CFD_LAUNCH(k_mass_mixed, blocks_for(N, TB), TB, 0, stream, N, d_esup_ptr, d_esup_slot, d_area,
+               (const double2*)d_gterms, &d_scal->dtmin, gcl ? 1 : 0, d_M, d_invM);
+    if (gcl) {  // putW, putArea
+        CFD_CUDA(cudaMemcpyAsync(d_Wxo, d_WX, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
+        CFD_CUDA(cudaMemcpyAsync(d_Wyo, d_WY, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
+        CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
+    }
+    tstop(TM_MASAS);
+    tstart(TM_LAPLACE);
+    CFD_CUDA(launch_laplace_mixed(laplace_fp64, stream, N, E, d_elem, d_esup_ptr, d_esup_slot,
+                                  d_lap_pos, d_geo, d_X, d_Y, d_rowptr, d_valf, d_val, d_diag,
+                                  d_invdiag));
+    tstop(TM_LAPLACE);
+    return CFD_OK;
+}
+
+int Ctx::step_once_mixed() {
+    const int N = npoin, E = nelem;
+    const int TB = 256;
+    iter += 1;
+    tstart(TM_DELTAT);
+    CFD_LAUNCH(k_deltat_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_T, d_VX, d_VY, d_WX,
+               d_WY, d_area, (float)prm.fsafe, (float)prm.t_inf, &d_scal->dtmin32_bits);
+    CFD_LAUNCH(k_deltat_refine, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_T, d_VX, d_VY, d_WX,
+               d_WY, d_area, (float)prm.fsafe, (float)prm.t_inf, d_scal);
+    CFD_LAUNCH(k_dt_finalize, 1, 1, 0, stream, d_scal);
+    tstop(TM_DELTAT);
+    CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
+    CFD_CUDA(cudaEventRecord(ev_scal, stream));
+    tstart(TM_ESTAB);
+    CFD_LAUNCH(k_estab_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_U, d_T,
+               (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VX, d_VY, d_WX, d_WY, d_geo,
+               (float)prm.fr, d_scal, (float)prm.rho_inf, (float)prm.t_inf, prm.estab_mode,
+               (float)estab_eps, (float)dir[0], (float)dir[1], d_shocf, d_ts1f, d_ts2f, d_ts3f);
+    tstop(TM_ESTAB);
+    GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte, prm.fr};
+    const bool viscous = prm.fmu > 2.2250738585072014e-308;
+    tstart(TM_CALCRHS);
+    CFD_CUDA(launch_elem_stage1_mixed(viscous, stream, E, d_elem, d_U, d_geo, d_area, d_shocf,
+                                      nullptr, &d_scal->dtmin, d_ts1f, d_ts2f, d_ts3f, gc, d_WX,
+                                      d_WY, d_slot_pos, d_rec));
+    tstop(TM_CALCRHS);
+    // T is read at the element's nodes and written per node: alternate two buffers so
+    // that stage s reads the T of stage s-1 (the reference's module T) and the 4th
+    // stage leaves it in d_T
+    double* Tb[2] = {d_T, d_T2};
+    const int NRK = 4;
+    for (int irk = 1; irk <= NRK; ++irk) {
+        const double rk_fact = 1.0 / (NRK + 1 - irk);
+        tstart(TM_UPDATE);
+        CFD_CUDA(launch_node_mixed(stream, N, d_esup_ptr, d_esup_slot, d_elem, d_rec,
+                                   Tb[(irk - 1) & 1], gc, viscous ? 1 : 0, d_U, d_invM, rk_fact,
+                                   d_bcflag, d_bcval, d_nrm, d_WX, d_WY, d_U1, d_RHO, d_VX, d_VY,
+                                   d_E, d_P, Tb[irk & 1], d_RMACH));
+        tstop(TM_UPDATE);
+    }
+    CFD_CUDA(cudaEventSynchronize(ev_scal));
+    const double dtmin = h_scal->dtmin;
+    time = time + dtmin;
+    last_dtmin = dtmin;
+    tstart(TM_FORCES);
+    CFD_LAUNCH(k_forces_tree, 1, 256, 0, stream, bc.nset_numb, d_set_ptr, d_set_edges, d_P, d_X, d_Y,
+               d_xref, d_yref, d_scal);
+    tstop(TM_FORCES);
+    const double PI = std::acos(-1.0);
+    double alphav = disn[1], yposrv = disn[0];
+    if (prm.motion_law == CFD_MOTION_HARMONIC) {
+        double ph = 2.0 * PI * prm.motion_freq * time;
+        disn[0] = prm.heave_amp * std::sin(ph);
+        disn[1] = prm.pitch_amp * std::sin(ph);
+    } else {
+        disn[1] = (PI / 8.0) * std::sin(10.0 * time);
+    }
+    const double alpha = disn[1] - alphav, yposr = disn[0] - yposrv;
+    const double ca = std::cos(alpha), sa = std::sin(alpha);
+    tstart(TM_TRANSF);
+    if (nnmove > 0)
+        CFD_LAUNCH(k_transf, blocks_for(nnmove, TB), TB, 0, stream, nnmove, d_fix_node, d_fix_set,
+                   d_X, d_Y, d_xref, d_yref, ca, sa, yposr, d_xfix[0], d_xfix[1]);
+    tstop(TM_TRANSF);
+    if (prm.guess_mode == CFD_GUESS_ZERO) {
+        CFD_CUDA(cudaMemsetAsync(d_pos[0], 0, sizeof(double) * N, stream));
+        CFD_CUDA(cudaMemsetAsync(d_pos[1], 0, sizeof(double) * N, stream));
+    }
+    tstart(TM_GRAD);
+    int st = run_pcg(2);
+    if (st) return st;
+    tstop(TM_GRAD);
+    CFD_LAUNCH(k_motion_update, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1], d_scal,
+               d_X, d_Y, d_WX, d_WY);
+    if (prm.moving == 1) {
+        st = geometry_mixed(false);
+        if (st) return st;
+    }
+    std::swap(d_U, d_U1);
+    bandera_host += 1;
     return tcollect();
 }
 

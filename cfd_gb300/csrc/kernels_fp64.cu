@@ -144,6 +144,7 @@ __global__ void k_dt_finalize(StepScal* sc) {
     unsigned long long b = sc->dtmin_bits;
     if (b != 0x7ff0000000000000ull) dtmin = __longlong_as_double((long long)b);
     sc->dtmin_bits = 0x7ff0000000000000ull;  // ready for the next step's k_deltat
+    sc->dtmin32_bits = 0x7ff0000000000000ull;
     sc->dtmin_raw = dtmin;
     if (sc->bandera == 1) {
         sc->dtmin1 = dtmin;
@@ -179,6 +180,7 @@ __global__ void k_estab(int nelem, const int4* __restrict__ elem, const double* 
                         const double* __restrict__ VY, const double* __restrict__ WX,
                         const double* __restrict__ WY, const double* __restrict__ geo,
                         double FR, const StepScal* __restrict__ sc, double RHOINF, double TINF,
+                        int estab_mode, double eps_dir, double dirx, double diry,
                         double* __restrict__ SHOC, double* __restrict__ TS1,
                         double* __restrict__ TS2, double* __restrict__ TS3) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,10 +211,31 @@ __global__ void k_estab(int nelem, const int4* __restrict__ elem, const double* 
     double dt2 = sqrt(dtx * dtx + dty * dty) + 1.0e-20;
     double dux = vel2 * DX[0] + vel2 * DX[1] + vel2 * DX[2];
     double duy = vel2 * DY[0] + vel2 * DY[1] + vel2 * DY[2];
+    if (estab_mode != CFD_ESTAB_REFERENCE) {
+        dux = 0.0;
+        duy = 0.0;
+    }
     double du2 = sqrt(dux * dux + duy * duy) + 1.0e-20;
     double rtx = dtx / dt2, rty = dty / dt2;
     double rjx = drx / dr2, rjy = dry / dr2;
     double rux = dux / du2, ruy = duy / du2;
+    if (estab_mode == CFD_ESTAB_REGULARIZED) {
+        // unit vectors continuous in the state: gradient + eps*scale*G_e along the
+        // freestream direction, normalised; the velocity-gradient direction is that d
+        double ge = 0.0;
+        for (int i = 0; i < 3; ++i) ge += sqrt(DX[i] * DX[i] + DY[i] * DY[i]);
+        const double sr = eps_dir * rho_elem * ge;
+        const double st = eps_dir * ((t1 + t2 + t3) / 3.0) * ge;
+        const double gx = drx + sr * dirx, gy = dry + sr * diry;
+        const double hx = dtx + st * dirx, hy = dty + st * diry;
+        const double gn = sqrt(gx * gx + gy * gy), hn = sqrt(hx * hx + hy * hy);
+        rjx = gx / gn;
+        rjy = gy / gn;
+        rtx = hx / hn;
+        rty = hy / hn;
+        rux = dirx;
+        ruy = diry;
+    }
     double temp = (t1 + t2 + t3) / 3.0;
     double c = sqrt(gm * FR * temp);
     const double smu = 110.0;

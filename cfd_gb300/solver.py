@@ -271,8 +271,11 @@ class Solver:
         return ms.value
 
     def timers(self):
+        """{timer name: (seconds, timed launches)} accumulated since create (CFD_TIMERS=1)."""
         s = np.zeros(16)
+        c = (C.c_longlong * 16)()
         n = C.c_int(0)
         check(abi.lib().cfd_ctx_timers(self.h, dptr(s), 16, C.byref(n)), "cfd_ctx_timers")
+        check(abi.lib().cfd_ctx_timer_calls(self.h, c, 16, C.byref(n)), "cfd_ctx_timer_calls")
         names = [abi.lib().cfd_timer_name(i).decode() for i in range(n.value)]
-        return dict(zip(names, s[:n.value].tolist()))
+        return {nm: (float(s[i]), int(c[i])) for i, nm in enumerate(names)}

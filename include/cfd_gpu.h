@@ -65,6 +65,18 @@ enum {
     CFD_GUESS_LEARNED = 2     /* edge message-passing network (falls back to PREVIOUS)  */
 };
 
+/* estab_mode: the "velocity gradient" of ESTAB (subrutinas.f90:380-383) is
+ * DUX = VEL2*sum(dNx), zero in exact arithmetic; as written its round-off decides
+ * whether H_RGN and T_SUGN2 vanish (a discontinuity at round-off level). */
+enum {
+    CFD_ESTAB_REFERENCE = 0,  /* evaluate DUX, DUY as written (bit-exact reference)     */
+    CFD_ESTAB_EXACT = 1,      /* take DUX = DUY = 0, their exact-arithmetic value       */
+    CFD_ESTAB_REGULARIZED = 2 /* unit vectors continuous in the state: grad(rho), grad(T)
+                                 plus 1e-3*scale*sum|grad N_i| along the freestream
+                                 direction d, normalised; the velocity-gradient direction
+                                 (round-off in the reference) is d                      */
+};
+
 /* ---------------------------------------------------------------- plain structs */
 
 /* InputData (dataLoader.f90:5-15) after readInputData's derivations (:58-64),
@@ -82,7 +94,8 @@ typedef struct cfd_params {
     int guess_mode;           /* CFD_GUESS_*                                           */
     double bicg_tol;          /* 1e-10 in biconjGrad.f90:135 (absolute, on r.z)        */
     int bicg_maxit;           /* 1000 in biconjGrad.f90:156                            */
-    int reserved[7];
+    int estab_mode;           /* CFD_ESTAB_*                                           */
+    int reserved[6];
 } cfd_params;
 
 /* MeshData (dataLoader.f90:68-91) as loadMeshData leaves it.  Host pointers, Fortran
@@ -242,6 +255,8 @@ int cfd_ctx_download_geometry(cfd_ctx* ctx, double* area, double* dNx, double* d
 /* Per-kernel timers (CUDA events) accumulated since create, in seconds; names follow
  * the reference TIMERS module (commonModules.f90:31-35).  n = slots written. */
 int cfd_ctx_timers(cfd_ctx* ctx, double* seconds, int max, int* n);
+/* Number of timed launches accumulated in each timer slot. */
+int cfd_ctx_timer_calls(cfd_ctx* ctx, long long* calls, int max, int* n);
 const char* cfd_timer_name(int slot);
 
 /* The cudaStream_t (as void*) every kernel of this context is launched on, so a caller

@@ -22,6 +22,11 @@ namespace {
 inline double pow15(double x) { return x * std::sqrt(x); }
 inline double powm05(double x) { return 1.0 / std::sqrt(x); }
 
+// ESTAB's DUX/DUY evaluation (CFD_ESTAB_*), set by or_set_estab_mode / the case params
+int g_estab_mode = CFD_ESTAB_REFERENCE;
+double g_estab_eps = 1.0e-3;  // CFD_ESTAB_REGULARIZED: relative gradient scale
+double g_dir[2] = {1.0, 0.0};  // CFD_ESTAB_REGULARIZED: freestream direction
+
 struct Clock {
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     double sec() const {
@@ -39,6 +44,14 @@ void or_set_threads(int n) {
 #else
     (void)n;
 #endif
+}
+
+void or_set_estab_mode(int mode) { g_estab_mode = mode; }
+void or_set_estab_eps(double eps) { g_estab_eps = eps; }
+void or_set_estab_dir(double ux, double uy) {
+    const double n = std::sqrt(ux * ux + uy * uy);
+    g_dir[0] = n > 0.0 ? ux / n : 1.0;
+    g_dir[1] = n > 0.0 ? uy / n : 0.0;
 }
 
 int or_get_threads(void) {
@@ -165,10 +178,32 @@ void or_estab(int npoin, int nelem, const double* U, const double* T, const doub
         double dt2 = std::sqrt(dtx * dtx + dty * dty) + 1.0e-20;
         double dux = vel2 * DX[0] + vel2 * DX[1] + vel2 * DX[2];  // :380-383 (A-4)
         double duy = vel2 * DY[0] + vel2 * DY[1] + vel2 * DY[2];
+        if (g_estab_mode != CFD_ESTAB_REFERENCE) {
+            dux = 0.0;
+            duy = 0.0;
+        }
         double du2 = std::sqrt(dux * dux + duy * duy) + 1.0e-20;
         double rtx = dtx / dt2, rty = dty / dt2;
         double rjx = drx / dr2, rjy = dry / dr2;
         double rux = dux / du2, ruy = duy / du2;
+        if (g_estab_mode == CFD_ESTAB_REGULARIZED) {
+            // unit vectors that stay unit vectors but are continuous in the state: the
+            // gradient plus eps*scale*G_e along the freestream direction d, normalised;
+            // the "velocity gradient" direction (zero in exact arithmetic) is d itself
+            double ge = 0.0;
+            for (int i = 0; i < 3; ++i) ge += std::sqrt(DX[i] * DX[i] + DY[i] * DY[i]);
+            const double sr = g_estab_eps * rho_elem * ge;
+            const double st = g_estab_eps * ((T[n1] + T[n2] + T[n3]) / 3.0) * ge;
+            const double gx = drx + sr * g_dir[0], gy = dry + sr * g_dir[1];
+            const double hx = dtx + st * g_dir[0], hy = dty + st * g_dir[1];
+            const double gn = std::sqrt(gx * gx + gy * gy), hn = std::sqrt(hx * hx + hy * hy);
+            rjx = gx / gn;
+            rjy = gy / gn;
+            rtx = hx / hn;
+            rty = hy / hn;
+            rux = g_dir[0];
+            ruy = g_dir[1];
+        }
         double temp = (T[n1] + T[n2] + T[n3]) / 3.0;
         double c = std::sqrt(gm * FR * temp);
         const double smu = 110.0;
@@ -1152,6 +1187,10 @@ void or_case_destroy(or_case* c) { delete c; }
 // loop body ns2DComp.ALE.f90:140-280
 int or_case_step(or_case* c, int nsteps, cfd_step_report* rep) {
     const int N = c->npoin;
+    const int saved_mode = g_estab_mode;  // the case's mode for its steps only
+    const double saved_dir[2] = {g_dir[0], g_dir[1]};
+    g_estab_mode = c->p.estab_mode;
+    or_set_estab_dir(c->p.u_inf, c->p.v_inf);
     for (int s = 0; s < nsteps; ++s) {
         c->iter += 1;
         Clock t;
@@ -1190,6 +1229,9 @@ int or_case_step(or_case* c, int nsteps, cfd_step_report* rep) {
         }
         c->U.swap(c->U1);  // :277-281 (U = U1)
     }
+    g_estab_mode = saved_mode;
+    g_dir[0] = saved_dir[0];
+    g_dir[1] = saved_dir[1];
     if (rep) {
         std::memset(rep, 0, sizeof(*rep));
         rep->iter = c->iter;

@@ -30,6 +30,7 @@ extern "C" {
 #endif
 
 void or_set_threads(int n);
+void or_set_estab_mode(int mode);  /* CFD_ESTAB_* for the per-routine or_estab */
 int or_get_threads(void);
 
 void or_deriv(int npoin, int nelem, const double* X, const double* Y, const int* inpoel,

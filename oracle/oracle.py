@@ -23,6 +23,8 @@ _d, _i = C.c_double, C.c_int
 
 _SIG = {
     "or_set_threads": (None, [_i]),
+    "or_set_estab_mode": (None, [_i]),
+    "or_set_estab_eps": (None, [_d]),
     "or_get_threads": (_i, []),
     "or_deriv": (None, [_i, _i, _dp, _dp, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "or_masas": (None, [_i, _i, _dp, _ip, _dp]),

@@ -1,0 +1,98 @@
+"""The mixed-precision form (FP32 calcRHS/FUENTE/ESTAB/deltat/Laplacian values with
+compensated node sums; FP64 state update, areas, gcl and BiCG) against the FP64 oracle.
+
+Accuracy is measured under CFD_ESTAB_REGULARIZED: with the reference's ESTAB the step is
+discontinuous at round-off level (unit vectors of round-off gradients), so no two
+implementations that differ in rounding agree to better than ~1e-4 after one step
+(test_reference_estab_is_discontinuous shows it on the oracle alone)."""
+import numpy as np
+import pytest
+
+from conftest import perturbed_state, small_case
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL_STATE = 1.0e-6   # rel L2 per conserved variable vs the FP64 oracle
+REL_TOL_FORCE = 1.0e-3   # lift/drag (pressure force) relative error
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def state_errors(ug, uo):
+    """rel L2 per conserved variable; rho*v (zero in the freestream) is measured against
+    the momentum scale max(|rho*v|, |rho*u|) so that round-off-sized fields do not count."""
+    out = []
+    for q in range(4):
+        den = np.linalg.norm(uo[:, q])
+        if q == 2:
+            den = max(den, np.linalg.norm(uo[:, 1]))
+        out.append(float(np.linalg.norm(ug[:, q] - uo[:, q]) / den))
+    return out
+
+
+def run_mixed_vs_oracle(k, steps):
+    from cfd_gb300 import abi, solver
+    from oracle import oracle as O
+    g = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    o = O.OracleCase(k)
+    worst = [0.0] * 4
+    fg, fo = [], []
+    for s in range(steps):
+        rg, ro = g.step(1), o.step(1)
+        assert abs(rg.dtmin - ro.dtmin) <= 1e-6 * ro.dtmin
+        e = state_errors(g.state()["U"], o.state()["U"])
+        worst = [max(a, b) for a, b in zip(worst, e)]
+        fg.append((rg.fx[0], rg.fy[0]))
+        fo.append((ro.fx[0], ro.fy[0]))
+    g.close()
+    o.close()
+    fg, fo = np.array(fg), np.array(fo)
+    # lift/drag error over the run, against the largest force of the run
+    fworst = float(np.abs(fg - fo).max() / np.abs(fo).max())
+    return worst, fworst
+
+
+@pytest.mark.parametrize("which,scale,steps", [(1, 16, 20), (3, 32, 20), (2, 32, 20)])
+def test_mixed_matches_fp64_regularized(gpu_lib, which, scale, steps):
+    k = small_case(which, scale=scale, seed=21, estab_mode=2)
+    # coarse meshes need FSAFE 0.25 (deltat has no acoustic limit; the reference's own
+    # step diverges at 0.5 on these sizes)
+    k.params.fsafe = min(k.params.fsafe, 0.25)
+    worst, fworst = run_mixed_vs_oracle(k, steps)
+    print("worst rel L2 per variable", worst, "force", fworst)
+    assert max(worst) <= REL_TOL_STATE
+    assert fworst <= REL_TOL_FORCE
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_fp64_estab_modes_bit_exact(gpu_lib, mode):
+    from test_gpu_parity import run_pair
+    k = small_case(3, scale=20, seed=5, estab_mode=mode)
+    run_pair(k, 3)
+
+
+def test_mixed_deterministic(gpu_lib):
+    from cfd_gb300 import abi, solver
+    k = small_case(3, scale=32, seed=2, estab_mode=2)
+    a = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    b = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    a.step(5)
+    b.step(5)
+    assert np.array_equal(a.state()["U"], b.state()["U"])
+    assert np.array_equal(a.state()["X"], b.state()["X"])
+
+
+def test_mixed_from_perturbed_state(gpu_lib):
+    from cfd_gb300 import abi, solver
+    from oracle import oracle as O
+    k = small_case(3, scale=32, seed=4, estab_mode=2)
+    U, T, u, v = perturbed_state(k, seed=3, amp=0.05)
+    g = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    o = O.OracleCase(k)
+    for side in (g, o):
+        side.set_state(U, T, u, v)
+    g.step(3)
+    o.step(3)
+    assert max(state_errors(g.state()["U"], o.state()["U"])) <= REL_TOL_STATE

@@ -254,3 +254,36 @@ def test_driver_heave_moves_body_rigidly(oracle):
     assert dy[0] == pytest.approx(0.2 * math.sin(2 * math.pi * 0.2 * rep.time), rel=1e-9)
     np.testing.assert_array_equal(st["Y"][k.ifm - 1], x0["Y"][k.ifm - 1])
     assert np.all(np.isfinite(st["U"]))
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_reference_estab_is_discontinuous(oracle):
+    """The reference ESTAB makes the step discontinuous at round-off level: unit vectors
+    of round-off gradients (subrutinas.f90:374-393).  A 1e-13 perturbation comes back
+    ~1e-4; under CFD_ESTAB_REGULARIZED the response is proportional."""
+    k = small_case(3, scale=96, seed=0, estab_mode=0)
+    k.params.fsafe = 0.25
+    a, b = oracle.OracleCase(k), oracle.OracleCase(k)
+    a.step(1)
+    b.step(1)
+    st, f = a.state(), a.fields()
+    rng = np.random.default_rng(0)
+    b.set_state(st["U"] * (1 + 1e-13 * rng.uniform(-1, 1, st["U"].shape)), st["T"], f["VEL_X"],
+                f["VEL_Y"])
+    a.step(1)
+    b.step(1)
+    d = _rel(b.state()["U"][:, 0], a.state()["U"][:, 0])
+    assert d > 1e-9, "the reference ESTAB should amplify a 1e-13 perturbation"
+    k.params.estab_mode = 2
+    a, b = oracle.OracleCase(k), oracle.OracleCase(k)
+    a.step(1)
+    b.step(1)
+    st, f = a.state(), a.fields()
+    b.set_state(st["U"] * (1 + 1e-13 * rng.uniform(-1, 1, st["U"].shape)), st["T"], f["VEL_X"],
+                f["VEL_Y"])
+    a.step(1)
+    b.step(1)
+    assert _rel(b.state()["U"][:, 0], a.state()["U"][:, 0]) < 1e-10
