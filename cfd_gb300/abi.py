@@ -110,6 +110,10 @@ SIGNATURES = {
                            C.POINTER(CfdSolveInfo)]),
     "cfd_bicg_ex": (C.c_int, [_dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _ip, C.c_double,
                               C.c_int, C.POINTER(CfdSolveInfo)]),
+    "cfd_bicg_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.c_double, C.c_int, C.c_void_p,
+                                          C.POINTER(CfdSolveInfo)]),
     "cfd_ctx_create": (C.c_int, [C.POINTER(_P), C.POINTER(CfdMesh), C.POINTER(CfdParams),
                                  C.c_int]),
     "cfd_ctx_destroy": (None, [_P]),

@@ -25,6 +25,7 @@ UNITS = [
     ("kernels_pcg_mixed.cu", []),
     ("context.cu", ["--fmad=false"]),
     ("abi.cu", ["--fmad=false"]),
+    ("noalloc.cu", ["--fmad=false"]),
     ("host_prep.cpp", []),
 ]
 

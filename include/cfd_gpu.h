@@ -216,6 +216,27 @@ int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr,
                 const int* x_fixIdx, const int* npoin, const int* nfix,
                 double tol, int maxit, cfd_solve_info* info);
 
+/* BiCG on arrays already in device memory, with no device allocation.  This entry has no
+ * counterpart in the reference: it is for callers that cannot call cudaMalloc where they
+ * solve (a host that owns all device memory itself, e.g. CUDA Fortran/OpenACC arrays or
+ * a framework pool with a fixed budget, or a time loop that must not allocate).  Work
+ * vectors live in one static device array of the library, reserved on every GPU that
+ * loads it until the process exits, which caps npoin at CFD_NOALLOC_MAX_NPOIN
+ * (about 2.5 MiB of device memory).
+ * All pointers are DEVICE pointers: CSR with 0-based col/rowptr (diagonal entries as in
+ * lap_*), isfix[npoin] nonzero on Dirichlet rows, x = initial guess that already holds the
+ * Dirichlet values on those rows (the reference's copy1), b may be NULL (zero).  Same
+ * arithmetic and result as cfd_bicg_ex.  Runs on `stream` (cudaStream_t, NULL = default)
+ * and waits for it before returning.  The first call on a device looks up the array's
+ * device address (call it once before any stream capture).  Every call shares the one
+ * array: calls that overlap on the GPU (other streams or threads) race.  npoin above the
+ * cap returns CFD_ERR_LIMIT. */
+#define CFD_NOALLOC_MAX_NPOIN 65536
+int cfd_bicg_device_noalloc(const double* spMtx, const int* col, const int* rowptr,
+                            const double* diag, const unsigned char* isfix, double* x,
+                            const double* b, int npoin, double tol, int maxit, void* stream,
+                            cfd_solve_info* info);
+
 /* ---------------------------------------------------------------- resident context */
 
 /* Builds adjacency, BC tables, the Laplacian pattern and every device buffer.
