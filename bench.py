@@ -160,29 +160,38 @@ def config_dict(k, args, ws):
 # or written once (gathers of node data count once per node).  N nodes, E elements, and
 # 3E element-around-point slots (~6 per node).
 def algorithmic_bytes(k, iters, precision):
+    """Algorithmic DRAM bytes per STEP of each timed group: every array element the group
+    must read or write once (gathered node/element values counted once)."""
     N, E = k.npoin, k.nelem
-    nnz = 7 * N
+    S = 3 * E          # (element, local node) slots
+    nnz = 7 * N        # mesh-Laplacian entries (structured triangulation)
+    it = float(iters)
+    # BiCG: initial residual (both right-hand sides), then per iteration two passes over
+    # the vectors and one FP32 SpMV per right-hand side
+    bicg = nnz * 8 + N * 45 + it * (N * 234 + nnz * 16) + (N * 56 + nnz * 16 if it > 0 else 0)
     if precision == "mixed":
+        # node pass of one RK stage: recVisc 16 + slot id 4 B/slot, element mu/lambda 8 B/E;
+        # slot pointers 4, stage-invariant sums 16, 1/M 4, BC flags 1, U hi 16, T 4 B/N
+        node_common = S * (16 + 4) + E * 8 + N * (4 + 16 + 4 + 1 + 16 + 4)
         return {
-            # elem 16 + slot_pos 12 + geo 48 + area 8 + shoc/tau 16 B/E, records 96 B/E;
-            # U 32 + W 16 B/N
-            "calcrhs_t": E * (16 + 12 + 48 + 8 + 16 + 96) + N * (32 + 16),
-            # ptr 4 + slots 12*... : 3E slot ids (4 B) and records (32 B), elem 16 B/E,
-            # T 8, U 32, 1/M 8, flags 1 B/N; writes U1 32 + 6 primitives 48 B/N
-            "update_t": 3 * E * (4 + 32) + E * 16 + N * (4 + 8 + 32 + 8 + 1 + 32 + 48),
-            "estab_t": E * (16 + 48 + 16) + N * (8 + 8 + 32 + 16),
-            "deltat_t": E * (16 + 8) + N * 40,
-            "laplace_t": 3 * E * (4 + 4) + E * (16 + 48) + N * 16 + nnz * 12 + N * 24,
-            "masas_t": E * (16 + 48 + 16 + 16) + N * 32 + 3 * E * 4 + N * 24,
-            "deriv_t": E * (16 + 8 + 48) + N * 16,
-            "grad_t": (nnz * 12 + N * 4) * (2 + iters) + N * 8 * 10 * (2 + iters),
+            # elem 16, slot_pos 12, geo 32, shoc/tau 16 B/E; recInv + recVisc 96 B/E;
+            # mu/lambda 8 B/E; U hi/lo 32 + W 8 + T 4 B/N
+            "calcrhs_t": E * (16 + 12 + 32 + 16 + 96 + 8) + N * 44,
+            # stage 1 adds recInv (16 B/slot); stage 4 adds U 32, U1 32, six primitives 24,
+            # U hi/lo 32 B/N; stages 2-4 recompute mu/lambda (elem 16 + 8 B/E, T 4 B/N)
+            "update_t": 4 * node_common + S * 16 + N * 120 + 3 * (E * 24 + N * 4),
+            "estab_t": E * (16 + 32 + 16) + N * 52,
+            "deltat_t": E * 20 + N * 20,
+            "deriv_t": E * (16 + 32 + 4 + 8 + 8) + N * 32,
+            "laplace_t": S * 8 + E * 40 + N * 52 + nnz * 4,
+            "grad_t": bicg,
         }
     return {
-        "calcrhs_t": E * (16 + 48 + 8 + 8 + 24 + 96) + N * 40 + (E * 96 + N * 16) / 4.0,
-        "update_t": N * (24 + 2 * 6 * 32 + 32 + 8 + 32 + 56),
+        "calcrhs_t": 4 * (E * (16 + 48 + 8 + 8 + 24 + 96) + N * 40) + E * 96 + N * 16,
+        "update_t": 4 * N * (24 + 2 * 6 * 32 + 32 + 8 + 32 + 56),
         "estab_t": E * (16 + 48 + 32) + N * (32 + 8 + 32),
         "deltat_t": E * (16 + 8 + 8) + N * 40,
-        "grad_t": (nnz * 12 + N * 4) * (2 + iters) + N * 8 * 10 * (2 + iters),
+        "grad_t": bicg,
     }
 
 
@@ -335,12 +344,13 @@ def main_ours(args):
     rep2 = S2.step(KT)
     t_after = S2.timers()
     S2.close()
-    per_step, per_launch = {}, {}
+    per_step, per_launch, calls_per_step = {}, {}, {}
     for n_, (sec, calls) in t_after.items():
         ds, dc = sec - t_before[n_][0], calls - t_before[n_][1]
         if dc > 0:
             per_step[n_] = ds / KT
             per_launch[n_] = ds / dc
+            calls_per_step[n_] = dc / KT
     iters = float(np.mean(list(rep2.bicg_iters)))
     ab = algorithmic_bytes(k, iters, args.precision)
     total = sum(per_step.values())
@@ -348,15 +358,16 @@ def main_ours(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    ach = ab[dom] / per_launch[dom] / 1e9 if dom in ab else None
+    ach = ab[dom] / per_step[dom] / 1e9 if dom in ab else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                 "frac": (ach / hbm_peak) if ach else None, "traffic": None,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
                 "share_of_step": per_step[dom] / total if total else None,
                 "launch_ms": per_launch[dom] * 1e3,
-                "algorithmic_bytes_per_launch": ab.get(dom)}
-    kernels = {n_: {"ms_per_launch": per_launch[n_] * 1e3,
-                    "GBps_algorithmic": (ab[n_] / per_launch[n_] / 1e9) if n_ in ab else None}
+                "launches_per_step": calls_per_step[dom],
+                "algorithmic_bytes_per_launch": (ab[dom] / calls_per_step[dom]) if dom in ab else None}
+    kernels = {n_: {"ms_per_launch": per_launch[n_] * 1e3, "launches_per_step": calls_per_step[n_],
+                    "GBps_algorithmic": (ab[n_] / per_step[n_] / 1e9) if n_ in ab else None}
                for n_ in per_launch}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -233,6 +233,8 @@ int cfd_ctx_upload_state(cfd_ctx* ctx, const double* U, const double* T, const d
         for (size_t i = 0; i < N; ++i) v[i] = U[4 * i + 2] / U[4 * i];
         CFD_CUDA(cudaMemcpyAsync(c.d_VY, v.data(), 8 * N, cudaMemcpyHostToDevice, c.stream));
     }
+    if (c.prec == CFD_PREC_MIXED)
+        TRY(c.narrow_mixed(U != nullptr, T != nullptr, VEL_X || U, VEL_Y || U, false, false));
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     return CFD_OK;
 }
@@ -248,6 +250,13 @@ int cfd_ctx_upload_mesh(cfd_ctx* ctx, const double* X, const double* Y, const do
     if (W_Y) CFD_CUDA(cudaMemcpyAsync(c.d_WY, W_Y, n8, cudaMemcpyHostToDevice, c.stream));
     if (xpos) CFD_CUDA(cudaMemcpyAsync(c.d_pos[0], xpos, n8, cudaMemcpyHostToDevice, c.stream));
     if (ypos) CFD_CUDA(cudaMemcpyAsync(c.d_pos[1], ypos, n8, cudaMemcpyHostToDevice, c.stream));
+    if (c.prec == CFD_PREC_MIXED)
+        for (int k = 0; k < 2; ++k)
+            if (k == 0 ? xpos != nullptr : ypos != nullptr)
+                CFD_LAUNCH(k_narrow, blocks_for(c.npoin, 256), 256, 0, c.stream, (long)c.npoin,
+                           (const double*)c.d_pos[k], c.d_posf[k]);
+    if (c.prec == CFD_PREC_MIXED && (X || Y || W_X || W_Y))
+        TRY(c.narrow_mixed(false, false, false, false, X || Y, W_X || W_Y));
     if (X || Y) TRY(c.prec == CFD_PREC_MIXED ? c.geometry_mixed(true) : c.geometry(true, true));
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     return c.tcollect();
@@ -281,6 +290,7 @@ int cfd_ctx_download_state(cfd_ctx* ctx, double* U, double* T, double* X, double
     if (!ctx) return arg_error("ctx");
     Ctx& c = ctx->impl;
     const size_t N = c.npoin;
+    if (T && c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed());
     if (U) CFD_CUDA(cudaMemcpyAsync(U, c.d_U, 32 * N, cudaMemcpyDeviceToHost, c.stream));
     if (T) CFD_CUDA(cudaMemcpyAsync(T, c.d_T, 8 * N, cudaMemcpyDeviceToHost, c.stream));
     if (X) CFD_CUDA(cudaMemcpyAsync(X, c.d_X, 8 * N, cudaMemcpyDeviceToHost, c.stream));
@@ -294,6 +304,7 @@ int cfd_ctx_download_fields(cfd_ctx* ctx, double* RHO, double* VEL_X, double* VE
     if (!ctx) return arg_error("ctx");
     Ctx& c = ctx->impl;
     const size_t n8 = 8 * (size_t)c.npoin;
+    if (c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed());
     const double* src[8] = {c.d_RHO, c.d_VX, c.d_VY, c.d_E, c.d_P, c.d_RMACH, c.d_WX, c.d_WY};
     double* dst[8] = {RHO, VEL_X, VEL_Y, E, P, RMACH, W_X, W_Y};
     for (int i = 0; i < 8; ++i)
@@ -316,6 +327,7 @@ int cfd_ctx_download_geometry(cfd_ctx* ctx, double* area, double* dNx, double* d
     if (!ctx) return arg_error("ctx");
     Ctx& c = ctx->impl;
     const size_t E = c.nelem;
+    if ((dNx || dNy || area) && c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed());
     if (area) CFD_CUDA(cudaMemcpyAsync(area, c.d_area, 8 * E, cudaMemcpyDeviceToHost, c.stream));
     if (M) CFD_CUDA(cudaMemcpyAsync(M, c.d_M, 8 * (size_t)c.npoin, cudaMemcpyDeviceToHost, c.stream));
     std::vector<double> g;

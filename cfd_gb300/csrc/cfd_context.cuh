@@ -29,7 +29,7 @@ struct Ctx {
     double time = 0.0, last_dtmin = 0.0;
     double disn[2] = {0.0, 0.0};
     // sizes
-    int nwn = 0, nnmove = 0, nufix = 0, pcg_grid = 1;
+    int nwn = 0, nnmove = 0, nufix = 0, pcg_grid = 1, nsm = 1;
     // mesh
     int4* d_elem = nullptr;
     double *d_X = nullptr, *d_Y = nullptr;
@@ -56,18 +56,33 @@ struct Ctx {
            *d_DTL = nullptr;
     double *d_SHOC = nullptr, *d_TS1 = nullptr, *d_TS2 = nullptr, *d_TS3 = nullptr;
     double *d_contrib = nullptr, *d_contribF = nullptr;
-    // mixed precision
-    double *d_T2 = nullptr, *d_invM = nullptr, *d_invdiag = nullptr;
+    // mixed precision: float shadows (FP64 arrays above are widened from them on download)
+    float4 *d_Uhi = nullptr, *d_Ulo = nullptr;  // U = hi + lo
+    float2 *d_Xhi = nullptr, *d_Xlo = nullptr;  // (X, Y) = hi + lo
+    float2 *d_Wf = nullptr, *d_Wof = nullptr;   // W and the gcl's previous W
+    float* d_Tf = nullptr;                      // T
+    float2* d_mulam = nullptr;                  // per element: mu, lambda of the RK stage
+    float *d_VXf = nullptr, *d_VYf = nullptr, *d_RHOf = nullptr, *d_Ef = nullptr, *d_Pf = nullptr,
+          *d_RMACHf = nullptr;
+    float *d_invMf = nullptr, *d_areaf = nullptr, *d_areaf_old = nullptr;
+    float4* d_geo8 = nullptr;  // per element: dNx(1:3), dNy(1:3), area, Laplacian weight
+    unsigned long long* d_blockmin = nullptr;  // per-block FP32 DTELEM minima
+    double* d_invdiag = nullptr;
     float *d_shocf = nullptr, *d_ts1f = nullptr, *d_ts2f = nullptr, *d_ts3f = nullptr;
     float* d_valf = nullptr;
     float* d_pf[2][2] = {};
     float* d_zf[2] = {};
+    float* d_posf[2] = {};  // (float) of d_pos, kept by the mixed BiCG kernels
+    double* d_part_r = nullptr;  // per-block partials of the mixed BiCG row kernels
+    double* d_bscal = nullptr;   // [2][4] first-direction scalars of the mixed BiCG
+    unsigned* d_bcount = nullptr;
+    float* d_invdiagf = nullptr;
     int* d_slot_pos = nullptr;
-    void* d_rec = nullptr;
-    double2* d_gterms = nullptr;
+    float4 *d_recInv = nullptr, *d_recVisc = nullptr;  // slot records, element-around-point order
+    float4* d_invSum = nullptr;                         // per node: sum of the recInv slots
+    float2* d_gterms = nullptr;
     double estab_eps = 1.0e-3;  // CFD_ESTAB_REGULARIZED relative gradient scale
     double dir[2] = {1.0, 0.0};  // CFD_ESTAB_REGULARIZED freestream direction
-    bool laplace_fp64 = false;  // mixed form: Laplacian values in FP64 arithmetic
     // mesh motion
     double* d_pos[2] = {nullptr, nullptr};  // xpos, ypos (guess in, solution out)
     double* d_xfix[2] = {nullptr, nullptr};
@@ -91,7 +106,9 @@ struct Ctx {
     ~Ctx();
     int create(const cfd_mesh* m, const cfd_params* p, int precision_mode);
     int geometry(bool masas, bool with_laplace);
-    int geometry_mixed(bool setup);
+    int geometry_mixed(bool setup, bool put_area = false);
+    int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
+    int widen_mixed();
     int run_pcg(int nsolve);
     int step_once();
     int step_once_mixed();

@@ -18,6 +18,9 @@ struct StepScal {
     int bandera;
     int pad;
     double fx[10], fy[10], rm[10];  // FORCES per set
+    double inv_dtmin;               // 1/DTMIN (mixed form: W = XPOS*(1/DTMIN))
+    float dtmin_f;                  // (float)DTMIN for the FP32 kernels
+    float pad_f;
 };
 
 // calcRHS.f90:5 imports: Cv => FCV, lambda_ref => FK, mu_ref => FMU, gamma0 => GAMA, T_inf, CTE
@@ -26,50 +29,72 @@ struct GasConst {
     double fr;  // FR (perfect-gas constant), used by the mixed node kernel
 };
 
+// the same constants rounded to FP32 once on the host (the FP32 kernels would otherwise
+// convert them per thread, on the FP64 pipe)
+struct GasConstF {
+    float cv, lambda_ref, mu_ref, gamma, t_inf, cte, fr;
+};
+inline GasConstF to_float(const GasConst& g) {
+    return GasConstF{(float)g.cv, (float)g.lambda_ref, (float)g.mu_ref, (float)g.gamma,
+                     (float)g.t_inf, (float)g.cte, (float)g.fr};
+}
+
 // ------------------------------------------------------------------ mixed precision
-__global__ void k_deltat_mixed(int nelem, const int4* elem, const double* T, const double* VX,
-                               const double* VY, const double* WX, const double* WY,
-                               const double* area, float fsafe, float t_inf,
-                               unsigned long long* dtmin_bits);
-__global__ void k_deltat_refine(int nelem, const int4* elem, const double* T, const double* VX,
-                                const double* VY, const double* WX, const double* WY,
-                                const double* area, float fsafe, float t_inf, StepScal* sc);
-__global__ void k_estab_mixed(int nelem, const int4* elem, const double* U, const double* T,
-                              float gm, const double* VX, const double* VY, const double* WX,
-                              const double* WY, const double* geo, float FR, const StepScal* sc,
+__global__ void k_narrow_state(int npoin, const double* U, const double* T, const double* VX,
+                               const double* VY, const double* X, const double* Y,
+                               const double* WX, const double* WY, float4* Uhi, float4* Ulo,
+                               float* Tf, float* VXf, float* VYf, float2* Xhi, float2* Xlo,
+                               float2* Wf);
+__global__ void k_widen(long n, const float* a, double* b);
+__global__ void k_narrow(long n, const double* a, float* b);
+__global__ void k_deltat_mixed(int nelem, const int4* elem, const float* T, const float* VX,
+                               const float* VY, const float2* W, const float* areaf, float fsafe,
+                               float t_inf, unsigned long long* dtmin_bits,
+                               unsigned long long* block_min);
+__global__ void k_deltat_refine(int nelem, const int4* elem, const float* T, const float* VX,
+                                const float* VY, const float2* W, const float* areaf,
+                                const unsigned long long* block_min, int nchunk, float fsafe,
+                                float t_inf, StepScal* sc);
+__global__ void k_estab_mixed(int nelem, const int4* elem, const float4* Uhi, const float4* Ulo,
+                              const float* T, float gm, const float* VX, const float* VY,
+                              const float2* W, const float4* geo, float FR, const StepScal* sc,
                               float RHOINF, float TINF, int estab_mode, float eps_dir,
                               float dirx, float diry, float* SHOC, float* TS1, float* TS2,
                               float* TS3);
 cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, const int4* elem,
-                                     const double* U, const double* geo, const double* area,
-                                     const float* shoc, const double* dtl_arr,
-                                     const double* dtl_scalar, const float* ts1, const float* ts2,
-                                     const float* ts3, GasConst gc, const double* WX,
-                                     const double* WY, const int* slot_pos, void* rec);
+                                     const float4* Uhi, const float4* Ulo, const float4* geo,
+                                     const float* shoc, const StepScal* sc,
+                                     const float* ts1, const float* ts2, const float* ts3,
+                                     GasConstF gc, const float2* W, const int* slot_pos,
+                                     const float* T, float4* recInv, float4* recVisc,
+                                     float2* mulam);
+__global__ void k_elem_mulam(int nelem, const int4* elem, const float* T, GasConstF gc,
+                             float2* mulam);
 cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, const int* esup_slot,
-                              const int4* elem, const void* rec, const double* T, GasConst gc,
-                              int viscous, const double* U, const double* invM, double rk_fact,
+                              const float2* mulam, const float4* recInv, const float4* recVisc,
+                              float4* invSum, int first_stage, GasConst gc, GasConstF gf,
+                              int viscous, const double* U, float4* Uhi, float4* Ulo,
+                              const float* invM, float rk_fact, int last_stage,
                               const unsigned char* bcflag, const double* bcval, const double2* nrm,
-                              const double* WX, const double* WY, double* U1, double* RHO,
-                              double* VX, double* VY, double* E, double* P, double* To,
-                              double* RMACH);
-size_t slot_record_bytes();
-__global__ void k_deriv_mixed(int nelem, const int4* elem, const double* X, const double* Y,
-                              double* area, double* geo);
-__global__ void k_gcl_elem(int nelem, const int4* elem, const double* geo, const double* area,
-                           const double* area_old, const double* Wx, const double* Wy,
-                           const double* Wxo, const double* Wyo, int literal, double2* terms);
-__global__ void k_mass_mixed(int npoin, const int* esup_ptr, const int* esup_slot,
-                             const double* area, const double2* terms, const double* dtp, int gcl,
-                             double* M, double* invM);
-cudaError_t launch_laplace_mixed(bool fp64, cudaStream_t st, int npoin, int nelem, const int4* elem,
-                                 const int* esup_ptr, const int* esup_slot, const uchar4* lap_pos,
-                                 const double* geo, const double* X, const double* Y,
-                                 const int* rowptr, float* valf, double* vals, double* diag,
-                                 double* invdiag);
+                              const double* WX, const double* WY, double* U1, float* RHO,
+                              float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH);
+__global__ void k_elem_geometry(int nelem, const int4* elem, const float2* Xhi, const float2* Xlo,
+                                int gcl, int literal, const float2* W, const float2* Wold,
+                                int put_area, float* area_old, float* areaf, float4* geo,
+                                float2* terms);
+constexpr int kGeoNodeBlock = 128;  // block size of k_node_geometry
+__global__ void k_node_geometry(int npoin, const int* esup_ptr, const int* esup_slot,
+                                const uchar4* lap_pos, const float4* geo, const float2* terms,
+                                const double* dtp, int gcl, const int* rowptr, float* valf,
+                                double* invdiag, float* invdiagf, double* M, float* invM,
+                                const float2* W, float2* Wold);
+__global__ void k_widen_geo(int nelem, const float4* geo, double* dN, double* area);
 __global__ void k_forces_tree(int nset_numb, const int* set_ptr, const int2* set_edges,
-                              const double* P, const double* X, const double* Y,
+                              const float* P, const double* X, const double* Y,
                               const double* xref, const double* yref, StepScal* sc);
+__global__ void k_motion_update_mixed(int npoin, const double* xpos, const double* ypos,
+                                      const StepScal* sc, double* X, double* Y, double* WX,
+                                      double* WY, float2* Xhi, float2* Xlo, float2* Wf);
 
 #define ELEM_RHS_ARGS                                                                    \
     int, const int4* __restrict__, const double* __restrict__, const double* __restrict__, \
@@ -160,6 +185,12 @@ struct PcgArgs {
     const double* invdiag;
     float* pf[2][2];
     float* zf[2];
+    float* xf[2];                // (float)x, kept equal to it on entry and exit
+    const float* invdiagf;       // (float)(1/diag), with invdiag = (double)invdiagf
+    double* part_r;              // [4][nblk_r] per-block partials of the row kernels
+    long nblk_r;                 // 256-row blocks of the row kernels
+    double* bscal;               // [2 solves][4]: r.r, r.p, p.y, alfa of the first direction
+    unsigned* bcount;            // [2] block counters of the row kernels (zero between uses)
     GridBar* bar;
     double tol;
     int maxit;
@@ -170,5 +201,8 @@ struct PcgArgs {
 
 __global__ void k_pcg_fp64(PcgArgs a);
 __global__ void k_pcg_mixed(PcgArgs a);
+__global__ void k_bicg_fix_mixed(PcgArgs a);
+__global__ void k_bicg_resid_mixed(PcgArgs a);
+__global__ void k_bicg_dir_mixed(PcgArgs a);
 
 }  // namespace cfd

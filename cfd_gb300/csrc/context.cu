@@ -2,6 +2,7 @@
 // of ns2DComp.ALE.f90:140-280 as a sequence of sm_103a kernels on one stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -151,7 +152,17 @@ int Ctx::run_pcg(int nsolve) {
             a.pf[s][0] = d_pf[s][0];
             a.pf[s][1] = d_pf[s][1];
             a.zf[s] = d_zf[s];
+            a.xf[s] = d_posf[s];
         }
+        a.invdiagf = d_invdiagf;
+        a.part_r = d_part_r;
+        a.nblk_r = blocks_for(npoin, 256);
+        a.bscal = d_bscal;
+        a.bcount = d_bcount;
+        if (nufix > 0)
+            CFD_LAUNCH(k_bicg_fix_mixed, blocks_for(nufix, 256), 256, 0, stream, a);
+        CFD_LAUNCH(k_bicg_resid_mixed, (unsigned)a.nblk_r, 256, 0, stream, a);
+        CFD_LAUNCH(k_bicg_dir_mixed, (unsigned)a.nblk_r, 256, 0, stream, a);
     }
     CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
     void* args[] = {&a};
@@ -347,7 +358,6 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         dir[0] = n > 0.0 ? prm.u_inf / n : 1.0;
         dir[1] = n > 0.0 ? prm.v_inf / n : 0.0;
     }
-    if (getenv("CFD_MIXED_LAPLACE_FP64")) laplace_fp64 = atoi(getenv("CFD_MIXED_LAPLACE_FP64")) != 0;
     CFD_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CFD_CUDA(cudaEventCreateWithFlags(&ev_scal, cudaEventDisableTiming));
     CFD_CUDA(cudaMallocHost((void**)&h_scal, sizeof(StepScal)));
@@ -431,7 +441,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     CFD_CUDA(cudaMemcpyAsync(d_scal, h_scal, sizeof(StepScal), cudaMemcpyHostToDevice, stream));
     CFD_CUDA(cudaStreamSynchronize(stream));
     // persistent BiCG grid: co-resident blocks only
-    int dev = 0, nsm = 0, per_sm = 0;
+    int dev = 0, per_sm = 0;
     CFD_CUDA(cudaGetDevice(&dev));
     CFD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     CFD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -464,35 +474,80 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
             set_last_message("the mixed-precision form runs with a global time step (ITLOCAL = 0)");
             return CFD_ERR_ARG;
         }
-        for (double** q : {&d_T2, &d_invM, &d_invdiag})
+        if ((st = dalloc(&d_invdiag, N))) return st;
+        for (float** q : {&d_Tf, &d_VXf, &d_VYf, &d_RHOf, &d_Ef, &d_Pf, &d_RMACHf,
+                          &d_invMf})
             if ((st = dalloc(q, N))) return st;
-        for (float** q : {&d_shocf, &d_ts1f, &d_ts2f, &d_ts3f})
+        for (float2** q : {&d_Xhi, &d_Xlo, &d_Wf, &d_Wof})
+            if ((st = dalloc(q, N))) return st;
+        for (float4** q : {&d_Uhi, &d_Ulo})
+            if ((st = dalloc(q, N))) return st;
+        for (float** q : {&d_shocf, &d_ts1f, &d_ts2f, &d_ts3f, &d_areaf, &d_areaf_old})
             if ((st = dalloc(q, E))) return st;
-        for (int s = 0; s < 2; ++s)
-            for (float** q : {&d_pf[s][0], &d_pf[s][1], &d_zf[s]})
+        if ((st = dalloc(&d_blockmin, blocks_for(E, 256)))) return st;
+        if ((st = dalloc(&d_geo8, 2 * (size_t)E))) return st;
+        if ((st = dalloc(&d_mulam, E))) return st;
+        for (float* q : {d_RHOf, d_Ef, d_Pf, d_RMACHf})
+            CFD_CUDA(cudaMemsetAsync(q, 0, sizeof(float) * N, stream));
+        CFD_CUDA(cudaMemsetAsync(d_Wof, 0, sizeof(float2) * N, stream));
+        for (int s = 0; s < 2; ++s) {
+            for (float** q : {&d_pf[s][0], &d_pf[s][1], &d_zf[s], &d_posf[s]})
                 if ((st = dalloc(q, N))) return st;
+            CFD_CUDA(cudaMemsetAsync(d_posf[s], 0, sizeof(float) * N, stream));
+        }
+        if ((st = dalloc(&d_part_r, 4 * (size_t)blocks_for(N, 256)))) return st;
+        if ((st = dalloc(&d_bscal, 8))) return st;
+        if ((st = dalloc(&d_bcount, 2))) return st;
+        if ((st = dalloc(&d_invdiagf, N))) return st;
+        CFD_CUDA(cudaMemsetAsync(d_bscal, 0, 8 * sizeof(double), stream));
+        CFD_CUDA(cudaMemsetAsync(d_bcount, 0, 2 * sizeof(unsigned), stream));
         if ((st = dalloc(&d_valf, adj.col.size()))) return st;
         if ((st = dalloc(&d_gterms, E))) return st;
         // slot (e, i) -> its position in element-around-point order
         std::vector<int> pos(3 * (size_t)E);
         for (size_t s = 0; s < adj.esup_slot.size(); ++s) pos[adj.esup_slot[s]] = (int)s;
         if ((st = upload(&d_slot_pos, pos.data(), pos.size()))) return st;
-        char* rec = nullptr;
-        if ((st = dalloc(&rec, slot_record_bytes() * 3 * (size_t)E))) return st;
-        d_rec = rec;
+        if ((st = dalloc(&d_recInv, 3 * (size_t)E))) return st;
+        if ((st = dalloc(&d_recVisc, 3 * (size_t)E))) return st;
+        if ((st = dalloc(&d_invSum, N))) return st;
+        if ((st = narrow_mixed(true, true, true, true, true, true))) return st;
     }
     // setup geometry: NORMALES, DERIV, MASAS, laplace (ns2DComp.ALE.f90:88-100)
-    st = (prec == CFD_PREC_MIXED) ? geometry_mixed(true) : geometry(true, true);
+    st = (prec == CFD_PREC_MIXED) ? geometry_mixed(true, true) : geometry(true, true);
     if (st) return st;
-    CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
+    if (prec != CFD_PREC_MIXED)
+        CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
     CFD_CUDA(cudaStreamSynchronize(stream));
     return tcollect();
 }
 
 // ------------------------------------------------------------------ mixed precision
-// Geometry of the current mesh for the mixed form: normales, deriv (FP64 areas), the
-// lumped mass (MASAS at setup; MASAS or gcl per step) with 1/M, FP32 Laplacian values.
-int Ctx::geometry_mixed(bool setup) {
+// FP64 arrays -> float shadows, for the arrays the caller replaced (uploads, setup)
+int Ctx::narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W) {
+    const int N = npoin;
+    CFD_LAUNCH(k_narrow_state, blocks_for(N, 256), 256, 0, stream, N, U ? d_U : nullptr,
+               T ? d_T : nullptr, VX ? d_VX : nullptr, VY ? d_VY : nullptr, XY ? d_X : nullptr,
+               XY ? d_Y : nullptr, W ? d_WX : nullptr, W ? d_WY : nullptr, d_Uhi, d_Ulo, d_Tf,
+               d_VXf, d_VYf, d_Xhi, d_Xlo, d_Wf);
+    return CFD_OK;
+}
+
+// float fields -> the FP64 arrays the download entries read
+int Ctx::widen_mixed() {
+    const long N = npoin, E = nelem;
+    const float* src[7] = {d_Tf, d_VXf, d_VYf, d_RHOf, d_Ef, d_Pf, d_RMACHf};
+    double* dst[7] = {d_T, d_VX, d_VY, d_RHO, d_E, d_P, d_RMACH};
+    for (int i = 0; i < 7; ++i)
+        CFD_LAUNCH(k_widen, blocks_for(N, 256), 256, 0, stream, N, src[i], dst[i]);
+    CFD_LAUNCH(k_widen_geo, blocks_for(E, 256), 256, 0, stream, (int)E, (const float4*)d_geo8, d_geo,
+               d_area);
+    return CFD_OK;
+}
+
+// Geometry of the current mesh for the mixed form: normales, then one element pass
+// (deriv, Laplacian weights, gcl element terms, putArea) and one node pass (Laplacian rows,
+// 1/diag, MASAS at setup or per step, or the gcl mass update and putW).
+int Ctx::geometry_mixed(bool setup, bool put_area) {
     const int N = npoin, E = nelem;
     const int TB = 256;
     tstart(TM_NORMALES);
@@ -500,27 +555,16 @@ int Ctx::geometry_mixed(bool setup) {
         CFD_LAUNCH(k_normales, blocks_for(nwn, TB), TB, 0, stream, nwn, d_wnode, d_wptr, d_wedge,
                    d_walls, d_X, d_Y, d_bcflag, d_nrm);
     tstop(TM_NORMALES);
-    tstart(TM_DERIV);
-    CFD_LAUNCH(k_deriv_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_X, d_Y, d_area, d_geo);
-    tstop(TM_DERIV);
-    tstart(TM_MASAS);
     const bool gcl = !setup && prm.mass_mode != CFD_MASS_MASAS;
-    if (gcl) {
-        CFD_LAUNCH(k_gcl_elem, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_geo, d_area, d_area_old,
-                   d_WX, d_WY, d_Wxo, d_Wyo, prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_gterms);
-    }
-    CFD_LAUNCH(k_mass_mixed, blocks_for(N, TB), TB, 0, stream, N, d_esup_ptr, d_esup_slot, d_area,
-               (const double2*)d_gterms, &d_scal->dtmin, gcl ? 1 : 0, d_M, d_invM);
-    if (gcl) {  // putW, putArea
-        CFD_CUDA(cudaMemcpyAsync(d_Wxo, d_WX, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
-        CFD_CUDA(cudaMemcpyAsync(d_Wyo, d_WY, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
-        CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
-    }
-    tstop(TM_MASAS);
+    tstart(TM_DERIV);
+    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Xhi, d_Xlo,
+               gcl ? 1 : 0, prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_Wf, d_Wof,
+               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, d_geo8, d_gterms);
+    tstop(TM_DERIV);
     tstart(TM_LAPLACE);
-    CFD_CUDA(launch_laplace_mixed(laplace_fp64, stream, N, E, d_elem, d_esup_ptr, d_esup_slot,
-                                  d_lap_pos, d_geo, d_X, d_Y, d_rowptr, d_valf, d_val, d_diag,
-                                  d_invdiag));
+    CFD_LAUNCH(k_node_geometry, blocks_for(N, kGeoNodeBlock), kGeoNodeBlock, 0, stream, N,
+               d_esup_ptr, d_esup_slot, d_lap_pos, d_geo8, d_gterms, &d_scal->dtmin, gcl ? 1 : 0,
+               d_rowptr, d_valf, d_invdiag, d_invdiagf, d_M, d_invMf, d_Wf, d_Wof);
     tstop(TM_LAPLACE);
     return CFD_OK;
 }
@@ -530,39 +574,48 @@ int Ctx::step_once_mixed() {
     const int TB = 256;
     iter += 1;
     tstart(TM_DELTAT);
-    CFD_LAUNCH(k_deltat_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_T, d_VX, d_VY, d_WX,
-               d_WY, d_area, (float)prm.fsafe, (float)prm.t_inf, &d_scal->dtmin32_bits);
-    CFD_LAUNCH(k_deltat_refine, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_T, d_VX, d_VY, d_WX,
-               d_WY, d_area, (float)prm.fsafe, (float)prm.t_inf, d_scal);
+    CFD_LAUNCH(k_deltat_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf, d_VYf,
+               d_Wf, d_areaf, (float)prm.fsafe, (float)prm.t_inf, &d_scal->dtmin32_bits, d_blockmin);
+    {
+        const int nchunk = (int)blocks_for(E, TB);
+        const int grid = std::min(nchunk, 2 * nsm);
+        CFD_LAUNCH(k_deltat_refine, grid, TB, 0, stream, E, d_elem, d_Tf, d_VXf, d_VYf, d_Wf,
+                   d_areaf, (const unsigned long long*)d_blockmin, nchunk, (float)prm.fsafe,
+                   (float)prm.t_inf, d_scal);
+    }
     CFD_LAUNCH(k_dt_finalize, 1, 1, 0, stream, d_scal);
     tstop(TM_DELTAT);
     CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
     CFD_CUDA(cudaEventRecord(ev_scal, stream));
     tstart(TM_ESTAB);
-    CFD_LAUNCH(k_estab_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_U, d_T,
-               (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VX, d_VY, d_WX, d_WY, d_geo,
+    CFD_LAUNCH(k_estab_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Uhi, d_Ulo, d_Tf,
+               (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VXf, d_VYf, d_Wf,
+               (const float4*)d_geo8,
                (float)prm.fr, d_scal, (float)prm.rho_inf, (float)prm.t_inf, prm.estab_mode,
                (float)estab_eps, (float)dir[0], (float)dir[1], d_shocf, d_ts1f, d_ts2f, d_ts3f);
     tstop(TM_ESTAB);
     GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte, prm.fr};
+    const GasConstF gf = to_float(gc);
     const bool viscous = prm.fmu > 2.2250738585072014e-308;
     tstart(TM_CALCRHS);
-    CFD_CUDA(launch_elem_stage1_mixed(viscous, stream, E, d_elem, d_U, d_geo, d_area, d_shocf,
-                                      nullptr, &d_scal->dtmin, d_ts1f, d_ts2f, d_ts3f, gc, d_WX,
-                                      d_WY, d_slot_pos, d_rec));
+    CFD_CUDA(launch_elem_stage1_mixed(viscous, stream, E, d_elem, d_Uhi, d_Ulo, d_geo8, d_shocf,
+                                      d_scal, d_ts1f, d_ts2f, d_ts3f, gf, d_Wf, d_slot_pos, d_Tf,
+                                      d_recInv, d_recVisc, d_mulam));
     tstop(TM_CALCRHS);
-    // T is read at the element's nodes and written per node: alternate two buffers so
-    // that stage s reads the T of stage s-1 (the reference's module T) and the 4th
-    // stage leaves it in d_T
-    double* Tb[2] = {d_T, d_T2};
+    // stage s uses mu, lambda from the T of stage s-1 (the reference's module T): stage 1's
+    // come from the element kernel above, the others from k_elem_mulam before the node pass
     const int NRK = 4;
     for (int irk = 1; irk <= NRK; ++irk) {
-        const double rk_fact = 1.0 / (NRK + 1 - irk);
+        const float rk_fact = 1.f / (float)(NRK + 1 - irk);
         tstart(TM_UPDATE);
-        CFD_CUDA(launch_node_mixed(stream, N, d_esup_ptr, d_esup_slot, d_elem, d_rec,
-                                   Tb[(irk - 1) & 1], gc, viscous ? 1 : 0, d_U, d_invM, rk_fact,
-                                   d_bcflag, d_bcval, d_nrm, d_WX, d_WY, d_U1, d_RHO, d_VX, d_VY,
-                                   d_E, d_P, Tb[irk & 1], d_RMACH));
+        if (irk > 1 && viscous)
+            CFD_LAUNCH(k_elem_mulam, blocks_for(E, TB), TB, 0, stream, E, d_elem, (const float*)d_Tf,
+                       gf, d_mulam);
+        CFD_CUDA(launch_node_mixed(stream, N, d_esup_ptr, d_esup_slot, d_mulam, d_recInv, d_recVisc,
+                                   d_invSum, irk == 1 ? 1 : 0, gc, gf, viscous ? 1 : 0, d_U, d_Uhi,
+                                   d_Ulo, d_invMf, rk_fact, irk == NRK ? 1 : 0, d_bcflag, d_bcval,
+                                   d_nrm, d_WX, d_WY, d_U1, d_RHOf, d_VXf, d_VYf, d_Ef, d_Pf, d_Tf,
+                                   d_RMACHf));
         tstop(TM_UPDATE);
     }
     CFD_CUDA(cudaEventSynchronize(ev_scal));
@@ -570,7 +623,7 @@ int Ctx::step_once_mixed() {
     time = time + dtmin;
     last_dtmin = dtmin;
     tstart(TM_FORCES);
-    CFD_LAUNCH(k_forces_tree, 1, 256, 0, stream, bc.nset_numb, d_set_ptr, d_set_edges, d_P, d_X, d_Y,
+    CFD_LAUNCH(k_forces_tree, 1, 256, 0, stream, bc.nset_numb, d_set_ptr, d_set_edges, d_Pf, d_X, d_Y,
                d_xref, d_yref, d_scal);
     tstop(TM_FORCES);
     const double PI = std::acos(-1.0);
@@ -590,15 +643,17 @@ int Ctx::step_once_mixed() {
                    d_X, d_Y, d_xref, d_yref, ca, sa, yposr, d_xfix[0], d_xfix[1]);
     tstop(TM_TRANSF);
     if (prm.guess_mode == CFD_GUESS_ZERO) {
-        CFD_CUDA(cudaMemsetAsync(d_pos[0], 0, sizeof(double) * N, stream));
-        CFD_CUDA(cudaMemsetAsync(d_pos[1], 0, sizeof(double) * N, stream));
+        for (int c = 0; c < 2; ++c) {
+            CFD_CUDA(cudaMemsetAsync(d_pos[c], 0, sizeof(double) * N, stream));
+            CFD_CUDA(cudaMemsetAsync(d_posf[c], 0, sizeof(float) * N, stream));
+        }
     }
     tstart(TM_GRAD);
     int st = run_pcg(2);
     if (st) return st;
     tstop(TM_GRAD);
-    CFD_LAUNCH(k_motion_update, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1], d_scal,
-               d_X, d_Y, d_WX, d_WY);
+    CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1],
+               d_scal, d_X, d_Y, d_WX, d_WY, d_Xhi, d_Xlo, d_Wf);
     if (prm.moving == 1) {
         st = geometry_mixed(false);
         if (st) return st;

@@ -159,6 +159,8 @@ __global__ void k_dt_finalize(StepScal* sc) {
     }
     sc->dtmin = dtmin;
     sc->cota = 10.0 * sc->dtmin_raw;
+    sc->inv_dtmin = 1.0 / dtmin;
+    sc->dtmin_f = (float)dtmin;
 }
 
 // ITLOCAL != 0 only: DTL = DTMIN*DTFACT + min(DT, COTA)*(1-DTFACT) (ns2DComp.ALE.f90:160-161)

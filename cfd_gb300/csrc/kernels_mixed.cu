@@ -1,18 +1,23 @@
 // kernels_mixed.cu — the mixed-precision form of the step (CFD_PREC_MIXED), sm_103a.
 //
 // FP32 for calcRHS, FUENTE, ESTAB, deltat and the Laplacian values; FP64 for the
-// conserved-state update U1 = U - rk_fact/M*RHS, the areas and the gcl mass update, and
-// (in the BiCG kernel) the vectors, dots and scalars.  Per-node sums of the FP32
-// contributions are compensated (Neumaier), then widened to FP64.
+// conserved-state update U1 = U - rk_fact/M*RHS, the areas and the gcl mass update, DTMIN,
+// and (in the BiCG kernel) the vectors, dots and scalars.  Per-node sums of the FP32
+// contributions are compensated (Neumaier).
 //
-// Stage invariance (the reference calls calcRHS/FUENTE with the step-start U in all four
-// RK stages, subrutinas.f90:685, :1064; only the module T changes, through mu and lambda
-// at calcRHS.f90:49-51): stage 1 evaluates every element once and stores, per (element,
-// local node) slot, the stage-invariant part Inv(0:3) (Galerkin, SUPG, shock capturing,
-// FUENTE) and the coefficients of the viscous part, which is linear in (mu, lambda):
-// Vmu(1:3), Vlam(3).  Slots are stored in element-around-point order, so each RK stage
-// is one node kernel that streams its node's slots, forms Inv + mu*Vmu + lambda*Vlam with
-// the stage's mu and lambda, and applies the update and boundary conditions.
+// GB300's FP64 pipe runs 2 thread-ops per clock per SM, 64x fewer than FP32, and it also
+// executes every double<->float conversion.  So the FP32 kernels read FP32 data only:
+// float shadows of the primitives, of the geometry and of W, and float hi/lo splits of U
+// and of (X, Y) (value = hi + lo), whose differences give gradients as accurate as FP64
+// differences rounded to FP32.  FP64 arithmetic is left to the few places that need it.
+//
+// Stage invariance (calcRHS/FUENTE see the step-start U in all four RK stages,
+// subrutinas.f90:685, :1064; only the module T changes, through mu and lambda,
+// calcRHS.f90:49-51): stage 1 evaluates each element once and stores, per (element, local
+// node) slot, the stage-invariant part Inv(0:3) (Galerkin, SUPG, shock capturing, FUENTE)
+// and the coefficients of the viscous part, which is linear in (mu, lambda): Vmu(1:3),
+// Vlam(3).  Slots are stored in element-around-point order, so each RK stage is one node
+// kernel that streams its slots and forms Inv + mu*Vmu + lambda*Vlam with the stage's T.
 #include "cfd_kernels.cuh"
 
 namespace cfd {
@@ -29,41 +34,96 @@ struct Acc {
         else c += (x - t) + s;
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+    __device__ __forceinline__ float value() const { return s + c; }
 };
 
-// ------------------------------------------------------------------ deltat (FP32)
-__global__ void k_deltat_mixed(int nelem, const int4* __restrict__ elem, const double* __restrict__ T,
+// hi/lo split of a double: hi = RN32(v), lo = RN32(v - hi)
+__device__ __forceinline__ void split(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// ------------------------------------------------------------------ float shadows
+// U -> (Uhi, Ulo); T, VX, VY -> float; (X, Y) -> (Xhi, Xlo); W -> Wf.  Any input may be NULL.
+__global__ void k_narrow_state(int npoin, const double* __restrict__ U, const double* __restrict__ T,
                                const double* __restrict__ VX, const double* __restrict__ VY,
+                               const double* __restrict__ X, const double* __restrict__ Y,
                                const double* __restrict__ WX, const double* __restrict__ WY,
-                               const double* __restrict__ area, float fsafe, float t_inf,
-                               unsigned long long* __restrict__ dtmin_bits) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
+                               float4* __restrict__ Uhi, float4* __restrict__ Ulo,
+                               float* __restrict__ Tf, float* __restrict__ VXf,
+                               float* __restrict__ VYf, float2* __restrict__ Xhi,
+                               float2* __restrict__ Xlo, float2* __restrict__ Wf) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npoin) return;
+    if (U) {
+        float h[4], l[4];
+        for (int q = 0; q < 4; ++q) split(U[4 * (size_t)p + q], h[q], l[q]);
+        Uhi[p] = make_float4(h[0], h[1], h[2], h[3]);
+        Ulo[p] = make_float4(l[0], l[1], l[2], l[3]);
+    }
+    if (T) Tf[p] = (float)T[p];
+    if (VX) VXf[p] = (float)VX[p];
+    if (VY) VYf[p] = (float)VY[p];
+    if (X) {
+        float hx, lx, hy, ly;
+        split(X[p], hx, lx);
+        split(Y[p], hy, ly);
+        Xhi[p] = make_float2(hx, hy);
+        Xlo[p] = make_float2(lx, ly);
+    }
+    if (WX) Wf[p] = make_float2((float)WX[p], (float)WY[p]);
+}
+
+// double -> float
+__global__ void k_narrow(long n, const double* __restrict__ a, float* __restrict__ b) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+// float -> double (downloads of the mixed form's float fields)
+__global__ void k_widen(long n, const float* __restrict__ a, double* __restrict__ b) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (double)a[i];
+}
+
+// ------------------------------------------------------------------ deltat
+__device__ __forceinline__ float dtelem_f32(const int4 n, const float* __restrict__ T,
+                                            const float* __restrict__ VX, const float* __restrict__ VY,
+                                            const float2* __restrict__ W, float area, float fsafe,
+                                            float t_inf) {
+    const int nn[3] = {n.x, n.y, n.z};
+    float vumax = 0.f, vvmax = 0.f;
+    const float T_iel = (T[nn[0]] + T[nn[1]] + T[nn[2]]) * (1.f / 3.f);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float2 w = W[nn[i]];
+        vumax = fmaxf(vumax, fabsf(VX[nn[i]] - w.x));
+        vvmax = fmaxf(vvmax, fabsf(VY[nn[i]] - w.y));
+    }
+    const float hh = sqrtf(2.f * area);
+    const float vel = sqrtf(vumax * vumax + vvmax * vvmax);
+    const float et = 0.017f * pow15f(T_iel / t_inf) * (t_inf + 110.f) / (T_iel + 110.f);
+    const float alpha = fminf((vel * hh) / (2.f * et) / 3.f, 1.f);
+    const float a = 4.f * et / (hh * hh);
+    // FSAFE/(1/DELTATC + 1/DELTATU) with 1/DELTATC = a, 1/DELTATU = a + alpha*vel/hh
+    return fsafe / (a + (a + alpha * vel / hh));
+}
+
+// subrutinas.f90:170-210 in FP32: the FP32 minimum (bit pattern of a positive double)
+__global__ void k_deltat_mixed(int nelem, const int4* __restrict__ elem, const float* __restrict__ T,
+                               const float* __restrict__ VX, const float* __restrict__ VY,
+                               const float2* __restrict__ W, const float* __restrict__ areaf,
+                               float fsafe, float t_inf, unsigned long long* __restrict__ dtmin_bits,
+                               unsigned long long* __restrict__ block_min) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long mybits = 0x7ff0000000000000ull;
     if (e < nelem) {
-        int4 n = elem[e];
-        const int nn[3] = {n.x, n.y, n.z};
-        float vumax = 0.f, vvmax = 0.f;
-        float T_iel = (float)((T[nn[0]] + T[nn[1]] + T[nn[2]]) * (1.0 / 3.0));
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            vumax = fmaxf(vumax, fabsf((float)(VX[nn[i]] - WX[nn[i]])));
-            vvmax = fmaxf(vvmax, fabsf((float)(VY[nn[i]] - WY[nn[i]])));
-        }
-        float hh = sqrtf(2.f * (float)area[e]);
-        float vel = sqrtf(vumax * vumax + vvmax * vvmax);
-        float et = 0.017f * pow15f(T_iel / t_inf) * (t_inf + 110.f) / (T_iel + 110.f);
-        float pe = (vel * hh) / (2.f * et);
-        float alpha = fminf(pe / 3.f, 1.f);
-        float a = 4.f * et / (hh * hh);
-        // FSAFE/(1/DELTATC + 1/DELTATU) with 1/DELTATC = a, 1/DELTATU = a + alpha*vel/hh
-        float dtelem = fsafe / (a + (a + alpha * vel / hh));
-        double d = (double)dtelem;
+        const double d = (double)dtelem_f32(elem[e], T, VX, VY, W, areaf[e], fsafe, t_inf);
         if (d < 1.0e20 && d > 0.0) mybits = (unsigned long long)__double_as_longlong(d);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        unsigned long long o = __shfl_down_sync(0xffffffffu, mybits, off);
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, mybits, off);
         mybits = o < mybits ? o : mybits;
     }
     __shared__ unsigned long long wmin[32];
@@ -72,104 +132,98 @@ __global__ void k_deltat_mixed(int nelem, const int4* __restrict__ elem, const d
     if (threadIdx.x == 0) {
         unsigned long long m = wmin[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = wmin[w] < m ? wmin[w] : m;
+        block_min[blockIdx.x] = m;
         atomicMin(dtmin_bits, m);
     }
 }
 
-// DTELEM in FP64 (subrutinas.f90:172-206), for the candidates of the FP32 minimum
-__device__ double dtelem_fp64(int4 n, const double* __restrict__ T, const double* __restrict__ VX,
-                              const double* __restrict__ VY, const double* __restrict__ WX,
-                              const double* __restrict__ WY, double area, double fsafe,
-                              double t_inf) {
+// Second pass: elements whose FP32 DTELEM is within 1e-4 of the FP32 minimum get their
+// DTELEM in FP64 (subrutinas.f90:172-206); the FP64 minimum over them is DTMIN, so the 1%
+// hysteresis of ns2DComp.ALE.f90:146-156 sees an FP64-accurate value.  The elements are
+// visited in the 256-element chunks of k_deltat_mixed (blockDim.x = 256), and only chunks
+// whose FP32 minimum lies in the band.
+__device__ __forceinline__ void refine_one(int e, const int4* __restrict__ elem,
+                                           const float* __restrict__ T, const float* __restrict__ VX,
+                                           const float* __restrict__ VY, const float2* __restrict__ W,
+                                           const float* __restrict__ areaf, float fsafe, float t_inf,
+                                           double m32, StepScal* __restrict__ sc) {
+    const int4 n = elem[e];
+    const float d32 = dtelem_f32(n, T, VX, VY, W, areaf[e], fsafe, t_inf);
+    if ((double)d32 > m32 * (1.0 + 1.0e-4)) return;
     const int nn[3] = {n.x, n.y, n.z};
     double vumax = 0.0, vvmax = 0.0;
-    const double T_iel = (T[nn[0]] + T[nn[1]] + T[nn[2]]) / 3.0;
+    const double T_iel = ((double)T[nn[0]] + (double)T[nn[1]] + (double)T[nn[2]]) / 3.0;
     for (int i = 0; i < 3; ++i) {
-        const double vu = fabs(VX[nn[i]] - WX[nn[i]]), vv = fabs(VY[nn[i]] - WY[nn[i]]);
+        const float2 w = W[nn[i]];
+        const double vu = fabs((double)VX[nn[i]] - (double)w.x), vv = fabs((double)VY[nn[i]] - (double)w.y);
         if (vu > vumax) vumax = vu;
         if (vv > vvmax) vvmax = vv;
     }
-    const double hh = sqrt(2.0 * area);
+    const double tinf = (double)t_inf;
+    const double hh = sqrt(2.0 * (double)areaf[e]);
     const double vel = sqrt(vumax * vumax + vvmax * vvmax);
-    const double et = 0.017 * (T_iel / t_inf) * sqrt(T_iel / t_inf) * (t_inf + 110.0) / (T_iel + 110.0);
-    const double pe = (vel * hh) / (2.0 * et);
-    const double alpha = fmin(pe / 3.0, 1.0);
+    const double et = 0.017 * (T_iel / tinf) * sqrt(T_iel / tinf) * (tinf + 110.0) / (T_iel + 110.0);
+    const double alpha = fmin((vel * hh) / (2.0 * et) / 3.0, 1.0);
     const double deltatu = 1.0 / (4.0 * et / (hh * hh) + alpha * vel / hh);
     const double deltatc = 1.0 / (4.0 * et / (hh * hh));
-    return fsafe / (1.0 / deltatc + 1.0 / deltatu);
+    const double d = (double)fsafe / (1.0 / deltatc + 1.0 / deltatu);
+    if (d > 0.0 && d < 1.0e20) atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(d));
 }
 
-// Second pass of the mixed deltat: elements whose FP32 DTELEM is within 1e-4 of the FP32
-// minimum get their FP64 DTELEM; the FP64 minimum over them is DTMIN, so the 1%
-// hysteresis of ns2DComp.ALE.f90:146-156 sees an FP64-accurate value.
-__global__ void k_deltat_refine(int nelem, const int4* __restrict__ elem, const double* __restrict__ T,
-                                const double* __restrict__ VX, const double* __restrict__ VY,
-                                const double* __restrict__ WX, const double* __restrict__ WY,
-                                const double* __restrict__ area, float fsafe, float t_inf,
-                                StepScal* __restrict__ sc) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nelem) return;
+__global__ void k_deltat_refine(int nelem, const int4* __restrict__ elem, const float* __restrict__ T,
+                                const float* __restrict__ VX, const float* __restrict__ VY,
+                                const float2* __restrict__ W, const float* __restrict__ areaf,
+                                const unsigned long long* __restrict__ block_min, int nchunk,
+                                float fsafe, float t_inf, StepScal* __restrict__ sc) {
     const double m32 = __longlong_as_double((long long)sc->dtmin32_bits);
-    const int4 n = elem[e];
-    const int nn[3] = {n.x, n.y, n.z};
-    float vumax = 0.f, vvmax = 0.f;
-    const float T_iel = (float)((T[nn[0]] + T[nn[1]] + T[nn[2]]) * (1.0 / 3.0));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        vumax = fmaxf(vumax, fabsf((float)(VX[nn[i]] - WX[nn[i]])));
-        vvmax = fmaxf(vvmax, fabsf((float)(VY[nn[i]] - WY[nn[i]])));
-    }
-    const float hh = sqrtf(2.f * (float)area[e]);
-    const float vel = sqrtf(vumax * vumax + vvmax * vvmax);
-    const float et = 0.017f * pow15f(T_iel / t_inf) * (t_inf + 110.f) / (T_iel + 110.f);
-    const float alpha = fminf((vel * hh) / (2.f * et) / 3.f, 1.f);
-    const float a = 4.f * et / (hh * hh);
-    const float d32 = fsafe / (a + (a + alpha * vel / hh));
-    if ((double)d32 <= m32 * (1.0 + 1.0e-4)) {
-        const double d = dtelem_fp64(n, T, VX, VY, WX, WY, area[e], (double)fsafe, (double)t_inf);
-        if (d > 0.0 && d < 1.0e20) atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(d));
+    const double band = m32 * (1.0 + 1.0e-4);
+    for (int b = blockIdx.x; b < nchunk; b += gridDim.x) {
+        if (__longlong_as_double((long long)block_min[b]) > band) continue;
+        const int e = b * blockDim.x + threadIdx.x;
+        if (e < nelem) refine_one(e, elem, T, VX, VY, W, areaf, fsafe, t_inf, m32, sc);
     }
 }
 
 // ------------------------------------------------------------------ ESTAB (FP32)
-// subrutinas.f90:346-443 in FP32; estab_mode as CFD_ESTAB_*.
-__global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const double* __restrict__ U,
-                              const double* __restrict__ T, float gm, const double* __restrict__ VX,
-                              const double* __restrict__ VY, const double* __restrict__ WX,
-                              const double* __restrict__ WY, const double* __restrict__ geo,
-                              float FR, const StepScal* __restrict__ sc, float RHOINF, float TINF,
+// subrutinas.f90:346-443; estab_mode as CFD_ESTAB_*.
+__global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
+                              const float4* __restrict__ Ulo, const float* __restrict__ T, float gm,
+                              const float* __restrict__ VX, const float* __restrict__ VY,
+                              const float2* __restrict__ W, const float4* __restrict__ geo, float FR,
+                              const StepScal* __restrict__ sc, float RHOINF, float TINF,
                               int estab_mode, float eps_dir, float dirx, float diry,
-                              float* __restrict__ SHOC,
-                              float* __restrict__ TS1, float* __restrict__ TS2,
-                              float* __restrict__ TS3) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
+                              float* __restrict__ SHOC, float* __restrict__ TS1,
+                              float* __restrict__ TS2, float* __restrict__ TS3) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nelem) return;
-    const size_t E = (size_t)nelem;
-    const float DTMIN = (float)sc->dtmin;
-    int4 n = elem[e];
+    const float DTMIN = sc->dtmin_f;
+    const int4 n = elem[e];
     const int n1 = n.x, n2 = n.y, n3 = n.z;
-    const float DX[3] = {(float)geo[e], (float)geo[E + e], (float)geo[2 * E + e]};
-    const float DY[3] = {(float)geo[3 * E + e], (float)geo[4 * E + e], (float)geo[5 * E + e]};
-    const double r1 = U[4 * (size_t)n1], r2 = U[4 * (size_t)n2], r3 = U[4 * (size_t)n3];
-    const float rho_elem = (float)((r1 + r2 + r3) * (1.0 / 3.0));
-    float vx = (float)(((VX[n1] + VX[n2] + VX[n3]) - (WX[n1] + WX[n2] + WX[n3])) * (1.0 / 3.0));
-    float vy = (float)(((VY[n1] + VY[n2] + VY[n3]) - (WY[n1] + WY[n2] + WY[n3])) * (1.0 / 3.0));
-    float vel2 = sqrtf(vx * vx + vy * vy);
-    // gradients from differences to node 1 (sum of the shape-function gradients is 0)
-    const float d2 = (float)(r2 - r1), d3 = (float)(r3 - r1);
-    float drx = d2 * DX[1] + d3 * DX[2], dry = d2 * DY[1] + d3 * DY[2];
-    const double t1 = T[n1], t2 = T[n2], t3 = T[n3];
-    const float e2 = (float)(t2 - t1), e3 = (float)(t3 - t1);
-    float dtx = e2 * DX[1] + e3 * DX[2], dty = e2 * DY[1] + e3 * DY[2];
-    const float temp = (float)((t1 + t2 + t3) * (1.0 / 3.0));
-    float dr2 = sqrtf(drx * drx + dry * dry) + 1.0e-20f;
-    float dt2 = sqrtf(dtx * dtx + dty * dty) + 1.0e-20f;
+    const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
+    const float DX[3] = {ga.x, ga.y, ga.z};
+    const float DY[3] = {ga.w, gb.x, gb.y};
+    const float rh1 = Uhi[n1].x, rh2 = Uhi[n2].x, rh3 = Uhi[n3].x;
+    const float rl1 = Ulo[n1].x, rl2 = Ulo[n2].x, rl3 = Ulo[n3].x;
+    const float rho_elem = ((rh1 + rh2 + rh3) + (rl1 + rl2 + rl3)) * (1.f / 3.f);
+    const float2 w1 = W[n1], w2 = W[n2], w3 = W[n3];
+    const float vx = ((VX[n1] + VX[n2] + VX[n3]) - (w1.x + w2.x + w3.x)) * (1.f / 3.f);
+    const float vy = ((VY[n1] + VY[n2] + VY[n3]) - (w1.y + w2.y + w3.y)) * (1.f / 3.f);
+    const float vel2 = sqrtf(vx * vx + vy * vy);
+    // gradients from differences to node 1 (the shape-function gradients sum to 0)
+    const float d2 = (rh2 - rh1) + (rl2 - rl1), d3 = (rh3 - rh1) + (rl3 - rl1);
+    const float drx = d2 * DX[1] + d3 * DX[2], dry = d2 * DY[1] + d3 * DY[2];
+    const float t1 = T[n1], t2 = T[n2], t3 = T[n3];
+    const float e2 = t2 - t1, e3 = t3 - t1;
+    const float dtx = e2 * DX[1] + e3 * DX[2], dty = e2 * DY[1] + e3 * DY[2];
+    const float temp = (t1 + t2 + t3) * (1.f / 3.f);
+    const float dr2 = sqrtf(drx * drx + dry * dry) + 1.0e-20f;
+    const float dt2 = sqrtf(dtx * dtx + dty * dty) + 1.0e-20f;
     float dux = 0.f, duy = 0.f;
     if (estab_mode == CFD_ESTAB_REFERENCE) {
         dux = vel2 * DX[0] + vel2 * DX[1] + vel2 * DX[2];
         duy = vel2 * DY[0] + vel2 * DY[1] + vel2 * DY[2];
     }
-    float du2 = sqrtf(dux * dux + duy * duy) + 1.0e-20f;
+    const float du2 = sqrtf(dux * dux + duy * duy) + 1.0e-20f;
     float rtx = dtx / dt2, rty = dty / dt2;
     float rjx = drx / dr2, rjy = dry / dr2;
     float rux = dux / du2, ruy = duy / du2;
@@ -193,8 +247,8 @@ __global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const do
     float tau = 0.f, h_rgne = 0.f, h_rgn = 0.f, h_jgn = 0.f;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        float term1 = fabsf(vx * DX[i] + vy * DY[i]);
-        float term2 = fabsf(rjx * DX[i] + rjy * DY[i]);
+        const float term1 = fabsf(vx * DX[i] + vy * DY[i]);
+        const float term2 = fabsf(rjx * DX[i] + rjy * DY[i]);
         tau += term1 + term2 * c;
         h_rgne += fabsf(rtx * DX[i] + rty * DY[i]);
         h_rgn += fabsf(rux * DX[i] + ruy * DY[i]);
@@ -211,62 +265,76 @@ __global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const do
     SHOC[e] = (tr1 + tr1 * tr1) * 0.5f * (c * c) * zzz;
     const float resumen = 1.f / (tau * tau) + (2.f / DTMIN) * (2.f / DTMIN);
     const float rrr = rsqrtf(resumen);
-    float s2 = rrr, s3 = rrr;
     const float k4 = 4.f * fmu / RHOINF;
-    // (resumen + 1/tau_s^2)^(-1/2) with tau_s = h^2/k4  ==  (resumen + k4^2/h^4)^(-1/2); h = 0 -> 0
+    // (resumen + 1/tau_s^2)^(-1/2), tau_s = h^2/k4, is (resumen + k4^2/h^4)^(-1/2); h = 0 -> 0
     const float hr2 = h_rgn * h_rgn, he2 = h_rgne * h_rgne;
-    s2 = (hr2 > 0.f) ? rsqrtf(resumen + (k4 * k4) / (hr2 * hr2)) : 0.f;
-    s3 = (he2 > 0.f) ? rsqrtf(resumen + (k4 * k4) / (he2 * he2)) : 0.f;
     TS1[e] = rrr;
-    TS2[e] = s2;
-    TS3[e] = s3;
+    TS2[e] = (hr2 > 0.f) ? rsqrtf(resumen + (k4 * k4) / (hr2 * hr2)) : 0.f;
+    TS3[e] = (he2 > 0.f) ? rsqrtf(resumen + (k4 * k4) / (he2 * he2)) : 0.f;
+}
+
+// ------------------------------------------------------------------ element mu, lambda
+// calcRHS.f90:49-51: Sutherland mu and lambda at the element's mean T, in FP32
+__device__ __forceinline__ float2 elem_mu_lambda(const int4 n, const float* __restrict__ T,
+                                                 const GasConstF& gc) {
+    const float t_inf = gc.t_inf;
+    const float Ta = (T[n.x] + T[n.y] + T[n.z]) * (1.f / 3.f);
+    const float r15 = pow15f(Ta / t_inf);
+    return make_float2(gc.mu_ref * r15 * (t_inf + 110.f) / (Ta + 110.f),
+                       gc.lambda_ref * r15 * (t_inf + 194.f) / (Ta + 194.f));
+}
+
+// mu, lambda of every element from the T of the previous RK stage (stages 2-4)
+__global__ void k_elem_mulam(int nelem, const int4* __restrict__ elem, const float* __restrict__ T,
+                             GasConstF gc, float2* __restrict__ mulam) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    mulam[e] = elem_mu_lambda(elem[e], T, gc);
 }
 
 // ------------------------------------------------------------------ stage-1 element kernel
 // calcRHS.f90:36-141 + FUENTE (subrutinas.f90:1060-1078) in FP32, folded with the
-// step's area*dtl/3, written as slot records in element-around-point order.
-struct __align__(16) SlotRec {
-    float4 inv;   // stage-invariant contributions to the 4 equations
-    float4 visc;  // Vmu(1), Vmu(2), Vmu(3), Vlam(3)
-};
+// step's area*dtl/3, written as slot records in element-around-point order: recInv holds
+// the stage-invariant contributions to the 4 equations, recVisc Vmu(1), Vmu(2), Vmu(3),
+// Vlam(3).
 
 template <bool VISCOUS>
 __global__ void __launch_bounds__(128)
-k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const double* __restrict__ U,
-                    const double* __restrict__ geo, const double* __restrict__ area,
-                    const float* __restrict__ shoc, const double* __restrict__ dtl_arr,
-                    const double* __restrict__ dtl_scalar, const float* __restrict__ ts1,
-                    const float* __restrict__ ts2, const float* __restrict__ ts3, GasConst gc,
-                    const double* __restrict__ WX, const double* __restrict__ WY,
-                    const int* __restrict__ slot_pos, SlotRec* __restrict__ rec) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
+k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
+                    const float4* __restrict__ Ulo, const float4* __restrict__ geo,
+                    const float* __restrict__ shoc,
+                    const StepScal* __restrict__ sc, const float* __restrict__ ts1,
+                    const float* __restrict__ ts2, const float* __restrict__ ts3, GasConstF gc,
+                    const float2* __restrict__ W, const int* __restrict__ slot_pos,
+                    const float* __restrict__ T, float4* __restrict__ recInv,
+                    float4* __restrict__ recVisc, float2* __restrict__ mulam) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nelem) return;
-    const size_t E = (size_t)nelem;
-    const float g = (float)gc.gamma, Cv = (float)gc.cv;
-    int4 n = elem[e];
+    const float g = gc.gamma, Cv = gc.cv;
+    const int4 n = elem[e];
+    if (VISCOUS) mulam[e] = elem_mu_lambda(n, T, gc);  // for the first RK stage
     const int p[3] = {n.x, n.y, n.z};
-    const float Nx[3] = {(float)geo[e], (float)geo[E + e], (float)geo[2 * E + e]};
-    const float Ny[3] = {(float)geo[3 * E + e], (float)geo[4 * E + e], (float)geo[5 * E + e]};
-    double Ud[3][4];
+    const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
+    const float Nx[3] = {ga.x, ga.y, ga.z};
+    const float Ny[3] = {ga.w, gb.x, gb.y};
+    float Un[3][4], Ul[3][4];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        const double2* u2 = reinterpret_cast<const double2*>(U + 4 * (size_t)p[i]);
-        double2 a = u2[0], b = u2[1];
-        Ud[i][0] = a.x; Ud[i][1] = a.y; Ud[i][2] = b.x; Ud[i][3] = b.y;
+        const float4 h = Uhi[p[i]], l = Ulo[p[i]];
+        Un[i][0] = h.x; Un[i][1] = h.y; Un[i][2] = h.z; Un[i][3] = h.w;
+        Ul[i][0] = l.x; Ul[i][1] = l.y; Ul[i][2] = l.z; Ul[i][3] = l.w;
     }
-    float Ux[4], Uy[4], Un[3][4];
+    float Ux[4], Uy[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const float d1 = (float)(Ud[1][q] - Ud[0][q]), d2 = (float)(Ud[2][q] - Ud[0][q]);
+        const float d1 = (Un[1][q] - Un[0][q]) + (Ul[1][q] - Ul[0][q]);
+        const float d2 = (Un[2][q] - Un[0][q]) + (Ul[2][q] - Ul[0][q]);
         Ux[q] = d1 * Nx[1] + d2 * Nx[2];
         Uy[q] = d1 * Ny[1] + d2 * Ny[2];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) Un[i][q] = (float)Ud[i][q];
     }
     const float tau[3] = {ts1[e], ts2[e], ts3[e]};
-    const float nu = shoc[e] * (float)gc.cte;
-    const double dtl = dtl_arr ? dtl_arr[e] : *dtl_scalar;
-    const float scale = (float)(area[e] * dtl / 3.0);
+    const float nu = shoc[e] * gc.cte;
+    const float scale = gb.z * sc->dtmin_f * (1.f / 3.f);
     float r[3][4], vm[3][3], vl[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -341,12 +409,10 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const double* __re
             }
         }
     }
-    // FUENTE: -AR*sum_k sp(i,k)*(Ux*wx_k + Uy*wy_k), AR = area*dtl/3 = scale
-    {
-        const float w0 = (float)WX[p[0]], w1 = (float)WX[p[1]], w2 = (float)WX[p[2]];
-        const float y0 = (float)WY[p[0]], y1 = (float)WY[p[1]], y2 = (float)WY[p[2]];
-        const float wx[3] = {0.5f * (w0 + w1), 0.5f * (w1 + w2), 0.5f * (w0 + w2)};
-        const float wy[3] = {0.5f * (y0 + y1), 0.5f * (y1 + y2), 0.5f * (y0 + y2)};
+    {  // FUENTE: -AR*sum_k sp(i,k)*(Ux*wx_k + Uy*wy_k), AR = area*dtl/3 = scale
+        const float2 w0 = W[p[0]], w1 = W[p[1]], w2 = W[p[2]];
+        const float wx[3] = {0.5f * (w0.x + w1.x), 0.5f * (w1.x + w2.x), 0.5f * (w0.x + w2.x)};
+        const float wy[3] = {0.5f * (w0.y + w1.y), 0.5f * (w1.y + w2.y), 0.5f * (w0.y + w2.y)};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const float q0 = Ux[q] * wx[0] + Uy[q] * wy[0];
@@ -359,78 +425,117 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const double* __re
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        SlotRec o;
-        o.inv = make_float4(r[i][0] * scale, r[i][1] * scale, r[i][2] * scale, r[i][3] * scale);
-        o.visc = make_float4(vm[i][0] * scale, vm[i][1] * scale, vm[i][2] * scale, vl[i] * scale);
-        rec[slot_pos[3 * (size_t)e + i]] = o;
+        const int pos = slot_pos[3 * (size_t)e + i];
+        recInv[pos] = make_float4(r[i][0] * scale, r[i][1] * scale, r[i][2] * scale, r[i][3] * scale);
+        if (VISCOUS)
+            recVisc[pos] = make_float4(vm[i][0] * scale, vm[i][1] * scale, vm[i][2] * scale, vl[i] * scale);
     }
 }
 
 // ------------------------------------------------------------------ RK stage, node side
-// subrutinas.f90:680-825 for one stage with the slot records: the node's RHS is the
-// compensated sum over its slots of Inv + mu_e*Vmu + lambda_e*Vlam (mu, lambda from the
-// stage's element temperature, calcRHS.f90:49-51); U1 = U - rk_fact/M*RHS in FP64.
-// Nodes without a boundary condition keep U1 as updated and get their primitives in
-// FP32; boundary nodes follow the reference's FP64 primitive round trip and BC order.
+// subrutinas.f90:680-825 for one stage.  The node's RHS is the compensated sum over its
+// slots of Inv, formed in the first stage and kept per node, plus the compensated sum of
+// mu_e*Vmu + lambda_e*Vlam (mu, lambda from the stage's element T, calcRHS.f90:49-51);
+// delta = rk_fact/M*RHS in FP32; U1 = U - delta in FP64.  Nodes
+// without a boundary condition keep U1 as updated and get FP32 primitives; boundary nodes
+// follow the reference's FP64 primitive round trip and BC order.
+// Only T of stages 1-3 is read later (through mu, lambda of the next stage; U1 and the
+// other primitives are rewritten by stage 4), so stages 1-3 write T alone at nodes without
+// a boundary condition.  The last stage writes U1, every primitive and the hi/lo split of
+// U1 (the next step's U).
+template <bool FIRST, bool LAST>
 __global__ void __launch_bounds__(256)
 k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
-             const int4* __restrict__ elem, const SlotRec* __restrict__ rec,
-             const double* __restrict__ Tst, GasConst gc, int viscous,
-             const double* __restrict__ U, const double* __restrict__ invM, double rk_fact,
+             const float2* __restrict__ mulam, const float4* __restrict__ recInv,
+             const float4* __restrict__ recVisc, float4* __restrict__ invSum, GasConst gc,
+             GasConstF gf, int viscous,
+             const double* __restrict__ U, float4* __restrict__ Uhi, float4* __restrict__ Ulo,
+             const float* __restrict__ invM, float rk_fact,
              const unsigned char* __restrict__ bcflag, const double* __restrict__ bcval,
              const double2* __restrict__ nrm, const double* __restrict__ WX,
-             const double* __restrict__ WY, double* __restrict__ U1, double* __restrict__ RHO,
-             double* __restrict__ VX, double* __restrict__ VY, double* __restrict__ Eo,
-             double* __restrict__ Po, double* __restrict__ To, double* __restrict__ RMACH) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
+             const double* __restrict__ WY, double* __restrict__ U1, float* __restrict__ RHO, float* __restrict__ VX,
+             float* __restrict__ VY, float* __restrict__ Eo, float* __restrict__ Po,
+             float* __restrict__ Tout, float* __restrict__ RMACH) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npoin) return;
-    const float t_inf = (float)gc.t_inf, mu_ref = (float)gc.mu_ref, lam_ref = (float)gc.lambda_ref;
-    Acc a0, a1, a2, a3;
+    Acc a0, a1, a2, a3, v1, v2, v3;
     a0.init(); a1.init(); a2.init(); a3.init();
+    v1.init(); v2.init(); v3.init();
     const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
-    for (int s = s0; s < s1; ++s) {
-        const SlotRec rc = rec[s];
-        float c1 = rc.inv.y, c2 = rc.inv.z, c3 = rc.inv.w;
-        if (viscous) {
-            const int4 n = elem[esup_slot[s] / 3];
-            const float Ta = (float)((Tst[n.x] + Tst[n.y] + Tst[n.z]) * (1.0 / 3.0));
-            const float r15 = pow15f(Ta / t_inf);
-            const float mu = mu_ref * r15 * (t_inf + 110.f) / (Ta + 110.f);
-            const float lam = lam_ref * r15 * (t_inf + 194.f) / (Ta + 194.f);
-            c1 += mu * rc.visc.x;
-            c2 += mu * rc.visc.y;
-            c3 += mu * rc.visc.z + lam * rc.visc.w;
+    // four slots per pass: their loads are issued together, the sums stay in slot order
+    for (int s = s0; s < s1; s += 4) {
+        float4 ri[4], rv[4];
+        int e[4];
+        float2 ml[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (s + j < s1) {
+                if (FIRST) ri[j] = recInv[s + j];
+                if (viscous) {
+                    rv[j] = recVisc[s + j];
+                    e[j] = esup_slot[s + j] / 3;
+                }
+            }
         }
-        a0.add(rc.inv.x);
-        a1.add(c1);
-        a2.add(c2);
-        a3.add(c3);
+        if (viscous) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (s + j < s1) ml[j] = mulam[e[j]];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (s + j < s1) {
+                if (FIRST) {
+                    a0.add(ri[j].x);
+                    a1.add(ri[j].y);
+                    a2.add(ri[j].z);
+                    a3.add(ri[j].w);
+                }
+                if (viscous) {
+                    v1.add(ml[j].x * rv[j].x);
+                    v2.add(ml[j].x * rv[j].y);
+                    v3.add(ml[j].x * rv[j].z + ml[j].y * rv[j].w);
+                }
+            }
+        }
     }
-    const double r0 = a0.value(), r1 = a1.value(), r2 = a2.value(), r3 = a3.value();
-    const double2* u2 = reinterpret_cast<const double2*>(U + 4 * (size_t)p);
-    const double2 ua = u2[0], ub = u2[1];
-    const double f = rk_fact * invM[p];
-    double u1_0 = ua.x - f * r0, u1_1 = ua.y - f * r1, u1_2 = ub.x - f * r2, u1_3 = ub.y - f * r3;
-    const float g = (float)gc.gamma;
-    const double FR = gc.fr;
+    float4 inv;
+    if (FIRST) {
+        inv = make_float4(a0.value(), a1.value(), a2.value(), a3.value());
+        invSum[p] = inv;
+    } else {
+        inv = invSum[p];
+    }
+    const float f = rk_fact * invM[p];
+    const float d0 = f * inv.x, d1 = f * (inv.y + v1.value()), d2 = f * (inv.z + v2.value()),
+                d3 = f * (inv.w + v3.value());
+    const float g = gf.gamma;
     const unsigned char fl = bcflag[p];
     if (!fl) {
-        const float rho = (float)u1_0, ir = 1.f / rho;
-        const float vx = (float)u1_1 * ir, vy = (float)u1_2 * ir, ee = (float)u1_3 * ir;
+        const float4 h = Uhi[p];
+        const float rho = h.x - d0, ir = 1.f / rho;
+        const float vx = (h.y - d1) * ir, vy = (h.z - d2) * ir, ee = (h.w - d3) * ir;
         const float vel2 = vx * vx + vy * vy;
         const float pp = rho * (g - 1.f) * (ee - 0.5f * vel2);
-        const float tt = pp / (rho * (float)FR);
-        RHO[p] = u1_0; VX[p] = vx; VY[p] = vy; Eo[p] = ee; Po[p] = pp; To[p] = tt;
-        RMACH[p] = sqrtf(vel2 / (tt * g * (float)FR));
-    } else {
-        const double gd = gc.gamma;
+        const float tt = pp / (rho * gf.fr);
+        Tout[p] = tt;
+        if (!LAST) return;
+        RHO[p] = rho; VX[p] = vx; VY[p] = vy; Eo[p] = ee; Po[p] = pp;
+        RMACH[p] = sqrtf(vel2 / (tt * g * gf.fr));
+    }
+    const double2* u2 = reinterpret_cast<const double2*>(U + 4 * (size_t)p);
+    const double2 ua = u2[0], ub = u2[1];
+    double u1_0 = ua.x - (double)d0, u1_1 = ua.y - (double)d1, u1_2 = ub.x - (double)d2,
+           u1_3 = ub.y - (double)d3;
+    if (fl) {
+        const double gd = gc.gamma, FR = gc.fr;
         double rho = u1_0;
         double vx = u1_1 / rho, vy = u1_2 / rho, ee = u1_3 / rho;
         const double vel2 = vx * vx + vy * vy;
         const double pp = rho * (gd - 1.0) * (ee - 0.5 * vel2);
         double tt = pp / (rho * FR);
-        RMACH[p] = sqrt(vel2 / (tt * gd * FR));
-        Po[p] = pp;
+        RMACH[p] = (float)sqrt(vel2 / (tt * gd * FR));
+        Po[p] = (float)pp;
         const double2* b2 = reinterpret_cast<const double2*>(bcval + 4 * (size_t)p);
         const double2 bva = b2[0], bvb = b2[1];
         if (fl & BC_FIXV) { vx = bva.x; vy = bva.y; }
@@ -446,167 +551,170 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
             tt = bvb.y;
             ee = tt * FR / (gd - 1.0) + 0.5 * (vx * vx + vy * vy);
         }
-        RHO[p] = rho; VX[p] = vx; VY[p] = vy; Eo[p] = ee; To[p] = tt;
+        RHO[p] = (float)rho; VX[p] = (float)vx; VY[p] = (float)vy; Eo[p] = (float)ee;
+        Tout[p] = (float)tt;
         u1_0 = rho; u1_1 = vx * rho; u1_2 = vy * rho; u1_3 = ee * rho;
     }
     double2* o = reinterpret_cast<double2*>(U1 + 4 * (size_t)p);
     o[0] = make_double2(u1_0, u1_1);
     o[1] = make_double2(u1_2, u1_3);
+    if (LAST) {
+        float h[4], l[4];
+        split(u1_0, h[0], l[0]);
+        split(u1_1, h[1], l[1]);
+        split(u1_2, h[2], l[2]);
+        split(u1_3, h[3], l[3]);
+        Uhi[p] = make_float4(h[0], h[1], h[2], h[3]);
+        Ulo[p] = make_float4(l[0], l[1], l[2], l[3]);
+    }
 }
 
 // ------------------------------------------------------------------ geometry (mixed)
-// deriv (subrutinas.f90:99-115): area in FP64, gradients through one reciprocal.
-__global__ void k_deriv_mixed(int nelem, const int4* __restrict__ elem, const double* __restrict__ X,
-                              const double* __restrict__ Y, double* __restrict__ area,
-                              double* __restrict__ geo) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
+// Per element, 8 floats (two float4): geo[2e] = (dNx1, dNx2, dNx3, dNy1),
+// geo[2e+1] = (dNy2, dNy3, area, q) with q the mesh-Laplacian weight of the element.
+//
+// Element pass: deriv (subrutinas.f90:102-115) in FP32 from edge vectors of the hi/lo
+// coordinates (as accurate as FP64 differences rounded to FP32); the Laplacian weight of
+// mLaplace.f90:28-56: with |grad N_i|^2 = l_i^2/(2a)^2 the quality
+// mu = 2*sqrt(3)*(2a)/sum(l_i^2) of mLaplace.f90:96-108 is sqrt(3)/(a*sum|grad N_i|^2), so
+// q = 1/mu^2 = (a*sum|grad N_i|^2)^2/3; with gcl, the element terms of gcl main
+// (gcl.f90:27-45) divW*area/3 and divW_old*area_old/3, then putArea (area_old = area).
+__global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
+                                const float2* __restrict__ Xhi, const float2* __restrict__ Xlo,
+                                int gcl, int literal, const float2* __restrict__ W,
+                                const float2* __restrict__ Wold, int put_area,
+                                float* __restrict__ area_old, float* __restrict__ areaf,
+                                float4* __restrict__ geo, float2* __restrict__ terms) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nelem) return;
-    int4 n = elem[e];
-    const double x0 = X[n.x], x1 = X[n.y], x2 = X[n.z];
-    const double y0 = Y[n.x], y1 = Y[n.y], y2 = Y[n.z];
-    // 2a = (x1-x0)(y2-y0) - (x2-x0)(y1-y0): the same signed area from differences
-    const double a2 = (x1 - x0) * (y2 - y0) - (x2 - x0) * (y1 - y0);
-    area[e] = 0.5 * a2;
-    const double ia = 1.0 / a2;
-    const size_t E = (size_t)nelem;
-    geo[e] = (y1 - y2) * ia;
-    geo[E + e] = (y2 - y0) * ia;
-    geo[2 * E + e] = (y0 - y1) * ia;
-    geo[3 * E + e] = (x2 - x1) * ia;
-    geo[4 * E + e] = (x0 - x2) * ia;
-    geo[5 * E + e] = (x1 - x0) * ia;
-}
-
-// gcl main (gcl.f90:29-45) as two passes: per element divW*area/3 and divW_old*area_old/3
-// (FP64), then the node gather and M += dt*(tot1+tot2)/2; also 1/M for the RK update.
-__global__ void k_gcl_elem(int nelem, const int4* __restrict__ elem, const double* __restrict__ geo,
-                           const double* __restrict__ area, const double* __restrict__ area_old,
-                           const double* __restrict__ Wx, const double* __restrict__ Wy,
-                           const double* __restrict__ Wxo, const double* __restrict__ Wyo,
-                           int literal, double2* __restrict__ terms) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nelem) return;
-    const size_t E = (size_t)nelem;
-    int4 n = elem[e];
-    const int nn[3] = {n.x, n.y, n.z};
-    double divW = 0.0, divWo = 0.0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const double dx = geo[i * E + e], dy = geo[(3 + i) * E + e];
-        const double wy = literal ? Wx[nn[i]] : Wy[nn[i]];
-        const double wyo = literal ? Wxo[nn[i]] : Wyo[nn[i]];
-        divW += dx * Wx[nn[i]] + dy * wy;
-        divWo += dx * Wxo[nn[i]] + dy * wyo;
-    }
-    terms[e] = make_double2(divW * area[e] * (1.0 / 3.0), divWo * area_old[e] * (1.0 / 3.0));
-}
-
-__global__ void k_mass_mixed(int npoin, const int* __restrict__ esup_ptr,
-                             const int* __restrict__ esup_slot, const double* __restrict__ area,
-                             const double2* __restrict__ terms, const double* __restrict__ dtp,
-                             int gcl, double* __restrict__ M, double* __restrict__ invM) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npoin) return;
-    double m;
+    const int4 n = elem[e];
+    const float2 h0 = Xhi[n.x], h1 = Xhi[n.y], h2 = Xhi[n.z];
+    const float2 l0 = Xlo[n.x], l1 = Xlo[n.y], l2 = Xlo[n.z];
+    const float x1 = (h1.x - h0.x) + (l1.x - l0.x), y1 = (h1.y - h0.y) + (l1.y - l0.y);
+    const float x2 = (h2.x - h0.x) + (l2.x - l0.x), y2 = (h2.y - h0.y) + (l2.y - l0.y);
+    // 2a = x1*y2 - x2*y1 (the reference's signed area from differences to node 1)
+    const float a2f = fmaf(x1, y2, -(x2 * y1));
+    const float area = 0.5f * a2f;
+    const float ia = 1.f / a2f;
+    const float gx[3] = {(y1 - y2) * ia, y2 * ia, -y1 * ia};  // (y_2 - y_3)/(2a), ... with y_1 = 0
+    const float gy[3] = {(x2 - x1) * ia, -x2 * ia, x1 * ia};
+    const float s2 = gx[0] * gx[0] + gy[0] * gy[0] + gx[1] * gx[1] + gy[1] * gy[1] +
+                     gx[2] * gx[2] + gy[2] * gy[2];
+    const float am = area * s2;
+    const float q = am * am * (1.f / 3.f);
+    geo[2 * (size_t)e] = make_float4(gx[0], gx[1], gx[2], gy[0]);
+    geo[2 * (size_t)e + 1] = make_float4(gy[1], gy[2], area, q);
+    areaf[e] = area;
     if (gcl) {
-        double t1 = 0.0, t2 = 0.0;
-        for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) {
-            const double2 t = terms[esup_slot[s] / 3];
-            t1 += t.x;
-            t2 += t.y;
+        const int nn[3] = {n.x, n.y, n.z};
+        float divW = 0.f, divWo = 0.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float2 w = W[nn[i]], wo = Wold[nn[i]];
+            divW += gx[i] * w.x + gy[i] * (literal ? w.x : w.y);
+            divWo += gx[i] * wo.x + gy[i] * (literal ? wo.x : wo.y);
         }
-        m = M[p] + (*dtp) * (t1 + t2) * 0.5;
-    } else {
-        double acc = 0.0;
-        for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) acc += area[esup_slot[s] / 3];
-        m = acc * (1.0 / 3.0);
+        terms[e] = make_float2(divW * area * (1.f / 3.f), divWo * area_old[e] * (1.f / 3.f));
     }
-    M[p] = m;
-    invM[p] = 1.0 / m;
+    if (put_area) area_old[e] = area;
 }
 
-// mLaplace.f90:28-56 in arithmetic R (float by default), row owner, element-around-point
-// order; writes the values as float (valf) and double (vals)
-template <typename R>
-__global__ void k_laplace_mixed_t(int npoin, int nelem, const int4* __restrict__ elem,
-                                  const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
-                                  const uchar4* __restrict__ lap_pos, const double* __restrict__ geo,
-                                  const double* __restrict__ X, const double* __restrict__ Y,
-                                  const int* __restrict__ rowptr, float* __restrict__ valf,
-                                  double* __restrict__ vals, double* __restrict__ diag,
-                                  double* __restrict__ invdiag) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
+// Node pass: the row of the mesh Laplacian (mLaplace.f90:28-56; rows of up to 16 entries
+// are summed in shared memory, longer ones in place), 1/diag, and the lumped mass: MASAS
+// (subrutinas.f90:128-153) as a compensated FP32 sum of area/3, or the gcl update
+// M += dt*(tot1+tot2)/2 in FP64 from compensated FP32 sums of the element terms, followed
+// by putW (W_old = W).
+constexpr int kLapRow = 16;
+constexpr int kGeoBlock = kGeoNodeBlock;
+
+__global__ void __launch_bounds__(kGeoBlock)
+k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
+                const uchar4* __restrict__ lap_pos, const float4* __restrict__ geo,
+                const float2* __restrict__ terms, const double* __restrict__ dtp, int gcl,
+                const int* __restrict__ rowptr, float* __restrict__ valf,
+                double* __restrict__ invdiag, float* __restrict__ invdiagf,
+                double* __restrict__ M, float* __restrict__ invM,
+                const float2* __restrict__ W, float2* __restrict__ Wold) {
+    __shared__ float row[kGeoBlock][kLapRow + 1];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npoin) return;
-    const size_t E = (size_t)nelem;
+    float* acc = row[threadIdx.x];
     const int r0 = rowptr[p], r1 = rowptr[p + 1];
-    R acc[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) acc[k] = R(0);
     const int len = r1 - r0;
-    if (len > 16)
-        for (int k = r0; k < r1; ++k) vals[k] = 0.0;
+    const bool in_smem = len <= kLapRow;
+    if (in_smem) {
+#pragma unroll
+        for (int k = 0; k < kLapRow; ++k) acc[k] = 0.f;
+    } else {
+        for (int k = r0; k < r1; ++k) valf[k] = 0.f;
+    }
+    Acc m1, m2;
+    m1.init();
+    m2.init();
     for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) {
         const int slot = esup_slot[s];
         const int e = slot / 3, i = slot - 3 * e;
-        const int4 n = elem[e];
-        const double xa = X[n.x], ya = Y[n.x];
-        const R x1 = (R)(X[n.y] - xa), y1 = (R)(Y[n.y] - ya);
-        const R x2 = (R)(X[n.z] - xa), y2 = (R)(Y[n.z] - ya);
-        // mu = 2*sqrt(3)*(2*area)/(l1+l2+l3) (mLaplace.f90:96-108) from edge vectors
-        const R a2 = x1 * y2 - x2 * y1;
-        const R l = (x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1) + x2 * x2 + y2 * y2 + x1 * x1 + y1 * y1;
-        const R m = R(3.46410161513775) * a2 / l;
-        const R q = R(1) / (m * m);
-        const R dxi = (R)geo[i * E + e], dyi = (R)geo[(3 + i) * E + e];
+        const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
         const uchar4 pos = lap_pos[s];
+        if (gcl) {
+            const float2 t = terms[e];
+            m1.add(t.x);
+            m2.add(t.y);
+        } else {
+            m1.add(gb.z);
+        }
+        const float gx[3] = {ga.x, ga.y, ga.z}, gy[3] = {ga.w, gb.x, gb.y};
+        const float q = gb.w;
+        const float dxi = (i == 0) ? gx[0] : (i == 1 ? gx[1] : gx[2]);
+        const float dyi = (i == 0) ? gy[0] : (i == 1 ? gy[1] : gy[2]);
         const unsigned char pj[3] = {pos.x, pos.y, pos.z};
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const R v = (dxi * (R)geo[j * E + e] + dyi * (R)geo[(3 + j) * E + e]) * q;
-            if (len <= 16) {
-#pragma unroll
-                for (int k = 0; k < 16; ++k)
-                    if (k == pj[j]) acc[k] += v;
-            } else {
-                vals[r0 + pj[j]] += v;  // long rows: accumulate in place (rare)
-            }
+            const float v = (dxi * gx[j] + dyi * gy[j]) * q;
+            if (in_smem) acc[pj[j]] += v;
+            else valf[r0 + pj[j]] += v;  // long rows (rare)
         }
     }
-    if (len <= 16) {
-#pragma unroll
-        for (int k = 0; k < 16; ++k)
-            if (k < len) {
-                valf[r0 + k] = (float)acc[k];
-                vals[r0 + k] = (double)acc[k];
-            }
+    float diag;
+    if (in_smem) {
+        for (int k = 0; k < len; ++k) valf[r0 + k] = acc[k];
+        diag = acc[0];
     } else {
-        for (int k = r0; k < r1; ++k) valf[k] = (float)vals[k];
+        diag = valf[r0];
     }
-    diag[p] = vals[r0];
-    invdiag[p] = 1.0 / vals[r0];
+    const float idf = 1.f / diag;
+    invdiagf[p] = idf;
+    invdiag[p] = (double)idf;
+    double m;
+    if (gcl) {
+        m = M[p] + (*dtp) * ((double)m1.value() + (double)m2.value()) * 0.5;
+        Wold[p] = W[p];
+    } else {
+        m = (double)m1.value() * (1.0 / 3.0);
+    }
+    M[p] = m;
+    invM[p] = 1.f / (float)m;
 }
 
-cudaError_t launch_laplace_mixed(bool fp64, cudaStream_t st, int npoin, int nelem, const int4* elem,
-                                 const int* esup_ptr, const int* esup_slot, const uchar4* lap_pos,
-                                 const double* geo, const double* X, const double* Y,
-                                 const int* rowptr, float* valf, double* vals, double* diag,
-                                 double* invdiag) {
-    const unsigned grid = blocks_for(npoin, 128);
-    if (fp64)
-        k_laplace_mixed_t<double><<<grid, 128, 0, st>>>(npoin, nelem, elem, esup_ptr, esup_slot,
-                                                        lap_pos, geo, X, Y, rowptr, valf, vals,
-                                                        diag, invdiag);
-    else
-        k_laplace_mixed_t<float><<<grid, 128, 0, st>>>(npoin, nelem, elem, esup_ptr, esup_slot,
-                                                       lap_pos, geo, X, Y, rowptr, valf, vals, diag,
-                                                       invdiag);
-    g_launches.fetch_add(1, std::memory_order_relaxed);
-    return cudaGetLastError();
+// geo -> the FP64 dNx/dNy (column-major [6][nelem]) and area the download entries read
+__global__ void k_widen_geo(int nelem, const float4* __restrict__ geo, double* __restrict__ dN,
+                            double* __restrict__ area) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    const size_t E = (size_t)nelem;
+    const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
+    dN[e] = ga.x;
+    dN[E + e] = ga.y;
+    dN[2 * E + e] = ga.z;
+    dN[3 * E + e] = ga.w;
+    dN[4 * E + e] = gb.x;
+    dN[5 * E + e] = gb.y;
+    area[e] = gb.z;
 }
 
 // FORCES (meshMove.f90:167-192) with a block tree per set instead of the serial sum
 __global__ void k_forces_tree(int nset_numb, const int* __restrict__ set_ptr,
-                              const int2* __restrict__ set_edges, const double* __restrict__ P,
+                              const int2* __restrict__ set_edges, const float* __restrict__ P,
                               const double* __restrict__ X, const double* __restrict__ Y,
                               const double* __restrict__ xref, const double* __restrict__ yref,
                               StepScal* __restrict__ sc) {
@@ -616,7 +724,7 @@ __global__ void k_forces_tree(int nset_numb, const int* __restrict__ set_ptr,
         const double xr = xref[s], yr = yref[s];
         for (int k = set_ptr[s] + threadIdx.x; k < set_ptr[s + 1]; k += blockDim.x) {
             const int2 ed = set_edges[k];
-            const double d_press = (P[ed.x] + P[ed.y]) * 0.5;
+            const double d_press = ((double)P[ed.x] + (double)P[ed.y]) * 0.5;
             const double a = d_press * (Y[ed.y] - Y[ed.x]);
             const double b = d_press * (X[ed.x] - X[ed.y]);
             fx += a;
@@ -630,41 +738,75 @@ __global__ void k_forces_tree(int nset_numb, const int* __restrict__ set_ptr,
     }
 }
 
+// meshMove.f90:99-126: X += XPOS, W = XPOS/DTMIN (as XPOS*(1/DTMIN), the reciprocal formed
+// once by k_dt_finalize), with the float shadows of (X, Y) and W
+__global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos,
+                                      const double* __restrict__ ypos, const StepScal* __restrict__ sc,
+                                      double* __restrict__ X, double* __restrict__ Y,
+                                      double* __restrict__ WX, double* __restrict__ WY,
+                                      float2* __restrict__ Xhi, float2* __restrict__ Xlo,
+                                      float2* __restrict__ Wf) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npoin) return;
+    const double idt = sc->inv_dtmin;
+    const double xp = xpos[p], yp = ypos[p];
+    const double x = X[p] + xp, y = Y[p] + yp;
+    X[p] = x;
+    Y[p] = y;
+    const double wx = xp * idt, wy = yp * idt;
+    WX[p] = wx;
+    WY[p] = wy;
+    Wf[p] = make_float2((float)wx, (float)wy);
+    float hx, lx, hy, ly;
+    split(x, hx, lx);
+    split(y, hy, ly);
+    Xhi[p] = make_float2(hx, hy);
+    Xlo[p] = make_float2(lx, ly);
+}
+
 // ------------------------------------------------------------------ host launchers
 cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, const int4* elem,
-                                     const double* U, const double* geo, const double* area,
-                                     const float* shoc, const double* dtl_arr,
-                                     const double* dtl_scalar, const float* ts1, const float* ts2,
-                                     const float* ts3, GasConst gc, const double* WX,
-                                     const double* WY, const int* slot_pos, void* rec) {
+                                     const float4* Uhi, const float4* Ulo, const float4* geo,
+                                     const float* shoc, const StepScal* sc,
+                                     const float* ts1, const float* ts2, const float* ts3,
+                                     GasConstF gc, const float2* W, const int* slot_pos,
+                                     const float* T, float4* recInv, float4* recVisc,
+                                     float2* mulam) {
     const unsigned grid = blocks_for(nelem, 128);
     if (viscous)
-        k_elem_stage1_mixed<true><<<grid, 128, 0, st>>>(nelem, elem, U, geo, area, shoc, dtl_arr,
-                                                         dtl_scalar, ts1, ts2, ts3, gc, WX, WY,
-                                                         slot_pos, (SlotRec*)rec);
+        k_elem_stage1_mixed<true><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, shoc, sc, ts1,
+                                                         ts2, ts3, gc, W, slot_pos, T, recInv,
+                                                         recVisc, mulam);
     else
-        k_elem_stage1_mixed<false><<<grid, 128, 0, st>>>(nelem, elem, U, geo, area, shoc, dtl_arr,
-                                                          dtl_scalar, ts1, ts2, ts3, gc, WX, WY,
-                                                          slot_pos, (SlotRec*)rec);
+        k_elem_stage1_mixed<false><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, shoc, sc, ts1,
+                                                          ts2, ts3, gc, W, slot_pos, T, recInv,
+                                                          recVisc, mulam);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }
 
 cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, const int* esup_slot,
-                              const int4* elem, const void* rec, const double* T, GasConst gc,
-                              int viscous, const double* U, const double* invM, double rk_fact,
+                              const float2* mulam, const float4* recInv, const float4* recVisc,
+                              float4* invSum, int first_stage, GasConst gc, GasConstF gf,
+                              int viscous, const double* U, float4* Uhi, float4* Ulo,
+                              const float* invM, float rk_fact, int last_stage,
                               const unsigned char* bcflag, const double* bcval, const double2* nrm,
-                              const double* WX, const double* WY, double* U1, double* RHO,
-                              double* VX, double* VY, double* E, double* P, double* To,
-                              double* RMACH) {
-    k_node_mixed<<<blocks_for(npoin, 256), 256, 0, st>>>(npoin, esup_ptr, esup_slot, elem,
-                                                          (const SlotRec*)rec, T, gc, viscous, U,
-                                                          invM, rk_fact, bcflag, bcval, nrm, WX,
-                                                          WY, U1, RHO, VX, VY, E, P, To, RMACH);
+                              const double* WX, const double* WY, double* U1, float* RHO,
+                              float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH) {
+    const unsigned grid = blocks_for(npoin, 256);
+#define CFD_NODE_ARGS                                                                          \
+    npoin, esup_ptr, esup_slot, mulam, recInv, recVisc, invSum, gc, gf, viscous, U, Uhi, Ulo, invM, \
+        rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH
+    if (first_stage)
+        k_node_mixed<true, false><<<grid, 256, 0, st>>>(CFD_NODE_ARGS);
+    else if (last_stage)
+        k_node_mixed<false, true><<<grid, 256, 0, st>>>(CFD_NODE_ARGS);
+    else
+        k_node_mixed<false, false><<<grid, 256, 0, st>>>(CFD_NODE_ARGS);
+#undef CFD_NODE_ARGS
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }
 
-size_t slot_record_bytes() { return sizeof(SlotRec); }
 
 }  // namespace cfd

@@ -1,4 +1,4 @@
-// kernels_pcg.cu — biCG (biconjGrad.f90:117-171) as one persistent cooperative kernel.
+// kernels_pcg.cu — biCG (biconjGrad.f90:8-62) as one persistent cooperative kernel.
 //
 // The reference's solver is Jacobi-preconditioned CG with Dirichlet rows handled by
 // overwrite and a 1e30 penalty; every vector operation is a separate OpenMP loop and the
@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
     const unsigned nb = gridDim.x;
     auto part = [&](int buf, int s) { return a.part + ((long)buf * 2 + s) * nc; };
 
-    // copy1 (biconjGrad.f90:137): x(fix) = x_fix
+    // copy1 (biconjGrad.f90:28): x(fix) = x_fix
     for (int k = blockIdx.x * blockDim.x + t; k < a.nfix; k += gridDim.x * blockDim.x)
         for (int s = 0; s < ns; ++s) a.x[s][a.fix_node[k]] = 1.0 * a.fixval[s][a.fix_src[k]];
     grid_barrier(a.bar, nb);

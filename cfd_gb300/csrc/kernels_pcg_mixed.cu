@@ -1,36 +1,244 @@
-// kernels_pcg_mixed.cu — biCG (biconjGrad.f90:117-171) for the mixed-precision form.
+// kernels_pcg_mixed.cu — biCG (biconjGrad.f90:8-62) for the mixed-precision form.
 //
 // Same persistent two-phase iteration as k_pcg_fp64 (kernels_pcg.cu) with the matrix in
-// FP32 and the SpMV accumulated in FP32 over FP32 shadows of the search direction p and of
-// z; the vectors x, r, z, p, y, the Jacobi scaling (as a multiply by 1/diag), the dots (in
-// the fixed tree of cfd_common.cuh) and the scalars alfa, beta stay FP64.
+// FP32 and every SpMV accumulated in FP32 over FP32 shadows (of x for the initial residual,
+// of the search direction p and of z in the iterations); the vectors x, r, z, p, y, the
+// Jacobi scaling (as a multiply by 1/diag), the dots (in the fixed tree of cfd_common.cuh)
+// and the scalars alfa, beta stay FP64.
+//
+// One solve is three launches: k_bicg_fix_mixed (Dirichlet values into x and xf),
+// k_bicg_resid_mixed (the initial residual, one row per thread, with per-256-row partials
+// of r.r) and the persistent cooperative k_pcg_mixed (convergence test, iterations).  The
+// shadow xf of x must equal (float)x on entry; the kernels keep it so on exit (the
+// Dirichlet scatter writes both, and a solve that iterated refreshes xf from the final x).
 #include "cfd_kernels.cuh"
 
 namespace cfd {
 
-__device__ __forceinline__ double spmv_row_f(const PcgArgs& a, int i, const double* v) {
-    float dot = 0.f;
-    const int j1 = a.rowptr[i + 1];
-    for (int j = a.rowptr[i]; j < j1; ++j) dot += a.valf[j] * (float)v[a.col[j]];
-    return (double)dot;
+// The SpMV rows gather in batches of B entries (8 in the residual kernel, 4 in the
+// register-limited persistent kernel): the column indices and values of a batch are loaded
+// together, then the gathered vector entries, so each batch costs two dependent memory
+// latencies instead of two per entry.  The products are still summed in column order.
+
+// row i of A times (v0, v1): one pass over the row's columns for both right-hand sides
+template <int NS, int kRowBatch = 8>
+__device__ __forceinline__ void spmv_row2_f(const PcgArgs& a, int i, const float* v0,
+                                            const float* v1, float& d0, float& d1) {
+    float s0 = 0.f, s1 = 0.f;
+    const int j0 = a.rowptr[i], j1 = a.rowptr[i + 1];
+    for (int jb = j0; jb < j1; jb += kRowBatch) {
+        int c[kRowBatch];
+        float m[kRowBatch], x0[kRowBatch], x1[kRowBatch];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                c[u] = a.col[jb + u];
+                m[u] = a.valf[jb + u];
+            }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                x0[u] = v0[c[u]];
+                if (NS == 2) x1[u] = v1[c[u]];
+            }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                s0 += m[u] * x0[u];
+                if (NS == 2) s1 += m[u] * x1[u];
+            }
+    }
+    d0 = s0;
+    d1 = s1;
 }
 
-__device__ __forceinline__ double spmv_row_dir_f(const PcgArgs& a, int i, const float* pf,
-                                                 const float* zf, float beta) {
+template <int kRowBatch = 4>
+__device__ __forceinline__ float spmv_row_dir_f(const PcgArgs& a, int i, const float* pf,
+                                                const float* zf, float beta) {
     float dot = 0.f;
-    const int j1 = a.rowptr[i + 1];
-    for (int j = a.rowptr[i]; j < j1; ++j) {
-        const int c = a.col[j];
-        dot += a.valf[j] * (beta * pf[c] + zf[c]);
+    const int j0 = a.rowptr[i], j1 = a.rowptr[i + 1];
+    for (int jb = j0; jb < j1; jb += kRowBatch) {
+        int c[kRowBatch];
+        float m[kRowBatch], pv[kRowBatch], zv[kRowBatch];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                c[u] = a.col[jb + u];
+                m[u] = a.valf[jb + u];
+            }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                pv[u] = pf[c[u]];
+                zv[u] = zf[c[u]];
+            }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) dot += m[u] * (beta * pv[u] + zv[u]);
     }
-    return (double)dot;
+    return dot;
 }
 
 __device__ __forceinline__ bool bar_failed_m(GridBar* gb) {
     return *((volatile int*)&gb->err) != 0;
 }
 
-__global__ void __launch_bounds__(256) k_pcg_mixed(PcgArgs a) {
+// x(fix) = x_fix (biconjGrad.f90:28), in x and in its shadow
+__global__ void k_bicg_fix_mixed(PcgArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.nfix) return;
+    const int i = a.fix_node[k];
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+        if (s < a.nsolve) {
+            const double v = a.fixval[s][a.fix_src[k]];
+            a.x[s][i] = v;
+            a.xf[s][i] = (float)v;
+        }
+}
+
+// Sums of 256 doubles per block for the row kernels: nsum arrays of 256 values in shared
+// memory; warp w sums array w, lane l the values l, l+32, ..., l+224 in that order, then a
+// shuffle-down tree.  (One warp per sum keeps the FP64 adds few: FP64 runs at 1/64 of the
+// FP32 rate here.)  Result in lane 0 of warp w.
+__device__ __forceinline__ double warp_sum256(const double* v) {
+    const int l = threadIdx.x & 31;
+    double acc = v[l];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) acc = acc + v[l + 32 * k];
+    return warp_tree32(acc);
+}
+
+// The last block to finish (block counter) folds the nb per-block partials of each of the
+// nsum sums in a fixed order: lane t of the block sums partials t, t+256, ..., then the
+// 256-value sum above.  Returns true in the last block, with the sums in out[0..nsum).
+__device__ bool last_block_fold(unsigned* count, const double* part, long nb, int nsum,
+                                double (*sh)[256], double* out) {
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(count, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    const int t = threadIdx.x;
+    for (int w = 0; w < nsum; ++w) {
+        double acc = 0.0;
+        for (long c = t; c < nb; c += 256) acc = acc + __ldcg(part + w * nb + c);
+        sh[w][t] = acc;
+    }
+    __syncthreads();
+    if ((t >> 5) < nsum) {
+        const double v = warp_sum256(sh[t >> 5]);
+        if ((t & 31) == 0) out[t >> 5] = v;
+    }
+    __syncthreads();
+    if (t == 0) *count = 0u;
+    return true;
+}
+
+// First pass of a solve, one row per thread: y = A.x (FP32 SpMV over the shadow of x),
+// r = b - y with r(fix) = 0, p = r/diag (as r*(1/diag)); per-block partials of r.r and r.p
+// (biconjGrad.f90:29-38).  y itself is not kept: the next pass overwrites it.
+template <int NS>
+__device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) {
+    const int t = threadIdx.x;
+    const long i = blockIdx.x * (long)blockDim.x + t;
+    double rr[2] = {0.0, 0.0}, rp[2] = {0.0, 0.0};
+    if (i < a.n) {
+        const bool fx = a.isfix[i];
+        float d[2] = {0.f, 0.f};
+        if (!fx) spmv_row2_f<NS>(a, (int)i, a.xf[0], a.xf[1], d[0], d[1]);
+        const double id = a.invdiag[i];
+        const float idf = a.invdiagf[i];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            double r, p;
+            float pf;
+            if (fx) {
+                r = 0.0;
+                p = 0.0;
+                pf = 0.f;
+            } else if (a.b[s]) {
+                r = a.b[s][i] - (double)d[s];
+                p = r * id;
+                pf = (float)p;
+            } else {
+                r = (double)(-d[s]);
+                p = r * id;
+                pf = -d[s] * idf;
+            }
+            a.r[s][i] = r;
+            a.p[s][0][i] = p;
+            a.pf[s][0][i] = pf;
+            rr[s] = r * r;
+            rp[s] = r * p;
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        sh[s][t] = rr[s];
+        sh[2 + s][t] = rp[s];
+    }
+    __syncthreads();
+    if ((t >> 5) < 4) {
+        const double v = warp_sum256(sh[t >> 5]);
+        if ((t & 31) == 0) a.part_r[(t >> 5) * a.nblk_r + blockIdx.x] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bicg_resid_mixed(PcgArgs a) {
+    __shared__ double sh[4][256];
+    __shared__ double out[4];
+    if (a.nsolve == 2) first_rows<2>(a, sh);
+    else first_rows<1>(a, sh);
+    if (last_block_fold(&a.bcount[0], a.part_r, a.nblk_r, 4, sh, out) && threadIdx.x == 0)
+        for (int s = 0; s < 2; ++s) {
+            a.bscal[4 * s + 0] = out[s];      // r.r
+            a.bscal[4 * s + 1] = out[2 + s];  // r.p
+        }
+}
+
+// Second pass, for the solves with r.r >= tol: y = A.p (FP32 over the shadow), y(fix) =
+// 1e30 p(fix); per-block partials of p.y; the last block forms alfa = r.p / p.y
+// (biconjGrad.f90:39-43)
+__global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
+    __shared__ double sh[4][256];
+    __shared__ double out[4];
+    const int t = threadIdx.x;
+    bool act[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) act[s] = s < a.nsolve && !(a.bscal[4 * s] < a.tol);
+    if (!act[0] && !act[1]) return;  // the same in every block
+    const long i = blockIdx.x * (long)blockDim.x + t;
+    double py[2] = {0.0, 0.0};
+    if (i < a.n) {
+        const bool fx = a.isfix[i];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            if (!act[s]) continue;
+            const double pi = a.p[s][0][i];
+            const double yi = fx ? 1.0e30 * pi : (double)spmv_row_dir_f<8>(a, (int)i, a.pf[s][0], a.pf[s][0], 0.f);
+            a.y[s][i] = yi;
+            py[s] = pi * yi;
+        }
+    }
+    sh[0][t] = py[0];
+    sh[1][t] = py[1];
+    __syncthreads();
+    if ((t >> 5) < 2) {
+        const double v = warp_sum256(sh[t >> 5]);
+        if ((t & 31) == 0) a.part_r[(t >> 5) * a.nblk_r + blockIdx.x] = v;
+    }
+    if (last_block_fold(&a.bcount[1], a.part_r, a.nblk_r, 2, sh, out) && t == 0)
+        for (int s = 0; s < 2; ++s)
+            if (act[s]) {
+                a.bscal[4 * s + 2] = out[s];
+                a.bscal[4 * s + 3] = a.bscal[4 * s + 1] / out[s];
+            }
+}
+
+__global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
     __shared__ double red[9];
     const int t = threadIdx.x;
     const int n = a.n;
@@ -39,112 +247,39 @@ __global__ void __launch_bounds__(256) k_pcg_mixed(PcgArgs a) {
     const unsigned nb = gridDim.x;
     auto part = [&](int buf, int s) { return a.part + ((long)buf * 2 + s) * nc; };
 
-    for (int k = blockIdx.x * blockDim.x + t; k < a.nfix; k += gridDim.x * blockDim.x)
-        for (int s = 0; s < ns; ++s) a.x[s][a.fix_node[k]] = a.fixval[s][a.fix_src[k]];
-    grid_barrier(a.bar, nb);
-    if (bar_failed_m(a.bar)) return;
-
-    // y = A.x; y(fix) = 1e30 x(fix); r = b - y; r(fix) = 0; r.r
-    for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-        double acc[2] = {0.0, 0.0};
-        for (int k = 0; k < 4; ++k) {
-            const long i = c * kChunk + t + 256L * k;
-            if (i >= n) break;
-            const bool fx = a.isfix[i];
-            for (int s = 0; s < ns; ++s) {
-                const double yi = fx ? 1.0e30 * a.x[s][i] : spmv_row_f(a, (int)i, a.x[s]);
-                a.y[s][i] = yi;
-                const double ri = fx ? 0.0 : (a.b[s] ? a.b[s][i] : 0.0) - yi;
-                a.r[s][i] = ri;
-                acc[s] = (k == 0) ? ri * ri : acc[s] + ri * ri;
-            }
-        }
-        for (int s = 0; s < ns; ++s) {
-            const double v = block_tree256(acc[s], red);
-            if (t == 0) part(0, s)[c] = v;
-        }
-    }
-    grid_barrier(a.bar, nb);
-    if (bar_failed_m(a.bar)) return;
+    // x(fix), r, p, err = r.p, y = A.p and alfa come from k_bicg_fix_mixed,
+    // k_bicg_resid_mixed and k_bicg_dir_mixed
     bool done[2] = {true, true};
     double err_old[2] = {0.0, 0.0}, alfa[2] = {0.0, 0.0};
-    for (int s = 0; s < ns; ++s) {
-        const double rr = fold_partials(part(0, s), nc, red);
-        done[s] = rr < a.tol;
-        if (done[s] && blockIdx.x == 0 && t == 0) {
-            a.iters_out[s] = 0;
-            a.rz_out[s] = rr;
-            a.conv_out[s] = 1;
-        }
-    }
-    if (done[0] && (ns < 2 || done[1])) return;
-
-    // p = r/diag; err = r.p
-    for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-        double acc[2] = {0.0, 0.0};
-        for (int k = 0; k < 4; ++k) {
-            const long i = c * kChunk + t + 256L * k;
-            if (i >= n) break;
-            const double id = a.invdiag[i];
-            for (int s = 0; s < ns; ++s) {
-                if (done[s]) continue;
-                const double ri = a.r[s][i];
-                const double pi = ri * id;
-                a.p[s][0][i] = pi;
-                a.pf[s][0][i] = (float)pi;
-                acc[s] = (k == 0) ? ri * pi : acc[s] + ri * pi;
-            }
-        }
-        for (int s = 0; s < ns; ++s) {
-            if (done[s]) continue;
-            const double v = block_tree256(acc[s], red);
-            if (t == 0) part(1, s)[c] = v;
-        }
-    }
-    grid_barrier(a.bar, nb);
-    if (bar_failed_m(a.bar)) return;
-    double err_new[2] = {0.0, 0.0};
-    for (int s = 0; s < ns; ++s)
-        if (!done[s]) err_new[s] = fold_partials(part(1, s), nc, red);
-
-    // y = A.p (FP32 over the shadow); py = p.y
-    for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-        double acc[2] = {0.0, 0.0};
-        for (int k = 0; k < 4; ++k) {
-            const long i = c * kChunk + t + 256L * k;
-            if (i >= n) break;
-            const bool fx = a.isfix[i];
-            for (int s = 0; s < ns; ++s) {
-                if (done[s]) continue;
-                const double pi = a.p[s][0][i];
-                const double yi = fx ? 1.0e30 * pi : spmv_row_dir_f(a, (int)i, a.pf[s][0], a.pf[s][0], 0.f);
-                a.y[s][i] = yi;
-                acc[s] = (k == 0) ? pi * yi : acc[s] + pi * yi;
-            }
-        }
-        for (int s = 0; s < ns; ++s) {
-            if (done[s]) continue;
-            const double v = block_tree256(acc[s], red);
-            if (t == 0) part(0, s)[c] = v;
-        }
-    }
-    grid_barrier(a.bar, nb);
-    if (bar_failed_m(a.bar)) return;
     bool pend[2] = {false, false};
     int cur[2] = {0, 0};
-    for (int s = 0; s < ns; ++s) {
-        if (done[s]) continue;
-        const double py = fold_partials(part(0, s), nc, red);
-        alfa[s] = err_new[s] / py;
-        err_old[s] = err_new[s];
-        pend[s] = true;
-    }
+    double err_new[2] = {0.0, 0.0};
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+        if (s < ns) {
+            const double rr = a.bscal[4 * s];
+            done[s] = rr < a.tol;
+            if (done[s]) {
+                if (blockIdx.x == 0 && t == 0) {
+                    a.iters_out[s] = 0;
+                    a.rz_out[s] = rr;
+                    a.conv_out[s] = 1;
+                }
+            } else {
+                err_new[s] = a.bscal[4 * s + 1];
+                alfa[s] = a.bscal[4 * s + 3];
+                err_old[s] = err_new[s];
+                pend[s] = true;
+            }
+        }
+    if (done[0] && done[1]) return;
 
     int k = 0;
     int last_iter[2] = {0, 0};
     while (true) {
         bool act[2] = {false, false};
-        for (int s = 0; s < ns; ++s) act[s] = !done[s] && fabs(err_old[s]) > a.tol && k < a.maxit;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) act[s] = !done[s] && fabs(err_old[s]) > a.tol && k < a.maxit;
         if (!act[0] && !act[1]) break;
         k = k + 1;
         // phase 1: x += alfa p; r -= alfa y; z = r/diag; r.z
@@ -154,7 +289,8 @@ __global__ void __launch_bounds__(256) k_pcg_mixed(PcgArgs a) {
                 const long i = c * kChunk + t + 256L * kk;
                 if (i >= n) break;
                 const double id = a.invdiag[i];
-                for (int s = 0; s < ns; ++s) {
+#pragma unroll
+                for (int s = 0; s < 2; ++s) {
                     if (pend[s]) a.x[s][i] += alfa[s] * a.p[s][cur[s]][i];
                     if (!act[s]) continue;
                     const double ri = a.r[s][i] - alfa[s] * a.y[s][i];
@@ -165,17 +301,20 @@ __global__ void __launch_bounds__(256) k_pcg_mixed(PcgArgs a) {
                     acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
                 }
             }
-            for (int s = 0; s < ns; ++s) {
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
                 if (!act[s]) continue;
                 const double v = block_tree256(acc[s], red);
                 if (t == 0) part(1, s)[c] = v;
             }
         }
-        for (int s = 0; s < ns; ++s) pend[s] = false;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) pend[s] = false;
         grid_barrier(a.bar, nb);
         if (bar_failed_m(a.bar)) return;
         double beta[2] = {0.0, 0.0};
-        for (int s = 0; s < ns; ++s) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
             if (!act[s]) continue;
             err_new[s] = fold_partials(part(1, s), nc, red);
             beta[s] = err_new[s] / err_old[s];
@@ -187,18 +326,21 @@ __global__ void __launch_bounds__(256) k_pcg_mixed(PcgArgs a) {
                 const long i = c * kChunk + t + 256L * kk;
                 if (i >= n) break;
                 const bool fx = a.isfix[i];
-                for (int s = 0; s < ns; ++s) {
+#pragma unroll
+                for (int s = 0; s < 2; ++s) {
                     if (!act[s]) continue;
                     const double pn = beta[s] * a.p[s][cur[s]][i] + a.z[s][i];
-                    const double yi = fx ? 1.0e30 * pn
-                                         : spmv_row_dir_f(a, (int)i, a.pf[s][cur[s]], a.zf[s], (float)beta[s]);
+                    const double yi =
+                        fx ? 1.0e30 * pn
+                           : (double)spmv_row_dir_f(a, (int)i, a.pf[s][cur[s]], a.zf[s], (float)beta[s]);
                     a.p[s][cur[s] ^ 1][i] = pn;
                     a.pf[s][cur[s] ^ 1][i] = (float)pn;
                     a.y[s][i] = yi;
                     acc[s] = (kk == 0) ? pn * yi : acc[s] + pn * yi;
                 }
             }
-            for (int s = 0; s < ns; ++s) {
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
                 if (!act[s]) continue;
                 const double v = block_tree256(acc[s], red);
                 if (t == 0) part(0, s)[c] = v;
@@ -206,7 +348,8 @@ __global__ void __launch_bounds__(256) k_pcg_mixed(PcgArgs a) {
         }
         grid_barrier(a.bar, nb);
         if (bar_failed_m(a.bar)) return;
-        for (int s = 0; s < ns; ++s) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
             if (!act[s]) continue;
             const double py = fold_partials(part(0, s), nc, red);
             alfa[s] = err_new[s] / py;
@@ -216,15 +359,25 @@ __global__ void __launch_bounds__(256) k_pcg_mixed(PcgArgs a) {
             last_iter[s] = k;
         }
     }
+    // last deferred x update; the shadow follows x for the solves that iterated
     for (long c = blockIdx.x; c < nc; c += gridDim.x)
         for (int kk = 0; kk < 4; ++kk) {
             const long i = c * kChunk + t + 256L * kk;
             if (i >= n) break;
-            for (int s = 0; s < ns; ++s)
-                if (pend[s]) a.x[s][i] += alfa[s] * a.p[s][cur[s]][i];
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                if (done[s]) continue;
+                double xi = a.x[s][i];
+                if (pend[s]) {
+                    xi += alfa[s] * a.p[s][cur[s]][i];
+                    a.x[s][i] = xi;
+                }
+                a.xf[s][i] = (float)xi;
+            }
         }
     if (blockIdx.x == 0 && t == 0)
-        for (int s = 0; s < ns; ++s) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
             if (done[s]) continue;
             a.iters_out[s] = last_iter[s];
             a.rz_out[s] = fabs(err_old[s]);

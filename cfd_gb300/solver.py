@@ -9,7 +9,7 @@ Drop-in routines keep the reference's names, argument order, array layout (U(4,n
     ESTAB(...), deltat(...), deriv(...), MASAS(...)            subrutinas.f90:332/155/88/128
     gcl_main(...)                                              gcl.f90:8
     getEsup / getPsup / laplace_pattern / laplace              pointNeighbor.f90, mLaplace.f90
-    biCG(spMtx, spIdx, spRowptr, diagMtx, x, b, x_fix, x_fixIdx)  biconjGrad.f90:117
+    biCG(spMtx, spIdx, spRowptr, diagMtx, x, b, x_fix, x_fixIdx)  biconjGrad.f90:8
 
 `Solver` is PROGRAM NSComp2D (ns2DComp.ALE.f90:8-282) over a resident GPU context.
 Every call runs the sm_103a kernels; a failing status raises abi.CfdError.
@@ -171,7 +171,7 @@ def laplace(inpoel, area, dNx, dNy, X, Y, lap_idx, lap_rowptr):
 
 
 def biCG(spMtx, spIdx, spRowptr, diagMtx, x, b, x_fix, x_fixIdx, tol=1.0e-10, maxit=1000):
-    """x (initial guess, copied) -> (solution, CfdSolveInfo) (biconjGrad.f90:117-171)."""
+    """x (initial guess, copied) -> (solution, CfdSolveInfo) (biconjGrad.f90:8-62)."""
     L = abi.lib()
     x = _f64(x).copy()
     info = abi.CfdSolveInfo()

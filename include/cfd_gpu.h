@@ -92,8 +92,8 @@ typedef struct cfd_params {
     double heave_amp, pitch_amp, motion_freq;
     int mass_mode;            /* CFD_MASS_*                                            */
     int guess_mode;           /* CFD_GUESS_*                                           */
-    double bicg_tol;          /* 1e-10 in biconjGrad.f90:135 (absolute, on r.z)        */
-    int bicg_maxit;           /* 1000 in biconjGrad.f90:156                            */
+    double bicg_tol;          /* 1e-10 in biconjGrad.f90:26 (absolute, on r.z)         */
+    int bicg_maxit;           /* 1000 in biconjGrad.f90:47                             */
     int estab_mode;           /* CFD_ESTAB_*                                           */
     int reserved[6];
 } cfd_params;
@@ -128,7 +128,7 @@ typedef struct cfd_step_report {
 } cfd_step_report;
 
 typedef struct cfd_solve_info {
-    int iters;                /* k of biconjGrad.f90:156                               */
+    int iters;                /* k of biconjGrad.f90:47-48                             */
     int converged;            /* 1 if |r.z| <= tol (or early exit at :144)             */
     double rz;                /* final |r.z|                                           */
 } cfd_solve_info;
@@ -202,7 +202,7 @@ int cfd_laplace(const int* inpoel, const double* area, const double* dNx, const 
                 double* lap_sparse, const int* lap_idx, const int* lap_rowptr,
                 double* lap_diag);
 
-/* biCG (biconjGrad.f90:117-171): Jacobi-preconditioned CG with Dirichlet rows by
+/* biCG (biconjGrad.f90:8-62): Jacobi-preconditioned CG with Dirichlet rows by
  * overwrite + 1e30 penalty.  x is the initial guess on entry, the solution on exit.
  * tol/maxit as the reference (1e-10 absolute on |r.z|, 1000) unless overridden by
  * cfd_bicg_ex.  info may be NULL.  Returns CFD_OK also when the cap is hit (like the

@@ -524,7 +524,7 @@ void or_laplace(const int* inpoel, const double* dNx, const double* dNy, int nel
     }
 }
 
-// vecdot (biconjGrad.f90:262-278) with its OpenMP REDUCTION(+) order pinned to a fixed
+// vecdot (biconjGrad.f90:153-169) with its OpenMP REDUCTION(+) order pinned to a fixed
 // tree: chunks of 1024 products (256 lanes x 4 strided terms, then a 32-lane shuffle-down
 // tree per warp and an 8-way tree over warps); chunk partials folded by 256 lanes with a
 // stride of 256, then the same 256-lane tree.  The GPU kernels take exactly this order.
@@ -568,7 +568,7 @@ double or_vecdot(int n, const double* x, const double* y) {
     return tree256(s);
 }
 
-// biCG: biconjGrad.f90:117-171 (+ vecdiv/vecsum/assign2/copy1/copy2/SpMV :173-299)
+// biCG: biconjGrad.f90:8-62 (+ vecdiv/vecsum/assign2/copy1/copy2/SpMV :64-190)
 void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
              const double* diagMtx, double* x, const double* b, const double* x_fix,
              const int* x_fixIdx, int npoin, int nfix, double tol, int maxit,
