@@ -36,6 +36,44 @@ inline unsigned blocks_for(long n, int threads) {
     return (unsigned)(b > 0 ? b : 1);
 }
 
+// ------------------------------------------------------------------ FP32 <-> FP64 by bits
+// GB300's FP64 pipe (1/64 of the FP32 rate) also executes the F2F conversions, so the
+// mixed-precision kernels move values between the two formats with integer operations.
+//   f2d_bits:  exact for normal floats, zeros, infinities and NaNs; a subnormal float (below
+//              1.2e-38) becomes a zero of the same sign.
+//   d2f_trunc: the significand truncated to 24 bits (error below 1 ulp of the float);
+//              magnitudes below the float normal range give a signed zero, above it an
+//              infinity.
+//   split_bits: hi = d2f_trunc(v), lo = d2f_trunc(v - hi); the subtraction is exact, and
+//              hi + lo equals v to within 2^-47 |v|.
+__device__ __forceinline__ double f2d_bits(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned long long frac = (unsigned long long)(u & 0x7fffffu) << 29;
+    if (e == 0u) return __longlong_as_double((long long)sign);
+    const unsigned long long ex = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);
+    return __longlong_as_double((long long)(sign | (ex << 52) | frac));
+}
+
+__device__ __forceinline__ float d2f_trunc(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7ffull);
+    const unsigned frac = (unsigned)((b >> 29) & 0x7fffffull);
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (frac ? 0x400000u : 0u));
+    const int fe = e - 896;
+    if (fe <= 0) return __uint_as_float(sign);
+    if (fe >= 0xff) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)fe << 23) | frac);
+}
+
+__device__ __forceinline__ void split_bits(double v, float& hi, float& lo) {
+    hi = d2f_trunc(v);
+    const double hd = __longlong_as_double(__double_as_longlong(v) & ~0x1fffffffLL);
+    lo = d2f_trunc(v - hd);
+}
+
 // ------------------------------------------------------------------ fixed-order sums
 // The dot-product order every FP64 reduction of this library takes (and the oracle's
 // or_vecdot restates): chunks of 1024 terms, lane t of a 256-thread block sums terms

@@ -578,10 +578,9 @@ int Ctx::step_once_mixed() {
                d_Wf, d_areaf, (float)prm.fsafe, (float)prm.t_inf, &d_scal->dtmin32_bits, d_blockmin);
     {
         const int nchunk = (int)blocks_for(E, TB);
-        const int grid = std::min(nchunk, 2 * nsm);
-        CFD_LAUNCH(k_deltat_refine, grid, TB, 0, stream, E, d_elem, d_Tf, d_VXf, d_VYf, d_Wf,
-                   d_areaf, (const unsigned long long*)d_blockmin, nchunk, (float)prm.fsafe,
-                   (float)prm.t_inf, d_scal);
+        CFD_LAUNCH(k_deltat_refine, blocks_for(nchunk, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf,
+                   d_VYf, d_Wf, d_areaf, (const unsigned long long*)d_blockmin, nchunk,
+                   (float)prm.fsafe, (float)prm.t_inf, d_scal);
     }
     CFD_LAUNCH(k_dt_finalize, 1, 1, 0, stream, d_scal);
     tstop(TM_DELTAT);

@@ -24,6 +24,10 @@ namespace cfd {
 
 __device__ __forceinline__ float pow15f(float x) { return x * sqrtf(x); }
 
+// FP32 quotients of these kernels: __fdividef (within 2 ulp), several times fewer
+// instructions than the IEEE quotient in kernels that are instruction-issue bound
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+
 // Neumaier-compensated float accumulator
 struct Acc {
     float s, c;
@@ -37,11 +41,8 @@ struct Acc {
     __device__ __forceinline__ float value() const { return s + c; }
 };
 
-// hi/lo split of a double: hi = RN32(v), lo = RN32(v - hi)
-__device__ __forceinline__ void split(double v, float& hi, float& lo) {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
-}
+// hi/lo split of a double (split_bits of cfd_common.cuh)
+__device__ __forceinline__ void split(double v, float& hi, float& lo) { split_bits(v, hi, lo); }
 
 // ------------------------------------------------------------------ float shadows
 // U -> (Uhi, Ulo); T, VX, VY -> float; (X, Y) -> (Xhi, Xlo); W -> Wf.  Any input may be NULL.
@@ -102,11 +103,11 @@ __device__ __forceinline__ float dtelem_f32(const int4 n, const float* __restric
     }
     const float hh = sqrtf(2.f * area);
     const float vel = sqrtf(vumax * vumax + vvmax * vvmax);
-    const float et = 0.017f * pow15f(T_iel / t_inf) * (t_inf + 110.f) / (T_iel + 110.f);
-    const float alpha = fminf((vel * hh) / (2.f * et) / 3.f, 1.f);
-    const float a = 4.f * et / (hh * hh);
+    const float et = 0.017f * pow15f(fdiv(T_iel, t_inf)) * fdiv(t_inf + 110.f, T_iel + 110.f);
+    const float alpha = fminf(fdiv(vel * hh, 2.f * et) * (1.f / 3.f), 1.f);
+    const float a = fdiv(4.f * et, hh * hh);
     // FSAFE/(1/DELTATC + 1/DELTATU) with 1/DELTATC = a, 1/DELTATU = a + alpha*vel/hh
-    return fsafe / (a + (a + alpha * vel / hh));
+    return fdiv(fsafe, a + (a + fdiv(alpha * vel, hh)));
 }
 
 // subrutinas.f90:170-210 in FP32: the FP32 minimum (bit pattern of a positive double)
@@ -118,7 +119,7 @@ __global__ void k_deltat_mixed(int nelem, const int4* __restrict__ elem, const f
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long mybits = 0x7ff0000000000000ull;
     if (e < nelem) {
-        const double d = (double)dtelem_f32(elem[e], T, VX, VY, W, areaf[e], fsafe, t_inf);
+        const double d = f2d_bits(dtelem_f32(elem[e], T, VX, VY, W, areaf[e], fsafe, t_inf));
         if (d < 1.0e20 && d > 0.0) mybits = (unsigned long long)__double_as_longlong(d);
     }
 #pragma unroll
@@ -139,9 +140,8 @@ __global__ void k_deltat_mixed(int nelem, const int4* __restrict__ elem, const f
 
 // Second pass: elements whose FP32 DTELEM is within 1e-4 of the FP32 minimum get their
 // DTELEM in FP64 (subrutinas.f90:172-206); the FP64 minimum over them is DTMIN, so the 1%
-// hysteresis of ns2DComp.ALE.f90:146-156 sees an FP64-accurate value.  The elements are
-// visited in the 256-element chunks of k_deltat_mixed (blockDim.x = 256), and only chunks
-// whose FP32 minimum lies in the band.
+// hysteresis of ns2DComp.ALE.f90:146-156 sees an FP64-accurate value.  Only the
+// 256-element chunks of k_deltat_mixed whose FP32 minimum lies in the band are visited.
 __device__ __forceinline__ void refine_one(int e, const int4* __restrict__ elem,
                                            const float* __restrict__ T, const float* __restrict__ VX,
                                            const float* __restrict__ VY, const float2* __restrict__ W,
@@ -175,11 +175,19 @@ __global__ void k_deltat_refine(int nelem, const int4* __restrict__ elem, const 
                                 const float2* __restrict__ W, const float* __restrict__ areaf,
                                 const unsigned long long* __restrict__ block_min, int nchunk,
                                 float fsafe, float t_inf, StepScal* __restrict__ sc) {
+    // thread t tests chunk blockIdx.x*256 + t; the block then refines the listed chunks
+    __shared__ int list[256];
+    __shared__ int nlist;
     const double m32 = __longlong_as_double((long long)sc->dtmin32_bits);
     const double band = m32 * (1.0 + 1.0e-4);
-    for (int b = blockIdx.x; b < nchunk; b += gridDim.x) {
-        if (__longlong_as_double((long long)block_min[b]) > band) continue;
-        const int e = b * blockDim.x + threadIdx.x;
+    if (threadIdx.x == 0) nlist = 0;
+    __syncthreads();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nchunk && !(__longlong_as_double((long long)block_min[c]) > band))
+        list[atomicAdd(&nlist, 1)] = c;
+    __syncthreads();
+    for (int k = 0; k < nlist; ++k) {
+        const int e = list[k] * 256 + threadIdx.x;
         if (e < nelem) refine_one(e, elem, T, VX, VY, W, areaf, fsafe, t_inf, m32, sc);
     }
 }
@@ -224,9 +232,10 @@ __global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const fl
         duy = vel2 * DY[0] + vel2 * DY[1] + vel2 * DY[2];
     }
     const float du2 = sqrtf(dux * dux + duy * duy) + 1.0e-20f;
-    float rtx = dtx / dt2, rty = dty / dt2;
-    float rjx = drx / dr2, rjy = dry / dr2;
-    float rux = dux / du2, ruy = duy / du2;
+    const float idt2 = fdiv(1.f, dt2), idr2 = fdiv(1.f, dr2), idu2 = fdiv(1.f, du2);
+    float rtx = dtx * idt2, rty = dty * idt2;
+    float rjx = drx * idr2, rjy = dry * idr2;
+    float rux = dux * idu2, ruy = duy * idu2;
     if (estab_mode == CFD_ESTAB_REGULARIZED) {
         float ge = 0.f;
 #pragma unroll
@@ -243,7 +252,7 @@ __global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const fl
         ruy = diry;
     }
     const float c = sqrtf(gm * FR * temp);
-    const float fmu = 0.017f * pow15f(temp / TINF) * (TINF + 110.f) / (temp + 110.f);
+    const float fmu = 0.017f * pow15f(fdiv(temp, TINF)) * fdiv(TINF + 110.f, temp + 110.f);
     float tau = 0.f, h_rgne = 0.f, h_rgn = 0.f, h_jgn = 0.f;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -254,23 +263,24 @@ __global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const fl
         h_rgn += fabsf(rux * DX[i] + ruy * DY[i]);
         h_jgn += term2;
     }
-    tau = 1.f / tau;
-    h_rgne = 2.f / h_rgne;
-    h_rgn = 2.f / h_rgn;
+    tau = fdiv(1.f, tau);
+    h_rgne = fdiv(2.f, h_rgne);
+    h_rgn = fdiv(2.f, h_rgn);
     if (!(h_rgn <= 10.f)) h_rgn = 0.f;  // > 10 (and inf from 2/0) -> 0
-    h_jgn = 2.f / h_jgn;
+    h_jgn = fdiv(2.f, h_jgn);
     if (!(h_jgn <= 10.f)) h_jgn = 0.f;
-    const float tr1 = dr2 * h_jgn / rho_elem;
-    const float zzz = h_jgn / (2.f * c);
+    const float tr1 = fdiv(dr2 * h_jgn, rho_elem);
+    const float zzz = fdiv(h_jgn, 2.f * c);
     SHOC[e] = (tr1 + tr1 * tr1) * 0.5f * (c * c) * zzz;
-    const float resumen = 1.f / (tau * tau) + (2.f / DTMIN) * (2.f / DTMIN);
+    const float two_dt = fdiv(2.f, DTMIN);
+    const float resumen = fdiv(1.f, tau * tau) + two_dt * two_dt;
     const float rrr = rsqrtf(resumen);
-    const float k4 = 4.f * fmu / RHOINF;
+    const float k4 = fdiv(4.f * fmu, RHOINF);
     // (resumen + 1/tau_s^2)^(-1/2), tau_s = h^2/k4, is (resumen + k4^2/h^4)^(-1/2); h = 0 -> 0
     const float hr2 = h_rgn * h_rgn, he2 = h_rgne * h_rgne;
     TS1[e] = rrr;
-    TS2[e] = (hr2 > 0.f) ? rsqrtf(resumen + (k4 * k4) / (hr2 * hr2)) : 0.f;
-    TS3[e] = (he2 > 0.f) ? rsqrtf(resumen + (k4 * k4) / (he2 * he2)) : 0.f;
+    TS2[e] = (hr2 > 0.f) ? rsqrtf(resumen + fdiv(k4 * k4, hr2 * hr2)) : 0.f;
+    TS3[e] = (he2 > 0.f) ? rsqrtf(resumen + fdiv(k4 * k4, he2 * he2)) : 0.f;
 }
 
 // ------------------------------------------------------------------ element mu, lambda
@@ -279,9 +289,9 @@ __device__ __forceinline__ float2 elem_mu_lambda(const int4 n, const float* __re
                                                  const GasConstF& gc) {
     const float t_inf = gc.t_inf;
     const float Ta = (T[n.x] + T[n.y] + T[n.z]) * (1.f / 3.f);
-    const float r15 = pow15f(Ta / t_inf);
-    return make_float2(gc.mu_ref * r15 * (t_inf + 110.f) / (Ta + 110.f),
-                       gc.lambda_ref * r15 * (t_inf + 194.f) / (Ta + 194.f));
+    const float r15 = pow15f(fdiv(Ta, t_inf));
+    return make_float2(gc.mu_ref * r15 * fdiv(t_inf + 110.f, Ta + 110.f),
+                       gc.lambda_ref * r15 * fdiv(t_inf + 194.f, Ta + 194.f));
 }
 
 // mu, lambda of every element from the T of the previous RK stage (stages 2-4)
@@ -353,7 +363,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 #pragma unroll
         for (int q = 0; q < 4; ++q) Uk[q] = 0.5f * (Un[ia][q] + Un[ib][q]);
         const float rho = Uk[0];
-        const float irho = 1.f / rho;
+        const float irho = fdiv(1.f, rho);
         const float v1 = Uk[1] * irho, v2 = Uk[2] * irho, ev = Uk[3] * irho;
         const float V_sq = v1 * v1 + v2 * v2;
         const float W0 = V_sq * gm1 - ev * g;
@@ -386,7 +396,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
             }
         if (VISCOUS) {
             // K1, K2 of calcRHS.f90:121-132 split as mu*(...) + lambda*(...)
-            const float icv = 1.f / (Cv * rho);
+            const float icv = fdiv(1.f, Cv * rho);
             const float m11 = (2.f / 3.f) * (-2.f * Ux[0] * v1 + 2.f * Ux[1] + Uy[0] * v2 - Uy[2]) * irho;
             const float m12 = (-Ux[0] * v2 + Ux[2] - Uy[0] * v1 + Uy[1]) * irho;
             const float m22 = (2.f / 3.f) * (Ux[0] * v1 - Ux[1] - 2.f * Uy[0] * v2 + 2.f * Uy[2]) * irho;
@@ -513,20 +523,20 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
     const unsigned char fl = bcflag[p];
     if (!fl) {
         const float4 h = Uhi[p];
-        const float rho = h.x - d0, ir = 1.f / rho;
+        const float rho = h.x - d0, ir = fdiv(1.f, rho);
         const float vx = (h.y - d1) * ir, vy = (h.z - d2) * ir, ee = (h.w - d3) * ir;
         const float vel2 = vx * vx + vy * vy;
         const float pp = rho * (g - 1.f) * (ee - 0.5f * vel2);
-        const float tt = pp / (rho * gf.fr);
+        const float tt = fdiv(pp, rho * gf.fr);
         Tout[p] = tt;
         if (!LAST) return;
         RHO[p] = rho; VX[p] = vx; VY[p] = vy; Eo[p] = ee; Po[p] = pp;
-        RMACH[p] = sqrtf(vel2 / (tt * g * gf.fr));
+        RMACH[p] = sqrtf(fdiv(vel2, tt * g * gf.fr));
     }
     const double2* u2 = reinterpret_cast<const double2*>(U + 4 * (size_t)p);
     const double2 ua = u2[0], ub = u2[1];
-    double u1_0 = ua.x - (double)d0, u1_1 = ua.y - (double)d1, u1_2 = ub.x - (double)d2,
-           u1_3 = ub.y - (double)d3;
+    double u1_0 = ua.x - f2d_bits(d0), u1_1 = ua.y - f2d_bits(d1), u1_2 = ub.x - f2d_bits(d2),
+           u1_3 = ub.y - f2d_bits(d3);
     if (fl) {
         const double gd = gc.gamma, FR = gc.fr;
         double rho = u1_0;
@@ -595,7 +605,7 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
     // 2a = x1*y2 - x2*y1 (the reference's signed area from differences to node 1)
     const float a2f = fmaf(x1, y2, -(x2 * y1));
     const float area = 0.5f * a2f;
-    const float ia = 1.f / a2f;
+    const float ia = fdiv(1.f, a2f);
     const float gx[3] = {(y1 - y2) * ia, y2 * ia, -y1 * ia};  // (y_2 - y_3)/(2a), ... with y_1 = 0
     const float gy[3] = {(x2 - x1) * ia, -x2 * ia, x1 * ia};
     const float s2 = gx[0] * gx[0] + gy[0] * gy[0] + gx[1] * gx[1] + gy[1] * gy[1] +
@@ -684,16 +694,16 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     }
     const float idf = 1.f / diag;
     invdiagf[p] = idf;
-    invdiag[p] = (double)idf;
+    invdiag[p] = f2d_bits(idf);
     double m;
     if (gcl) {
-        m = M[p] + (*dtp) * ((double)m1.value() + (double)m2.value()) * 0.5;
+        m = M[p] + (*dtp) * (f2d_bits(m1.value()) + f2d_bits(m2.value())) * 0.5;
         Wold[p] = W[p];
     } else {
-        m = (double)m1.value() * (1.0 / 3.0);
+        m = f2d_bits(m1.value()) * (1.0 / 3.0);
     }
     M[p] = m;
-    invM[p] = 1.f / (float)m;
+    invM[p] = 1.f / d2f_trunc(m);
 }
 
 // geo -> the FP64 dNx/dNy (column-major [6][nelem]) and area the download entries read
@@ -756,7 +766,7 @@ __global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos
     const double wx = xp * idt, wy = yp * idt;
     WX[p] = wx;
     WY[p] = wy;
-    Wf[p] = make_float2((float)wx, (float)wy);
+    Wf[p] = make_float2(d2f_trunc(wx), d2f_trunc(wy));
     float hx, lx, hy, ly;
     split(x, hx, lx);
     split(y, hy, ly);

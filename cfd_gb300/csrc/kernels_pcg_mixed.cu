@@ -1,16 +1,17 @@
 // kernels_pcg_mixed.cu — biCG (biconjGrad.f90:8-62) for the mixed-precision form.
 //
-// Same persistent two-phase iteration as k_pcg_fp64 (kernels_pcg.cu) with the matrix in
-// FP32 and every SpMV accumulated in FP32 over FP32 shadows (of x for the initial residual,
-// of the search direction p and of z in the iterations); the vectors x, r, z, p, y, the
-// Jacobi scaling (as a multiply by 1/diag), the dots (in the fixed tree of cfd_common.cuh)
-// and the scalars alfa, beta stay FP64.
+// The matrix is FP32 and every SpMV accumulates in FP32 over FP32 shadows (of x for the
+// first residual, of the search direction p and of z in the iterations); the vectors x, r,
+// z, p, y, the Jacobi scaling (as a multiply by 1/diag), the dots and the scalars alfa,
+// beta stay FP64.
 //
-// One solve is three launches: k_bicg_fix_mixed (Dirichlet values into x and xf),
-// k_bicg_resid_mixed (the initial residual, one row per thread, with per-256-row partials
-// of r.r) and the persistent cooperative k_pcg_mixed (convergence test, iterations).  The
-// shadow xf of x must equal (float)x on entry; the kernels keep it so on exit (the
-// Dirichlet scatter writes both, and a solve that iterated refreshes xf from the final x).
+// A solve is four launches: k_bicg_fix_mixed (Dirichlet values into x and its shadow),
+// k_bicg_resid_mixed (r = b - A.x, p = r/diag, r.r and r.p), k_bicg_dir_mixed (y = A.p,
+// p.y, alfa) — row kernels with one row per thread whose last block folds the per-block
+// sums — and the persistent cooperative k_pcg_mixed (convergence test and iterations).
+// The shadow xf of x (d2f_trunc of cfd_common.cuh) must match x on entry; the kernels keep
+// it so on exit (the Dirichlet scatter writes both, and a solve that iterated refreshes xf
+// from the final x).
 #include "cfd_kernels.cuh"
 
 namespace cfd {
@@ -93,7 +94,7 @@ __global__ void k_bicg_fix_mixed(PcgArgs a) {
         if (s < a.nsolve) {
             const double v = a.fixval[s][a.fix_src[k]];
             a.x[s][i] = v;
-            a.xf[s][i] = (float)v;
+            a.xf[s][i] = d2f_trunc(v);
         }
 }
 
@@ -160,11 +161,11 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
                 p = 0.0;
                 pf = 0.f;
             } else if (a.b[s]) {
-                r = a.b[s][i] - (double)d[s];
+                r = a.b[s][i] - f2d_bits(d[s]);
                 p = r * id;
-                pf = (float)p;
+                pf = d2f_trunc(p);
             } else {
-                r = (double)(-d[s]);
+                r = f2d_bits(-d[s]);
                 p = r * id;
                 pf = -d[s] * idf;
             }
@@ -218,7 +219,8 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
         for (int s = 0; s < 2; ++s) {
             if (!act[s]) continue;
             const double pi = a.p[s][0][i];
-            const double yi = fx ? 1.0e30 * pi : (double)spmv_row_dir_f<8>(a, (int)i, a.pf[s][0], a.pf[s][0], 0.f);
+            const double yi =
+                fx ? 1.0e30 * pi : f2d_bits(spmv_row_dir_f<8>(a, (int)i, a.pf[s][0], a.pf[s][0], 0.f));
             a.y[s][i] = yi;
             py[s] = pi * yi;
         }
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
                     const double zi = ri * id;
                     a.r[s][i] = ri;
                     a.z[s][i] = zi;
-                    a.zf[s][i] = (float)zi;
+                    a.zf[s][i] = d2f_trunc(zi);
                     acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
                 }
             }
@@ -313,11 +315,13 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
         grid_barrier(a.bar, nb);
         if (bar_failed_m(a.bar)) return;
         double beta[2] = {0.0, 0.0};
+        float betaf[2] = {0.f, 0.f};
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (!act[s]) continue;
             err_new[s] = fold_partials(part(1, s), nc, red);
             beta[s] = err_new[s] / err_old[s];
+            betaf[s] = d2f_trunc(beta[s]);
         }
         // phase 2: p_new = beta p + z (FP64 for the row, FP32 shadow for the SpMV); y = A p_new
         for (long c = blockIdx.x; c < nc; c += gridDim.x) {
@@ -332,9 +336,9 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
                     const double pn = beta[s] * a.p[s][cur[s]][i] + a.z[s][i];
                     const double yi =
                         fx ? 1.0e30 * pn
-                           : (double)spmv_row_dir_f(a, (int)i, a.pf[s][cur[s]], a.zf[s], (float)beta[s]);
+                           : f2d_bits(spmv_row_dir_f(a, (int)i, a.pf[s][cur[s]], a.zf[s], betaf[s]));
                     a.p[s][cur[s] ^ 1][i] = pn;
-                    a.pf[s][cur[s] ^ 1][i] = (float)pn;
+                    a.pf[s][cur[s] ^ 1][i] = d2f_trunc(pn);
                     a.y[s][i] = yi;
                     acc[s] = (kk == 0) ? pn * yi : acc[s] + pn * yi;
                 }
@@ -372,7 +376,7 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
                     xi += alfa[s] * a.p[s][cur[s]][i];
                     a.x[s][i] = xi;
                 }
-                a.xf[s][i] = (float)xi;
+                a.xf[s][i] = d2f_trunc(xi);
             }
         }
     if (blockIdx.x == 0 && t == 0)
