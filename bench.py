@@ -42,6 +42,9 @@ def parse():
                     help="skip the plain-FP64 timing and the mixed-vs-FP64 error")
     ap.add_argument("--scale", type=int, default=None, help="nr = ntheta (reduced-size runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="instead of the benchmark: run the mixed and the FP64 forms side by "
+                         "side for this many steps and print their state and force errors")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only run warmup + this many steps (for ncu captures)")
     return ap.parse_args()
@@ -259,6 +262,38 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def main_accuracy(args):
+    """Mixed form against the FP64 form (same ESTAB mode) on the workload, stepped in
+    lockstep: state rel L2 per conserved variable every 100 steps and at the end, and the
+    pressure-force (lift, drag) error over the run relative to the largest FP64 force."""
+    from cfd_gb300 import abi, build, solver
+    build.build()
+    km, kd = workload(args), workload(args)
+    for k in (km, kd):
+        k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
+    Sm = solver.Solver(km, precision=abi.CFD_PREC_MIXED)
+    Sd = solver.Solver(kd, precision=abi.CFD_PREC_FP64)
+    fmax, ferr, hist = 0.0, [0.0, 0.0], []
+    for s in range(1, args.accuracy_steps + 1):
+        rm, rd = Sm.step(1), Sd.step(1)
+        fmax = max(fmax, abs(rd.fx[0]), abs(rd.fy[0]))
+        ferr[0] = max(ferr[0], abs(rm.fx[0] - rd.fx[0]))
+        ferr[1] = max(ferr[1], abs(rm.fy[0] - rd.fy[0]))
+        if s % 100 == 0 or s == args.accuracy_steps:
+            Um, Ud = Sm.state()["U"], Sd.state()["U"]
+            hist.append({"step": s, "rel_l2": [rel_l2(Um[:, q], Ud[:, q]) for q in range(4)],
+                         "finite": bool(np.isfinite(Um).all() and np.isfinite(Ud).all())})
+    Sm.close()
+    Sd.close()
+    line = {"accuracy": "mixed vs fp64", "workload": config_dict(km, args, 1)["workload"],
+            "npoin": km.npoin, "steps": args.accuracy_steps, "estab_mode": "regularized",
+            "final_rel_l2": hist[-1]["rel_l2"] if hist else None,
+            "max_rel_l2": [max(h["rel_l2"][q] for h in hist) for q in range(4)] if hist else None,
+            "force_err_rel_max": [e / fmax if fmax > 0 else None for e in ferr],
+            "history": hist}
+    print(json.dumps(line), flush=True)
+
+
 def main_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -396,5 +431,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         main_reference(a)
+    elif a.accuracy_steps > 0:
+        main_accuracy(a)
     else:
         main_ours(a)

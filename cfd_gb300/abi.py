@@ -26,6 +26,7 @@ CFD_ESTAB_REFERENCE, CFD_ESTAB_EXACT, CFD_ESTAB_REGULARIZED = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
 
 
 class CfdParams(C.Structure):
@@ -114,6 +115,21 @@ SIGNATURES = {
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                           C.c_double, C.c_int, C.c_void_p,
                                           C.POINTER(CfdSolveInfo)]),
+    "cfd_mpnn_nparams": (C.c_int, []),
+    "cfd_mpnn_create": (C.c_int, [C.POINTER(_P), _fp]),
+    "cfd_mpnn_destroy": (None, [_P]),
+    "cfd_mpnn_get_weights": (C.c_int, [_P, _fp]),
+    "cfd_mpnn_set_weights": (C.c_int, [_P, _fp]),
+    "cfd_mpnn_adam_state": (C.c_int, [_P, _fp, _fp, _ip]),
+    "cfd_mpnn_graph_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int, _ip, _dp, _dp, C.c_int,
+                                        _ip, _ip]),
+    "cfd_mpnn_graph_destroy": (None, [_P]),
+    "cfd_mpnn_graph_set_bc": (C.c_int, [_P, _dp, _dp]),
+    "cfd_mpnn_graph_globals": (C.c_int, [_P, _dp]),
+    "cfd_mpnn_graph_set_target": (C.c_int, [_P, _dp, _dp, _dp]),
+    "cfd_mpnn_loss_grad": (C.c_int, [_P, _P, _fp, _fp]),
+    "cfd_mpnn_train_step": (C.c_int, [_P, _P, C.c_float, _fp]),
+    "cfd_mpnn_forward": (C.c_int, [_P, _P, C.c_int, _dp, _dp]),
     "cfd_ctx_create": (C.c_int, [C.POINTER(_P), C.POINTER(CfdMesh), C.POINTER(CfdParams),
                                  C.c_int]),
     "cfd_ctx_destroy": (None, [_P]),

@@ -26,6 +26,8 @@ UNITS = [
     ("context.cu", ["--fmad=false"]),
     ("abi.cu", ["--fmad=false"]),
     ("noalloc.cu", ["--fmad=false"]),
+    ("kernels_mpnn.cu", []),
+    ("mpnn.cu", []),
     ("host_prep.cpp", []),
 ]
 

@@ -24,8 +24,10 @@ namespace cfd {
 
 __device__ __forceinline__ float pow15f(float x) { return x * sqrtf(x); }
 
-// FP32 quotients of these kernels: __fdividef (within 2 ulp), several times fewer
-// instructions than the IEEE quotient in kernels that are instruction-issue bound
+// FP32 quotients of the stabilisation, time-step and Sutherland kernels: __fdividef
+// (within 2 ulp), several times fewer instructions than the IEEE quotient in kernels that
+// are instruction-issue bound.  The RHS element kernel and the node update keep IEEE
+// quotients.
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
 // Neumaier-compensated float accumulator
@@ -363,7 +365,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 #pragma unroll
         for (int q = 0; q < 4; ++q) Uk[q] = 0.5f * (Un[ia][q] + Un[ib][q]);
         const float rho = Uk[0];
-        const float irho = fdiv(1.f, rho);
+        const float irho = 1.f / rho;
         const float v1 = Uk[1] * irho, v2 = Uk[2] * irho, ev = Uk[3] * irho;
         const float V_sq = v1 * v1 + v2 * v2;
         const float W0 = V_sq * gm1 - ev * g;
@@ -396,7 +398,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
             }
         if (VISCOUS) {
             // K1, K2 of calcRHS.f90:121-132 split as mu*(...) + lambda*(...)
-            const float icv = fdiv(1.f, Cv * rho);
+            const float icv = 1.f / (Cv * rho);
             const float m11 = (2.f / 3.f) * (-2.f * Ux[0] * v1 + 2.f * Ux[1] + Uy[0] * v2 - Uy[2]) * irho;
             const float m12 = (-Ux[0] * v2 + Ux[2] - Uy[0] * v1 + Uy[1]) * irho;
             const float m22 = (2.f / 3.f) * (Ux[0] * v1 - Ux[1] - 2.f * Uy[0] * v2 + 2.f * Uy[2]) * irho;
@@ -523,11 +525,11 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
     const unsigned char fl = bcflag[p];
     if (!fl) {
         const float4 h = Uhi[p];
-        const float rho = h.x - d0, ir = fdiv(1.f, rho);
+        const float rho = h.x - d0, ir = 1.f / rho;
         const float vx = (h.y - d1) * ir, vy = (h.z - d2) * ir, ee = (h.w - d3) * ir;
         const float vel2 = vx * vx + vy * vy;
         const float pp = rho * (g - 1.f) * (ee - 0.5f * vel2);
-        const float tt = fdiv(pp, rho * gf.fr);
+        const float tt = pp / (rho * gf.fr);
         Tout[p] = tt;
         if (!LAST) return;
         RHO[p] = rho; VX[p] = vx; VY[p] = vy; Eo[p] = ee; Po[p] = pp;

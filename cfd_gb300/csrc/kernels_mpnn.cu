@@ -1,0 +1,725 @@
+// kernels_mpnn.cu — kernels of the learned mesh-motion guess (mpnn.cuh): boundary
+// statistics and features, the FP32 training forward and backward passes, Adam, and the
+// BF16 tensor-core inference pass.
+//
+// Graph arrays: ptr/nbr = CSR point neighbours (0-based, symmetric); src[k] = the source
+// node of edge k = (src[k] -> nbr[k]); rev[k] = the index of the reverse edge.
+// Reductions over nodes or edges (weight gradients, loss) go through per-block partials
+// folded in a fixed order, so a training step is deterministic.
+#include <algorithm>
+
+#include "mpnn_kernels.cuh"
+
+namespace cfd {
+namespace mpnn {
+
+// ------------------------------------------------------------------ globals and features
+__device__ __forceinline__ double block_max256(double v, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double w = lane < 8 ? red[lane] : 0.0;
+#pragma unroll
+        for (int off = 4; off > 0; off >>= 1) w = fmax(w, __shfl_down_sync(0xffffffffu, w, off));
+        if (lane == 0) red[8] = w;
+    }
+    __syncthreads();
+    const double r = red[8];
+    __syncthreads();
+    return r;
+}
+
+// One block of 256 threads.  Boundary nodes are listed in bnode[0..nb) with their kind and
+// prescribed displacement (gx, gy).  Body geometry (c, L, R) and the least-squares affine
+// fit g = t + M d, d = p - c, over the body nodes: since sum d = 0, t = mean g and each row
+// of M solves [Sxx Sxy; Sxy Syy] m = [sum g d_x; sum g d_y].
+__global__ void k_globals(int nb, const int* __restrict__ bnode, const int* __restrict__ bkind,
+                          const double* __restrict__ gx, const double* __restrict__ gy,
+                          const double* __restrict__ X, const double* __restrict__ Y,
+                          Globals* __restrict__ G) {
+    __shared__ double red[9];
+    const int t = threadIdx.x;
+    double nbody = 0, sx = 0, sy = 0, sgx = 0, sgy = 0, nout = 0;
+    for (int k = t; k < nb; k += 256) {
+        const int p = bnode[k];
+        if (bkind[k] == KIND_BODY) {
+            nbody += 1.0;
+            sx += X[p];
+            sy += Y[p];
+            sgx += gx[k];
+            sgy += gy[k];
+        } else {
+            nout += 1.0;
+        }
+    }
+    nbody = block_tree256(nbody, red);
+    sx = block_tree256(sx, red);
+    sy = block_tree256(sy, red);
+    sgx = block_tree256(sgx, red);
+    sgy = block_tree256(sgy, red);
+    nout = block_tree256(nout, red);
+    const double inb = nbody > 0 ? 1.0 / nbody : 0.0;
+    const double cx = sx * inb, cy = sy * inb;
+    double rmax = 0, rsum = 0, sxx = 0, sxy = 0, syy = 0, gxdx = 0, gxdy = 0, gydx = 0, gydy = 0;
+    for (int k = t; k < nb; k += 256) {
+        const int p = bnode[k];
+        const double dx = X[p] - cx, dy = Y[p] - cy;
+        const double r = sqrt(dx * dx + dy * dy);
+        if (bkind[k] == KIND_BODY) {
+            rmax = fmax(rmax, r);
+            sxx += dx * dx;
+            sxy += dx * dy;
+            syy += dy * dy;
+            gxdx += gx[k] * dx;
+            gxdy += gx[k] * dy;
+            gydx += gy[k] * dx;
+            gydy += gy[k] * dy;
+        } else {
+            rsum += r;
+        }
+    }
+    rmax = block_max256(rmax, red);
+    rsum = block_tree256(rsum, red);
+    sxx = block_tree256(sxx, red);
+    sxy = block_tree256(sxy, red);
+    syy = block_tree256(syy, red);
+    gxdx = block_tree256(gxdx, red);
+    gxdy = block_tree256(gxdy, red);
+    gydx = block_tree256(gydx, red);
+    gydy = block_tree256(gydy, red);
+    if (t == 0) {
+        Globals g;
+        g.cx = cx;
+        g.cy = cy;
+        g.L = rmax > 0 ? 2.0 * rmax : 1.0;
+        g.R = nout > 0 ? rsum / nout : g.L;
+        g.tx = sgx * inb;
+        g.ty = sgy * inb;
+        const double det = sxx * syy - sxy * sxy;
+        const double id = det > 0 ? 1.0 / det : 0.0;
+        g.m11 = (syy * gxdx - sxy * gxdy) * id;
+        g.m12 = (sxx * gxdy - sxy * gxdx) * id;
+        g.m21 = (syy * gydx - sxy * gydy) * id;
+        g.m22 = (sxx * gydy - sxy * gydx) * id;
+        // second-moment ellipse: eigenvalues of [sxx sxy; sxy syy] / nbody
+        const double hx = 0.5 * (sxx - syy) * inb, mxy = sxy * inb, tr = 0.5 * (sxx + syy) * inb;
+        const double rt = sqrt(hx * hx + mxy * mxy);
+        g.ea = sqrt(2.0 * (tr + rt));
+        g.eb = sqrt(fmax(2.0 * (tr - rt), 0.0));
+        const double al = 0.5 * atan2(2.0 * mxy, 2.0 * hx);
+        g.ec = cos(al);
+        g.es = sin(al);
+        *G = g;
+    }
+}
+
+// per-node prescribed displacement (0 at free nodes) from the boundary list
+__global__ void k_scatter_bc(int nb, const int* __restrict__ bnode, const double* __restrict__ gx,
+                             const double* __restrict__ gy, double* __restrict__ gnx,
+                             double* __restrict__ gny) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nb) return;
+    gnx[bnode[k]] = gx[k];
+    gny[bnode[k]] = gy[k];
+}
+
+// Geometry-only node features: position, log-radius, boundary kinds, and the three fields
+// of a continuum model of the mesh-motion operator, which the network corrects.  The
+// operator's entries grad N_i . grad N_j q carry no area factor (mLaplace.f90:40, 48), so in
+// the continuum it is div(k grad u) with k ~ 1/(element area), k ~ 1/r^2 on O-grids whose
+// spacing grows with r.  For a circular body of radius a = L/2 inside a circle of radius R:
+// Phi = (R^2 - r^2)/(R^2 - a^2) (clamped to [0, 1]) and Psi = psi(rho) d / rho with
+// psi(r) = a ((r/R)^p - (r/R)^q) / ((a/R)^p - (a/R)^q), p, q = 1 +- sqrt(2), over L, where
+// rho = r a / r_b(theta) stretches the body's second-moment ellipse (radius r_b along the
+// node's direction) onto the circle of radius a, so that Psi = d on the body.  Feature 9 is
+// the ellipse's aspect ratio.
+__global__ void k_features(int n, const double* __restrict__ X, const double* __restrict__ Y,
+                           const int* __restrict__ kind, const Globals* __restrict__ G,
+                           float* __restrict__ f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Globals g = *G;
+    const double dx = X[i] - g.cx, dy = Y[i] - g.cy;
+    const double r2 = dx * dx + dy * dy, r = sqrt(r2);
+    const double a = 0.5 * g.L, R = g.R;
+    float* o = f + (size_t)i * F_IN;
+    o[0] = (float)(dx / g.L);
+    o[1] = (float)(dy / g.L);
+    o[2] = (float)log(r / g.L + 1e-6);
+    o[3] = (float)log(R / g.L);
+    o[4] = kind[i] == KIND_BODY ? 1.f : 0.f;
+    o[5] = kind[i] == KIND_OUTER ? 1.f : 0.f;
+    const double sq2 = 1.4142135623730951, p = 1.0 + sq2, q = 1.0 - sq2;
+    double phi = 0.0, c = 0.0;
+    if (R > a && r < R) {
+        phi = (R * R - r2) / (R * R - a * a);
+        const double rs = fmax(r, 1e-6 * g.L);
+        // body radius along the node's direction (frame of the ellipse's axes)
+        const double u = (dx * g.ec + dy * g.es) / rs, v = (-dx * g.es + dy * g.ec) / rs;
+        const double rb = g.ea * g.eb / fmax(sqrt(g.eb * g.eb * u * u + g.ea * g.ea * v * v), 1e-300);
+        const double rho = fmin(rs * a / fmax(rb, 1e-6 * g.L), 0.999999 * R);
+        const double rr = rho / R, ar = a / R;
+        const double psi = a * (pow(rr, p) - pow(rr, q)) / (pow(ar, p) - pow(ar, q));
+        c = psi / rho;
+    }
+    o[6] = (float)fmin(fmax(phi, 0.0), 1.0);
+    o[7] = (float)(c * dx / g.L);
+    o[8] = (float)(c * dy / g.L);
+    o[9] = (float)(g.ea > 0 ? g.eb / g.ea : 1.0);
+}
+
+__global__ void k_edge_features(int m, const int* __restrict__ src, const int* __restrict__ nbr,
+                                const double* __restrict__ X, const double* __restrict__ Y,
+                                const Globals* __restrict__ G, float* __restrict__ e) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    const int i = src[k], j = nbr[k];
+    const double dx = X[j] - X[i], dy = Y[j] - Y[i];
+    const double ln = sqrt(dx * dx + dy * dy);
+    e[3 * (size_t)k] = (float)(dx / ln);
+    e[3 * (size_t)k + 1] = (float)(dy / ln);
+    e[3 * (size_t)k + 2] = (float)log(ln / G->L);
+}
+
+// ------------------------------------------------------------------ FP32 dense layers
+// Y[n][O] = [X1 | X2][n][I1 + I2] . W^T + b   (W: O x (I1+I2) row-major; b may be null)
+__global__ void __launch_bounds__(128) k_dense(int n, const float* __restrict__ X1, int I1,
+                                               const float* __restrict__ X2, int I2,
+                                               const float* __restrict__ W,
+                                               const float* __restrict__ b, int O,
+                                               float* __restrict__ Y) {
+    __shared__ float xs[DT][2 * HID + 1];
+    const int I = I1 + I2;
+    const int base = blockIdx.x * DT;
+    for (int q = threadIdx.x; q < DT * I; q += blockDim.x) {
+        const int r = q / I, k = q - r * I, node = base + r;
+        float v = 0.f;
+        if (node < n) v = (k < I1) ? X1[(size_t)node * I1 + k] : X2[(size_t)node * I2 + (k - I1)];
+        xs[r][k] = v;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < O; o += blockDim.x) {
+        float acc[DT];
+        const float bo = b ? b[o] : 0.f;
+#pragma unroll
+        for (int r = 0; r < DT; ++r) acc[r] = bo;
+        for (int k = 0; k < I; ++k) {
+            const float wv = W[(size_t)o * I + k];
+#pragma unroll
+            for (int r = 0; r < DT; ++r) acc[r] += wv * xs[r][k];
+        }
+#pragma unroll
+        for (int r = 0; r < DT; ++r)
+            if (base + r < n) Y[(size_t)(base + r) * O + o] = acc[r];
+    }
+}
+
+// dX[n][I] = dY[n][O] . W   (W: O x I row-major)
+__global__ void __launch_bounds__(128) k_dense_t(int n, const float* __restrict__ dY, int O,
+                                                 const float* __restrict__ W, int I,
+                                                 float* __restrict__ dX) {
+    __shared__ float ys[DT][2 * HID + 1];
+    const int base = blockIdx.x * DT;
+    for (int q = threadIdx.x; q < DT * O; q += blockDim.x) {
+        const int r = q / O, o = q - r * O, node = base + r;
+        ys[r][o] = node < n ? dY[(size_t)node * O + o] : 0.f;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < I; k += blockDim.x) {
+        float acc[DT];
+#pragma unroll
+        for (int r = 0; r < DT; ++r) acc[r] = 0.f;
+        for (int o = 0; o < O; ++o) {
+            const float wv = W[(size_t)o * I + k];
+#pragma unroll
+            for (int r = 0; r < DT; ++r) acc[r] += wv * ys[r][o];
+        }
+#pragma unroll
+        for (int r = 0; r < DT; ++r)
+            if (base + r < n) dX[(size_t)(base + r) * I + k] = acc[r];
+    }
+}
+
+// Weight gradient partials over chunks of WG rows: part[chunk][O*I (+O)] =
+// sum_r dY[r][o] X[r][k] (and sum_r dY[r][o] for the bias)
+__global__ void __launch_bounds__(256) k_wgrad(int n, const float* __restrict__ dY, int O,
+                                               const float* __restrict__ X1, int I1,
+                                               const float* __restrict__ X2, int I2, int with_bias,
+                                               float* __restrict__ part) {
+    extern __shared__ float sm[];
+    const int I = I1 + I2;
+    float* ys = sm;              // WG x O
+    float* xs = sm + WG * O;     // WG x I
+    const int base = blockIdx.x * WG;
+    for (int q = threadIdx.x; q < WG * O; q += blockDim.x) {
+        const int r = q / O, o = q - r * O, row = base + r;
+        ys[q] = row < n ? dY[(size_t)row * O + o] : 0.f;
+    }
+    for (int q = threadIdx.x; q < WG * I; q += blockDim.x) {
+        const int r = q / I, k = q - r * I, row = base + r;
+        float v = 0.f;
+        if (row < n) v = (k < I1) ? X1[(size_t)row * I1 + k] : X2[(size_t)row * I2 + (k - I1)];
+        xs[q] = v;
+    }
+    __syncthreads();
+    const int stride = O * I + (with_bias ? O : 0);
+    float* out = part + (size_t)blockIdx.x * stride;
+    for (int q = threadIdx.x; q < O * I; q += blockDim.x) {
+        const int o = q / I, k = q - o * I;
+        float acc = 0.f;
+        for (int r = 0; r < WG; ++r) acc += ys[r * O + o] * xs[r * I + k];
+        out[q] = acc;
+    }
+    if (with_bias)
+        for (int o = threadIdx.x; o < O; o += blockDim.x) {
+            float acc = 0.f;
+            for (int r = 0; r < WG; ++r) acc += ys[r * O + o];
+            out[O * I + o] = acc;
+        }
+}
+
+// out[q] (+)= sum over chunks c (in order) of part[c][q]
+__global__ void k_fold(int nchunk, int stride, const float* __restrict__ part, int accumulate,
+                       float* __restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= stride) return;
+    float acc = 0.f;
+    for (int c = 0; c < nchunk; ++c) acc += part[(size_t)c * stride + q];
+    out[q] = accumulate ? out[q] + acc : acc;
+}
+
+// ------------------------------------------------------------------ elementwise
+__global__ void k_relu(long n, const float* __restrict__ a, float* __restrict__ h) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) h[i] = fmaxf(a[i], 0.f);
+}
+
+// h1 = h0 + relu(v)
+__global__ void k_residual(long n, const float* __restrict__ h0, const float* __restrict__ v,
+                           float* __restrict__ h1) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) h1[i] = h0[i] + fmaxf(v[i], 0.f);
+}
+
+// d = g * (a > 0)
+__global__ void k_relu_bwd(long n, const float* __restrict__ g, const float* __restrict__ a,
+                           float* __restrict__ d) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) d[i] = a[i] > 0.f ? g[i] : 0.f;
+}
+
+// dh[i][o] = dh[i][o] + dhc[i][o] (first HID of the 2*HID row) + dpq[i][o]
+__global__ void k_add_dh(int n, const float* __restrict__ dhc, const float* __restrict__ dpqh,
+                         float* __restrict__ dh) {
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)n * HID) return;
+    const long i = q / HID, o = q - i * HID;
+    dh[q] = dh[q] + dhc[i * 2 * HID + o] + dpqh[q];
+}
+
+// ------------------------------------------------------------------ message passing
+// z[k][o] = PQ[i][o] + PQ[j][HID+o] + C[o] . e[k] + c[o]   for edge k = (i -> j)
+__global__ void k_edge_fwd(int m, const int* __restrict__ src, const int* __restrict__ nbr,
+                           const float* __restrict__ PQ, const float* __restrict__ e,
+                           const float* __restrict__ C, const float* __restrict__ c,
+                           float* __restrict__ z) {
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)m * HID) return;
+    const long k = q / HID;
+    const int o = (int)(q - k * HID);
+    const int i = src[k], j = nbr[k];
+    const float* ek = e + 3 * k;
+    z[q] = PQ[(size_t)i * 2 * HID + o] + PQ[(size_t)j * 2 * HID + HID + o] +
+           (C[o * 3] * ek[0] + C[o * 3 + 1] * ek[1] + C[o * 3 + 2] * ek[2]) + c[o];
+}
+
+// agg[i][o] = sum over the edges k of i of relu(z[k][o]) / max(deg_i, 1)
+__global__ void k_node_agg(int n, const int* __restrict__ ptr, const float* __restrict__ z,
+                           float* __restrict__ agg) {
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)n * HID) return;
+    const long i = q / HID;
+    const int o = (int)(q - i * HID);
+    const int k0 = ptr[i], k1 = ptr[i + 1];
+    float s = 0.f;
+    for (int k = k0; k < k1; ++k) s += fmaxf(z[(size_t)k * HID + o], 0.f);
+    agg[q] = s / (float)max(k1 - k0, 1);
+}
+
+// dz[k][o] = dhc[i][HID+o] / max(deg_i, 1) * (z[k][o] > 0)  (dhc holds d[h; agg])
+__global__ void k_edge_bwd(int m, const int* __restrict__ src, const int* __restrict__ ptr,
+                           const float* __restrict__ dhc, const float* __restrict__ z,
+                           float* __restrict__ dz) {
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)m * HID) return;
+    const long k = q / HID;
+    const int o = (int)(q - k * HID);
+    const int i = src[k];
+    const int deg = max(ptr[i + 1] - ptr[i], 1);
+    dz[q] = z[q] > 0.f ? dhc[(size_t)i * 2 * HID + HID + o] / (float)deg : 0.f;
+}
+
+// dPQ[i][o] = sum_{k in edges(i)} dz[k][o];  dPQ[i][HID+o] = sum_{k in edges(i)} dz[rev[k]][o]
+__global__ void k_node_dpq(int n, const int* __restrict__ ptr, const int* __restrict__ rev,
+                           const float* __restrict__ dz, float* __restrict__ dPQ) {
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)n * HID) return;
+    const long i = q / HID;
+    const int o = (int)(q - i * HID);
+    float sp = 0.f, sq = 0.f;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+        sp += dz[(size_t)k * HID + o];
+        sq += dz[(size_t)rev[k] * HID + o];
+    }
+    dPQ[(size_t)i * 2 * HID + o] = sp;
+    dPQ[(size_t)i * 2 * HID + HID + o] = sq;
+}
+
+// ------------------------------------------------------------------ loss and Adam
+// dy = 2 (y - t) / nfree at free nodes; per-block partial sums of |y - t|^2 (256 threads)
+__global__ void __launch_bounds__(256) k_loss(int n, const float* __restrict__ y,
+                                              const float* __restrict__ t,
+                                              const int* __restrict__ kind, float inv_nfree,
+                                              float* __restrict__ dy, float* __restrict__ part) {
+    __shared__ float red[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (i < n) {
+        const bool fr = kind[i] == KIND_FREE;
+#pragma unroll
+        for (int q = 0; q < OUT; ++q) {
+            const float d = fr ? y[OUT * i + q] - t[OUT * i + q] : 0.f;
+            l += d * d;
+            dy[OUT * i + q] = 2.f * d * inv_nfree;
+        }
+    }
+    red[threadIdx.x] = l;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_adam(int np, float* __restrict__ w, const float* __restrict__ g,
+                       float* __restrict__ m, float* __restrict__ v, float lr, float b1, float b2,
+                       float eps, float bc1, float bc2) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const float gq = g[q];
+    const float mq = b1 * m[q] + (1.f - b1) * gq;
+    const float vq = b2 * v[q] + (1.f - b2) * gq * gq;
+    m[q] = mq;
+    v[q] = vq;
+    const float mh = mq / bc1, vh = vq / bc2;
+    w[q] = w[q] - lr * mh / (sqrtf(vh) + eps);
+}
+
+// training targets: the fields (Phi, Psi_x, Psi_y) of the plain solve, stored as
+// (Phi, Psi_x / L, Psi_y / L)
+__global__ void k_targets(int n, const double* __restrict__ phi, const double* __restrict__ psx,
+                          const double* __restrict__ psy, const Globals* __restrict__ G,
+                          float* __restrict__ t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double iL = 1.0 / G->L;
+    t[OUT * i] = (float)phi[i];
+    t[OUT * i + 1] = (float)(psx[i] * iL);
+    t[OUT * i + 2] = (float)(psy[i] * iL);
+}
+
+// guess at free nodes: u = t Phi + L M (Psi_x/L, Psi_y/L); boundary nodes keep their
+// prescribed values
+__global__ void k_guess(int n, const float* __restrict__ y, const int* __restrict__ kind,
+                        const double* __restrict__ gnx, const double* __restrict__ gny,
+                        const Globals* __restrict__ G, double* __restrict__ ux,
+                        double* __restrict__ uy) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (kind[i] != KIND_FREE) {
+        ux[i] = gnx[i];
+        uy[i] = gny[i];
+        return;
+    }
+    const Globals g = *G;
+    const double phi = y[OUT * i], px = g.L * (double)y[OUT * i + 1], py = g.L * (double)y[OUT * i + 2];
+    ux[i] = g.tx * phi + g.m11 * px + g.m12 * py;
+    uy[i] = g.ty * phi + g.m21 * px + g.m22 * py;
+}
+
+}  // namespace mpnn
+}  // namespace cfd
+
+namespace cfd {
+namespace mpnn {
+
+// ------------------------------------------------------------------ BF16 inference
+// Tensor-core pass (mma.sync m16n8k16, BF16 operands, FP32 accumulation).  A warp owns 16
+// nodes, a block of IW warps a tile of 16*IW nodes; blocks loop over tiles so that each
+// loads the layer's weights into shared memory once.  Per layer one kernel: the message
+// aggregation of the layer (FP32 arithmetic on the BF16 P, Q of the previous kernel), the
+// update GEMM U [h; agg], the residual, then the next layer's P|Q GEMM or, after the last
+// layer, the decoder.  P|Q alternates between two buffers.
+constexpr int IW = 4;
+constexpr int TILE = 16 * IW;
+constexpr int XS = 2 * HID + 8;  // shared row stride (bf16) of 128-wide tiles
+constexpr int HS = HID + 8;      // of 64-wide tiles (the +8 keeps fragment loads
+                                 // free of bank conflicts)
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ unsigned ld_b32(const bf16* p) {
+    return *reinterpret_cast<const unsigned*>(p);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], unsigned a0, unsigned a1, unsigned a2,
+                                         unsigned a3, unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// acc[nt] += X[16][K] . W[nt*8 .. nt*8+8)[K]^T, X and W in shared memory (row strides xs,
+// ws in elements).  Fragment layout of m16n8k16: lane = 4 g + t; A rows g and g+8, columns
+// 2t, 2t+1 (+8); B column g, rows 2t, 2t+1 (+8); D rows g and g+8, columns 2t, 2t+1.
+template <int K, int NT>
+__device__ __forceinline__ void warp_gemm(const bf16* X, int xs, const bf16* W, int ws,
+                                          float (&acc)[NT][4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int kk = 0; kk < K / 16; ++kk) {
+        const int k0 = kk * 16 + 2 * t;
+        const unsigned a0 = ld_b32(X + g * xs + k0);
+        const unsigned a1 = ld_b32(X + (g + 8) * xs + k0);
+        const unsigned a2 = ld_b32(X + g * xs + k0 + 8);
+        const unsigned a3 = ld_b32(X + (g + 8) * xs + k0 + 8);
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const bf16* wr = W + (nt * 8 + g) * ws + k0;
+            mma_bf16(acc[nt], a0, a1, a2, a3, ld_b32(wr), ld_b32(wr + 8));
+        }
+    }
+}
+
+// D (16 x NT*8, FP32 fragments) -> global rows base.. (row stride ld), BF16
+template <int NT>
+__device__ __forceinline__ void store_tile_bf16(const float (&acc)[NT][4], int base, int n, bf16* out,
+                                                int ld) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        const int col = nt * 8 + 2 * t;
+        if (base + g < n)
+            *reinterpret_cast<__nv_bfloat162*>(out + (size_t)(base + g) * ld + col) =
+                __floats2bfloat162_rn(acc[nt][0], acc[nt][1]);
+        if (base + g + 8 < n)
+            *reinterpret_cast<__nv_bfloat162*>(out + (size_t)(base + g + 8) * ld + col) =
+                __floats2bfloat162_rn(acc[nt][2], acc[nt][3]);
+    }
+}
+
+__global__ void k_to_bf16(int np, const float* __restrict__ w, bf16* __restrict__ wb) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < np) wb[q] = __float2bfloat16_rn(w[q]);
+}
+
+// rows x cols of a row-major BF16 matrix into shared memory with row stride ld
+__device__ __forceinline__ void load_mat(bf16* dst, int ld, const bf16* src, int rows, int cols) {
+    for (int q = threadIdx.x; q < rows * cols / 2; q += blockDim.x) {
+        const int r = (2 * q) / cols, c = 2 * q - r * cols;
+        *reinterpret_cast<unsigned*>(dst + r * ld + c) =
+            *reinterpret_cast<const unsigned*>(src + (size_t)r * cols + c);
+    }
+}
+
+// h0 = relu(W_in f + b_in) (FP32), then P|Q of layer 0
+__global__ void __launch_bounds__(32 * IW) k_infer_encode(int n, const float* __restrict__ f,
+                                                          const float* __restrict__ w,
+                                                          const bf16* __restrict__ wb,
+                                                          bf16* __restrict__ hb,
+                                                          bf16* __restrict__ pq_out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* Ws = reinterpret_cast<bf16*>(smem_raw);   // 128 x HS: [A0; B0]
+    bf16* Hs = Ws + 2 * HID * HS;                    // IW x 16 x HS
+    float* Wi = reinterpret_cast<float*>(Hs + IW * 16 * HS);  // HID x F_IN, then b_in
+    load_mat(Ws, HS, wb + layer_off(0) + L_A, 2 * HID, HID);
+    for (int q = threadIdx.x; q < HID * F_IN + HID; q += blockDim.x) Wi[q] = w[OFF_W_IN + q];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    bf16* H = Hs + warp * 16 * HS;
+    const int ntile = (n + TILE - 1) / TILE;
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int base = tile * TILE + warp * 16;
+        for (int r = 0; r < 16; ++r) {
+            const int node = base + r;
+            float fi[F_IN];
+#pragma unroll
+            for (int k = 0; k < F_IN; ++k) fi[k] = node < n ? f[(size_t)node * F_IN + k] : 0.f;
+            float hv[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int o = 2 * lane + q;
+                float a = Wi[HID * F_IN + o];
+#pragma unroll
+                for (int k = 0; k < F_IN; ++k) a += Wi[o * F_IN + k] * fi[k];
+                hv[q] = node < n ? fmaxf(a, 0.f) : 0.f;
+            }
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(hv[0], hv[1]);
+            *reinterpret_cast<__nv_bfloat162*>(H + r * HS + 2 * lane) = h2;
+            if (node < n) *reinterpret_cast<__nv_bfloat162*>(hb + (size_t)node * HID + 2 * lane) = h2;
+        }
+        __syncwarp();
+        float acc[16][4];
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+        warp_gemm<HID, 16>(H, HS, Ws, HS, acc);
+        store_tile_bf16<16>(acc, base, n, pq_out, 2 * HID);
+        __syncwarp();
+    }
+}
+
+// layer l: aggregation, update GEMM, residual; then P|Q of layer l+1 (wb_next) or the
+// decoder (wb_next == null)
+__global__ void __launch_bounds__(32 * IW) k_infer_layer(
+    int n, int l, const int* __restrict__ ptr, const int* __restrict__ nbr,
+    const float* __restrict__ e, const float* __restrict__ w, const bf16* __restrict__ wb,
+    int has_next, const bf16* __restrict__ pq_in, bf16* __restrict__ hb,
+    bf16* __restrict__ pq_out, float* __restrict__ y) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* Us = reinterpret_cast<bf16*>(smem_raw);  // HID x XS
+    bf16* Ws = Us + HID * XS;                       // 128 x HS: [A; B] of layer l+1
+    bf16* Xs = Ws + 2 * HID * HS;                   // IW x 16 x XS
+    float* Cs = reinterpret_cast<float*>(Xs + IW * 16 * XS);  // C (HID x 3), c, u
+    float* cs = Cs + HID * E_F;
+    float* us = cs + HID;
+    const float* W = w + layer_off(l);
+    load_mat(Us, XS, wb + layer_off(l) + L_U, HID, 2 * HID);
+    if (has_next) load_mat(Ws, HS, wb + layer_off(l + 1) + L_A, 2 * HID, HID);
+    for (int q = threadIdx.x; q < HID * E_F; q += blockDim.x) Cs[q] = W[L_C + q];
+    for (int q = threadIdx.x; q < HID; q += blockDim.x) {
+        cs[q] = W[L_c + q];
+        us[q] = W[L_u + q];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    bf16* X = Xs + warp * 16 * XS;
+    const int o0 = 2 * lane;
+    const int ntile = (n + TILE - 1) / TILE;
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int base = tile * TILE + warp * 16;
+        // [h; agg] rows of the warp's 16 nodes
+        for (int r = 0; r < 16; ++r) {
+            const int node = base + r;
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(0.f, 0.f), a2 = h2;
+            if (node < n) {
+                h2 = *reinterpret_cast<const __nv_bfloat162*>(hb + (size_t)node * HID + o0);
+                const float2 P = __bfloat1622float2(
+                    *reinterpret_cast<const __nv_bfloat162*>(pq_in + (size_t)node * 2 * HID + o0));
+                float s0 = 0.f, s1 = 0.f;
+                const int k0 = ptr[node], k1 = ptr[node + 1];
+                for (int k = k0; k < k1; ++k) {
+                    const int j = nbr[k];
+                    const float2 Q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(
+                        pq_in + (size_t)j * 2 * HID + HID + o0));
+                    const float e0 = e[3 * (size_t)k], e1 = e[3 * (size_t)k + 1],
+                                e2 = e[3 * (size_t)k + 2];
+                    const float z0 = P.x + Q.x +
+                                     (Cs[o0 * 3] * e0 + Cs[o0 * 3 + 1] * e1 + Cs[o0 * 3 + 2] * e2) +
+                                     cs[o0];
+                    const float z1 = P.y + Q.y +
+                                     (Cs[o0 * 3 + 3] * e0 + Cs[o0 * 3 + 4] * e1 + Cs[o0 * 3 + 5] * e2) +
+                                     cs[o0 + 1];
+                    s0 += fmaxf(z0, 0.f);
+                    s1 += fmaxf(z1, 0.f);
+                }
+                const float inv = 1.f / (float)max(k1 - k0, 1);
+                a2 = __floats2bfloat162_rn(s0 * inv, s1 * inv);
+            }
+            *reinterpret_cast<__nv_bfloat162*>(X + r * XS + o0) = h2;
+            *reinterpret_cast<__nv_bfloat162*>(X + r * XS + HID + o0) = a2;
+        }
+        __syncwarp();
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+        warp_gemm<2 * HID, 8>(X, XS, Us, XS, acc);
+        __syncwarp();
+        // h <- h + relu(v + u), written back over the h half of the tile and to hb
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int col = nt * 8 + 2 * t;
+#pragma unroll
+            for (int hlf = 0; hlf < 2; ++hlf) {
+                const int row = g + 8 * hlf;
+                const float2 hv = __bfloat1622float2(
+                    *reinterpret_cast<const __nv_bfloat162*>(X + row * XS + col));
+                const float n0 = hv.x + fmaxf(acc[nt][2 * hlf] + us[col], 0.f);
+                const float n1 = hv.y + fmaxf(acc[nt][2 * hlf + 1] + us[col + 1], 0.f);
+                const __nv_bfloat162 nh = __floats2bfloat162_rn(n0, n1);
+                *reinterpret_cast<__nv_bfloat162*>(X + row * XS + col) = nh;
+                if (base + row < n)
+                    *reinterpret_cast<__nv_bfloat162*>(hb + (size_t)(base + row) * HID + col) = nh;
+            }
+        }
+        __syncwarp();
+        if (has_next) {
+            float acc2[16][4];
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt)
+                acc2[nt][0] = acc2[nt][1] = acc2[nt][2] = acc2[nt][3] = 0.f;
+            warp_gemm<HID, 16>(X, XS, Ws, HS, acc2);
+            store_tile_bf16<16>(acc2, base, n, pq_out, 2 * HID);
+        } else {
+            // decoder: 16 nodes x OUT outputs over the warp's lanes
+            for (int q = lane; q < 16 * OUT; q += 32) {
+                const int r = q / OUT, o = q - r * OUT, node = base + r;
+                float a = w[OFF_B_OUT + o];
+                for (int k = 0; k < HID; ++k)
+                    a += w[OFF_W_OUT + o * HID + k] * __bfloat162float(X[r * XS + k]);
+                if (node < n) y[(size_t)OUT * node + o] = a;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+int infer_bf16(cudaStream_t st, const float* w, bf16* wb, bool* wb_valid, int n, const int* ptr,
+               const int* nbr, const float* f, const float* e, bf16* hb, bf16* pqb, float* y) {
+    if (!*wb_valid) {
+        CFD_LAUNCH(k_to_bf16, blocks_for(N_PARAMS, 256), 256, 0, st, N_PARAMS, w, wb);
+        *wb_valid = true;
+    }
+    const size_t smem_enc = sizeof(bf16) * (2 * HID * HS + IW * 16 * HS) +
+                            sizeof(float) * (HID * F_IN + HID);
+    const size_t smem_layer = sizeof(bf16) * (HID * XS + 2 * HID * HS + IW * 16 * XS) +
+                              sizeof(float) * (HID * E_F + 2 * HID);
+    static bool attr_set = false;
+    if (!attr_set) {
+        CFD_CUDA(cudaFuncSetAttribute(k_infer_encode, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem_enc));
+        CFD_CUDA(cudaFuncSetAttribute(k_infer_layer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem_layer));
+        attr_set = true;
+    }
+    int dev = 0, nsm = 1;
+    CFD_CUDA(cudaGetDevice(&dev));
+    CFD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int ntile = (n + TILE - 1) / TILE;
+    const int grid = std::min(ntile, 4 * nsm);
+    bf16* pq[2] = {pqb, pqb + (size_t)n * 2 * HID};
+    CFD_LAUNCH(k_infer_encode, grid, 32 * IW, smem_enc, st, n, f, w, (const bf16*)wb, hb, pq[0]);
+    for (int l = 0; l < LAYERS; ++l) {
+        const int next = l + 1 < LAYERS ? 1 : 0;
+        CFD_LAUNCH(k_infer_layer, grid, 32 * IW, smem_layer, st, n, l, ptr, nbr, e, w,
+                   (const bf16*)wb, next, (const bf16*)pq[l & 1], hb, pq[(l + 1) & 1], y);
+    }
+    return CFD_OK;
+}
+
+}  // namespace mpnn
+}  // namespace cfd

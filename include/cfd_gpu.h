@@ -292,6 +292,48 @@ int cfd_ctx_elapsed(cfd_ctx* ctx, int a, int b, double* ms);
  * calling host thread (one process per GPU sets its local rank). */
 int cfd_set_device(int ordinal);
 
+/* ---------------------------------------------------------------- learned guess */
+/* An edge message-passing network (4 layers, width 64) that gives the initial guess of
+ * the mesh-motion solve; BiCG then finishes the solve from it (no reference counterpart:
+ * the reference starts from the previous step's increment, meshMove.f90:44,97).  From the
+ * node coordinates and boundary kinds it predicts the three fields Phi, Psi_x, Psi_y whose
+ * combination t Phi + M (Psi_x, Psi_y) is the solve's displacement for an affine body
+ * motion g = t + M (p - c); (t, M) is the least-squares fit of the prescribed body
+ * displacement.  Training runs on the GPU (FP32 forward/backward, Adam); inference uses
+ * BF16 tensor cores with FP32 accumulation.  Parameters: cfd_mpnn_nparams() floats in the
+ * packing of cfd_gb300/csrc/mpnn.cuh. */
+typedef struct cfd_mpnn cfd_mpnn;
+typedef struct cfd_mpnn_graph cfd_mpnn_graph;
+
+int cfd_mpnn_nparams(void);
+int cfd_mpnn_create(cfd_mpnn** net, const float* weights);
+void cfd_mpnn_destroy(cfd_mpnn* net);
+int cfd_mpnn_get_weights(cfd_mpnn* net, float* weights);
+int cfd_mpnn_set_weights(cfd_mpnn* net, const float* weights);
+/* Adam moments (may be NULL) and step count */
+int cfd_mpnn_adam_state(cfd_mpnn* net, float* m, float* v, int* t);
+/* Graph of a mesh; bnode (1-based) lists the boundary nodes with their kind: 1 moving body,
+ * 2 fixed outer boundary. */
+int cfd_mpnn_graph_create(cfd_mpnn_graph** g, int npoin, int nelem, const int* inpoel,
+                          const double* x, const double* y, int nb, const int* bnode,
+                          const int* bkind);
+void cfd_mpnn_graph_destroy(cfd_mpnn_graph* g);
+/* prescribed displacement of the boundary nodes (bnode order) and its affine fit */
+int cfd_mpnn_graph_set_bc(cfd_mpnn_graph* g, const double* gx, const double* gy);
+/* cx, cy, L, R (body geometry) and the fit tx, ty, m11, m12, m21, m22 */
+int cfd_mpnn_graph_globals(cfd_mpnn_graph* g, double* out10);
+/* training target: the fields the plain solve gives for the boundary data 1, x - c_x and
+ * y - c_y on the body (0 on the outer boundary), npoin each */
+int cfd_mpnn_graph_set_target(cfd_mpnn_graph* g, const double* phi, const double* psi_x,
+                              const double* psi_y);
+/* FP32 forward + backward: loss and (grad may be NULL) the gradient of every parameter */
+int cfd_mpnn_loss_grad(cfd_mpnn* net, cfd_mpnn_graph* g, float* loss, float* grad);
+/* loss_grad, then one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) with rate lr */
+int cfd_mpnn_train_step(cfd_mpnn* net, cfd_mpnn_graph* g, float lr, float* loss);
+/* The guess (npoin each; the boundary nodes carry their prescribed values): bf16 = 1 for
+ * the tensor-core pass, 0 for the FP32 pass. */
+int cfd_mpnn_forward(cfd_mpnn* net, cfd_mpnn_graph* g, int bf16, double* ux, double* uy);
+
 /* Number of kernels this library launched since process start (all contexts). */
 long long cfd_kernel_launches(void);
 
