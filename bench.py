@@ -42,6 +42,11 @@ def parse():
                     help="skip the plain-FP64 timing and the mixed-vs-FP64 error")
     ap.add_argument("--scale", type=int, default=None, help="nr = ntheta (reduced-size runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--guess", choices=["learned", "previous", "zero"], default="learned",
+                    help="initial guess of the mesh-motion solve in the mixed form")
+    ap.add_argument("--guess-gate", type=float, default=20.0,
+                    help="learned guess: iterations of the previous solve above which the "
+                         "network runs (it also runs on the first solve)")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of the benchmark: run the mixed and the FP64 forms side by "
                          "side for this many steps and print their state and force errors")
@@ -154,6 +159,7 @@ def config_dict(k, args, ws):
     return {"workload": f"ellipse O-grid {m['nr']}x{m['ntheta']} ({k.npoin} nodes, {k.nelem} "
                         f"triangles), Mach 0.8, Re 5000, heave 0.05 @ f=0.1, ALE + gcl",
             "npoin": k.npoin, "nelem": k.nelem, "precision": args.precision,
+            "guess": args.guess if args.precision == "mixed" else "previous",
             "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
             "l2": "inputs larger than L2 (state + element arrays ~0.9 GB at 1M nodes)",
             "data": "seeded synthetic O-grid (seed 0)"}
@@ -243,10 +249,13 @@ def main_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def timed_run(solver_mod, k, prec, W, K, L):
-    """Create a context, W warm-up steps, then K steps between CUDA events on the
-    context's stream.  Returns (solver, ms per step, kernel launches, report)."""
+def timed_run(solver_mod, k, prec, W, K, L, net=None, gate=0.0):
+    """Create a context (with the learned-guess network attached when given), W warm-up
+    steps, then K steps between CUDA events on the context's stream.  Returns (solver, ms
+    per step, kernel launches, report)."""
     S = solver_mod.Solver(k, precision=prec)
+    if net is not None:
+        S.set_guess_net(net, gate)
     S.step(W)
     import torch
     torch.cuda.synchronize()
@@ -294,6 +303,51 @@ def main_accuracy(args):
     print(json.dumps(line), flush=True)
 
 
+def guess_report(args, W, K):
+    """Mesh-motion solve with the previous-step, zero and learned guesses on the workload
+    (mixed form): BiCG iterations on the first (cold) step and per step after warm-up, the
+    mesh-motion time per step (timer of the BiCG group, which holds the network), the step
+    time, and for the learned guess how often it ran and how often its guess was taken."""
+    from cfd_gb300 import abi, learned, solver
+    net = learned.Net.load()
+    out = {}
+    modes = (("previous", abi.CFD_GUESS_PREVIOUS, None), ("zero", abi.CFD_GUESS_ZERO, None),
+             ("learned_every_step", abi.CFD_GUESS_LEARNED, 0.0),
+             ("learned", abi.CFD_GUESS_LEARNED, args.guess_gate))
+    os.environ["CFD_TIMERS"] = "1"
+    try:
+        for name, mode, gate in modes:
+            k = workload(args)
+            k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
+            k.params.guess_mode = mode
+            S = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+            if gate is not None:
+                S.set_guess_net(net, gate)
+            r1 = S.step(1)
+            S.step(max(W - 1, 0))
+            t0 = S.timers()
+            its = []
+            S.mark(0)
+            for _ in range(K):
+                its.append(sum(S.step(1).bicg_iters))
+            S.mark(1)
+            ms = S.elapsed_ms(0, 1) / K
+            t1 = S.timers()
+            d = {"first_step_iters": list(r1.bicg_iters), "iters_per_step": float(np.mean(its)),
+                 "mesh_motion_ms_per_step": (t1["grad_t"][0] - t0["grad_t"][0]) * 1e3 / K,
+                 "ms_per_step": ms}
+            if gate is not None:
+                ev, tx, ty, n = S.guess_stats()
+                d.update({"gate": gate, "network_steps": ev, "network_taken": tx + ty,
+                          "fallback_rate": (1.0 - (tx + ty) / (2.0 * ev)) if ev else None,
+                          "steps": n})
+            S.close()
+            out[name] = d
+    finally:
+        os.environ.pop("CFD_TIMERS", None)
+    return out
+
+
 def main_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -309,8 +363,17 @@ def main_ours(args):
     # is discontinuous at round-off level); the plain form runs the reference's
     k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED if mixed else abi.CFD_ESTAB_REFERENCE
     W, K = max(3, args.warmup), args.steps
+    net, gate = None, 0.0
+    if mixed and args.guess == "learned":
+        from cfd_gb300 import learned
+        k.params.guess_mode = abi.CFD_GUESS_LEARNED
+        net, gate = learned.Net.load(), args.guess_gate
+    elif args.guess == "zero":
+        k.params.guess_mode = abi.CFD_GUESS_ZERO
     if args.profile_steps:
         S = solver.Solver(k, precision=prec)
+        if net is not None:
+            S.set_guess_net(net, gate)
         S.step(W)
         S.step(args.profile_steps)
         return
@@ -319,7 +382,8 @@ def main_ours(args):
     dist.barrier()
     clocks = Clocks(local)
     clocks.start()
-    S, ms_step, launches, rep = timed_run(solver, k, prec, W, K, L)
+    S, ms_step, launches, rep = timed_run(solver, k, prec, W, K, L, net, gate)
+    guess_stats = S.guess_stats() if net is not None else None
     torch.cuda.synchronize()
     dist.barrier()
     clk = clocks.stop()
@@ -363,12 +427,27 @@ def main_ours(args):
         repr_ = Sr.step(W + K)
         Ur = Sr.state()["U"]
         Sr.close()
+        # precision error: the mixed form against the FP64 form, both with the previous-
+        # step guess (the same mesh-motion solves)
+        km = workload(args)
+        km.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
+        Sm = solver.Solver(km, precision=abi.CFD_PREC_MIXED)
+        repm = Sm.step(W + K)
+        Um = Sm.state()["U"]
+        Sm.close()
         forms["mixed_vs_fp64"] = {
-            "steps": W + K, "estab_mode": "regularized",
-            "rel_l2": [rel_l2(final_U[:, q], Ur[:, q]) for q in range(4)],
-            "force_rel_err": float(np.hypot(rep.fx[0] - repr_.fx[0], rep.fy[0] - repr_.fy[0])
+            "steps": W + K, "estab_mode": "regularized", "guess": "previous",
+            "rel_l2": [rel_l2(Um[:, q], Ur[:, q]) for q in range(4)],
+            "force_rel_err": float(np.hypot(repm.fx[0] - repr_.fx[0], repm.fy[0] - repr_.fy[0])
                                    / np.hypot(repr_.fx[0], repr_.fy[0]))}
+        if net is not None:
+            # the learned guess changes the mesh motion within the solve's absolute tolerance
+            forms["learned_vs_previous_guess"] = {
+                "steps": W + K, "rel_l2": [rel_l2(final_U[:, q], Um[:, q]) for q in range(4)],
+                "guess_stats": list(guess_stats)}
         forms["speedup_vs_fp64_plain"] = value / forms["fp64_plain"]["value"]
+        if mixed:
+            forms["guess"] = guess_report(args, W, min(K, 10))
     # ---- per-kernel breakdown and roofline of the dominant kernel (timers on, own ctx)
     os.environ["CFD_TIMERS"] = "1"
     S2 = solver.Solver(k, precision=prec)

@@ -281,6 +281,26 @@ int cfd_ctx_set_clock(cfd_ctx* ctx, int iter, double time, double dtmin1, int ba
     return CFD_OK;
 }
 
+int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate) {
+    if (!ctx) return arg_error("ctx");
+    if (!(gate >= 0.0)) return arg_error("gate");
+    return ctx->impl.set_guess_net(net, gate);
+}
+
+int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4) {
+    if (!ctx || !out4) return arg_error("null pointer");
+    Ctx& c = ctx->impl;
+    if (!c.d_gstats) {
+        for (int k = 0; k < 4; ++k) out4[k] = 0;
+        return CFD_OK;
+    }
+    CFD_CUDA(cudaMemcpyAsync(out4, c.d_gstats, 3 * sizeof(long long), cudaMemcpyDeviceToHost,
+                             c.stream));
+    CFD_CUDA(cudaStreamSynchronize(c.stream));
+    out4[3] = c.guess_steps;
+    return CFD_OK;
+}
+
 int cfd_step(cfd_ctx* ctx, int nsteps, cfd_step_report* rep) {
     if (!ctx) return arg_error("ctx");
     return ctx->impl.step(nsteps, rep);

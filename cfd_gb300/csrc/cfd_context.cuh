@@ -6,7 +6,20 @@
 #include "cfd_kernels.cuh"
 #include "host_prep.h"
 
+struct cfd_mpnn;
+struct cfd_mpnn_graph;
+
 namespace cfd {
+
+namespace mpnn {
+int graph_build(cfd_mpnn_graph** out, int npoin, const std::vector<int>& rowptr,
+                const std::vector<int>& col, const double* x, const double* y, int nb,
+                const int* bnode0, const int* bkind, bool training, cudaStream_t st);
+int guess_on_stream(cfd_mpnn* net, cfd_mpnn_graph* g, cudaStream_t st, const double* X,
+                    const double* Y, const double* bgx, const double* bgy, double* ux,
+                    double* uy, const int* gate);
+void graph_free(cfd_mpnn_graph* g);
+}  // namespace mpnn
 
 enum { TM_DELTAT, TM_ESTAB, TM_CALCRHS, TM_FUENTE, TM_UPDATE, TM_FORCES, TM_TRANSF, TM_GRAD,
        TM_NORMALES, TM_DERIV, TM_MASAS, TM_LAPLACE, TM_N };
@@ -77,6 +90,19 @@ struct Ctx {
     double* d_bscal = nullptr;   // [2][4] first-direction scalars of the mixed BiCG
     unsigned* d_bcount = nullptr;
     float* d_invdiagf = nullptr;
+    // learned guess (mixed form, CFD_GUESS_LEARNED): the network (not owned), its graph of
+    // this mesh, the candidate guesses, gate flags, judge sums and counters
+    cfd_mpnn* net = nullptr;
+    cfd_mpnn_graph* lgraph = nullptr;
+    double* d_cand[2] = {};
+    int* d_gflag = nullptr;
+    double* d_grr = nullptr;
+    long long* d_gstats = nullptr;
+    double guess_gate = 0.0;     // 0: every solve; > 0: iterations of the previous solve
+                                 // above which the network runs
+    bool guess_first = false;    // the first solve after attaching runs the network
+    long long guess_steps = 0;
+    int* h_iters = nullptr;      // pinned copy of the last solve's iteration counts
     int* d_slot_pos = nullptr;
     float4 *d_recInv = nullptr, *d_recVisc = nullptr;  // slot records, element-around-point order
     float4* d_invSum = nullptr;                         // per node: sum of the recInv slots
@@ -110,6 +136,7 @@ struct Ctx {
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
     int widen_mixed();
     int run_pcg(int nsolve);
+    int set_guess_net(cfd_mpnn* n, double gate);
     int step_once();
     int step_once_mixed();
     int step(int nsteps, cfd_step_report* rep);

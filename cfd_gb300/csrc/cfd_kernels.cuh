@@ -190,7 +190,12 @@ struct PcgArgs {
     double* part_r;              // [4][nblk_r] per-block partials of the row kernels
     long nblk_r;                 // 256-row blocks of the row kernels
     double* bscal;               // [2 solves][4]: r.r, r.p, p.y, alfa of the first direction
-    unsigned* bcount;            // [2] block counters of the row kernels (zero between uses)
+    unsigned* bcount;            // [3] block counters of the row kernels (zero between uses)
+    // learned guess (null: off): the first residual pass sets gflag[0] = (sum r.z >= gate)
+    // and clears gflag[1]; a pass with only_if != null runs only when *only_if != 0
+    int* gflag;
+    double gate;
+    const int* only_if;
     GridBar* bar;
     double tol;
     int maxit;
@@ -204,5 +209,11 @@ __global__ void k_pcg_mixed(PcgArgs a);
 __global__ void k_bicg_fix_mixed(PcgArgs a);
 __global__ void k_bicg_resid_mixed(PcgArgs a);
 __global__ void k_bicg_dir_mixed(PcgArgs a);
+// learned-guess judge: r.z of the candidate (cand[s]) per solve when gflag[0] is set
+__global__ void k_guess_judge(PcgArgs a, const double* cand0, const double* cand1, double* rr);
+// per solve, the candidate replaces x (and its shadow) when its r.z is the smaller; sets
+// gflag[1]; stats[0..3) += (gate open, solve 0 took it, solve 1 took it)
+__global__ void k_guess_select(PcgArgs a, const double* cand0, const double* cand1,
+                               const double* rr, long long* stats);
 
 }  // namespace cfd

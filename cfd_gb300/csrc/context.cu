@@ -78,8 +78,10 @@ int Ctx::tcollect() {
 
 Ctx::~Ctx() {
     if (stream) cudaStreamSynchronize(stream);
+    if (lgraph) mpnn::graph_free(lgraph);
     for (void* p : allocs) cudaFree(p);
     if (h_scal) cudaFreeHost(h_scal);
+    if (h_iters) cudaFreeHost(h_iters);
     if (ev_scal) cudaEventDestroy(ev_scal);
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (auto& m : mark)
@@ -159,9 +161,42 @@ int Ctx::run_pcg(int nsolve) {
         a.nblk_r = blocks_for(npoin, 256);
         a.bscal = d_bscal;
         a.bcount = d_bcount;
+        // learned guess: the network runs on the first solve after it was attached, and
+        // when the previous step's solve took more than guess_gate iterations (every solve
+        // when guess_gate is 0); the judge then keeps, per solve, the guess with the
+        // smaller r.z.  The previous step's counts are in pinned memory, complete since
+        // the host waited for this step's DTMIN.
+        const bool has_net = prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph;
+        bool learned = false;
+        if (has_net) {
+            guess_steps += 1;
+            learned = guess_first || guess_gate <= 0.0 ||
+                      (double)std::max(h_iters[0], h_iters[1]) > guess_gate;
+            guess_first = false;
+        }
+        a.gflag = learned ? d_gflag : nullptr;
+        a.gate = 0.0;
+        a.only_if = nullptr;
         if (nufix > 0)
             CFD_LAUNCH(k_bicg_fix_mixed, blocks_for(nufix, 256), 256, 0, stream, a);
         CFD_LAUNCH(k_bicg_resid_mixed, (unsigned)a.nblk_r, 256, 0, stream, a);
+        if (learned) {
+            // the network runs only when the previous-step guess leaves r.z >= gate; its
+            // guess replaces it, per solve, when its r.z is the smaller; the first pass is
+            // then redone on the chosen guess
+            int st = mpnn::guess_on_stream(net, lgraph, stream, d_X, d_Y, d_xfix[0], d_xfix[1],
+                                           d_cand[0], d_cand[1], d_gflag);
+            if (st) return st;
+            // grid-stride grids of a few waves: a closed gate costs little
+            const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
+            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                       (const double*)d_cand[1], d_grr);
+            CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                       (const double*)d_cand[1], (const double*)d_grr, d_gstats);
+            PcgArgs b = a;
+            b.only_if = d_gflag + 1;
+            CFD_LAUNCH(k_bicg_resid_mixed, gsz, 256, 0, stream, b);
+        }
         CFD_LAUNCH(k_bicg_dir_mixed, (unsigned)a.nblk_r, 256, 0, stream, a);
     }
     CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
@@ -169,6 +204,52 @@ int Ctx::run_pcg(int nsolve) {
     CFD_CUDA(cudaLaunchCooperativeKernel(mixed ? (void*)k_pcg_mixed : (void*)k_pcg_fp64, dim3(pcg_grid),
                                          dim3(256), args, 0, stream));
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (h_iters)
+        CFD_CUDA(cudaMemcpyAsync(h_iters, d_pcg_iters, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                                 stream));
+    return CFD_OK;
+}
+
+// Attach the learned-guess network (mixed form): builds the network's graph of this mesh
+// (neighbours = the Laplacian pattern, boundary = the mesh-motion Dirichlet list: moving
+// entries are the body, the others the fixed outer boundary).
+int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
+    if (prec != CFD_PREC_MIXED) {
+        set_last_message("the learned guess runs in the mixed-precision form");
+        return CFD_ERR_ARG;
+    }
+    if (nnmove <= 0) {
+        set_last_message("the mesh has no mesh-motion boundary nodes");
+        return CFD_ERR_ARG;
+    }
+    net = n;
+    guess_gate = gate;
+    guess_first = true;
+    guess_steps = 0;
+    if (d_gstats) CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 4 * sizeof(long long), stream));
+    if (!n) return CFD_OK;
+    if (!lgraph) {
+        const int N = npoin;
+        std::vector<double> x(N), y(N);
+        CFD_CUDA(cudaMemcpyAsync(x.data(), d_X, sizeof(double) * N, cudaMemcpyDeviceToHost, stream));
+        CFD_CUDA(cudaMemcpyAsync(y.data(), d_Y, sizeof(double) * N, cudaMemcpyDeviceToHost, stream));
+        CFD_CUDA(cudaStreamSynchronize(stream));
+        std::vector<int> bkind(nnmove);
+        for (int k = 0; k < nnmove; ++k) bkind[k] = bc.fix_set[k] >= 0 ? 1 : 2;
+        int st = mpnn::graph_build(&lgraph, N, adj.rowptr, adj.col, x.data(), y.data(), nnmove,
+                                   bc.fix_node.data(), bkind.data(), false, stream);
+        if (st) return st;
+        for (int s = 0; s < 2; ++s)
+            if ((st = dalloc(&d_cand[s], N))) return st;
+        if ((st = dalloc(&d_gflag, 2))) return st;
+        if ((st = dalloc(&d_grr, 2))) return st;
+        if ((st = dalloc(&d_gstats, 4))) return st;
+        CFD_CUDA(cudaMallocHost((void**)&h_iters, 2 * sizeof(int)));
+        h_iters[0] = h_iters[1] = 0;
+        CFD_CUDA(cudaMemsetAsync(d_gflag, 0, 2 * sizeof(int), stream));
+        CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 4 * sizeof(long long), stream));
+        CFD_CUDA(cudaStreamSynchronize(stream));
+    }
     return CFD_OK;
 }
 
@@ -497,10 +578,10 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         }
         if ((st = dalloc(&d_part_r, 4 * (size_t)blocks_for(N, 256)))) return st;
         if ((st = dalloc(&d_bscal, 8))) return st;
-        if ((st = dalloc(&d_bcount, 2))) return st;
+        if ((st = dalloc(&d_bcount, 3))) return st;
         if ((st = dalloc(&d_invdiagf, N))) return st;
         CFD_CUDA(cudaMemsetAsync(d_bscal, 0, 8 * sizeof(double), stream));
-        CFD_CUDA(cudaMemsetAsync(d_bcount, 0, 2 * sizeof(unsigned), stream));
+        CFD_CUDA(cudaMemsetAsync(d_bcount, 0, 3 * sizeof(unsigned), stream));
         if ((st = dalloc(&d_valf, adj.col.size()))) return st;
         if ((st = dalloc(&d_gterms, E))) return st;
         // slot (e, i) -> its position in element-around-point order

@@ -39,7 +39,8 @@ __device__ __forceinline__ double block_max256(double v, double* red) {
 __global__ void k_globals(int nb, const int* __restrict__ bnode, const int* __restrict__ bkind,
                           const double* __restrict__ gx, const double* __restrict__ gy,
                           const double* __restrict__ X, const double* __restrict__ Y,
-                          Globals* __restrict__ G) {
+                          Globals* __restrict__ G, const int* __restrict__ gate) {
+    if (gate && !*gate) return;
     __shared__ double red[9];
     const int t = threadIdx.x;
     double nbody = 0, sx = 0, sy = 0, sgx = 0, sgy = 0, nout = 0;
@@ -119,7 +120,8 @@ __global__ void k_globals(int nb, const int* __restrict__ bnode, const int* __re
 // per-node prescribed displacement (0 at free nodes) from the boundary list
 __global__ void k_scatter_bc(int nb, const int* __restrict__ bnode, const double* __restrict__ gx,
                              const double* __restrict__ gy, double* __restrict__ gnx,
-                             double* __restrict__ gny) {
+                             double* __restrict__ gny, const int* __restrict__ gate) {
+    if (gate && !*gate) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nb) return;
     gnx[bnode[k]] = gx[k];
@@ -138,50 +140,58 @@ __global__ void k_scatter_bc(int nb, const int* __restrict__ bnode, const double
 // the ellipse's aspect ratio.
 __global__ void k_features(int n, const double* __restrict__ X, const double* __restrict__ Y,
                            const int* __restrict__ kind, const Globals* __restrict__ G,
-                           float* __restrict__ f) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                           float* __restrict__ f, const int* __restrict__ gate) {
+    if (gate && !*gate) return;
+    // per-graph constants (FP32 arithmetic below; positions are differenced in FP64)
     const Globals g = *G;
-    const double dx = X[i] - g.cx, dy = Y[i] - g.cy;
-    const double r2 = dx * dx + dy * dy, r = sqrt(r2);
-    const double a = 0.5 * g.L, R = g.R;
-    float* o = f + (size_t)i * F_IN;
-    o[0] = (float)(dx / g.L);
-    o[1] = (float)(dy / g.L);
-    o[2] = (float)log(r / g.L + 1e-6);
-    o[3] = (float)log(R / g.L);
-    o[4] = kind[i] == KIND_BODY ? 1.f : 0.f;
-    o[5] = kind[i] == KIND_OUTER ? 1.f : 0.f;
-    const double sq2 = 1.4142135623730951, p = 1.0 + sq2, q = 1.0 - sq2;
-    double phi = 0.0, c = 0.0;
-    if (R > a && r < R) {
-        phi = (R * R - r2) / (R * R - a * a);
-        const double rs = fmax(r, 1e-6 * g.L);
-        // body radius along the node's direction (frame of the ellipse's axes)
-        const double u = (dx * g.ec + dy * g.es) / rs, v = (-dx * g.es + dy * g.ec) / rs;
-        const double rb = g.ea * g.eb / fmax(sqrt(g.eb * g.eb * u * u + g.ea * g.ea * v * v), 1e-300);
-        const double rho = fmin(rs * a / fmax(rb, 1e-6 * g.L), 0.999999 * R);
-        const double rr = rho / R, ar = a / R;
-        const double psi = a * (pow(rr, p) - pow(rr, q)) / (pow(ar, p) - pow(ar, q));
-        c = psi / rho;
+    const float L = (float)g.L, iL = 1.f / L, a = 0.5f * L, R = (float)g.R;
+    const float ea = (float)g.ea, eb = (float)g.eb, ec = (float)g.ec, es = (float)g.es;
+    const float p = 2.41421356f, q = -0.41421356f;
+    const float ar = a / R, den = powf(ar, p) - powf(ar, q);
+    const float logRL = logf(R * iL), aspect = ea > 0.f ? eb / ea : 1.f;
+    const bool annulus = R > a;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float dx = (float)(X[i] - g.cx), dy = (float)(Y[i] - g.cy);
+        const float r2 = dx * dx + dy * dy, r = sqrtf(r2);
+        float* o = f + (size_t)i * F_IN;
+        o[0] = dx * iL;
+        o[1] = dy * iL;
+        o[2] = logf(r * iL + 1e-6f);
+        o[3] = logRL;
+        o[4] = kind[i] == KIND_BODY ? 1.f : 0.f;
+        o[5] = kind[i] == KIND_OUTER ? 1.f : 0.f;
+        float phi = 0.f, c = 0.f;
+        if (annulus && r < R) {
+            phi = (R * R - r2) / (R * R - a * a);
+            const float rs = fmaxf(r, 1e-6f * L);
+            // body radius along the node's direction (frame of the ellipse's axes)
+            const float u = (dx * ec + dy * es) / rs, v = (-dx * es + dy * ec) / rs;
+            const float rb = ea * eb / fmaxf(sqrtf(eb * eb * u * u + ea * ea * v * v), 1e-30f);
+            const float rho = fminf(rs * a / fmaxf(rb, 1e-6f * L), 0.999999f * R);
+            const float rr = rho / R;
+            c = a * (powf(rr, p) - powf(rr, q)) / den / rho;
+        }
+        o[6] = fminf(fmaxf(phi, 0.f), 1.f);
+        o[7] = c * dx * iL;
+        o[8] = c * dy * iL;
+        o[9] = aspect;
     }
-    o[6] = (float)fmin(fmax(phi, 0.0), 1.0);
-    o[7] = (float)(c * dx / g.L);
-    o[8] = (float)(c * dy / g.L);
-    o[9] = (float)(g.ea > 0 ? g.eb / g.ea : 1.0);
 }
 
 __global__ void k_edge_features(int m, const int* __restrict__ src, const int* __restrict__ nbr,
                                 const double* __restrict__ X, const double* __restrict__ Y,
-                                const Globals* __restrict__ G, float* __restrict__ e) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= m) return;
-    const int i = src[k], j = nbr[k];
-    const double dx = X[j] - X[i], dy = Y[j] - Y[i];
-    const double ln = sqrt(dx * dx + dy * dy);
-    e[3 * (size_t)k] = (float)(dx / ln);
-    e[3 * (size_t)k + 1] = (float)(dy / ln);
-    e[3 * (size_t)k + 2] = (float)log(ln / G->L);
+                                const Globals* __restrict__ G, float* __restrict__ e,
+                                const int* __restrict__ gate) {
+    if (gate && !*gate) return;
+    const float iL = (float)(1.0 / G->L);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const int i = src[k], j = nbr[k];
+        const float dx = (float)(X[j] - X[i]), dy = (float)(Y[j] - Y[i]);
+        const float ln = sqrtf(dx * dx + dy * dy), il = 1.f / ln;
+        e[3 * (size_t)k] = dx * il;
+        e[3 * (size_t)k + 1] = dy * il;
+        e[3 * (size_t)k + 2] = logf(ln * iL);
+    }
 }
 
 // ------------------------------------------------------------------ FP32 dense layers
@@ -437,18 +447,20 @@ __global__ void k_targets(int n, const double* __restrict__ phi, const double* _
 __global__ void k_guess(int n, const float* __restrict__ y, const int* __restrict__ kind,
                         const double* __restrict__ gnx, const double* __restrict__ gny,
                         const Globals* __restrict__ G, double* __restrict__ ux,
-                        double* __restrict__ uy) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (kind[i] != KIND_FREE) {
-        ux[i] = gnx[i];
-        uy[i] = gny[i];
-        return;
-    }
+                        double* __restrict__ uy, const int* __restrict__ gate) {
+    if (gate && !*gate) return;
     const Globals g = *G;
-    const double phi = y[OUT * i], px = g.L * (double)y[OUT * i + 1], py = g.L * (double)y[OUT * i + 2];
-    ux[i] = g.tx * phi + g.m11 * px + g.m12 * py;
-    uy[i] = g.ty * phi + g.m21 * px + g.m22 * py;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (kind[i] != KIND_FREE) {
+            ux[i] = gnx[i];
+            uy[i] = gny[i];
+            continue;
+        }
+        const double phi = y[OUT * i], px = g.L * (double)y[OUT * i + 1],
+                     py = g.L * (double)y[OUT * i + 2];
+        ux[i] = g.tx * phi + g.m11 * px + g.m12 * py;
+        uy[i] = g.ty * phi + g.m21 * px + g.m22 * py;
+    }
 }
 
 }  // namespace mpnn
@@ -464,7 +476,7 @@ namespace mpnn {
 // aggregation of the layer (FP32 arithmetic on the BF16 P, Q of the previous kernel), the
 // update GEMM U [h; agg], the residual, then the next layer's P|Q GEMM or, after the last
 // layer, the decoder.  P|Q alternates between two buffers.
-constexpr int IW = 4;
+constexpr int IW = 8;
 constexpr int TILE = 16 * IW;
 constexpr int XS = 2 * HID + 8;  // shared row stride (bf16) of 128-wide tiles
 constexpr int HS = HID + 8;      // of 64-wide tiles (the +8 keeps fragment loads
@@ -542,7 +554,9 @@ __global__ void __launch_bounds__(32 * IW) k_infer_encode(int n, const float* __
                                                           const float* __restrict__ w,
                                                           const bf16* __restrict__ wb,
                                                           bf16* __restrict__ hb,
-                                                          bf16* __restrict__ pq_out) {
+                                                          bf16* __restrict__ pq_out,
+                                                          const int* __restrict__ gate) {
+    if (gate && !*gate) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     bf16* Ws = reinterpret_cast<bf16*>(smem_raw);   // 128 x HS: [A0; B0]
     bf16* Hs = Ws + 2 * HID * HS;                    // IW x 16 x HS
@@ -555,23 +569,34 @@ __global__ void __launch_bounds__(32 * IW) k_infer_encode(int n, const float* __
     const int ntile = (n + TILE - 1) / TILE;
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const int base = tile * TILE + warp * 16;
-        for (int r = 0; r < 16; ++r) {
-            const int node = base + r;
+        {  // all 16 nodes at once: lane l owns node l/2 and the outputs [32 (l%2), +32)
+            const int r = lane >> 1, o0 = 32 * (lane & 1), node = base + r;
             float fi[F_IN];
 #pragma unroll
             for (int k = 0; k < F_IN; ++k) fi[k] = node < n ? f[(size_t)node * F_IN + k] : 0.f;
-            float hv[2];
+            unsigned w16[16];
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const int o = 2 * lane + q;
-                float a = Wi[HID * F_IN + o];
+            for (int q = 0; q < 16; ++q) {
+                float hv[2];
 #pragma unroll
-                for (int k = 0; k < F_IN; ++k) a += Wi[o * F_IN + k] * fi[k];
-                hv[q] = node < n ? fmaxf(a, 0.f) : 0.f;
+                for (int u = 0; u < 2; ++u) {
+                    const int o = o0 + 2 * q + u;
+                    float a = Wi[HID * F_IN + o];
+#pragma unroll
+                    for (int k = 0; k < F_IN; ++k) a += Wi[o * F_IN + k] * fi[k];
+                    hv[u] = node < n ? fmaxf(a, 0.f) : 0.f;
+                }
+                const __nv_bfloat162 h2 = __floats2bfloat162_rn(hv[0], hv[1]);
+                w16[q] = *reinterpret_cast<const unsigned*>(&h2);
             }
-            const __nv_bfloat162 h2 = __floats2bfloat162_rn(hv[0], hv[1]);
-            *reinterpret_cast<__nv_bfloat162*>(H + r * HS + 2 * lane) = h2;
-            if (node < n) *reinterpret_cast<__nv_bfloat162*>(hb + (size_t)node * HID + 2 * lane) = h2;
+            uint4* hs = reinterpret_cast<uint4*>(H + r * HS + o0);
+            uint4* hg = reinterpret_cast<uint4*>(hb + (size_t)node * HID + o0);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const uint4 w = make_uint4(w16[4 * v], w16[4 * v + 1], w16[4 * v + 2], w16[4 * v + 3]);
+                hs[v] = w;
+                if (node < n) hg[v] = w;
+            }
         }
         __syncwarp();
         float acc[16][4];
@@ -585,11 +610,12 @@ __global__ void __launch_bounds__(32 * IW) k_infer_encode(int n, const float* __
 
 // layer l: aggregation, update GEMM, residual; then P|Q of layer l+1 (wb_next) or the
 // decoder (wb_next == null)
-__global__ void __launch_bounds__(32 * IW) k_infer_layer(
+__global__ void __launch_bounds__(32 * IW, 2) k_infer_layer(
     int n, int l, const int* __restrict__ ptr, const int* __restrict__ nbr,
     const float* __restrict__ e, const float* __restrict__ w, const bf16* __restrict__ wb,
     int has_next, const bf16* __restrict__ pq_in, bf16* __restrict__ hb,
-    bf16* __restrict__ pq_out, float* __restrict__ y) {
+    bf16* __restrict__ pq_out, float* __restrict__ y, const int* __restrict__ gate) {
+    if (gate && !*gate) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     bf16* Us = reinterpret_cast<bf16*>(smem_raw);  // HID x XS
     bf16* Ws = Us + HID * XS;                       // 128 x HS: [A; B] of layer l+1
@@ -612,36 +638,69 @@ __global__ void __launch_bounds__(32 * IW) k_infer_layer(
     const int ntile = (n + TILE - 1) / TILE;
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const int base = tile * TILE + warp * 16;
-        // [h; agg] rows of the warp's 16 nodes
-        for (int r = 0; r < 16; ++r) {
-            const int node = base + r;
-            __nv_bfloat162 h2 = __floats2bfloat162_rn(0.f, 0.f), a2 = h2;
+        // [h; agg] rows of the warp's 16 nodes, 8 at a time: lane l owns node l/4 (+8) and
+        // the 16 features [16 (l%4), 16 (l%4) + 16); rows are read as 16-byte vectors
+        for (int pass = 0; pass < 2; ++pass) {
+            const int r = (lane >> 2) + 8 * pass, f0 = 16 * (lane & 3), node = base + r;
+            float acc16[16], pz[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) acc16[q] = 0.f;
+            uint4 hv4[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
             if (node < n) {
-                h2 = *reinterpret_cast<const __nv_bfloat162*>(hb + (size_t)node * HID + o0);
-                const float2 P = __bfloat1622float2(
-                    *reinterpret_cast<const __nv_bfloat162*>(pq_in + (size_t)node * 2 * HID + o0));
-                float s0 = 0.f, s1 = 0.f;
+                const uint4* hp = reinterpret_cast<const uint4*>(hb + (size_t)node * HID + f0);
+                const uint4* pp = reinterpret_cast<const uint4*>(pq_in + (size_t)node * 2 * HID + f0);
+#pragma unroll
+                for (int v = 0; v < 2; ++v) {
+                    hv4[v] = hp[v];
+                    const uint4 pv = pp[v];
+                    const unsigned w4[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float2 f2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w4[u]));
+                        pz[8 * v + 2 * u] = f2.x + cs[f0 + 8 * v + 2 * u];  // P_i + c
+                        pz[8 * v + 2 * u + 1] = f2.y + cs[f0 + 8 * v + 2 * u + 1];
+                    }
+                }
                 const int k0 = ptr[node], k1 = ptr[node + 1];
                 for (int k = k0; k < k1; ++k) {
                     const int j = nbr[k];
-                    const float2 Q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(
-                        pq_in + (size_t)j * 2 * HID + HID + o0));
                     const float e0 = e[3 * (size_t)k], e1 = e[3 * (size_t)k + 1],
                                 e2 = e[3 * (size_t)k + 2];
-                    const float z0 = P.x + Q.x +
-                                     (Cs[o0 * 3] * e0 + Cs[o0 * 3 + 1] * e1 + Cs[o0 * 3 + 2] * e2) +
-                                     cs[o0];
-                    const float z1 = P.y + Q.y +
-                                     (Cs[o0 * 3 + 3] * e0 + Cs[o0 * 3 + 4] * e1 + Cs[o0 * 3 + 5] * e2) +
-                                     cs[o0 + 1];
-                    s0 += fmaxf(z0, 0.f);
-                    s1 += fmaxf(z1, 0.f);
+                    const uint4* qp =
+                        reinterpret_cast<const uint4*>(pq_in + (size_t)j * 2 * HID + HID + f0);
+                    const uint4 qa = qp[0], qb = qp[1];
+                    const unsigned w8[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const float2 q2 =
+                            __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w8[u]));
+                        const int o = f0 + 2 * u;
+                        const float z0 = pz[2 * u] + q2.x +
+                                         (Cs[o * 3] * e0 + Cs[o * 3 + 1] * e1 + Cs[o * 3 + 2] * e2);
+                        const float z1 = pz[2 * u + 1] + q2.y +
+                                         (Cs[o * 3 + 3] * e0 + Cs[o * 3 + 4] * e1 + Cs[o * 3 + 5] * e2);
+                        acc16[2 * u] += fmaxf(z0, 0.f);
+                        acc16[2 * u + 1] += fmaxf(z1, 0.f);
+                    }
                 }
                 const float inv = 1.f / (float)max(k1 - k0, 1);
-                a2 = __floats2bfloat162_rn(s0 * inv, s1 * inv);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc16[q] *= inv;
             }
-            *reinterpret_cast<__nv_bfloat162*>(X + r * XS + o0) = h2;
-            *reinterpret_cast<__nv_bfloat162*>(X + r * XS + HID + o0) = a2;
+            uint4* xh = reinterpret_cast<uint4*>(X + r * XS + f0);
+            uint4* xa = reinterpret_cast<uint4*>(X + r * XS + HID + f0);
+#pragma unroll
+            for (int v = 0; v < 2; ++v) {
+                xh[v] = hv4[v];
+                unsigned w4[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const __nv_bfloat162 b2 =
+                        __floats2bfloat162_rn(acc16[8 * v + 2 * u], acc16[8 * v + 2 * u + 1]);
+                    w4[u] = *reinterpret_cast<const unsigned*>(&b2);
+                }
+                xa[v] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+            }
         }
         __syncwarp();
         float acc[8][4];
@@ -689,7 +748,8 @@ __global__ void __launch_bounds__(32 * IW) k_infer_layer(
 }
 
 int infer_bf16(cudaStream_t st, const float* w, bf16* wb, bool* wb_valid, int n, const int* ptr,
-               const int* nbr, const float* f, const float* e, bf16* hb, bf16* pqb, float* y) {
+               const int* nbr, const float* f, const float* e, bf16* hb, bf16* pqb, float* y,
+               const int* gate) {
     if (!*wb_valid) {
         CFD_LAUNCH(k_to_bf16, blocks_for(N_PARAMS, 256), 256, 0, st, N_PARAMS, w, wb);
         *wb_valid = true;
@@ -710,13 +770,14 @@ int infer_bf16(cudaStream_t st, const float* w, bf16* wb, bool* wb_valid, int n,
     CFD_CUDA(cudaGetDevice(&dev));
     CFD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int ntile = (n + TILE - 1) / TILE;
-    const int grid = std::min(ntile, 4 * nsm);
+    const int grid = std::min(ntile, 2 * nsm);  // resident blocks (registers, shared memory)
     bf16* pq[2] = {pqb, pqb + (size_t)n * 2 * HID};
-    CFD_LAUNCH(k_infer_encode, grid, 32 * IW, smem_enc, st, n, f, w, (const bf16*)wb, hb, pq[0]);
+    CFD_LAUNCH(k_infer_encode, grid, 32 * IW, smem_enc, st, n, f, w, (const bf16*)wb, hb, pq[0],
+               gate);
     for (int l = 0; l < LAYERS; ++l) {
         const int next = l + 1 < LAYERS ? 1 : 0;
         CFD_LAUNCH(k_infer_layer, grid, 32 * IW, smem_layer, st, n, l, ptr, nbr, e, w,
-                   (const bf16*)wb, next, (const bf16*)pq[l & 1], hb, pq[(l + 1) & 1], y);
+                   (const bf16*)wb, next, (const bf16*)pq[l & 1], hb, pq[(l + 1) & 1], y, gate);
     }
     return CFD_OK;
 }

@@ -140,12 +140,15 @@ __device__ bool last_block_fold(unsigned* count, const double* part, long nb, in
 
 // First pass of a solve, one row per thread: y = A.x (FP32 SpMV over the shadow of x),
 // r = b - y with r(fix) = 0, p = r/diag (as r*(1/diag)); per-block partials of r.r and r.p
-// (biconjGrad.f90:29-38).  y itself is not kept: the next pass overwrites it.
+// (biconjGrad.f90:29-38).  y itself is not kept: the next pass overwrites it.  A block
+// visits the 256-row groups blockIdx.x, blockIdx.x + gridDim.x, ... (one group when the
+// grid has a block per group); there is one partial per block.
 template <int NS>
 __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) {
     const int t = threadIdx.x;
-    const long i = blockIdx.x * (long)blockDim.x + t;
     double rr[2] = {0.0, 0.0}, rp[2] = {0.0, 0.0};
+    for (long rb = blockIdx.x; rb < a.nblk_r; rb += gridDim.x) {
+    const long i = rb * 256 + t;
     if (i < a.n) {
         const bool fx = a.isfix[i];
         float d[2] = {0.f, 0.f};
@@ -172,9 +175,10 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
             a.r[s][i] = r;
             a.p[s][0][i] = p;
             a.pf[s][0][i] = pf;
-            rr[s] = r * r;
-            rp[s] = r * p;
+            rr[s] += r * r;
+            rp[s] += r * p;
         }
+    }
     }
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
@@ -184,20 +188,90 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
     __syncthreads();
     if ((t >> 5) < 4) {
         const double v = warp_sum256(sh[t >> 5]);
-        if ((t & 31) == 0) a.part_r[(t >> 5) * a.nblk_r + blockIdx.x] = v;
+        if ((t & 31) == 0) a.part_r[(t >> 5) * gridDim.x + blockIdx.x] = v;
     }
 }
 
 __global__ void __launch_bounds__(256) k_bicg_resid_mixed(PcgArgs a) {
     __shared__ double sh[4][256];
     __shared__ double out[4];
+    if (a.only_if && !*a.only_if) return;  // the same in every block
     if (a.nsolve == 2) first_rows<2>(a, sh);
     else first_rows<1>(a, sh);
-    if (last_block_fold(&a.bcount[0], a.part_r, a.nblk_r, 4, sh, out) && threadIdx.x == 0)
+    if (last_block_fold(&a.bcount[0], a.part_r, gridDim.x, 4, sh, out) && threadIdx.x == 0) {
         for (int s = 0; s < 2; ++s) {
             a.bscal[4 * s + 0] = out[s];      // r.r
             a.bscal[4 * s + 1] = out[2 + s];  // r.p
         }
+        if (a.gflag && !a.only_if) {  // gate on r.z, the convergence measure of the solve
+            a.gflag[0] = (out[2] + out[3] >= a.gate) ? 1 : 0;
+            a.gflag[1] = 0;
+        }
+    }
+}
+
+// r.z = r.r/diag of the candidate guesses (FP32 SpMV over their d2f_trunc values), per
+// 256-row block, folded by the last block; fixed rows contribute 0 as in the first pass
+__global__ void __launch_bounds__(256) k_guess_judge(PcgArgs a, const double* __restrict__ cand0,
+                                                     const double* __restrict__ cand1,
+                                                     double* __restrict__ rr) {
+    __shared__ double sh[4][256];
+    __shared__ double out[4];
+    if (!a.gflag[0]) return;  // the same in every block
+    const int t = threadIdx.x;
+    const double* cand[2] = {cand0, cand1};
+    double q[2] = {0.0, 0.0};
+    for (long i = blockIdx.x * (long)blockDim.x + t; i < a.n; i += (long)gridDim.x * blockDim.x) {
+        if (a.isfix[i]) continue;
+        const int j0 = a.rowptr[i], j1 = a.rowptr[i + 1];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            if (s >= a.nsolve) continue;
+            float d = 0.f;
+            for (int j = j0; j < j1; ++j) d += a.valf[j] * d2f_trunc(cand[s][a.col[j]]);
+            const double r = f2d_bits(-d);
+            q[s] += r * r * a.invdiag[i];
+        }
+    }
+    sh[0][t] = q[0];
+    sh[1][t] = q[1];
+    __syncthreads();
+    if ((t >> 5) < 2) {
+        const double v = warp_sum256(sh[t >> 5]);
+        if ((t & 31) == 0) a.part_r[(t >> 5) * gridDim.x + blockIdx.x] = v;
+    }
+    if (last_block_fold(&a.bcount[2], a.part_r, gridDim.x, 2, sh, out) && t == 0) {
+        rr[0] = out[0];
+        rr[1] = out[1];
+    }
+}
+
+__global__ void k_guess_select(PcgArgs a, const double* __restrict__ cand0,
+                               const double* __restrict__ cand1, const double* __restrict__ rr,
+                               long long* __restrict__ stats) {
+    const bool open = a.gflag[0] != 0;
+    bool use[2] = {false, false};
+    if (open)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) use[s] = s < a.nsolve && rr[s] < a.bscal[4 * s + 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        stats[0] += open ? 1 : 0;
+        stats[1] += use[0] ? 1 : 0;
+        stats[2] += use[1] ? 1 : 0;
+        a.gflag[1] = (use[0] || use[1]) ? 1 : 0;
+    }
+    if (!use[0] && !use[1]) return;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < a.n;
+         i += (long)gridDim.x * blockDim.x) {
+        if (use[0]) {
+            a.x[0][i] = cand0[i];
+            a.xf[0][i] = d2f_trunc(cand0[i]);
+        }
+        if (use[1]) {
+            a.x[1][i] = cand1[i];
+            a.xf[1][i] = d2f_trunc(cand1[i]);
+        }
+    }
 }
 
 // Second pass, for the solves with r.r >= tol: y = A.p (FP32 over the shadow), y(fix) =

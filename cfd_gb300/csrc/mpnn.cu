@@ -3,6 +3,7 @@
 // buffers of one forward/backward pass) and their extern "C" entries (include/cfd_gpu.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -68,6 +69,7 @@ struct cfd_mpnn_graph {
     __nv_bfloat16 *hb = nullptr, *pqb = nullptr;
     float* yb = nullptr;
     double *ux = nullptr, *uy = nullptr, *uz = nullptr;
+    bool training = false;
     ~cfd_mpnn_graph() {
         if (stream) {
             cudaStreamSynchronize(stream);
@@ -181,6 +183,153 @@ int backward_fp32(cfd_mpnn& net, cfd_mpnn_graph& g, float* loss_out) {
 
 }  // namespace
 
+namespace cfd {
+namespace mpnn {
+
+// Graph from the Laplacian pattern (rowptr, col: 0-based, diagonal first), host coordinates,
+// boundary nodes (0-based) and kinds.  training = false leaves out the buffers of the FP32
+// forward/backward passes.  Features are formed on `st` (the graph's own stream if null).
+int graph_build(cfd_mpnn_graph** out, int npoin, const std::vector<int>& rowptr,
+                const std::vector<int>& col, const double* x, const double* y, int nb,
+                const int* bnode0, const int* bkind, bool training, cudaStream_t st) {
+    *out = nullptr;
+    for (int k = 0; k < nb; ++k) {
+        if (bkind[k] != KIND_BODY && bkind[k] != KIND_OUTER) return arg_err("bkind (1 body, 2 outer)");
+        if (bnode0[k] < 0 || bnode0[k] >= npoin) return arg_err("boundary node index");
+    }
+    // neighbours = the Laplacian pattern without its diagonal (first entry of each row)
+    std::vector<int> ptr(npoin + 1, 0), nbr, src, rev;
+    for (int i = 0; i < npoin; ++i) {
+        for (int k = rowptr[i] + 1; k < rowptr[i + 1]; ++k) {
+            nbr.push_back(col[k]);
+            src.push_back(i);
+        }
+        ptr[i + 1] = (int)nbr.size();
+    }
+    const int m = (int)nbr.size();
+    rev.assign(m, -1);
+    for (int k = 0; k < m; ++k) {
+        const int i = src[k], j = nbr[k];
+        for (int q = ptr[j]; q < ptr[j + 1]; ++q)
+            if (nbr[q] == i) {
+                rev[k] = q;
+                break;
+            }
+        if (rev[k] < 0) {
+            set_last_message("mpnn: point neighbours are not symmetric");
+            return CFD_ERR_MESH;
+        }
+    }
+    std::vector<int> kind(npoin, KIND_FREE);
+    for (int k = 0; k < nb; ++k) kind[bnode0[k]] = bkind[k];
+    int nfree = 0;
+    for (int i = 0; i < npoin; ++i) nfree += kind[i] == KIND_FREE;
+    std::unique_ptr<cfd_mpnn_graph> g(new cfd_mpnn_graph());
+    g->n = npoin;
+    g->m = m;
+    g->nb = nb;
+    g->nfree = nfree;
+    CFD_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    if (!st) st = g->stream;
+    auto& o = g->owned;
+    auto up = [&](auto** p, const auto* h, size_t cnt) -> int {
+        int r = dev_alloc(o, p, cnt);
+        if (r) return r;
+        CFD_CUDA(cudaMemcpy(*p, h, cnt * sizeof(**p), cudaMemcpyHostToDevice));
+        return CFD_OK;
+    };
+    int rc;
+    if ((rc = up(&g->ptr, ptr.data(), npoin + 1))) return rc;
+    if ((rc = up(&g->nbr, nbr.data(), m))) return rc;
+    if ((rc = up(&g->src, src.data(), m))) return rc;
+    if ((rc = up(&g->rev, rev.data(), m))) return rc;
+    if ((rc = up(&g->kind, kind.data(), npoin))) return rc;
+    if ((rc = up(&g->bnode, bnode0, nb))) return rc;
+    if ((rc = up(&g->bkind, bkind, nb))) return rc;
+    if ((rc = up(&g->X, x, npoin))) return rc;
+    if ((rc = up(&g->Y, y, npoin))) return rc;
+    for (double** q : {&g->bgx, &g->bgy})
+        if ((rc = dev_alloc(o, q, nb))) return rc;
+    for (double** q : {&g->gnx, &g->gny, &g->ux, &g->uy, &g->uz})
+        if ((rc = dev_alloc(o, q, npoin))) return rc;
+    CFD_CUDA(cudaMemset(g->gnx, 0, sizeof(double) * npoin));
+    CFD_CUDA(cudaMemset(g->gny, 0, sizeof(double) * npoin));
+    CFD_CUDA(cudaMemset(g->bgx, 0, sizeof(double) * nb));
+    CFD_CUDA(cudaMemset(g->bgy, 0, sizeof(double) * nb));
+    if ((rc = dev_alloc(o, &g->G, 1))) return rc;
+    const size_t n = npoin;
+    if ((rc = dev_alloc(o, &g->f, n * F_IN))) return rc;
+    if ((rc = dev_alloc(o, &g->e, (size_t)m * E_F))) return rc;
+    if (training) {
+        if ((rc = dev_alloc(o, &g->target, n * OUT))) return rc;
+        if ((rc = dev_alloc(o, &g->a0, n * HID))) return rc;
+        for (int l = 0; l <= LAYERS; ++l)
+            if ((rc = dev_alloc(o, &g->h[l], n * HID))) return rc;
+        for (int l = 0; l < LAYERS; ++l) {
+            if ((rc = dev_alloc(o, &g->agg[l], n * HID))) return rc;
+            if ((rc = dev_alloc(o, &g->v[l], n * HID))) return rc;
+            if ((rc = dev_alloc(o, &g->z[l], (size_t)m * HID))) return rc;
+        }
+        if ((rc = dev_alloc(o, &g->pq, n * 2 * HID))) return rc;
+        if ((rc = dev_alloc(o, &g->y, n * OUT))) return rc;
+        if ((rc = dev_alloc(o, &g->dy, n * OUT))) return rc;
+        if ((rc = dev_alloc(o, &g->dh, n * HID))) return rc;
+        if ((rc = dev_alloc(o, &g->dhc, n * 2 * HID))) return rc;
+        if ((rc = dev_alloc(o, &g->dz, (size_t)m * HID))) return rc;
+        if ((rc = dev_alloc(o, &g->dpq, n * 2 * HID))) return rc;
+        if ((rc = dev_alloc(o, &g->dpqh, n * HID))) return rc;
+        // partials of the largest weight gradient: rows/WG chunks x (128*64 + 128) floats
+        const long rows = std::max<long>(npoin, m);
+        g->part_floats = (size_t)blocks_for(rows, WG) * (2 * HID * HID + 2 * HID);
+        if ((rc = dev_alloc(o, &g->part, g->part_floats))) return rc;
+        if ((rc = dev_alloc(o, &g->lpart, blocks_for(npoin, 256) + 1))) return rc;
+    }
+    g->training = training;
+    if ((rc = dev_alloc(o, &g->hb, n * HID))) return rc;
+    if ((rc = dev_alloc(o, &g->pqb, 2 * n * 2 * HID))) return rc;  // two P|Q buffers
+    if ((rc = dev_alloc(o, &g->yb, n * OUT))) return rc;
+    // geometry globals (zero displacement), node and edge features
+    const int* ng = nullptr;
+    CFD_LAUNCH(k_globals, 1, 256, 0, st, g->nb, g->bnode, g->bkind, (const double*)g->bgx,
+               (const double*)g->bgy, (const double*)g->X, (const double*)g->Y, g->G, ng);
+    CFD_LAUNCH(k_features, blocks_for(g->n, 256), 256, 0, st, g->n, (const double*)g->X,
+               (const double*)g->Y, g->kind, (const Globals*)g->G, g->f, ng);
+    CFD_LAUNCH(k_edge_features, blocks_for(g->m, 256), 256, 0, st, g->m, g->src, g->nbr,
+               (const double*)g->X, (const double*)g->Y, (const Globals*)g->G, g->e, ng);
+    CFD_CUDA(cudaStreamSynchronize(st));
+    *out = g.release();
+    return CFD_OK;
+}
+
+// The guess (ux, uy) on stream st for the mesh (X, Y) and the boundary displacement
+// (bgx, bgy) in bnode order (device arrays); every kernel returns at once when gate is
+// non-null and *gate == 0.
+int guess_on_stream(cfd_mpnn* net, cfd_mpnn_graph* g, cudaStream_t st, const double* X,
+                    const double* Y, const double* bgx, const double* bgy, double* ux,
+                    double* uy, const int* gate) {
+    // grid-stride launches of a few waves: a closed gate costs little
+    const unsigned gs = 1216;
+    const int nbk = (int)blocks_for(g->nb, 256);
+    CFD_LAUNCH(k_scatter_bc, nbk, 256, 0, st, g->nb, g->bnode, bgx, bgy, g->gnx, g->gny, gate);
+    CFD_LAUNCH(k_globals, 1, 256, 0, st, g->nb, g->bnode, g->bkind, bgx, bgy, X, Y, g->G, gate);
+    CFD_LAUNCH(k_features, std::min(blocks_for(g->n, 256), gs), 256, 0, st, g->n, X, Y, g->kind,
+               (const Globals*)g->G, g->f, gate);
+    CFD_LAUNCH(k_edge_features, std::min(blocks_for(g->m, 256), gs), 256, 0, st, g->m, g->src,
+               g->nbr, X, Y, (const Globals*)g->G, g->e, gate);
+    int rc = infer_bf16(st, net->w, net->wb, &net->wb_valid, g->n, g->ptr, g->nbr, g->f, g->e,
+                        g->hb, g->pqb, g->yb, gate);
+    if (rc) return rc;
+    CFD_LAUNCH(k_guess, std::min(blocks_for(g->n, 256), gs), 256, 0, st, g->n,
+               (const float*)g->yb, g->kind, (const double*)g->gnx, (const double*)g->gny,
+               (const Globals*)g->G, ux, uy, gate);
+    return CFD_OK;
+}
+
+void graph_free(cfd_mpnn_graph* g) { delete g; }
+
+}  // namespace mpnn
+}  // namespace cfd
+
 // ------------------------------------------------------------------ extern "C"
 extern "C" {
 
@@ -225,8 +374,6 @@ int cfd_mpnn_graph_create(cfd_mpnn_graph** out, int npoin, int nelem, const int*
     if (npoin <= 0 || nelem <= 0 || nb <= 0) return arg_err("sizes");
     if (!check_index_range(inpoel, 3L * nelem, 1, npoin) || !check_index_range(bnode, nb, 1, npoin))
         return CFD_ERR_MESH;
-    for (int k = 0; k < nb; ++k)
-        if (bkind[k] != KIND_BODY && bkind[k] != KIND_OUTER) return arg_err("bkind (1 body, 2 outer)");
     Adjacency adj;
     std::string why;
     int rc = build_adjacency(npoin, nelem, inpoel, adj, &why);
@@ -234,106 +381,9 @@ int cfd_mpnn_graph_create(cfd_mpnn_graph** out, int npoin, int nelem, const int*
         set_last_message(why);
         return rc;
     }
-    // neighbours = the Laplacian pattern without its diagonal (first entry of each row)
-    std::vector<int> ptr(npoin + 1, 0), nbr, src, rev;
-    for (int i = 0; i < npoin; ++i) {
-        for (int k = adj.rowptr[i] + 1; k < adj.rowptr[i + 1]; ++k) {
-            nbr.push_back(adj.col[k]);
-            src.push_back(i);
-        }
-        ptr[i + 1] = (int)nbr.size();
-    }
-    const int m = (int)nbr.size();
-    rev.assign(m, -1);
-    for (int k = 0; k < m; ++k) {
-        const int i = src[k], j = nbr[k];
-        for (int q = ptr[j]; q < ptr[j + 1]; ++q)
-            if (nbr[q] == i) {
-                rev[k] = q;
-                break;
-            }
-        if (rev[k] < 0) {
-            set_last_message("mpnn: point neighbours are not symmetric");
-            return CFD_ERR_MESH;
-        }
-    }
-    std::vector<int> kind(npoin, KIND_FREE), bn(nb);
-    for (int k = 0; k < nb; ++k) {
-        bn[k] = bnode[k] - 1;
-        kind[bn[k]] = bkind[k];
-    }
-    int nfree = 0;
-    for (int i = 0; i < npoin; ++i) nfree += kind[i] == KIND_FREE;
-    std::unique_ptr<cfd_mpnn_graph> g(new cfd_mpnn_graph());
-    g->n = npoin;
-    g->m = m;
-    g->nb = nb;
-    g->nfree = nfree;
-    CFD_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
-    auto& o = g->owned;
-    auto up = [&](auto** p, const auto* h, size_t cnt) -> int {
-        int r = dev_alloc(o, p, cnt);
-        if (r) return r;
-        CFD_CUDA(cudaMemcpy(*p, h, cnt * sizeof(**p), cudaMemcpyHostToDevice));
-        return CFD_OK;
-    };
-    if ((rc = up(&g->ptr, ptr.data(), npoin + 1))) return rc;
-    if ((rc = up(&g->nbr, nbr.data(), m))) return rc;
-    if ((rc = up(&g->src, src.data(), m))) return rc;
-    if ((rc = up(&g->rev, rev.data(), m))) return rc;
-    if ((rc = up(&g->kind, kind.data(), npoin))) return rc;
-    if ((rc = up(&g->bnode, bn.data(), nb))) return rc;
-    if ((rc = up(&g->bkind, bkind, nb))) return rc;
-    if ((rc = up(&g->X, x, npoin))) return rc;
-    if ((rc = up(&g->Y, y, npoin))) return rc;
-    for (double** q : {&g->bgx, &g->bgy})
-        if ((rc = dev_alloc(o, q, nb))) return rc;
-    for (double** q : {&g->gnx, &g->gny, &g->ux, &g->uy, &g->uz})
-        if ((rc = dev_alloc(o, q, npoin))) return rc;
-    CFD_CUDA(cudaMemset(g->gnx, 0, sizeof(double) * npoin));
-    CFD_CUDA(cudaMemset(g->gny, 0, sizeof(double) * npoin));
-    CFD_CUDA(cudaMemset(g->bgx, 0, sizeof(double) * nb));
-    CFD_CUDA(cudaMemset(g->bgy, 0, sizeof(double) * nb));
-    if ((rc = dev_alloc(o, &g->G, 1))) return rc;
-    const size_t n = npoin;
-    if ((rc = dev_alloc(o, &g->f, n * F_IN))) return rc;
-    if ((rc = dev_alloc(o, &g->e, (size_t)m * E_F))) return rc;
-    if ((rc = dev_alloc(o, &g->target, n * OUT))) return rc;
-    if ((rc = dev_alloc(o, &g->a0, n * HID))) return rc;
-    for (int l = 0; l <= LAYERS; ++l)
-        if ((rc = dev_alloc(o, &g->h[l], n * HID))) return rc;
-    for (int l = 0; l < LAYERS; ++l) {
-        if ((rc = dev_alloc(o, &g->agg[l], n * HID))) return rc;
-        if ((rc = dev_alloc(o, &g->v[l], n * HID))) return rc;
-        if ((rc = dev_alloc(o, &g->z[l], (size_t)m * HID))) return rc;
-    }
-    if ((rc = dev_alloc(o, &g->pq, n * 2 * HID))) return rc;
-    if ((rc = dev_alloc(o, &g->y, n * OUT))) return rc;
-    if ((rc = dev_alloc(o, &g->dy, n * OUT))) return rc;
-    if ((rc = dev_alloc(o, &g->dh, n * HID))) return rc;
-    if ((rc = dev_alloc(o, &g->dhc, n * 2 * HID))) return rc;
-    if ((rc = dev_alloc(o, &g->dz, (size_t)m * HID))) return rc;
-    if ((rc = dev_alloc(o, &g->dpq, n * 2 * HID))) return rc;
-    if ((rc = dev_alloc(o, &g->dpqh, n * HID))) return rc;
-    // partials of the largest weight gradient: rows/WG chunks x (128*64) floats
-    const long rows = std::max<long>(npoin, m);
-    g->part_floats = (size_t)blocks_for(rows, WG) * (2 * HID * HID + 2 * HID);
-    if ((rc = dev_alloc(o, &g->part, g->part_floats))) return rc;
-    if ((rc = dev_alloc(o, &g->lpart, blocks_for(npoin, 256) + 1))) return rc;
-    if ((rc = dev_alloc(o, &g->hb, n * HID))) return rc;
-    if ((rc = dev_alloc(o, &g->pqb, 2 * n * 2 * HID))) return rc;  // two P|Q buffers
-    if ((rc = dev_alloc(o, &g->yb, n * OUT))) return rc;
-    // geometry globals (zero displacement), node and edge features
-    cudaStream_t st = g->stream;
-    CFD_LAUNCH(k_globals, 1, 256, 0, st, g->nb, g->bnode, g->bkind, (const double*)g->bgx,
-               (const double*)g->bgy, (const double*)g->X, (const double*)g->Y, g->G);
-    CFD_LAUNCH(k_features, blocks_for(g->n, 256), 256, 0, st, g->n, (const double*)g->X,
-               (const double*)g->Y, g->kind, (const Globals*)g->G, g->f);
-    CFD_LAUNCH(k_edge_features, blocks_for(g->m, 256), 256, 0, st, g->m, g->src, g->nbr,
-               (const double*)g->X, (const double*)g->Y, (const Globals*)g->G, g->e);
-    CFD_CUDA(cudaStreamSynchronize(st));
-    *out = g.release();
-    return CFD_OK;
+    std::vector<int> bn(nb);
+    for (int k = 0; k < nb; ++k) bn[k] = bnode[k] - 1;
+    return graph_build(out, npoin, adj.rowptr, adj.col, x, y, nb, bn.data(), bkind, true, nullptr);
 }
 
 void cfd_mpnn_graph_destroy(cfd_mpnn_graph* g) { delete g; }
@@ -343,10 +393,11 @@ int cfd_mpnn_graph_set_bc(cfd_mpnn_graph* g, const double* gx, const double* gy)
     cudaStream_t st = g->stream;
     CFD_CUDA(cudaMemcpyAsync(g->bgx, gx, sizeof(double) * g->nb, cudaMemcpyHostToDevice, st));
     CFD_CUDA(cudaMemcpyAsync(g->bgy, gy, sizeof(double) * g->nb, cudaMemcpyHostToDevice, st));
+    const int* ng = nullptr;
     CFD_LAUNCH(k_scatter_bc, blocks_for(g->nb, 256), 256, 0, st, g->nb, g->bnode,
-               (const double*)g->bgx, (const double*)g->bgy, g->gnx, g->gny);
+               (const double*)g->bgx, (const double*)g->bgy, g->gnx, g->gny, ng);
     CFD_LAUNCH(k_globals, 1, 256, 0, st, g->nb, g->bnode, g->bkind, (const double*)g->bgx,
-               (const double*)g->bgy, (const double*)g->X, (const double*)g->Y, g->G);
+               (const double*)g->bgy, (const double*)g->X, (const double*)g->Y, g->G, ng);
     CFD_CUDA(cudaStreamSynchronize(st));
     return CFD_OK;
 }
@@ -364,6 +415,7 @@ int cfd_mpnn_graph_globals(cfd_mpnn_graph* g, double* out10) {
 int cfd_mpnn_graph_set_target(cfd_mpnn_graph* g, const double* phi, const double* psi_x,
                               const double* psi_y) {
     if (!g || !phi || !psi_x || !psi_y) return arg_err("null pointer");
+    if (!g->training) return arg_err("graph without training buffers");
     cudaStream_t st = g->stream;
     CFD_CUDA(cudaMemcpyAsync(g->ux, phi, sizeof(double) * g->n, cudaMemcpyHostToDevice, st));
     CFD_CUDA(cudaMemcpyAsync(g->uy, psi_x, sizeof(double) * g->n, cudaMemcpyHostToDevice, st));
@@ -376,6 +428,7 @@ int cfd_mpnn_graph_set_target(cfd_mpnn_graph* g, const double* phi, const double
 
 int cfd_mpnn_loss_grad(cfd_mpnn* net, cfd_mpnn_graph* g, float* loss, float* grad) {
     if (!net || !g) return arg_err("null pointer");
+    if (!g->training) return arg_err("graph without training buffers");
     int rc = forward_fp32(*net, *g);
     if (rc) return rc;
     float l = 0.f;
@@ -392,6 +445,7 @@ int cfd_mpnn_loss_grad(cfd_mpnn* net, cfd_mpnn_graph* g, float* loss, float* gra
 int cfd_mpnn_train_step(cfd_mpnn* net, cfd_mpnn_graph* g, float lr, float* loss) {
     if (!net || !g) return arg_err("null pointer");
     if (!(lr > 0.f)) return arg_err("lr");
+    if (!g->training) return arg_err("graph without training buffers");
     int rc = forward_fp32(*net, *g);
     if (rc) return rc;
     float l = 0.f;
@@ -417,11 +471,12 @@ int cfd_mpnn_adam_state(cfd_mpnn* net, float* m, float* v, int* t) {
 
 int cfd_mpnn_forward(cfd_mpnn* net, cfd_mpnn_graph* g, int bf16, double* ux, double* uy) {
     if (!net || !g) return arg_err("null pointer");
+    if (!bf16 && !g->training) return arg_err("graph without training buffers (FP32 pass)");
     int rc;
     const float* y = nullptr;
     if (bf16) {
         if ((rc = infer_bf16(g->stream, net->w, net->wb, &net->wb_valid, g->n, g->ptr, g->nbr, g->f,
-                             g->e, g->hb, g->pqb, g->yb)))
+                             g->e, g->hb, g->pqb, g->yb, nullptr)))
             return rc;
         y = g->yb;
     } else {
@@ -429,7 +484,8 @@ int cfd_mpnn_forward(cfd_mpnn* net, cfd_mpnn_graph* g, int bf16, double* ux, dou
         y = g->y;
     }
     CFD_LAUNCH(k_guess, blocks_for(g->n, 256), 256, 0, g->stream, g->n, y, g->kind,
-               (const double*)g->gnx, (const double*)g->gny, (const Globals*)g->G, g->ux, g->uy);
+               (const double*)g->gnx, (const double*)g->gny, (const Globals*)g->G, g->ux, g->uy,
+               (const int*)nullptr);
     if (ux) CFD_CUDA(cudaMemcpyAsync(ux, g->ux, sizeof(double) * g->n, cudaMemcpyDeviceToHost, g->stream));
     if (uy) CFD_CUDA(cudaMemcpyAsync(uy, g->uy, sizeof(double) * g->n, cudaMemcpyDeviceToHost, g->stream));
     CFD_CUDA(cudaStreamSynchronize(g->stream));

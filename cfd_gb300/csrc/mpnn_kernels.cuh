@@ -8,14 +8,16 @@ namespace mpnn {
 constexpr int DT = 32;  // nodes per block of the FP32 dense kernels
 constexpr int WG = 64;  // rows per weight-gradient partial
 
+// kernels with a `gate` argument return at once when gate != null and *gate == 0
 __global__ void k_globals(int nb, const int* bnode, const int* bkind, const double* gx,
-                          const double* gy, const double* X, const double* Y, Globals* G);
+                          const double* gy, const double* X, const double* Y, Globals* G,
+                          const int* gate);
 __global__ void k_scatter_bc(int nb, const int* bnode, const double* gx, const double* gy,
-                             double* gnx, double* gny);
+                             double* gnx, double* gny, const int* gate);
 __global__ void k_features(int n, const double* X, const double* Y, const int* kind,
-                           const Globals* G, float* f);
+                           const Globals* G, float* f, const int* gate);
 __global__ void k_edge_features(int m, const int* src, const int* nbr, const double* X,
-                                const double* Y, const Globals* G, float* e);
+                                const double* Y, const Globals* G, float* e, const int* gate);
 __global__ void k_dense(int n, const float* X1, int I1, const float* X2, int I2, const float* W,
                         const float* b, int O, float* Y);
 __global__ void k_dense_t(int n, const float* dY, int O, const float* W, int I, float* dX);
@@ -39,13 +41,14 @@ __global__ void k_adam(int np, float* w, const float* g, float* m, float* v, flo
 __global__ void k_targets(int n, const double* phi, const double* psx, const double* psy,
                           const Globals* G, float* t);
 __global__ void k_guess(int n, const float* y, const int* kind, const double* gnx,
-                        const double* gny, const Globals* G, double* ux, double* uy);
+                        const double* gny, const Globals* G, double* ux, double* uy,
+                        const int* gate);
 
 // BF16 tensor-core inference: y[n][OUT] from the features; wb (BF16 copy of w) is refreshed
 // when *wb_valid is false
 int infer_bf16(cudaStream_t st, const float* w, __nv_bfloat16* wb, bool* wb_valid, int n,
                const int* ptr, const int* nbr, const float* f, const float* e,
-               __nv_bfloat16* hb, __nv_bfloat16* pqb, float* y);
+               __nv_bfloat16* hb, __nv_bfloat16* pqb, float* y, const int* gate);
 
 }  // namespace mpnn
 }  // namespace cfd

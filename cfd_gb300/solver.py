@@ -210,6 +210,22 @@ class Solver:
         except Exception:
             pass
 
+    def set_guess_net(self, net, gate=20.0):
+        """Attach a learned-guess network (cfd_gb300.learned.Net; None detaches) to this
+        mixed-form context; used when the case's guess_mode is CFD_GUESS_LEARNED.  The
+        network runs on the first solve and after any solve that took more than `gate`
+        iterations (every solve when gate is 0)."""
+        self._net = net
+        check(abi.lib().cfd_ctx_set_guess_net(self.h, net.h if net is not None else None,
+                                              float(gate)), "cfd_ctx_set_guess_net")
+
+    def guess_stats(self):
+        """(steps with the network evaluated, x solves and y solves that took its guess,
+        steps) since the network was attached."""
+        out = (C.c_longlong * 4)()
+        check(abi.lib().cfd_ctx_guess_stats(self.h, out), "cfd_ctx_guess_stats")
+        return tuple(int(v) for v in out)
+
     def step(self, n=1):
         rep = abi.CfdStepReport()
         check(abi.lib().cfd_step(self.h, int(n), C.byref(rep)), "cfd_step")

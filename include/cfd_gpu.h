@@ -334,6 +334,18 @@ int cfd_mpnn_train_step(cfd_mpnn* net, cfd_mpnn_graph* g, float lr, float* loss)
  * the tensor-core pass, 0 for the FP32 pass. */
 int cfd_mpnn_forward(cfd_mpnn* net, cfd_mpnn_graph* g, int bf16, double* ux, double* uy);
 
+/* Learned guess in a resident context (mixed form, params.guess_mode = CFD_GUESS_LEARNED):
+ * the network's guess is formed on the first mesh-motion solve after attaching, and then
+ * whenever the previous step's solve took more than `gate` iterations (every step when
+ * gate = 0); per solve it replaces the previous-step guess if its r.z (the solve's measure
+ * of convergence) is the smaller, so the plain guess stays the fallback and the judge.
+ * net = NULL detaches it (previous-step guess).  The network must outlive its use by the
+ * context. */
+int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate);
+/* counters since attach: steps with the network evaluated, solves 1 (x) and 2 (y) that
+ * took the network's guess, steps */
+int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4);
+
 /* Number of kernels this library launched since process start (all contexts). */
 long long cfd_kernel_launches(void);
 

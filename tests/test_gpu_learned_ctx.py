@@ -1,0 +1,70 @@
+"""The learned guess inside the resident mixed-form step (CFD_GUESS_LEARNED): the network
+is evaluated when the gate opens, its guess is taken only when its residual is smaller,
+and BiCG still finishes to the plain tolerance.  The solve's tolerance is absolute
+(r.z < 1e-10, biconjGrad.f90:26) and loose against the per-step increments of these
+cases, so two guesses give two admissible mesh motions: the flow is compared with the
+previous-step-guess run to the bound that this allows."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import small_case
+
+pytestmark = pytest.mark.gpu
+
+
+def run(k, steps, net=None, gate=0.0):
+    from cfd_gb300 import abi, solver
+    S = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    if net is not None:
+        S.set_guess_net(net, gate)
+    reps = [S.step(1) for _ in range(steps)]
+    st = S.state()
+    stats = S.guess_stats() if net is not None else None
+    S.close()
+    return reps, st, stats
+
+
+def test_learned_guess_in_the_step(gpu_lib):
+    from cfd_gb300 import abi, learned
+    if not os.path.exists(learned.DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights in the package")
+    net = learned.Net.load()
+    kw = dict(scale=48, seed=13, estab_mode=abi.CFD_ESTAB_REGULARIZED, fsafe=0.25)
+    kp = small_case(3, **kw)
+    kl = small_case(3, **kw)
+    kl.params.guess_mode = abi.CFD_GUESS_LEARNED
+    steps = 6
+    rp, sp, _ = run(kp, steps)
+    rl, sl, stats = run(kl, steps, net, gate=0.0)
+    # gate 0: evaluated every step; the cold first step takes the network's guess
+    assert stats[0] == steps and stats[3] == steps
+    assert stats[2] >= 1
+    it_prev = sum(rp[0].bicg_iters)
+    it_net = sum(rl[0].bicg_iters)
+    assert it_net < it_prev, (it_net, it_prev)
+    for r in rl:
+        assert all(r.bicg_converged)
+    for q in range(4):
+        d = np.linalg.norm(sl["U"][:, q] - sp["U"][:, q])
+        assert d <= 2e-5 * np.linalg.norm(sp["U"][:, q]) + 1e-12
+
+
+def test_gate_runs_the_network_on_the_cold_solve_only(gpu_lib):
+    """gate = iteration threshold: the network runs on the first solve after attaching and
+    again only after a solve that took more iterations than the gate."""
+    from cfd_gb300 import abi, learned
+    if not os.path.exists(learned.DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights in the package")
+    net = learned.Net.load()
+    kw = dict(scale=48, seed=13, estab_mode=abi.CFD_ESTAB_REGULARIZED, fsafe=0.25)
+    kl = small_case(3, **kw)
+    kl.params.guess_mode = abi.CFD_GUESS_LEARNED
+    reps, _, stats = run(kl, 6, net, gate=1.0e9)
+    assert stats[0] == 1 and stats[3] == 6
+    reps2, _, stats2 = run(small_case(3, **dict(kw, guess_mode=abi.CFD_GUESS_LEARNED)), 6, net,
+                           gate=0.5)
+    # after the cold solve, steps whose solve took >= 1 iteration trigger the next one
+    expect = 1 + sum(1 for r in reps2[:-1] if max(r.bicg_iters) > 0.5)
+    assert stats2[0] == expect and stats2[3] == 6
