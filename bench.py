@@ -168,6 +168,18 @@ def config_dict(k, args, ws):
 # Algorithmic bytes per launch of each timed group: every array a launch must touch, read
 # or written once (gathers of node data count once per node).  N nodes, E elements, and
 # 3E element-around-point slots (~6 per node).
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per step of the timed groups
+# of the mixed form on the 1,048,576-node workload, from the ncu capture summarised in
+# profiles/step_mixed_1M_launches.md (the full-size workload fits the capture rules: ~2.5 GB
+# on the device, kernels of 13-130 us).
+NCU_TRAFFIC_PER_STEP = {
+    "update_t": 1063.7e6,   # 4 node passes + 3 mu/lambda passes
+    "calcrhs_t": 374.8e6,
+    "estab_t": 174.2e6,
+    "laplace_t": 198.0e6,
+}
+
+
 def algorithmic_bytes(k, iters, precision):
     """Algorithmic DRAM bytes per STEP of each timed group: every array element the group
     must read or write once (gathered node/element values counted once)."""
@@ -290,7 +302,10 @@ def main_accuracy(args):
         ferr[1] = max(ferr[1], abs(rm.fy[0] - rd.fy[0]))
         if s % 100 == 0 or s == args.accuracy_steps:
             Um, Ud = Sm.state()["U"], Sd.state()["U"]
+            mom = np.linalg.norm(Ud[:, 1:3])
             hist.append({"step": s, "rel_l2": [rel_l2(Um[:, q], Ud[:, q]) for q in range(4)],
+                         "rel_l2_state": rel_l2(Um, Ud),
+                         "rel_l2_momentum": float(np.linalg.norm(Um[:, 1:3] - Ud[:, 1:3]) / mom),
                          "finite": bool(np.isfinite(Um).all() and np.isfinite(Ud).all())})
     Sm.close()
     Sd.close()
@@ -298,6 +313,8 @@ def main_accuracy(args):
             "npoin": km.npoin, "steps": args.accuracy_steps, "estab_mode": "regularized",
             "final_rel_l2": hist[-1]["rel_l2"] if hist else None,
             "max_rel_l2": [max(h["rel_l2"][q] for h in hist) for q in range(4)] if hist else None,
+            "final_rel_l2_state": hist[-1]["rel_l2_state"] if hist else None,
+            "final_rel_l2_momentum": hist[-1]["rel_l2_momentum"] if hist else None,
             "force_err_rel_max": [e / fmax if fmax > 0 else None for e in ferr],
             "history": hist}
     print(json.dumps(line), flush=True)
@@ -473,8 +490,13 @@ def main_ours(args):
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     ach = ab[dom] / per_step[dom] / 1e9 if dom in ab else None
+    traffic = None
+    if mixed and args.scale is None and dom in NCU_TRAFFIC_PER_STEP:
+        traffic = NCU_TRAFFIC_PER_STEP[dom] / calls_per_step[dom]
     roofline = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                "frac": (ach / hbm_peak) if ach else None, "traffic": None,
+                "frac": (ach / hbm_peak) if ach else None, "traffic": traffic,
+                "traffic_source": "ncu capture, profiles/step_mixed_1M_launches.md"
+                if traffic else None,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
                 "share_of_step": per_step[dom] / total if total else None,
                 "launch_ms": per_launch[dom] * 1e3,
