@@ -132,6 +132,7 @@ SIGNATURES = {
     "cfd_mpnn_forward": (C.c_int, [_P, _P, C.c_int, _dp, _dp]),
     "cfd_ctx_set_guess_net": (C.c_int, [_P, _P, C.c_double]),
     "cfd_ctx_guess_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "cfd_ctx_graph_state": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_create": (C.c_int, [C.POINTER(_P), C.POINTER(CfdMesh), C.POINTER(CfdParams),
                                  C.c_int]),
     "cfd_ctx_destroy": (None, [_P]),

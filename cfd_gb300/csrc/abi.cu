@@ -277,6 +277,13 @@ int cfd_ctx_set_clock(cfd_ctx* ctx, int iter, double time, double dtmin1, int ba
     sc.dtmin1 = dtmin1;
     sc.bandera = bandera;
     CFD_CUDA(cudaMemcpyAsync(c.d_scal, &sc, sizeof(sc), cudaMemcpyHostToDevice, c.stream));
+    MotionScal ms{};
+    ms.time = time;
+    ms.disn0 = disn1;
+    ms.disn1 = disn2;
+    ms.ca = 1.0;
+    if (c.d_motion)
+        CFD_CUDA(cudaMemcpyAsync(c.d_motion, &ms, sizeof(ms), cudaMemcpyHostToDevice, c.stream));
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     return CFD_OK;
 }
@@ -298,6 +305,15 @@ int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4) {
                              c.stream));
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     out4[3] = c.guess_steps;
+    return CFD_OK;
+}
+
+int cfd_ctx_graph_state(cfd_ctx* ctx, long long* out3) {
+    if (!ctx || !out3) return arg_error("null pointer");
+    const Ctx& c = ctx->impl;
+    out3[0] = c.graphs_on ? 1 : 0;
+    out3[1] = c.graph_replays;
+    out3[2] = c.graph_kernels;
     return CFD_OK;
 }
 

@@ -103,6 +103,17 @@ struct Ctx {
     bool guess_first = false;    // the first solve after attaching runs the network
     long long guess_steps = 0;
     int* h_iters = nullptr;      // pinned copy of the last solve's iteration counts
+    cudaEvent_t ev_iters = nullptr;  // recorded after that copy
+    // mixed form: the clock and the motion increment live on the device
+    MotionScal* d_motion = nullptr;
+    // mixed form: one step (the network not run) captured as a CUDA graph and replayed;
+    // off with the timers or CFD_GRAPHS=0, or when the capture fails
+    bool graphs_on = false, capturing = false;
+    cudaGraph_t step_graph = nullptr;
+    cudaGraphExec_t step_exec = nullptr;
+    long long graph_kernels = 0;  // kernels of one replay
+    long long mixed_steps = 0;    // steps of this context (the first runs uncaptured)
+    long long graph_replays = 0;
     int* d_slot_pos = nullptr;
     float4 *d_recInv = nullptr, *d_recVisc = nullptr;  // slot records, element-around-point order
     float4* d_invSum = nullptr;                         // per node: sum of the recInv slots
@@ -135,7 +146,9 @@ struct Ctx {
     int geometry_mixed(bool setup, bool put_area = false);
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
     int widen_mixed();
-    int run_pcg(int nsolve);
+    int run_pcg(int nsolve, bool learned = false);
+    int enqueue_mixed(bool learned);
+    int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);
     int step_once();
     int step_once_mixed();

@@ -39,6 +39,19 @@ inline GasConstF to_float(const GasConst& g) {
                      (float)g.t_inf, (float)g.cte, (float)g.fr};
 }
 
+// Device-side clock and motion increment of the mixed form (the FP64 form keeps them on the
+// host, where the oracle computes its sin/cos)
+struct MotionScal {
+    double time, disn0, disn1;  // TIME, DISN(1:2) (heave, pitch)
+    double ca, sa, yposr;       // this step's TRANSF increment
+    double dtmin;               // DTMIN of the step
+};
+__global__ void k_motion_law(const StepScal* sc, MotionScal* m, int law, double heave_amp,
+                             double pitch_amp, double freq);
+__global__ void k_transf_dev(int nnmove, const int* fix_node, const int* fix_set, const double* X,
+                             const double* Y, const double* xref, const double* yref,
+                             const MotionScal* m, double* xfix_x, double* xfix_y);
+
 // ------------------------------------------------------------------ mixed precision
 __global__ void k_narrow_state(int npoin, const double* U, const double* T, const double* VX,
                                const double* VY, const double* X, const double* Y,

@@ -82,6 +82,9 @@ Ctx::~Ctx() {
     for (void* p : allocs) cudaFree(p);
     if (h_scal) cudaFreeHost(h_scal);
     if (h_iters) cudaFreeHost(h_iters);
+    if (step_exec) cudaGraphExecDestroy(step_exec);
+    if (step_graph) cudaGraphDestroy(step_graph);
+    if (ev_iters) cudaEventDestroy(ev_iters);
     if (ev_scal) cudaEventDestroy(ev_scal);
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (auto& m : mark)
@@ -117,7 +120,7 @@ int Ctx::geometry(bool masas, bool with_laplace) {
 }
 
 // ------------------------------------------------------------------ PCG launch
-int Ctx::run_pcg(int nsolve) {
+int Ctx::run_pcg(int nsolve, bool learned) {
     PcgArgs a{};
     a.n = npoin;
     a.nsolve = nsolve;
@@ -161,19 +164,8 @@ int Ctx::run_pcg(int nsolve) {
         a.nblk_r = blocks_for(npoin, 256);
         a.bscal = d_bscal;
         a.bcount = d_bcount;
-        // learned guess: the network runs on the first solve after it was attached, and
-        // when the previous step's solve took more than guess_gate iterations (every solve
-        // when guess_gate is 0); the judge then keeps, per solve, the guess with the
-        // smaller r.z.  The previous step's counts are in pinned memory, complete since
-        // the host waited for this step's DTMIN.
-        const bool has_net = prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph;
-        bool learned = false;
-        if (has_net) {
-            guess_steps += 1;
-            learned = guess_first || guess_gate <= 0.0 ||
-                      (double)std::max(h_iters[0], h_iters[1]) > guess_gate;
-            guess_first = false;
-        }
+        // learned guess (decided by the caller): the judge keeps, per solve, the network's
+        // guess or the previous step's, whichever has the smaller r.z
         a.gflag = learned ? d_gflag : nullptr;
         a.gate = 0.0;
         a.only_if = nullptr;
@@ -204,9 +196,13 @@ int Ctx::run_pcg(int nsolve) {
     CFD_CUDA(cudaLaunchCooperativeKernel(mixed ? (void*)k_pcg_mixed : (void*)k_pcg_fp64, dim3(pcg_grid),
                                          dim3(256), args, 0, stream));
     g_launches.fetch_add(1, std::memory_order_relaxed);
-    if (h_iters)
+    if (h_iters) {  // the next step's learned-guess decision reads these
         CFD_CUDA(cudaMemcpyAsync(h_iters, d_pcg_iters, 2 * sizeof(int), cudaMemcpyDeviceToHost,
                                  stream));
+        // inside a capture the record becomes a node of the graph
+        CFD_CUDA(cudaEventRecordWithFlags(ev_iters, stream,
+                                          capturing ? cudaEventRecordExternal : cudaEventRecordDefault));
+    }
     return CFD_OK;
 }
 
@@ -246,6 +242,9 @@ int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
         if ((st = dalloc(&d_gstats, 4))) return st;
         CFD_CUDA(cudaMallocHost((void**)&h_iters, 2 * sizeof(int)));
         h_iters[0] = h_iters[1] = 0;
+        // the captured step has no copy of the counts yet: capture it again
+        if (step_exec) { cudaGraphExecDestroy(step_exec); step_exec = nullptr; }
+        if (step_graph) { cudaGraphDestroy(step_graph); step_graph = nullptr; }
         CFD_CUDA(cudaMemsetAsync(d_gflag, 0, 2 * sizeof(int), stream));
         CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 4 * sizeof(long long), stream));
         CFD_CUDA(cudaStreamSynchronize(stream));
@@ -373,7 +372,16 @@ int Ctx::step(int nsteps, cfd_step_report* rep) {
     CFD_CUDA(cudaMemcpyAsync(cv, d_pcg_conv, sizeof(cv), cudaMemcpyDeviceToHost, stream));
     CFD_CUDA(cudaMemcpyAsync(rz, d_pcg_rz, sizeof(rz), cudaMemcpyDeviceToHost, stream));
     CFD_CUDA(cudaMemcpyAsync(&gb, d_bar, sizeof(gb), cudaMemcpyDeviceToHost, stream));
+    MotionScal ms{};
+    if (d_motion)
+        CFD_CUDA(cudaMemcpyAsync(&ms, d_motion, sizeof(ms), cudaMemcpyDeviceToHost, stream));
     CFD_CUDA(cudaStreamSynchronize(stream));
+    if (d_motion && nsteps > 0) {  // the mixed form's clock is kept on the device
+        time = ms.time;
+        last_dtmin = ms.dtmin;
+        disn[0] = ms.disn0;
+        disn[1] = ms.disn1;
+    }
     if (gb.err) {
         set_last_message("a grid barrier of the BiCG kernel gave up waiting");
         return CFD_ERR_BARRIER;
@@ -441,6 +449,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     }
     CFD_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CFD_CUDA(cudaEventCreateWithFlags(&ev_scal, cudaEventDisableTiming));
+    CFD_CUDA(cudaEventCreateWithFlags(&ev_iters, cudaEventDisableTiming));
     CFD_CUDA(cudaMallocHost((void**)&h_scal, sizeof(StepScal)));
     // mesh
     std::vector<int4> el(E);
@@ -591,6 +600,9 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_recInv, 3 * (size_t)E))) return st;
         if ((st = dalloc(&d_recVisc, 3 * (size_t)E))) return st;
         if ((st = dalloc(&d_invSum, N))) return st;
+        if ((st = dalloc(&d_motion, 1))) return st;
+        CFD_CUDA(cudaMemsetAsync(d_motion, 0, sizeof(MotionScal), stream));
+        graphs_on = !timers_on && !(getenv("CFD_GRAPHS") && atoi(getenv("CFD_GRAPHS")) == 0);
         if ((st = narrow_mixed(true, true, true, true, true, true))) return st;
     }
     // setup geometry: NORMALES, DERIV, MASAS, laplace (ns2DComp.ALE.f90:88-100)
@@ -650,10 +662,11 @@ int Ctx::geometry_mixed(bool setup, bool put_area) {
     return CFD_OK;
 }
 
-int Ctx::step_once_mixed() {
+// The device work of one mixed step, in order.  No host wait: DTMIN, the clock and the
+// motion increment stay on the device, so the sequence can be captured as a graph.
+int Ctx::enqueue_mixed(bool learned) {
     const int N = npoin, E = nelem;
     const int TB = 256;
-    iter += 1;
     tstart(TM_DELTAT);
     CFD_LAUNCH(k_deltat_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf, d_VYf,
                d_Wf, d_areaf, (float)prm.fsafe, (float)prm.t_inf, &d_scal->dtmin32_bits, d_blockmin);
@@ -665,8 +678,6 @@ int Ctx::step_once_mixed() {
     }
     CFD_LAUNCH(k_dt_finalize, 1, 1, 0, stream, d_scal);
     tstop(TM_DELTAT);
-    CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
-    CFD_CUDA(cudaEventRecord(ev_scal, stream));
     tstart(TM_ESTAB);
     CFD_LAUNCH(k_estab_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Uhi, d_Ulo, d_Tf,
                (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VXf, d_VYf, d_Wf,
@@ -683,7 +694,8 @@ int Ctx::step_once_mixed() {
                                       d_recInv, d_recVisc, d_mulam));
     tstop(TM_CALCRHS);
     // stage s uses mu, lambda from the T of stage s-1 (the reference's module T): stage 1's
-    // come from the element kernel above, the others from k_elem_mulam before the node pass
+    // come from the element kernel above, the others from k_elem_mulam before the node pass.
+    // The last stage updates U in place.
     const int NRK = 4;
     for (int irk = 1; irk <= NRK; ++irk) {
         const float rk_fact = 1.f / (float)(NRK + 1 - irk);
@@ -694,33 +706,21 @@ int Ctx::step_once_mixed() {
         CFD_CUDA(launch_node_mixed(stream, N, d_esup_ptr, d_esup_slot, d_mulam, d_recInv, d_recVisc,
                                    d_invSum, irk == 1 ? 1 : 0, gc, gf, viscous ? 1 : 0, d_U, d_Uhi,
                                    d_Ulo, d_invMf, rk_fact, irk == NRK ? 1 : 0, d_bcflag, d_bcval,
-                                   d_nrm, d_WX, d_WY, d_U1, d_RHOf, d_VXf, d_VYf, d_Ef, d_Pf, d_Tf,
+                                   d_nrm, d_WX, d_WY, d_U, d_RHOf, d_VXf, d_VYf, d_Ef, d_Pf, d_Tf,
                                    d_RMACHf));
         tstop(TM_UPDATE);
     }
-    CFD_CUDA(cudaEventSynchronize(ev_scal));
-    const double dtmin = h_scal->dtmin;
-    time = time + dtmin;
-    last_dtmin = dtmin;
     tstart(TM_FORCES);
     CFD_LAUNCH(k_forces_tree, 1, 256, 0, stream, bc.nset_numb, d_set_ptr, d_set_edges, d_Pf, d_X, d_Y,
                d_xref, d_yref, d_scal);
     tstop(TM_FORCES);
-    const double PI = std::acos(-1.0);
-    double alphav = disn[1], yposrv = disn[0];
-    if (prm.motion_law == CFD_MOTION_HARMONIC) {
-        double ph = 2.0 * PI * prm.motion_freq * time;
-        disn[0] = prm.heave_amp * std::sin(ph);
-        disn[1] = prm.pitch_amp * std::sin(ph);
-    } else {
-        disn[1] = (PI / 8.0) * std::sin(10.0 * time);
-    }
-    const double alpha = disn[1] - alphav, yposr = disn[0] - yposrv;
-    const double ca = std::cos(alpha), sa = std::sin(alpha);
     tstart(TM_TRANSF);
+    CFD_LAUNCH(k_motion_law, 1, 1, 0, stream, (const StepScal*)d_scal, d_motion, prm.motion_law,
+               prm.heave_amp, prm.pitch_amp, prm.motion_freq);
     if (nnmove > 0)
-        CFD_LAUNCH(k_transf, blocks_for(nnmove, TB), TB, 0, stream, nnmove, d_fix_node, d_fix_set,
-                   d_X, d_Y, d_xref, d_yref, ca, sa, yposr, d_xfix[0], d_xfix[1]);
+        CFD_LAUNCH(k_transf_dev, blocks_for(nnmove, TB), TB, 0, stream, nnmove, d_fix_node,
+                   d_fix_set, d_X, d_Y, d_xref, d_yref, (const MotionScal*)d_motion, d_xfix[0],
+                   d_xfix[1]);
     tstop(TM_TRANSF);
     if (prm.guess_mode == CFD_GUESS_ZERO) {
         for (int c = 0; c < 2; ++c) {
@@ -729,7 +729,7 @@ int Ctx::step_once_mixed() {
         }
     }
     tstart(TM_GRAD);
-    int st = run_pcg(2);
+    int st = run_pcg(2, learned);
     if (st) return st;
     tstop(TM_GRAD);
     CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1],
@@ -738,8 +738,71 @@ int Ctx::step_once_mixed() {
         st = geometry_mixed(false);
         if (st) return st;
     }
-    std::swap(d_U, d_U1);
+    return CFD_OK;
+}
+
+// Replay the captured step, capturing it first.  *launched = false when the capture is
+// not possible here (the caller then enqueues the step launch by launch, and stays so).
+int Ctx::launch_step_graph(bool* launched) {
+    *launched = false;
+    if (!step_exec) {
+        const long long k0 = g_launches.load();
+        CFD_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        capturing = true;
+        const int st = enqueue_mixed(false);
+        capturing = false;
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(stream, &g);
+        const long long nk = g_launches.load() - k0;
+        g_launches.fetch_sub(nk);  // captured, not run
+        cudaGraphExec_t ex = nullptr;
+        if (st == CFD_OK && ce == cudaSuccess && g &&
+            cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+            step_graph = g;
+            step_exec = ex;
+            graph_kernels = nk;
+        } else {
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            graphs_on = false;
+            return CFD_OK;
+        }
+    }
+    CFD_CUDA(cudaGraphLaunch(step_exec, stream));
+    g_launches.fetch_add(graph_kernels, std::memory_order_relaxed);
+    graph_replays += 1;
+    *launched = true;
+    return CFD_OK;
+}
+
+// One mixed step.  The learned guess runs on the first solve after the network was
+// attached, and when the previous solve took more than guess_gate iterations (every solve
+// when guess_gate is 0): the host reads the previous solve's counts once they are in
+// pinned memory (mid previous step, while the device finishes its mesh update).  The
+// steps without the network replay a captured graph from the second step on.
+int Ctx::step_once_mixed() {
+    iter += 1;
+    bool learned = false;
+    if (prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph) {
+        guess_steps += 1;
+        if (!guess_first && guess_gate > 0.0) CFD_CUDA(cudaEventSynchronize(ev_iters));
+        learned = guess_first || guess_gate <= 0.0 ||
+                  (double)std::max(h_iters[0], h_iters[1]) > guess_gate;
+        guess_first = false;
+    }
     bandera_host += 1;
+    if (graphs_on && !learned && mixed_steps > 0) {
+        bool launched = false;
+        int st = launch_step_graph(&launched);
+        if (st) return st;
+        if (launched) {
+            mixed_steps += 1;
+            return CFD_OK;
+        }
+    }
+    int st = enqueue_mixed(learned);
+    if (st) return st;
+    mixed_steps += 1;
     return tcollect();
 }
 

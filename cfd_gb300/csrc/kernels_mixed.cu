@@ -454,18 +454,19 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 // Only T of stages 1-3 is read later (through mu, lambda of the next stage; U1 and the
 // other primitives are rewritten by stage 4), so stages 1-3 write T alone at nodes without
 // a boundary condition.  The last stage writes U1, every primitive and the hi/lo split of
-// U1 (the next step's U).
+// U1 (the next step's U).  Node p alone reads U[p] and writes U1[p], so U1 may be U (the
+// update in place, U = U1 of ns2DComp.ALE.f90:277-281 without a copy).
 template <bool FIRST, bool LAST>
 __global__ void __launch_bounds__(256)
 k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
              const float2* __restrict__ mulam, const float4* __restrict__ recInv,
              const float4* __restrict__ recVisc, float4* __restrict__ invSum, GasConst gc,
              GasConstF gf, int viscous,
-             const double* __restrict__ U, float4* __restrict__ Uhi, float4* __restrict__ Ulo,
+             const double* U, float4* __restrict__ Uhi, float4* __restrict__ Ulo,
              const float* __restrict__ invM, float rk_fact,
              const unsigned char* __restrict__ bcflag, const double* __restrict__ bcval,
              const double2* __restrict__ nrm, const double* __restrict__ WX,
-             const double* __restrict__ WY, double* __restrict__ U1, float* __restrict__ RHO, float* __restrict__ VX,
+             const double* __restrict__ WY, double* U1, float* __restrict__ RHO, float* __restrict__ VX,
              float* __restrict__ VY, float* __restrict__ Eo, float* __restrict__ Po,
              float* __restrict__ Tout, float* __restrict__ RMACH) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -567,10 +568,10 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
         Tout[p] = (float)tt;
         u1_0 = rho; u1_1 = vx * rho; u1_2 = vy * rho; u1_3 = ee * rho;
     }
-    double2* o = reinterpret_cast<double2*>(U1 + 4 * (size_t)p);
-    o[0] = make_double2(u1_0, u1_1);
-    o[1] = make_double2(u1_2, u1_3);
-    if (LAST) {
+    if (LAST) {  // U1 of stages 1-3 is never read (only their T is), so it is not written
+        double2* o = reinterpret_cast<double2*>(U1 + 4 * (size_t)p);
+        o[0] = make_double2(u1_0, u1_1);
+        o[1] = make_double2(u1_2, u1_3);
         float h[4], l[4];
         split(u1_0, h[0], l[0]);
         split(u1_1, h[1], l[1]);
@@ -774,6 +775,58 @@ __global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos
     split(y, hy, ly);
     Xhi[p] = make_float2(hx, hy);
     Xlo[p] = make_float2(lx, ly);
+}
+
+// ------------------------------------------------------------------ clock and motion law
+// TIME = TIME + DTMIN (ns2DComp.ALE.f90:163) and fluidStructure's motion increment
+// (meshMove.f90:55-71 for the reference law: pitch pi/8 sin(10 t); the harmonic law: heave
+// A_h sin(2 pi f t), pitch A_p sin(2 pi f t)), for TRANSF, in the same operations as the
+// FP64 form's host code.
+__global__ void k_motion_law(const StepScal* __restrict__ sc, MotionScal* __restrict__ m, int law,
+                             double heave_amp, double pitch_amp, double freq) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const double PI = 3.141592653589793;  // acos(-1)
+    const double dt = sc->dtmin;
+    const double t = m->time + dt;
+    const double alphav = m->disn1, yposrv = m->disn0;
+    double d0 = m->disn0, d1;
+    if (law == CFD_MOTION_HARMONIC) {
+        const double ph = 2.0 * PI * freq * t;
+        d0 = heave_amp * sin(ph);
+        d1 = pitch_amp * sin(ph);
+    } else {
+        d1 = (PI / 8.0) * sin(10.0 * t);
+    }
+    const double alpha = d1 - alphav;
+    m->time = t;
+    m->disn0 = d0;
+    m->disn1 = d1;
+    m->ca = cos(alpha);
+    m->sa = sin(alpha);
+    m->yposr = d0 - yposrv;
+    m->dtmin = dt;
+}
+
+// TRANSF (meshMove.f90:369-392) with the increment from k_motion_law
+__global__ void k_transf_dev(int nnmove, const int* __restrict__ fix_node,
+                             const int* __restrict__ fix_set, const double* __restrict__ X,
+                             const double* __restrict__ Y, const double* __restrict__ xref,
+                             const double* __restrict__ yref, const MotionScal* __restrict__ m,
+                             double* __restrict__ xfix_x, double* __restrict__ xfix_y) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnmove) return;
+    const double ca = m->ca, sa = m->sa, yposr = m->yposr;
+    const int s = fix_set[k];
+    double dx = 0.0, dy = 0.0;
+    if (s >= 0) {
+        const int n = fix_node[k];
+        const double distx = X[n] - xref[s];
+        const double disty = Y[n] - yref[s] + yposr;
+        dx = ca * distx + sa * disty - distx;
+        dy = -(sa * distx) + ca * disty - disty + yposr;
+    }
+    xfix_x[k] = dx;
+    xfix_y[k] = dy;
 }
 
 // ------------------------------------------------------------------ host launchers

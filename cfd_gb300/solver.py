@@ -226,6 +226,12 @@ class Solver:
         check(abi.lib().cfd_ctx_guess_stats(self.h, out), "cfd_ctx_guess_stats")
         return tuple(int(v) for v in out)
 
+    def graph_state(self):
+        """(1 if steps replay a captured CUDA graph, replays so far, kernels per replay)."""
+        out = (C.c_longlong * 3)()
+        check(abi.lib().cfd_ctx_graph_state(self.h, out), "cfd_ctx_graph_state")
+        return tuple(int(v) for v in out)
+
     def step(self, n=1):
         rep = abi.CfdStepReport()
         check(abi.lib().cfd_step(self.h, int(n), C.byref(rep)), "cfd_step")

@@ -346,6 +346,13 @@ int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate);
  * took the network's guess, steps */
 int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4);
 
+/* Mixed form: out3 = (1 if steps replay a captured CUDA graph, steps replayed so far,
+ * kernels in one replay).  The first step of a context, and steps that run the learned
+ * guess, are enqueued launch by launch; CFD_GRAPHS=0 or CFD_TIMERS=1 at create turn the
+ * graph off.  No counterpart in the reference (its time loop calls the routines of
+ * ns2DComp.ALE.f90:114-283 one by one). */
+int cfd_ctx_graph_state(cfd_ctx* ctx, long long* out3);
+
 /* Number of kernels this library launched since process start (all contexts). */
 long long cfd_kernel_launches(void);
 

@@ -96,3 +96,32 @@ def test_mixed_from_perturbed_state(gpu_lib):
     g.step(3)
     o.step(3)
     assert max(state_errors(g.state()["U"], o.state()["U"])) <= REL_TOL_STATE
+
+
+def test_graph_replay_matches_launches(gpu_lib, monkeypatch):
+    """Steps replayed from the captured CUDA graph give the state, clock and forces of the
+    same steps enqueued launch by launch (CFD_GRAPHS=0), bit for bit, across downloads
+    and a restart of the clock between steps."""
+    from cfd_gb300 import abi, solver
+    k = small_case(3, scale=32, seed=6, estab_mode=2)
+    monkeypatch.setenv("CFD_GRAPHS", "0")
+    a = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    monkeypatch.delenv("CFD_GRAPHS")
+    b = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    for n in (1, 3, 2):
+        if n == 2:
+            for s in (a, b):
+                s.set_clock(iter=10, time=0.25, dtmin1=ra.dtmin, bandera=3, disn1=0.01,
+                            disn2=0.02)
+        ra, rb = a.step(n), b.step(n)
+        assert (ra.time, ra.dtmin, ra.iter) == (rb.time, rb.dtmin, rb.iter)
+        assert list(ra.fx) == list(rb.fx) and list(ra.fy) == list(rb.fy)
+        assert list(ra.bicg_iters) == list(rb.bicg_iters)
+        sa, sb = a.state(), b.state()
+        for key in ("U", "X", "Y"):
+            assert np.array_equal(sa[key], sb[key]), key
+    assert a.graph_state()[0] == 0
+    on, replays, kernels = b.graph_state()
+    assert on == 1 and replays == 5 and kernels > 10
+    a.close()
+    b.close()
