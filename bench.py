@@ -148,6 +148,12 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_value(ws, npoin, sec_step):
+    """Whole-job node-steps/s of ws replicas of an npoin-node mesh whose slowest rank took
+    sec_step per step."""
+    return ws * npoin / sec_step
+
+
 def workload(args):
     from cfd_gb300 import case as C
     k = C.config_case(3, scale=args.scale)
@@ -405,7 +411,7 @@ def main_ours(args):
     dist.barrier()
     clk = clocks.stop()
     sec_step = dist.max(ms_step) / 1e3
-    value = ws * k.npoin / sec_step
+    value = replica_value(ws, k.npoin, sec_step)
     final_U = S.state()["U"]
     # ---- e2e through the C-ABI with pinned host buffers, copies inside the timed region
     N = k.npoin
