@@ -106,6 +106,9 @@ struct Ctx {
     cudaEvent_t ev_iters = nullptr;  // recorded after that copy
     // mixed form: the clock and the motion increment live on the device
     MotionScal* d_motion = nullptr;
+    unsigned* d_tcount = nullptr;  // last-block counters: [0] DTMIN refinement, [1] motion tail
+    double* d_tpart = nullptr;     // per-block force sums of the motion tail
+    int tail_blocks = 1;
     // mixed form: one step (the network not run) captured as a CUDA graph and replayed;
     // off with the timers or CFD_GRAPHS=0, or when the capture fails
     bool graphs_on = false, capturing = false;
@@ -146,7 +149,7 @@ struct Ctx {
     int geometry_mixed(bool setup, bool put_area = false);
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
     int widen_mixed();
-    int run_pcg(int nsolve, bool learned = false);
+    int run_pcg(int nsolve, bool learned = false, bool fix_done = false);
     int enqueue_mixed(bool learned);
     int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);

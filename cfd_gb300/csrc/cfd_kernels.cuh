@@ -23,6 +23,30 @@ struct StepScal {
     float pad_f;
 };
 
+// DTMIN from the minimum DTELEM (b: its bit pattern, +inf for none) with the 1% hysteresis
+// of ns2DComp.ALE.f90:146-156, and the scalars derived from it
+__device__ __forceinline__ void dt_finalize_from(StepScal* sc, unsigned long long b) {
+    double dtmin = 1.0e20;
+    if (b != 0x7ff0000000000000ull) dtmin = __longlong_as_double((long long)b);
+    sc->dtmin32_bits = 0x7ff0000000000000ull;
+    sc->dtmin_raw = dtmin;
+    if (sc->bandera == 1) {
+        sc->dtmin1 = dtmin;
+        sc->bandera = 2;
+    }
+    double porc = fabs((dtmin - sc->dtmin1) / dtmin);
+    if (100.0 * porc <= 1.0) {
+        dtmin = sc->dtmin1;
+    } else {
+        sc->dtmin1 = dtmin;
+        sc->bandera = 2;
+    }
+    sc->dtmin = dtmin;
+    sc->cota = 10.0 * sc->dtmin_raw;
+    sc->inv_dtmin = 1.0 / dtmin;
+    sc->dtmin_f = (float)dtmin;
+}
+
 // calcRHS.f90:5 imports: Cv => FCV, lambda_ref => FK, mu_ref => FMU, gamma0 => GAMA, T_inf, CTE
 struct GasConst {
     double cv, lambda_ref, mu_ref, gamma, t_inf, cte;
@@ -46,11 +70,27 @@ struct MotionScal {
     double ca, sa, yposr;       // this step's TRANSF increment
     double dtmin;               // DTMIN of the step
 };
-__global__ void k_motion_law(const StepScal* sc, MotionScal* m, int law, double heave_amp,
-                             double pitch_amp, double freq);
-__global__ void k_transf_dev(int nnmove, const int* fix_node, const int* fix_set, const double* X,
-                             const double* Y, const double* xref, const double* yref,
-                             const MotionScal* m, double* xfix_x, double* xfix_y);
+struct MotionTailArgs {
+    int nset;  // FORCES
+    const int* set_ptr;
+    const int2* set_edges;
+    const float* P;
+    const double *X, *Y, *xref, *yref;
+    int law;  // motion law
+    double heave_amp, pitch_amp, freq;
+    MotionScal* m;
+    int nnmove;  // TRANSF
+    const int *fix_node, *fix_set;
+    double *xfix_x, *xfix_y;
+    int nufix;  // Dirichlet values of the BiCG solves
+    const int *ufix_node, *ufix_src;
+    double *x0, *x1;
+    float *xf0, *xf1;
+    double* part;  // [3 * nset][gridDim.x] per-block force sums
+    unsigned* count;
+    StepScal* sc;
+};
+__global__ void k_motion_tail(MotionTailArgs a);
 
 // ------------------------------------------------------------------ mixed precision
 __global__ void k_narrow_state(int npoin, const double* U, const double* T, const double* VX,
@@ -60,20 +100,17 @@ __global__ void k_narrow_state(int npoin, const double* U, const double* T, cons
                                float2* Wf);
 __global__ void k_widen(long n, const float* a, double* b);
 __global__ void k_narrow(long n, const double* a, float* b);
-__global__ void k_deltat_mixed(int nelem, const int4* elem, const float* T, const float* VX,
-                               const float* VY, const float2* W, const float* areaf, float fsafe,
-                               float t_inf, unsigned long long* dtmin_bits,
-                               unsigned long long* block_min);
+__global__ void k_deltat_estab(int nelem, const int4* elem, const float4* Uhi, const float4* Ulo,
+                               const float* T, float gm, const float* VX, const float* VY,
+                               const float2* W, const float4* geo, float FR, float RHOINF,
+                               float TINF, int estab_mode, float eps_dir, float dirx, float diry,
+                               float fsafe, unsigned long long* dtmin_bits,
+                               unsigned long long* block_min, float* SHOC, float* ES1,
+                               float* ES2, float* ES3);
 __global__ void k_deltat_refine(int nelem, const int4* elem, const float* T, const float* VX,
                                 const float* VY, const float2* W, const float* areaf,
                                 const unsigned long long* block_min, int nchunk, float fsafe,
-                                float t_inf, StepScal* sc);
-__global__ void k_estab_mixed(int nelem, const int4* elem, const float4* Uhi, const float4* Ulo,
-                              const float* T, float gm, const float* VX, const float* VY,
-                              const float2* W, const float4* geo, float FR, const StepScal* sc,
-                              float RHOINF, float TINF, int estab_mode, float eps_dir,
-                              float dirx, float diry, float* SHOC, float* TS1, float* TS2,
-                              float* TS3);
+                                float t_inf, StepScal* sc, unsigned* count);
 cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, const int4* elem,
                                      const float4* Uhi, const float4* Ulo, const float4* geo,
                                      const float* shoc, const StepScal* sc,
@@ -102,9 +139,6 @@ __global__ void k_node_geometry(int npoin, const int* esup_ptr, const int* esup_
                                 double* invdiag, float* invdiagf, double* M, float* invM,
                                 const float2* W, float2* Wold);
 __global__ void k_widen_geo(int nelem, const float4* geo, double* dN, double* area);
-__global__ void k_forces_tree(int nset_numb, const int* set_ptr, const int2* set_edges,
-                              const float* P, const double* X, const double* Y,
-                              const double* xref, const double* yref, StepScal* sc);
 __global__ void k_motion_update_mixed(int npoin, const double* xpos, const double* ypos,
                                       const StepScal* sc, double* X, double* Y, double* WX,
                                       double* WY, float2* Xhi, float2* Xlo, float2* Wf);

@@ -120,7 +120,7 @@ int Ctx::geometry(bool masas, bool with_laplace) {
 }
 
 // ------------------------------------------------------------------ PCG launch
-int Ctx::run_pcg(int nsolve, bool learned) {
+int Ctx::run_pcg(int nsolve, bool learned, bool fix_done) {
     PcgArgs a{};
     a.n = npoin;
     a.nsolve = nsolve;
@@ -169,7 +169,7 @@ int Ctx::run_pcg(int nsolve, bool learned) {
         a.gflag = learned ? d_gflag : nullptr;
         a.gate = 0.0;
         a.only_if = nullptr;
-        if (nufix > 0)
+        if (nufix > 0 && !fix_done)
             CFD_LAUNCH(k_bicg_fix_mixed, blocks_for(nufix, 256), 256, 0, stream, a);
         CFD_LAUNCH(k_bicg_resid_mixed, (unsigned)a.nblk_r, 256, 0, stream, a);
         if (learned) {
@@ -601,6 +601,14 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_recVisc, 3 * (size_t)E))) return st;
         if ((st = dalloc(&d_invSum, N))) return st;
         if ((st = dalloc(&d_motion, 1))) return st;
+        if ((st = dalloc(&d_tcount, 4))) return st;
+        {  // blocks of the motion tail: a block per 256 edges, moving nodes or fixed values
+            int w = std::max(nnmove, nufix);
+            for (int s = 0; s < bc.nset_numb; ++s) w = std::max(w, bc.set_ptr[s + 1] - bc.set_ptr[s]);
+            tail_blocks = std::min(64, std::max(1, (int)blocks_for(w, 256)));
+        }
+        if ((st = dalloc(&d_tpart, 3 * 10 * 64))) return st;
+        CFD_CUDA(cudaMemsetAsync(d_tcount, 0, 4 * sizeof(unsigned), stream));
         CFD_CUDA(cudaMemsetAsync(d_motion, 0, sizeof(MotionScal), stream));
         graphs_on = !timers_on && !(getenv("CFD_GRAPHS") && atoi(getenv("CFD_GRAPHS")) == 0);
         if ((st = narrow_mixed(true, true, true, true, true, true))) return st;
@@ -667,24 +675,21 @@ int Ctx::geometry_mixed(bool setup, bool put_area) {
 int Ctx::enqueue_mixed(bool learned) {
     const int N = npoin, E = nelem;
     const int TB = 256;
+    // deltat and the DTMIN-free part of ESTAB in one element pass; the FP64 refinement of
+    // the elements near the FP32 minimum, whose last block forms DTMIN
     tstart(TM_DELTAT);
-    CFD_LAUNCH(k_deltat_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf, d_VYf,
-               d_Wf, d_areaf, (float)prm.fsafe, (float)prm.t_inf, &d_scal->dtmin32_bits, d_blockmin);
+    CFD_LAUNCH(k_deltat_estab, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Uhi, d_Ulo, d_Tf,
+               (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VXf, d_VYf, d_Wf,
+               (const float4*)d_geo8, (float)prm.fr, (float)prm.rho_inf, (float)prm.t_inf,
+               prm.estab_mode, (float)estab_eps, (float)dir[0], (float)dir[1], (float)prm.fsafe,
+               &d_scal->dtmin32_bits, d_blockmin, d_shocf, d_ts1f, d_ts2f, d_ts3f);
     {
         const int nchunk = (int)blocks_for(E, TB);
         CFD_LAUNCH(k_deltat_refine, blocks_for(nchunk, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf,
                    d_VYf, d_Wf, d_areaf, (const unsigned long long*)d_blockmin, nchunk,
-                   (float)prm.fsafe, (float)prm.t_inf, d_scal);
+                   (float)prm.fsafe, (float)prm.t_inf, d_scal, d_tcount);
     }
-    CFD_LAUNCH(k_dt_finalize, 1, 1, 0, stream, d_scal);
     tstop(TM_DELTAT);
-    tstart(TM_ESTAB);
-    CFD_LAUNCH(k_estab_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Uhi, d_Ulo, d_Tf,
-               (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VXf, d_VYf, d_Wf,
-               (const float4*)d_geo8,
-               (float)prm.fr, d_scal, (float)prm.rho_inf, (float)prm.t_inf, prm.estab_mode,
-               (float)estab_eps, (float)dir[0], (float)dir[1], d_shocf, d_ts1f, d_ts2f, d_ts3f);
-    tstop(TM_ESTAB);
     GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte, prm.fr};
     const GasConstF gf = to_float(gc);
     const bool viscous = prm.fmu > 2.2250738585072014e-308;
@@ -710,26 +715,49 @@ int Ctx::enqueue_mixed(bool learned) {
                                    d_RMACHf));
         tstop(TM_UPDATE);
     }
-    tstart(TM_FORCES);
-    CFD_LAUNCH(k_forces_tree, 1, 256, 0, stream, bc.nset_numb, d_set_ptr, d_set_edges, d_Pf, d_X, d_Y,
-               d_xref, d_yref, d_scal);
-    tstop(TM_FORCES);
-    tstart(TM_TRANSF);
-    CFD_LAUNCH(k_motion_law, 1, 1, 0, stream, (const StepScal*)d_scal, d_motion, prm.motion_law,
-               prm.heave_amp, prm.pitch_amp, prm.motion_freq);
-    if (nnmove > 0)
-        CFD_LAUNCH(k_transf_dev, blocks_for(nnmove, TB), TB, 0, stream, nnmove, d_fix_node,
-                   d_fix_set, d_X, d_Y, d_xref, d_yref, (const MotionScal*)d_motion, d_xfix[0],
-                   d_xfix[1]);
-    tstop(TM_TRANSF);
     if (prm.guess_mode == CFD_GUESS_ZERO) {
         for (int c = 0; c < 2; ++c) {
             CFD_CUDA(cudaMemsetAsync(d_pos[c], 0, sizeof(double) * N, stream));
             CFD_CUDA(cudaMemsetAsync(d_posf[c], 0, sizeof(float) * N, stream));
         }
     }
+    // FORCES, clock and motion law, TRANSF and the solves' Dirichlet values: one launch
+    tstart(TM_FORCES);
+    {
+        MotionTailArgs t{};
+        t.nset = bc.nset_numb;
+        t.set_ptr = d_set_ptr;
+        t.set_edges = d_set_edges;
+        t.P = d_Pf;
+        t.X = d_X;
+        t.Y = d_Y;
+        t.xref = d_xref;
+        t.yref = d_yref;
+        t.law = prm.motion_law;
+        t.heave_amp = prm.heave_amp;
+        t.pitch_amp = prm.pitch_amp;
+        t.freq = prm.motion_freq;
+        t.m = d_motion;
+        t.nnmove = nnmove;
+        t.fix_node = d_fix_node;
+        t.fix_set = d_fix_set;
+        t.xfix_x = d_xfix[0];
+        t.xfix_y = d_xfix[1];
+        t.nufix = nufix;
+        t.ufix_node = d_ufix_node;
+        t.ufix_src = d_ufix_src;
+        t.x0 = d_pos[0];
+        t.x1 = d_pos[1];
+        t.xf0 = d_posf[0];
+        t.xf1 = d_posf[1];
+        t.part = d_tpart;
+        t.count = d_tcount + 1;
+        t.sc = d_scal;
+        CFD_LAUNCH(k_motion_tail, (unsigned)tail_blocks, 256, 0, stream, t);
+    }
+    tstop(TM_FORCES);
     tstart(TM_GRAD);
-    int st = run_pcg(2, learned);
+    int st = run_pcg(2, learned, true);
     if (st) return st;
     tstop(TM_GRAD);
     CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1],

@@ -140,27 +140,9 @@ __global__ void k_deltat(int nelem, const int4* __restrict__ elem, const double*
 // DTMIN (1.d20 when no element is finite), the 1% hysteresis of ns2DComp.ALE.f90:146-156
 // and the DT clamp of subrutinas.f90:211-215.  One thread.
 __global__ void k_dt_finalize(StepScal* sc) {
-    double dtmin = 1.0e20;
-    unsigned long long b = sc->dtmin_bits;
-    if (b != 0x7ff0000000000000ull) dtmin = __longlong_as_double((long long)b);
+    const unsigned long long b = sc->dtmin_bits;
     sc->dtmin_bits = 0x7ff0000000000000ull;  // ready for the next step's k_deltat
-    sc->dtmin32_bits = 0x7ff0000000000000ull;
-    sc->dtmin_raw = dtmin;
-    if (sc->bandera == 1) {
-        sc->dtmin1 = dtmin;
-        sc->bandera = 2;
-    }
-    double porc = fabs((dtmin - sc->dtmin1) / dtmin);
-    if (100.0 * porc <= 1.0) {
-        dtmin = sc->dtmin1;
-    } else {
-        sc->dtmin1 = dtmin;
-        sc->bandera = 2;
-    }
-    sc->dtmin = dtmin;
-    sc->cota = 10.0 * sc->dtmin_raw;
-    sc->inv_dtmin = 1.0 / dtmin;
-    sc->dtmin_f = (float)dtmin;
+    dt_finalize_from(sc, b);
 }
 
 // ITLOCAL != 0 only: DTL = DTMIN*DTFACT + min(DT, COTA)*(1-DTFACT) (ns2DComp.ALE.f90:160-161)

@@ -112,34 +112,6 @@ __device__ __forceinline__ float dtelem_f32(const int4 n, const float* __restric
     return fdiv(fsafe, a + (a + fdiv(alpha * vel, hh)));
 }
 
-// subrutinas.f90:170-210 in FP32: the FP32 minimum (bit pattern of a positive double)
-__global__ void k_deltat_mixed(int nelem, const int4* __restrict__ elem, const float* __restrict__ T,
-                               const float* __restrict__ VX, const float* __restrict__ VY,
-                               const float2* __restrict__ W, const float* __restrict__ areaf,
-                               float fsafe, float t_inf, unsigned long long* __restrict__ dtmin_bits,
-                               unsigned long long* __restrict__ block_min) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long mybits = 0x7ff0000000000000ull;
-    if (e < nelem) {
-        const double d = f2d_bits(dtelem_f32(elem[e], T, VX, VY, W, areaf[e], fsafe, t_inf));
-        if (d < 1.0e20 && d > 0.0) mybits = (unsigned long long)__double_as_longlong(d);
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long o = __shfl_down_sync(0xffffffffu, mybits, off);
-        mybits = o < mybits ? o : mybits;
-    }
-    __shared__ unsigned long long wmin[32];
-    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = mybits;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long m = wmin[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = wmin[w] < m ? wmin[w] : m;
-        block_min[blockIdx.x] = m;
-        atomicMin(dtmin_bits, m);
-    }
-}
-
 // Second pass: elements whose FP32 DTELEM is within 1e-4 of the FP32 minimum get their
 // DTELEM in FP64 (subrutinas.f90:172-206); the FP64 minimum over them is DTMIN, so the 1%
 // hysteresis of ns2DComp.ALE.f90:146-156 sees an FP64-accurate value.  Only the
@@ -176,7 +148,8 @@ __global__ void k_deltat_refine(int nelem, const int4* __restrict__ elem, const 
                                 const float* __restrict__ VX, const float* __restrict__ VY,
                                 const float2* __restrict__ W, const float* __restrict__ areaf,
                                 const unsigned long long* __restrict__ block_min, int nchunk,
-                                float fsafe, float t_inf, StepScal* __restrict__ sc) {
+                                float fsafe, float t_inf, StepScal* __restrict__ sc,
+                                unsigned* __restrict__ count) {
     // thread t tests chunk blockIdx.x*256 + t; the block then refines the listed chunks
     __shared__ int list[256];
     __shared__ int nlist;
@@ -192,37 +165,39 @@ __global__ void k_deltat_refine(int nelem, const int4* __restrict__ elem, const 
         const int e = list[k] * 256 + threadIdx.x;
         if (e < nelem) refine_one(e, elem, T, VX, VY, W, areaf, fsafe, t_inf, m32, sc);
     }
+    // the last block to finish forms DTMIN (k_dt_finalize of the FP64 form)
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(count, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        *count = 0u;
+        dt_finalize_from(sc, atomicExch(&sc->dtmin_bits, 0x7ff0000000000000ull));
+    }
 }
 
-// ------------------------------------------------------------------ ESTAB (FP32)
-// subrutinas.f90:346-443; estab_mode as CFD_ESTAB_*.
-__global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
-                              const float4* __restrict__ Ulo, const float* __restrict__ T, float gm,
-                              const float* __restrict__ VX, const float* __restrict__ VY,
-                              const float2* __restrict__ W, const float4* __restrict__ geo, float FR,
-                              const StepScal* __restrict__ sc, float RHOINF, float TINF,
-                              int estab_mode, float eps_dir, float dirx, float diry,
-                              float* __restrict__ SHOC, float* __restrict__ TS1,
-                              float* __restrict__ TS2, float* __restrict__ TS3) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nelem) return;
-    const float DTMIN = sc->dtmin_f;
-    const int4 n = elem[e];
-    const int n1 = n.x, n2 = n.y, n3 = n.z;
-    const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
-    const float DX[3] = {ga.x, ga.y, ga.z};
-    const float DY[3] = {ga.w, gb.x, gb.y};
-    const float rh1 = Uhi[n1].x, rh2 = Uhi[n2].x, rh3 = Uhi[n3].x;
-    const float rl1 = Ulo[n1].x, rl2 = Ulo[n2].x, rl3 = Ulo[n3].x;
+// ------------------------------------------------------------------ deltat + ESTAB (FP32)
+// ESTAB (subrutinas.f90:346-443; estab_mode as CFD_ESTAB_*) up to, not including, its use
+// of DTMIN: SHOC, 1/tau^2 and the squared viscous terms (k4/h^2)^2 of the two lengths
+// h_rgn, h_rgne (-1 where h = 0, whose TS is 0).  The stage-1 element kernel forms
+// TS1 = (1/tau^2 + (2/DTMIN)^2)^(-1/2), TS2, TS3 = (1/tau^2 + (2/DTMIN)^2 + (k4/h^2)^2)^(-1/2).
+struct EstabPre {
+    float shoc, inv_tau2, v_rgn, v_rgne;
+};
+
+__device__ __forceinline__ EstabPre estab_pre(const float DX[3], const float DY[3], float rh1,
+                                              float rh2, float rh3, float rl1, float rl2,
+                                              float rl3, float vx, float vy, float t1, float t2,
+                                              float t3, float gm, float FR, float RHOINF,
+                                              float TINF, int estab_mode, float eps_dir,
+                                              float dirx, float diry) {
     const float rho_elem = ((rh1 + rh2 + rh3) + (rl1 + rl2 + rl3)) * (1.f / 3.f);
-    const float2 w1 = W[n1], w2 = W[n2], w3 = W[n3];
-    const float vx = ((VX[n1] + VX[n2] + VX[n3]) - (w1.x + w2.x + w3.x)) * (1.f / 3.f);
-    const float vy = ((VY[n1] + VY[n2] + VY[n3]) - (w1.y + w2.y + w3.y)) * (1.f / 3.f);
     const float vel2 = sqrtf(vx * vx + vy * vy);
     // gradients from differences to node 1 (the shape-function gradients sum to 0)
     const float d2 = (rh2 - rh1) + (rl2 - rl1), d3 = (rh3 - rh1) + (rl3 - rl1);
     const float drx = d2 * DX[1] + d3 * DX[2], dry = d2 * DY[1] + d3 * DY[2];
-    const float t1 = T[n1], t2 = T[n2], t3 = T[n3];
     const float e2 = t2 - t1, e3 = t3 - t1;
     const float dtx = e2 * DX[1] + e3 * DX[2], dty = e2 * DY[1] + e3 * DY[2];
     const float temp = (t1 + t2 + t3) * (1.f / 3.f);
@@ -273,16 +248,79 @@ __global__ void k_estab_mixed(int nelem, const int4* __restrict__ elem, const fl
     if (!(h_jgn <= 10.f)) h_jgn = 0.f;
     const float tr1 = fdiv(dr2 * h_jgn, rho_elem);
     const float zzz = fdiv(h_jgn, 2.f * c);
-    SHOC[e] = (tr1 + tr1 * tr1) * 0.5f * (c * c) * zzz;
-    const float two_dt = fdiv(2.f, DTMIN);
-    const float resumen = fdiv(1.f, tau * tau) + two_dt * two_dt;
-    const float rrr = rsqrtf(resumen);
+    EstabPre o;
+    o.shoc = (tr1 + tr1 * tr1) * 0.5f * (c * c) * zzz;
+    o.inv_tau2 = fdiv(1.f, tau * tau);
     const float k4 = fdiv(4.f * fmu, RHOINF);
     // (resumen + 1/tau_s^2)^(-1/2), tau_s = h^2/k4, is (resumen + k4^2/h^4)^(-1/2); h = 0 -> 0
     const float hr2 = h_rgn * h_rgn, he2 = h_rgne * h_rgne;
-    TS1[e] = rrr;
-    TS2[e] = (hr2 > 0.f) ? rsqrtf(resumen + fdiv(k4 * k4, hr2 * hr2)) : 0.f;
-    TS3[e] = (he2 > 0.f) ? rsqrtf(resumen + fdiv(k4 * k4, he2 * he2)) : 0.f;
+    o.v_rgn = (hr2 > 0.f) ? fdiv(k4 * k4, hr2 * hr2) : -1.f;
+    o.v_rgne = (he2 > 0.f) ? fdiv(k4 * k4, he2 * he2) : -1.f;
+    return o;
+}
+
+// One element pass for deltat (subrutinas.f90:170-210, FP32 DTELEM; per-block minima and
+// the FP32 minimum as the bit pattern of a positive double) and for the DTMIN-free part of
+// ESTAB: the two routines gather the same node data.
+__global__ void __launch_bounds__(256)
+k_deltat_estab(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
+               const float4* __restrict__ Ulo, const float* __restrict__ T, float gm,
+               const float* __restrict__ VX, const float* __restrict__ VY,
+               const float2* __restrict__ W, const float4* __restrict__ geo, float FR,
+               float RHOINF, float TINF, int estab_mode, float eps_dir, float dirx, float diry,
+               float fsafe, unsigned long long* __restrict__ dtmin_bits,
+               unsigned long long* __restrict__ block_min, float* __restrict__ SHOC,
+               float* __restrict__ ES1, float* __restrict__ ES2, float* __restrict__ ES3) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long mybits = 0x7ff0000000000000ull;
+    if (e < nelem) {
+        const int4 n = elem[e];
+        const int n1 = n.x, n2 = n.y, n3 = n.z;
+        const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
+        const float DX[3] = {ga.x, ga.y, ga.z};
+        const float DY[3] = {ga.w, gb.x, gb.y};
+        const float rh1 = Uhi[n1].x, rh2 = Uhi[n2].x, rh3 = Uhi[n3].x;
+        const float rl1 = Ulo[n1].x, rl2 = Ulo[n2].x, rl3 = Ulo[n3].x;
+        const float2 w1 = W[n1], w2 = W[n2], w3 = W[n3];
+        const float vx1 = VX[n1], vx2 = VX[n2], vx3 = VX[n3];
+        const float vy1 = VY[n1], vy2 = VY[n2], vy3 = VY[n3];
+        const float t1 = T[n1], t2 = T[n2], t3 = T[n3];
+        // deltat: dtelem_f32 on the gathered values (area = the element's FP32 area)
+        {
+            float vumax = fmaxf(fmaxf(fabsf(vx1 - w1.x), fabsf(vx2 - w2.x)), fabsf(vx3 - w3.x));
+            float vvmax = fmaxf(fmaxf(fabsf(vy1 - w1.y), fabsf(vy2 - w2.y)), fabsf(vy3 - w3.y));
+            const float T_iel = (t1 + t2 + t3) * (1.f / 3.f);
+            const float hh = sqrtf(2.f * gb.z);
+            const float vel = sqrtf(vumax * vumax + vvmax * vvmax);
+            const float et = 0.017f * pow15f(fdiv(T_iel, TINF)) * fdiv(TINF + 110.f, T_iel + 110.f);
+            const float alpha = fminf(fdiv(vel * hh, 2.f * et) * (1.f / 3.f), 1.f);
+            const float a = fdiv(4.f * et, hh * hh);
+            const double d = f2d_bits(fdiv(fsafe, a + (a + fdiv(alpha * vel, hh))));
+            if (d < 1.0e20 && d > 0.0) mybits = (unsigned long long)__double_as_longlong(d);
+        }
+        const float vx = ((vx1 + vx2 + vx3) - (w1.x + w2.x + w3.x)) * (1.f / 3.f);
+        const float vy = ((vy1 + vy2 + vy3) - (w1.y + w2.y + w3.y)) * (1.f / 3.f);
+        const EstabPre o = estab_pre(DX, DY, rh1, rh2, rh3, rl1, rl2, rl3, vx, vy, t1, t2, t3, gm,
+                                     FR, RHOINF, TINF, estab_mode, eps_dir, dirx, diry);
+        SHOC[e] = o.shoc;
+        ES1[e] = o.inv_tau2;
+        ES2[e] = o.v_rgn;
+        ES3[e] = o.v_rgne;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long q = __shfl_down_sync(0xffffffffu, mybits, off);
+        mybits = q < mybits ? q : mybits;
+    }
+    __shared__ unsigned long long wmin[32];
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = mybits;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = wmin[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = wmin[w] < m ? wmin[w] : m;
+        block_min[blockIdx.x] = m;
+        atomicMin(dtmin_bits, m);
+    }
 }
 
 // ------------------------------------------------------------------ element mu, lambda
@@ -311,7 +349,7 @@ __global__ void k_elem_mulam(int nelem, const int4* __restrict__ elem, const flo
 // Vlam(3).
 
 template <bool VISCOUS>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 5)
 k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
                     const float4* __restrict__ Ulo, const float4* __restrict__ geo,
                     const float* __restrict__ shoc,
@@ -344,17 +382,31 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
         Ux[q] = d1 * Nx[1] + d2 * Nx[2];
         Uy[q] = d1 * Ny[1] + d2 * Ny[2];
     }
-    const float tau[3] = {ts1[e], ts2[e], ts3[e]};
+    // TS1-3 of ESTAB from its DTMIN-free part (k_deltat_estab) and this step's DTMIN
+    float tau[3];
+    {
+        const float two_dt = fdiv(2.f, sc->dtmin_f);
+        const float resumen = ts1[e] + two_dt * two_dt;
+        const float v2 = ts2[e], v3 = ts3[e];
+        tau[0] = rsqrtf(resumen);
+        tau[1] = (v2 >= 0.f) ? rsqrtf(resumen + v2) : 0.f;
+        tau[2] = (v3 >= 0.f) ? rsqrtf(resumen + v3) : 0.f;
+    }
     const float nu = shoc[e] * gc.cte;
     const float scale = gb.z * sc->dtmin_f * (1.f / 3.f);
-    float r[3][4], vm[3][3], vl[3];
+    // Over the three edge-midpoint quadrature points k, only A (the Galerkin flux
+    // divergence, to the two nodes other than k), B1, B2 and the viscous coefficients
+    // depend on k; the test-function gradients and tau do not.  So the k-loop sums A per
+    // node, B1, B2 and the seven viscous coefficients, and the products with Nx, Ny, tau
+    // and the shock-capturing term (the same at every k) are formed once.
+    float r[3][4], SB1[4], SB2[4];
+    float Sm11 = 0.f, Sm12 = 0.f, Sm22 = 0.f, Sm13 = 0.f, Sm23 = 0.f, Sl13 = 0.f, Sl23 = 0.f;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        vl[i] = 0.f;
+    for (int q = 0; q < 4; ++q) {
+        SB1[q] = 0.f;
+        SB2[q] = 0.f;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) r[i][q] = 0.f;
-#pragma unroll
-        for (int q = 0; q < 3; ++q) vm[i][q] = 0.f;
+        for (int i = 0; i < 3; ++i) r[i][q] = 0.f;
     }
     const float gm1 = g - 1.f, gm3 = g - 3.f;
 #pragma unroll
@@ -389,13 +441,12 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
         B2[2] = -v1 * gm1 * A[1] + v2 * (3.f - g) * A[2] + gm1 * A[3] + (h0 - v2 * v2) * A[0];
         B2[3] = g * v2 * A[3] - v1 * v2 * gm1 * A[1] + v2 * W0 * A[0] + (-h0 + ev * g - v2 * v2 * gm1) * A[2];
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                float t = tau[i] * (Nx[i] * B1[q] + Ny[i] * B2[q]) + nu * (Nx[i] * Ux[q] + Ny[i] * Uy[q]);
-                if (i != k) t += 0.5f * A[q];
-                r[i][q] += t;
-            }
+        for (int q = 0; q < 4; ++q) {
+            SB1[q] += B1[q];
+            SB2[q] += B2[q];
+            r[ia][q] += 0.5f * A[q];
+            r[ib][q] += 0.5f * A[q];
+        }
         if (VISCOUS) {
             // K1, K2 of calcRHS.f90:121-132 split as mu*(...) + lambda*(...)
             const float icv = 1.f / (Cv * rho);
@@ -412,15 +463,22 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
                                Uy[0] * (3.f * V_sq + v2 * v2) + 3.f * Uy[1] * v1 + 4.f * Uy[2] * v2) * icv;
             const float l23 = (1.f / 3.f) *
                               (3.f * Uy[0] * (V_sq - ev) - 3.f * Uy[1] * v1 - 3.f * Uy[2] * v2 + 3.f * Uy[3]) * icv;
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                vm[i][0] += Nx[i] * m11 + Ny[i] * m12;
-                vm[i][1] += Nx[i] * m12 + Ny[i] * m22;
-                vm[i][2] += Nx[i] * m13 + Ny[i] * m23;
-                vl[i] += Nx[i] * l13 + Ny[i] * l23;
-            }
+            Sm11 += m11;
+            Sm12 += m12;
+            Sm22 += m22;
+            Sm13 += m13;
+            Sm23 += m23;
+            Sl13 += l13;
+            Sl23 += l23;
         }
     }
+    // SUPG (tau) and shock capturing (nu, three quadrature points of the same value)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            r[i][q] += tau[i] * (Nx[i] * SB1[q] + Ny[i] * SB2[q]) +
+                       3.f * nu * (Nx[i] * Ux[q] + Ny[i] * Uy[q]);
     {  // FUENTE: -AR*sum_k sp(i,k)*(Ux*wx_k + Uy*wy_k), AR = area*dtl/3 = scale
         const float2 w0 = W[p[0]], w1 = W[p[1]], w2 = W[p[2]];
         const float wx[3] = {0.5f * (w0.x + w1.x), 0.5f * (w1.x + w2.x), 0.5f * (w0.x + w2.x)};
@@ -439,8 +497,11 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
     for (int i = 0; i < 3; ++i) {
         const int pos = slot_pos[3 * (size_t)e + i];
         recInv[pos] = make_float4(r[i][0] * scale, r[i][1] * scale, r[i][2] * scale, r[i][3] * scale);
-        if (VISCOUS)
-            recVisc[pos] = make_float4(vm[i][0] * scale, vm[i][1] * scale, vm[i][2] * scale, vl[i] * scale);
+        if (VISCOUS) {
+            const float vm0 = Nx[i] * Sm11 + Ny[i] * Sm12, vm1 = Nx[i] * Sm12 + Ny[i] * Sm22;
+            const float vm2 = Nx[i] * Sm13 + Ny[i] * Sm23, vl = Nx[i] * Sl13 + Ny[i] * Sl23;
+            recVisc[pos] = make_float4(vm0 * scale, vm1 * scale, vm2 * scale, vl * scale);
+        }
     }
 }
 
@@ -725,32 +786,6 @@ __global__ void k_widen_geo(int nelem, const float4* __restrict__ geo, double* _
     area[e] = gb.z;
 }
 
-// FORCES (meshMove.f90:167-192) with a block tree per set instead of the serial sum
-__global__ void k_forces_tree(int nset_numb, const int* __restrict__ set_ptr,
-                              const int2* __restrict__ set_edges, const float* __restrict__ P,
-                              const double* __restrict__ X, const double* __restrict__ Y,
-                              const double* __restrict__ xref, const double* __restrict__ yref,
-                              StepScal* __restrict__ sc) {
-    __shared__ double red[9];
-    for (int s = 0; s < nset_numb; ++s) {
-        double fx = 0.0, fy = 0.0, rm = 0.0;
-        const double xr = xref[s], yr = yref[s];
-        for (int k = set_ptr[s] + threadIdx.x; k < set_ptr[s + 1]; k += blockDim.x) {
-            const int2 ed = set_edges[k];
-            const double d_press = ((double)P[ed.x] + (double)P[ed.y]) * 0.5;
-            const double a = d_press * (Y[ed.y] - Y[ed.x]);
-            const double b = d_press * (X[ed.x] - X[ed.y]);
-            fx += a;
-            fy += b;
-            rm += b * ((X[ed.x] + X[ed.y]) * 0.5 - xr) - a * ((Y[ed.y] + Y[ed.x]) * 0.5 - yr);
-        }
-        fx = block_tree256(fx, red);
-        fy = block_tree256(fy, red);
-        rm = block_tree256(rm, red);
-        if (threadIdx.x == 0) { sc->fx[s] = fx; sc->fy[s] = fy; sc->rm[s] = rm; }
-    }
-}
-
 // meshMove.f90:99-126: X += XPOS, W = XPOS/DTMIN (as XPOS*(1/DTMIN), the reciprocal formed
 // once by k_dt_finalize), with the float shadows of (X, Y) and W
 __global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos,
@@ -777,19 +812,17 @@ __global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos
     Xlo[p] = make_float2(lx, ly);
 }
 
-// ------------------------------------------------------------------ clock and motion law
+// ------------------------------------------------------------------ end of the flow part
 // TIME = TIME + DTMIN (ns2DComp.ALE.f90:163) and fluidStructure's motion increment
 // (meshMove.f90:55-71 for the reference law: pitch pi/8 sin(10 t); the harmonic law: heave
-// A_h sin(2 pi f t), pitch A_p sin(2 pi f t)), for TRANSF, in the same operations as the
-// FP64 form's host code.
-__global__ void k_motion_law(const StepScal* __restrict__ sc, MotionScal* __restrict__ m, int law,
-                             double heave_amp, double pitch_amp, double freq) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+// A_h sin(2 pi f t), pitch A_p sin(2 pi f t)), in the same operations as the FP64 form's
+// host code
+__device__ MotionScal motion_step(const MotionScal& m, double dt, int law, double heave_amp,
+                                  double pitch_amp, double freq) {
     const double PI = 3.141592653589793;  // acos(-1)
-    const double dt = sc->dtmin;
-    const double t = m->time + dt;
-    const double alphav = m->disn1, yposrv = m->disn0;
-    double d0 = m->disn0, d1;
+    const double t = m.time + dt;
+    const double alphav = m.disn1, yposrv = m.disn0;
+    double d0 = m.disn0, d1;
     if (law == CFD_MOTION_HARMONIC) {
         const double ph = 2.0 * PI * freq * t;
         d0 = heave_amp * sin(ph);
@@ -798,35 +831,92 @@ __global__ void k_motion_law(const StepScal* __restrict__ sc, MotionScal* __rest
         d1 = (PI / 8.0) * sin(10.0 * t);
     }
     const double alpha = d1 - alphav;
-    m->time = t;
-    m->disn0 = d0;
-    m->disn1 = d1;
-    m->ca = cos(alpha);
-    m->sa = sin(alpha);
-    m->yposr = d0 - yposrv;
-    m->dtmin = dt;
+    MotionScal o;
+    o.time = t;
+    o.disn0 = d0;
+    o.disn1 = d1;
+    o.ca = cos(alpha);
+    o.sa = sin(alpha);
+    o.yposr = d0 - yposrv;
+    o.dtmin = dt;
+    return o;
 }
 
-// TRANSF (meshMove.f90:369-392) with the increment from k_motion_law
-__global__ void k_transf_dev(int nnmove, const int* __restrict__ fix_node,
-                             const int* __restrict__ fix_set, const double* __restrict__ X,
-                             const double* __restrict__ Y, const double* __restrict__ xref,
-                             const double* __restrict__ yref, const MotionScal* __restrict__ m,
-                             double* __restrict__ xfix_x, double* __restrict__ xfix_y) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nnmove) return;
-    const double ca = m->ca, sa = m->sa, yposr = m->yposr;
-    const int s = fix_set[k];
-    double dx = 0.0, dy = 0.0;
-    if (s >= 0) {
-        const int n = fix_node[k];
-        const double distx = X[n] - xref[s];
-        const double disty = Y[n] - yref[s] + yposr;
-        dx = ca * distx + sa * disty - distx;
-        dy = -(sa * distx) + ca * disty - disty + yposr;
+// TRANSF (meshMove.f90:369-392) of moving-list entry k
+__device__ __forceinline__ double2 transf_one(const MotionTailArgs& a, const MotionScal& mv,
+                                              int k) {
+    const int s = a.fix_set[k];
+    if (s < 0) return make_double2(0.0, 0.0);
+    const int n = a.fix_node[k];
+    const double distx = a.X[n] - a.xref[s];
+    const double disty = a.Y[n] - a.yref[s] + mv.yposr;
+    return make_double2(mv.ca * distx + mv.sa * disty - distx,
+                        -(mv.sa * distx) + mv.ca * disty - disty + mv.yposr);
+}
+
+// One launch of a few blocks after the RK stages: FORCES (meshMove.f90:167-192; per-block
+// trees of the edge terms, folded in block order by the last block), the clock and the
+// motion law, TRANSF into x_fix, and the Dirichlet values of the two BiCG solves
+// (biconjGrad.f90:28: x(fix) = x_fix, in x and in its float shadow).  Every block forms
+// the motion from the step-start MotionScal; the last block stores the new one.
+__global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
+    __shared__ MotionScal mv;
+    __shared__ double red[9];
+    __shared__ bool last;
+    if (threadIdx.x == 0) mv = motion_step(*a.m, a.sc->dtmin, a.law, a.heave_amp, a.pitch_amp,
+                                           a.freq);
+    __syncthreads();
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    for (int k = gt; k < a.nnmove; k += gs) {
+        const double2 d = transf_one(a, mv, k);
+        a.xfix_x[k] = d.x;
+        a.xfix_y[k] = d.y;
     }
-    xfix_x[k] = dx;
-    xfix_y[k] = dy;
+    for (int k = gt; k < a.nufix; k += gs) {
+        const int i = a.ufix_node[k];
+        const double2 d = transf_one(a, mv, a.ufix_src[k]);
+        a.x0[i] = d.x;
+        a.xf0[i] = d2f_trunc(d.x);
+        a.x1[i] = d.y;
+        a.xf1[i] = d2f_trunc(d.y);
+    }
+    for (int s = 0; s < a.nset; ++s) {
+        double fx = 0.0, fy = 0.0, rm = 0.0;
+        const double xr = a.xref[s], yr = a.yref[s];
+        for (int k = a.set_ptr[s] + gt; k < a.set_ptr[s + 1]; k += gs) {
+            const int2 ed = a.set_edges[k];
+            const double d_press = ((double)a.P[ed.x] + (double)a.P[ed.y]) * 0.5;
+            const double fa = d_press * (a.Y[ed.y] - a.Y[ed.x]);
+            const double fb = d_press * (a.X[ed.x] - a.X[ed.y]);
+            fx += fa;
+            fy += fb;
+            rm += fb * ((a.X[ed.x] + a.X[ed.y]) * 0.5 - xr) - fa * ((a.Y[ed.y] + a.Y[ed.x]) * 0.5 - yr);
+        }
+        fx = block_tree256(fx, red);
+        fy = block_tree256(fy, red);
+        rm = block_tree256(rm, red);
+        if (threadIdx.x == 0) {
+            a.part[(3 * s + 0) * gridDim.x + blockIdx.x] = fx;
+            a.part[(3 * s + 1) * gridDim.x + blockIdx.x] = fy;
+            a.part[(3 * s + 2) * gridDim.x + blockIdx.x] = rm;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(a.count, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if ((int)threadIdx.x < 3 * a.nset) {
+        double v = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) v += __ldcg(a.part + threadIdx.x * gridDim.x + b);
+        const int s = threadIdx.x / 3, q = threadIdx.x % 3;
+        (q == 0 ? a.sc->fx : q == 1 ? a.sc->fy : a.sc->rm)[s] = v;
+    }
+    if (threadIdx.x == 0) {
+        *a.m = mv;
+        *a.count = 0u;
+    }
 }
 
 // ------------------------------------------------------------------ host launchers
