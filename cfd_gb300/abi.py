@@ -20,7 +20,7 @@ STATUS_NAMES = {0: "CFD_OK", 1: "CFD_ERR_ARG", 2: "CFD_ERR_MESH", 3: "CFD_ERR_CU
 
 CFD_PREC_FP64, CFD_PREC_MIXED = 0, 1
 CFD_MASS_MASAS, CFD_MASS_GCL_LITERAL, CFD_MASS_GCL_CORRECTED = 0, 1, 2
-CFD_MOTION_REFERENCE, CFD_MOTION_HARMONIC = 0, 1
+CFD_MOTION_REFERENCE, CFD_MOTION_HARMONIC, CFD_MOTION_NEWMARK = 0, 1, 2
 CFD_GUESS_PREVIOUS, CFD_GUESS_ZERO, CFD_GUESS_LEARNED = 0, 1, 2
 CFD_ESTAB_REFERENCE, CFD_ESTAB_EXACT, CFD_ESTAB_REGULARIZED = 0, 1, 2
 
@@ -133,6 +133,9 @@ SIGNATURES = {
     "cfd_ctx_set_guess_net": (C.c_int, [_P, _P, C.c_double]),
     "cfd_ctx_guess_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_graph_state": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "cfd_ctx_set_force_visc": (C.c_int, [_P, C.c_int]),
+    "cfd_ctx_force_visc": (C.c_int, [_P, _dp, _dp, _dp]),
+    "cfd_force_visc": (C.c_int, [_ip] * 7 + [_dp] * 4 + [_dp] * 10 + [_dp, _dp, _dp]),
     "cfd_ctx_create": (C.c_int, [C.POINTER(_P), C.POINTER(CfdMesh), C.POINTER(CfdParams),
                                  C.c_int]),
     "cfd_ctx_destroy": (None, [_P]),

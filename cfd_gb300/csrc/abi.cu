@@ -277,13 +277,15 @@ int cfd_ctx_set_clock(cfd_ctx* ctx, int iter, double time, double dtmin1, int ba
     sc.dtmin1 = dtmin1;
     sc.bandera = bandera;
     CFD_CUDA(cudaMemcpyAsync(c.d_scal, &sc, sizeof(sc), cudaMemcpyHostToDevice, c.stream));
-    MotionScal ms{};
-    ms.time = time;
-    ms.disn0 = disn1;
-    ms.disn1 = disn2;
-    ms.ca = 1.0;
-    if (c.d_motion)
+    if (c.d_motion) {  // the structural model's velocities and accelerations are kept
+        MotionScal ms{};
+        CFD_CUDA(cudaMemcpyAsync(&ms, c.d_motion, sizeof(ms), cudaMemcpyDeviceToHost, c.stream));
+        CFD_CUDA(cudaStreamSynchronize(c.stream));
+        ms.time = time;
+        ms.disn0 = disn1;
+        ms.disn1 = disn2;
         CFD_CUDA(cudaMemcpyAsync(c.d_motion, &ms, sizeof(ms), cudaMemcpyHostToDevice, c.stream));
+    }
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     return CFD_OK;
 }
@@ -305,6 +307,32 @@ int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4) {
                              c.stream));
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     out4[3] = c.guess_steps;
+    return CFD_OK;
+}
+
+int cfd_ctx_set_force_visc(cfd_ctx* ctx, int each_step) {
+    if (!ctx) return arg_error("ctx");
+    Ctx& c = ctx->impl;
+    TRY(c.set_force_visc_each_step(each_step != 0));
+    CFD_CUDA(cudaStreamSynchronize(c.stream));
+    return CFD_OK;
+}
+
+int cfd_ctx_force_visc(cfd_ctx* ctx, double* F_VX, double* F_VY, double* skin) {
+    if (!ctx || !F_VX || !F_VY) return arg_error("null pointer");
+    Ctx& c = ctx->impl;
+    if (!c.fv_each) TRY(c.force_visc_now());
+    double fv[20];
+    CFD_CUDA(cudaMemcpyAsync(fv, c.d_fv, sizeof(fv), cudaMemcpyDeviceToHost, c.stream));
+    const size_t ne = c.bc.set_elem.size();
+    if (skin && ne)
+        CFD_CUDA(cudaMemcpyAsync(skin, c.d_fv_skin, 3 * ne * sizeof(double),
+                                 cudaMemcpyDeviceToHost, c.stream));
+    CFD_CUDA(cudaStreamSynchronize(c.stream));
+    for (int s = 0; s < 10; ++s) {
+        F_VX[s] = fv[s];
+        F_VY[s] = fv[10 + s];
+    }
     return CFD_OK;
 }
 
@@ -597,6 +625,73 @@ int cfd_deltat(const double* T, const double* VEL_X, const double* VEL_Y, const 
     TRY(s.get(&sc, d_sc, 1));
     TRY(s.sync());
     *DTMIN = sc.dtmin_raw;
+    return CFD_OK;
+}
+
+int cfd_force_visc(const int* NELEM, const int* npoin, const int* nsets, const int* IELEM_SETS,
+                   const int* ISET, const int* inpoel, const int* NSET_NUMB, const double* U_inf,
+                   const double* V_inf, const double* RHO_inf, const double* T_inf,
+                   const double* X, const double* Y, const double* P, const double* T,
+                   const double* VEL_X, const double* VEL_Y, const double* DNX,
+                   const double* DNY, const double* RMU, const double* RHO, double* F_VX,
+                   double* F_VY, double* skin) {
+    (void)RMU;
+    (void)RHO;
+    if (!NELEM || !npoin || !nsets || !IELEM_SETS || !ISET || !inpoel || !NSET_NUMB || !U_inf ||
+        !V_inf || !RHO_inf || !T_inf || !X || !Y || !P || !T || !VEL_X || !VEL_Y || !DNX ||
+        !DNY || !F_VX || !F_VY || bad_sizes(NELEM, npoin))
+        return arg_error("cfd_force_visc");
+    const int E = *NELEM, N = *npoin, NS = *nsets, nset = *NSET_NUMB;
+    if (nset < 0 || nset > 10) return arg_error("NSET_NUMB");
+    std::vector<int> ptr(11, 0), eel;
+    std::vector<int2> edges;
+    for (int s = 0; s < nset; ++s) {
+        if (IELEM_SETS[s] < 0 || IELEM_SETS[s] > NS) return arg_error("IELEM_SETS");
+        for (int ii = 0; ii < IELEM_SETS[s]; ++ii) {
+            const int* e = ISET + 3 * (s + 10 * (size_t)ii);
+            if (e[0] < 1 || e[0] > N || e[1] < 1 || e[1] > N || e[2] < 1 || e[2] > E)
+                return arg_error("ISET");
+            edges.push_back(make_int2(e[0] - 1, e[1] - 1));
+            eel.push_back(e[2] - 1);
+        }
+        ptr[s + 1] = (int)edges.size();
+    }
+    for (int s = nset; s < 10; ++s) ptr[s + 1] = ptr[s];
+    std::vector<int4> el;
+    TRY(make_elems(inpoel, E, N, el));
+    const int ne = (int)edges.size();
+    Scratch s;
+    TRY(s.init());
+    int4* d_el;
+    int2* d_ed;
+    int *d_ptr, *d_eel;
+    double *d_X, *d_Y, *d_P, *d_T, *d_vx, *d_vy, *d_dnx, *d_dny, *d_terms, *d_skin, *d_fv;
+    TRY(s.put(&d_el, el.data(), E));
+    TRY(s.put(&d_ed, edges.data(), edges.size()));
+    TRY(s.put(&d_ptr, ptr.data(), ptr.size()));
+    TRY(s.put(&d_eel, eel.data(), eel.size()));
+    TRY(s.put(&d_X, X, N));
+    TRY(s.put(&d_Y, Y, N));
+    TRY(s.put(&d_P, P, N));
+    TRY(s.put(&d_T, T, N));
+    TRY(s.put(&d_vx, VEL_X, N));
+    TRY(s.put(&d_vy, VEL_Y, N));
+    TRY(s.put(&d_dnx, DNX, 3 * (size_t)E));
+    TRY(s.put(&d_dny, DNY, 3 * (size_t)E));
+    TRY(s.alloc(&d_terms, 2 * (size_t)ne));
+    TRY(s.alloc(&d_skin, 3 * (size_t)ne));
+    TRY(s.alloc(&d_fv, 20));
+    CFD_CUDA(launch_force_visc(s.stream, 0, nset, d_ptr, ne, d_ed, d_eel, d_el, d_dnx, d_dny, 3, 1,
+                               nullptr, d_P, d_T, d_vx, d_vy, d_X, d_Y, *U_inf, *V_inf, *RHO_inf,
+                               *T_inf, d_terms, skin ? d_skin : nullptr, d_fv));
+    double fv[20];
+    TRY(s.get(fv, d_fv, 20));
+    if (skin) TRY(s.get(skin, d_skin, 3 * (size_t)ne));
+    TRY(s.sync());
+    for (int k = 0; k < 10; ++k) {
+        F_VX[k] = fv[k];
+        F_VY[k] = fv[10 + k];
+    }
     return CFD_OK;
 }
 

@@ -5,6 +5,7 @@
 
 #include "cfd_kernels.cuh"
 #include "host_prep.h"
+#include "newmark.h"
 
 struct cfd_mpnn;
 struct cfd_mpnn_graph;
@@ -41,6 +42,7 @@ struct Ctx {
     int bandera_host = 1;
     double time = 0.0, last_dtmin = 0.0;
     double disn[2] = {0.0, 0.0};
+    NewmarkState nm{};  // FP64 form, CFD_MOTION_NEWMARK: velocities and accelerations
     // sizes
     int nwn = 0, nnmove = 0, nufix = 0, pcg_grid = 1, nsm = 1;
     // mesh
@@ -58,6 +60,10 @@ struct Ctx {
     int2 *d_wedge = nullptr, *d_walls = nullptr;
     int* d_set_ptr = nullptr;
     int2* d_set_edges = nullptr;
+    int* d_set_elem = nullptr;
+    // FORCE_VISC: [F_VX(10), F_VY(10)], per-edge terms (scratch) and SKIN.DAT rows
+    double *d_fv = nullptr, *d_fv_terms = nullptr, *d_fv_skin = nullptr;
+    bool fv_each = false;
     double *d_xref = nullptr, *d_yref = nullptr;
     int *d_fix_node = nullptr, *d_fix_set = nullptr, *d_ufix_node = nullptr, *d_ufix_src = nullptr;
     unsigned char* d_isfix = nullptr;
@@ -153,6 +159,8 @@ struct Ctx {
     int enqueue_mixed(bool learned);
     int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);
+    int force_visc_now();
+    int set_force_visc_each_step(bool on);
     int step_once();
     int step_once_mixed();
     int step(int nsteps, cfd_step_report* rep);

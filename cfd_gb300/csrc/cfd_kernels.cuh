@@ -69,6 +69,7 @@ struct MotionScal {
     double time, disn0, disn1;  // TIME, DISN(1:2) (heave, pitch)
     double ca, sa, yposr;       // this step's TRANSF increment
     double dtmin;               // DTMIN of the step
+    double veln0, veln1, accn0, accn1;  // CFD_MOTION_NEWMARK: VELN, ACCN
 };
 struct MotionTailArgs {
     int nset;  // FORCES
@@ -91,6 +92,17 @@ struct MotionTailArgs {
     StepScal* sc;
 };
 __global__ void k_motion_tail(MotionTailArgs a);
+
+// FORCE_VISC over the force sets' edges: form 0 reads FP64 fields and dNx(j,e) =
+// dnx[e*se + j*sj]; form 1 reads float fields and the mixed form's geo8.  terms: 2 per
+// edge (scratch); skin: 3 per edge or null; fv[0..9] = F_VX, fv[10..19] = F_VY.
+cudaError_t launch_force_visc(cudaStream_t st, int form, int nset, const int* set_ptr,
+                              int nedges, const int2* edges, const int* eelem, const int4* elem,
+                              const double* dnx, const double* dny, size_t se, size_t sj,
+                              const float4* geo8, const void* P, const void* T, const void* VX,
+                              const void* VY, const double* X, const double* Y, double u_inf,
+                              double v_inf, double rho_inf, double t_inf, double* terms,
+                              double* skin, double* fv);
 
 // ------------------------------------------------------------------ mixed precision
 __global__ void k_narrow_state(int npoin, const double* U, const double* T, const double* VX,

@@ -252,6 +252,40 @@ int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
     return CFD_OK;
 }
 
+// ------------------------------------------------------------------ FORCE_VISC
+// ns2DComp.ALE.f90:819-893 on the current fields, mesh and dNx into d_fv (F_VX, F_VY) and
+// d_fv_skin (the SKIN.DAT rows)
+int Ctx::force_visc_now() {
+    const int ne = (int)bc.set_elem.size();
+    if (!d_fv) {
+        int st;
+        if ((st = dalloc(&d_fv, 20))) return st;
+        if ((st = dalloc(&d_fv_terms, 2 * (size_t)ne))) return st;
+        if ((st = dalloc(&d_fv_skin, 3 * (size_t)ne))) return st;
+    }
+    const bool mixed = prec == CFD_PREC_MIXED;
+    const size_t E = (size_t)nelem;
+    CFD_CUDA(launch_force_visc(
+        stream, mixed ? 1 : 0, bc.nset_numb, d_set_ptr, ne, d_set_edges, d_set_elem, d_elem,
+        d_geo, d_geo ? d_geo + 3 * E : nullptr, 1, E, d_geo8,
+        mixed ? (const void*)d_Pf : (const void*)d_P, mixed ? (const void*)d_Tf : (const void*)d_T,
+        mixed ? (const void*)d_VXf : (const void*)d_VX, mixed ? (const void*)d_VYf : (const void*)d_VY,
+        d_X, d_Y, prm.u_inf, prm.v_inf, prm.rho_inf, prm.t_inf, d_fv_terms, d_fv_skin, d_fv));
+    return CFD_OK;
+}
+
+// Every step computes FORCE_VISC at the reference's print-block point (on), or only
+// cfd_ctx_force_visc computes it, on the state and mesh of the call (off).  The captured
+// step is captured again.
+int Ctx::set_force_visc_each_step(bool on) {
+    if (on == fv_each) return CFD_OK;
+    fv_each = on;
+    if (step_exec) { cudaGraphExecDestroy(step_exec); step_exec = nullptr; }
+    if (step_graph) { cudaGraphDestroy(step_graph); step_graph = nullptr; }
+    if (on && !d_fv) return force_visc_now();  // buffers, and a defined first readout
+    return CFD_OK;
+}
+
 // ------------------------------------------------------------------ one time step
 int Ctx::step_once() {
     const int N = npoin, E = nelem;
@@ -314,6 +348,17 @@ int Ctx::step_once() {
         double ph = 2.0 * PI * prm.motion_freq * time;
         disn[0] = prm.heave_amp * std::sin(ph);
         disn[1] = prm.pitch_amp * std::sin(ph);
+    } else if (prm.motion_law == CFD_MOTION_NEWMARK) {
+        // the structural model needs this step's set-1 force and moment
+        CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
+        CFD_CUDA(cudaStreamSynchronize(stream));
+        double F[2];
+        nm.dis[0] = disn[0];
+        nm.dis[1] = disn[1];
+        newmark_load(nm, h_scal->fx[0], h_scal->fy[0], h_scal->rm[0], F);
+        newmark_step(nm, F, dtmin);
+        disn[0] = nm.dis[0];
+        disn[1] = nm.dis[1];
     } else {
         const double ampli = PI / 8.0;
         disn[1] = ampli * std::sin(10.0 * time);
@@ -335,6 +380,10 @@ int Ctx::step_once() {
     tstop(TM_GRAD);
     CFD_LAUNCH(k_motion_update, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1], d_scal,
                d_X, d_Y, d_WX, d_WY);
+    if (fv_each) {  // FORCE_VISC at the print block's point: moved mesh, previous dNx
+        st = force_visc_now();
+        if (st) return st;
+    }
     if (prm.moving == 1) {  // ns2DComp.ALE.f90:259-275
         st = geometry(prm.mass_mode == CFD_MASS_MASAS, false);
         if (st) return st;
@@ -487,6 +536,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if ((st = upload(&d_walls, (const int2*)bc.walls.data(), bc.walls.size() / 2))) return st;
     if ((st = upload(&d_set_ptr, bc.set_ptr.data(), bc.set_ptr.size()))) return st;
     if ((st = upload(&d_set_edges, (const int2*)bc.set_edges.data(), bc.set_edges.size() / 2))) return st;
+    if ((st = upload(&d_set_elem, bc.set_elem.data(), bc.set_elem.size()))) return st;
     if ((st = upload(&d_xref, prm.xref, 10))) return st;
     if ((st = upload(&d_yref, prm.yref, 10))) return st;
     nnmove = (int)bc.fix_node.size();
@@ -762,6 +812,10 @@ int Ctx::enqueue_mixed(bool learned) {
     tstop(TM_GRAD);
     CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1],
                d_scal, d_X, d_Y, d_WX, d_WY, d_Xhi, d_Xlo, d_Wf);
+    if (fv_each) {  // FORCE_VISC at the print block's point: moved mesh, previous dNx
+        st = force_visc_now();
+        if (st) return st;
+    }
     if (prm.moving == 1) {
         st = geometry_mixed(false);
         if (st) return st;

@@ -154,6 +154,7 @@ int build_bc_tables(const cfd_mesh* m, BcTables& bc, std::string* why) {
     bc.nset_numb = m->nset_numb;
     bc.set_ptr.assign(11, 0);
     bc.set_edges.clear();
+    bc.set_elem.clear();
     std::vector<int> last_set(N, -1);
     for (int s = 0; s < m->nset_numb; ++s) {
         if (m->ielem_sets[s] < 0 || m->ielem_sets[s] > m->nsets) {
@@ -162,9 +163,11 @@ int build_bc_tables(const cfd_mesh* m, BcTables& bc, std::string* why) {
         }
         for (int ii = 0; ii < m->ielem_sets[s]; ++ii) {
             const int* e = m->iset + 3 * (s + 10 * (size_t)ii);
-            if (e[0] < 1 || e[0] > N || e[1] < 1 || e[1] > N) return bad("iset");
+            if (e[0] < 1 || e[0] > N || e[1] < 1 || e[1] > N || e[2] < 1 || e[2] > m->nelem)
+                return bad("iset");
             bc.set_edges.push_back(e[0] - 1);
             bc.set_edges.push_back(e[1] - 1);
+            bc.set_elem.push_back(e[2] - 1);
             last_set[e[0] - 1] = s;  // TRANSF loop order: set, edge, JJ=1,2
             last_set[e[1] - 1] = s;
         }

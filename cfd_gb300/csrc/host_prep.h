@@ -35,6 +35,7 @@ struct BcTables {
     std::vector<int> walls;        // 2*nwall, 0-based
     // FORCES sets: per set the (n1, n2) edges in ISET order
     std::vector<int> set_ptr, set_edges;  // set_edges 2 per edge, 0-based
+    std::vector<int> set_elem;            // owning element of each set edge, 0-based
     int nset_numb = 0;
     // mesh-motion Dirichlet list: ilaux order; per entry the node and the set whose
     // TRANSF write wins for it (-1: none / fixed-movement entry)

@@ -714,4 +714,123 @@ __global__ void k_min_positive(long n, const double* __restrict__ x, unsigned lo
     if ((threadIdx.x & 31) == 0) atomicMin(bits, m);
 }
 
+// ------------------------------------------------------------------ FORCE_VISC
+// ns2DComp.ALE.f90:819-893: per wall edge of the force sets, the stress of its element on
+// the edge's outward normal (Sutherland mu at the edge's mean T with the hard-coded 0.017,
+// :838-840; element-mean pressure and velocity gradients), in the reference's operation
+// order.  One thread per edge writes its two force terms and its SKIN.DAT row (:887); the
+// per-set sums run in edge order in a second kernel, as the reference's loop does.
+struct DnStrided {  // dNx(j, e) = dnx[e*se + j*sj], dNy likewise
+    const double *dnx, *dny;
+    size_t se, sj;
+    __device__ void get(int e, double nx[3], double ny[3]) const {
+        for (int j = 0; j < 3; ++j) {
+            nx[j] = dnx[e * se + j * sj];
+            ny[j] = dny[e * se + j * sj];
+        }
+    }
+};
+struct DnGeo8 {  // the mixed form's per-element float4 pair
+    const float4* g;
+    __device__ void get(int e, double nx[3], double ny[3]) const {
+        const float4 a = g[2 * (size_t)e], b = g[2 * (size_t)e + 1];
+        nx[0] = a.x; nx[1] = a.y; nx[2] = a.z;
+        ny[0] = a.w; ny[1] = b.x; ny[2] = b.y;
+    }
+};
+
+template <class Dn, class Fld>
+__global__ void k_force_visc_terms(int nedges, const int2* __restrict__ edges,
+                                   const int* __restrict__ eelem, const int4* __restrict__ elem,
+                                   Dn dn, const Fld* __restrict__ P, const Fld* __restrict__ T,
+                                   const Fld* __restrict__ VX, const Fld* __restrict__ VY,
+                                   const double* __restrict__ X, const double* __restrict__ Y,
+                                   double u_inf, double v_inf, double rho_inf, double t_inf,
+                                   double* __restrict__ terms, double* __restrict__ skin) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nedges) return;
+    const int2 ed = edges[k];
+    const int nn1 = ed.x, nn2 = ed.y, ielem = eelem[k];
+    const double temp = ((double)T[nn1] + (double)T[nn2]) / 2.0;
+    const double smu = 110.0;
+    const double r = temp / t_inf;
+    const double fmu = 0.017 * (r * sqrt(r)) * (t_inf + smu) / (temp + smu);
+    double rly = -(X[nn2] - X[nn1]);
+    double rlx = Y[nn2] - Y[nn1];
+    const double rmod = sqrt(rlx * rlx + rly * rly);
+    rlx = rlx / rmod;
+    rly = rly / rmod;
+    double nx[3], ny[3];
+    dn.get(ielem, nx, ny);
+    const int4 el = elem[ielem];
+    const int nn[3] = {el.x, el.y, el.z};
+    double dux = 0.0, duy = 0.0, dvx = 0.0, dvy = 0.0, press = 0.0;
+    for (int jj = 0; jj < 3; ++jj) {
+        const double vx = VX[nn[jj]], vy = VY[nn[jj]];
+        dux = dux + nx[jj] * vx;
+        duy = duy + ny[jj] * vx;
+        dvx = dvx + nx[jj] * vy;
+        dvy = dvy + ny[jj] * vy;
+        press = press + (double)P[nn[jj]];
+    }
+    press = press / 3.0;
+    const double txx = -press - fmu * (2.0 / 3.0 * (dux + dvy) - 2.0 * dux);
+    const double txy = fmu * (duy + dvx);
+    const double tyx = txy;
+    const double tyy = -press - fmu * (2.0 / 3.0 * (dux + dvy) - 2.0 * dvy);
+    const double ttx = txx * rlx + txy * rly;
+    const double tty = tyx * rlx + tyy * rly;
+    const double tmod = -ttx * rly + tty * rlx;
+    const double uu = u_inf * u_inf + v_inf * v_inf;
+    terms[2 * k] = ttx * rmod;
+    terms[2 * k + 1] = tty * rmod;
+    if (skin) {
+        skin[3 * k] = tmod / (.5 * rho_inf * uu);
+        skin[3 * k + 1] = (X[nn2] + X[nn1]) / 2.0;
+        skin[3 * k + 2] = press / 82713.27;
+    }
+}
+
+__global__ void k_force_visc_sum(int nset, const int* __restrict__ set_ptr,
+                                 const double* __restrict__ terms, double* __restrict__ fv) {
+    const int s = threadIdx.x;
+    if (s >= 10) return;
+    double fx = 0.0, fy = 0.0;
+    if (s < nset)
+        for (int k = set_ptr[s]; k < set_ptr[s + 1]; ++k) {
+            fx = fx + terms[2 * k];
+            fy = fy + terms[2 * k + 1];
+        }
+    fv[s] = fx;
+    fv[10 + s] = fy;
+}
+
+cudaError_t launch_force_visc(cudaStream_t st, int form, int nset, const int* set_ptr,
+                              int nedges, const int2* edges, const int* eelem, const int4* elem,
+                              const double* dnx, const double* dny, size_t se, size_t sj,
+                              const float4* geo8, const void* P, const void* T, const void* VX,
+                              const void* VY, const double* X, const double* Y, double u_inf,
+                              double v_inf, double rho_inf, double t_inf, double* terms,
+                              double* skin, double* fv) {
+    const unsigned grid = blocks_for(nedges > 0 ? nedges : 1, 128);
+    if (nedges > 0) {
+        if (form == 0)
+            k_force_visc_terms<<<grid, 128, 0, st>>>(
+                nedges, edges, eelem, elem, DnStrided{dnx, dny, se, sj}, (const double*)P,
+                (const double*)T, (const double*)VX, (const double*)VY, X, Y, u_inf, v_inf,
+                rho_inf, t_inf, terms, skin);
+        else
+            k_force_visc_terms<<<grid, 128, 0, st>>>(
+                nedges, edges, eelem, elem, DnGeo8{geo8}, (const float*)P, (const float*)T,
+                (const float*)VX, (const float*)VY, X, Y, u_inf, v_inf, rho_inf, t_inf, terms,
+                skin);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    k_force_visc_sum<<<1, 32, 0, st>>>(nset, set_ptr, terms, fv);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
 }  // namespace cfd

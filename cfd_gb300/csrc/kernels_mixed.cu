@@ -19,6 +19,7 @@
 // Vlam(3).  Slots are stored in element-around-point order, so each RK stage is one node
 // kernel that streams its slots and forms Inv + mu*Vmu + lambda*Vlam with the stage's T.
 #include "cfd_kernels.cuh"
+#include "newmark.h"
 
 namespace cfd {
 
@@ -822,7 +823,13 @@ __device__ MotionScal motion_step(const MotionScal& m, double dt, int law, doubl
     const double PI = 3.141592653589793;  // acos(-1)
     const double t = m.time + dt;
     const double alphav = m.disn1, yposrv = m.disn0;
-    double d0 = m.disn0, d1;
+    double d0 = m.disn0, d1 = m.disn1;
+    if (law == CFD_MOTION_NEWMARK) {  // the increment needs this step's forces: later
+        MotionScal o = m;
+        o.time = t;
+        o.dtmin = dt;
+        return o;
+    }
     if (law == CFD_MOTION_HARMONIC) {
         const double ph = 2.0 * PI * freq * t;
         d0 = heave_amp * sin(ph);
@@ -839,8 +846,16 @@ __device__ MotionScal motion_step(const MotionScal& m, double dt, int law, doubl
     o.sa = sin(alpha);
     o.yposr = d0 - yposrv;
     o.dtmin = dt;
+    o.veln0 = m.veln0;
+    o.veln1 = m.veln1;
+    o.accn0 = m.accn0;
+    o.accn1 = m.accn1;
     return o;
 }
+
+// TRANSF into x_fix and the Dirichlet values of the solves, entries k0, k0 + ks, ...
+__device__ __forceinline__ void tail_transf(const MotionTailArgs& a, const MotionScal& mv,
+                                            int k0, int ks);
 
 // TRANSF (meshMove.f90:369-392) of moving-list entry k
 __device__ __forceinline__ double2 transf_one(const MotionTailArgs& a, const MotionScal& mv,
@@ -867,19 +882,8 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
                                            a.freq);
     __syncthreads();
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
-    for (int k = gt; k < a.nnmove; k += gs) {
-        const double2 d = transf_one(a, mv, k);
-        a.xfix_x[k] = d.x;
-        a.xfix_y[k] = d.y;
-    }
-    for (int k = gt; k < a.nufix; k += gs) {
-        const int i = a.ufix_node[k];
-        const double2 d = transf_one(a, mv, a.ufix_src[k]);
-        a.x0[i] = d.x;
-        a.xf0[i] = d2f_trunc(d.x);
-        a.x1[i] = d.y;
-        a.xf1[i] = d2f_trunc(d.y);
-    }
+    const bool structural = a.law == CFD_MOTION_NEWMARK;
+    if (!structural) tail_transf(a, mv, gt, gs);
     for (int s = 0; s < a.nset; ++s) {
         double fx = 0.0, fy = 0.0, rm = 0.0;
         const double xr = a.xref[s], yr = a.yref[s];
@@ -913,9 +917,53 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
         const int s = threadIdx.x / 3, q = threadIdx.x % 3;
         (q == 0 ? a.sc->fx : q == 1 ? a.sc->fy : a.sc->rm)[s] = v;
     }
+    if (structural) {  // the Newmark step under set 1's load, then TRANSF by this block
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            NewmarkState ns;
+            ns.dis[0] = mv.disn0;
+            ns.dis[1] = mv.disn1;
+            ns.vel[0] = mv.veln0;
+            ns.vel[1] = mv.veln1;
+            ns.acc[0] = mv.accn0;
+            ns.acc[1] = mv.accn1;
+            double F[2];
+            newmark_load(ns, a.sc->fx[0], a.sc->fy[0], a.sc->rm[0], F);
+            newmark_step(ns, F, mv.dtmin);
+            const double alpha = ns.dis[1] - mv.disn1;
+            mv.yposr = ns.dis[0] - mv.disn0;
+            mv.ca = cos(alpha);
+            mv.sa = sin(alpha);
+            mv.disn0 = ns.dis[0];
+            mv.disn1 = ns.dis[1];
+            mv.veln0 = ns.vel[0];
+            mv.veln1 = ns.vel[1];
+            mv.accn0 = ns.acc[0];
+            mv.accn1 = ns.acc[1];
+        }
+        __syncthreads();
+        tail_transf(a, mv, threadIdx.x, blockDim.x);
+    }
     if (threadIdx.x == 0) {
         *a.m = mv;
         *a.count = 0u;
+    }
+}
+
+__device__ __forceinline__ void tail_transf(const MotionTailArgs& a, const MotionScal& mv,
+                                            int k0, int ks) {
+    for (int k = k0; k < a.nnmove; k += ks) {
+        const double2 d = transf_one(a, mv, k);
+        a.xfix_x[k] = d.x;
+        a.xfix_y[k] = d.y;
+    }
+    for (int k = k0; k < a.nufix; k += ks) {
+        const int i = a.ufix_node[k];
+        const double2 d = transf_one(a, mv, a.ufix_src[k]);
+        a.x0[i] = d.x;
+        a.xf0[i] = d2f_trunc(d.x);
+        a.x1[i] = d.y;
+        a.xf1[i] = d2f_trunc(d.y);
     }
 }
 

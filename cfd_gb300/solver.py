@@ -99,6 +99,26 @@ def deriv(X, Y, inpoel):
     return r
 
 
+def FORCE_VISC(NELEM, npoin, nsets, IELEM_SETS, ISET, inpoel, NSET_NUMB, U_inf, V_inf, RHO_inf,
+               T_inf, X, Y, P, T, VEL_X, VEL_Y, DNX, DNY, RMU=0.0, RHO=None, skin=False):
+    """ns2DComp.ALE.f90:819-893 -> (F_VX(10), F_VY(10)[, skin rows (nedges, 3)]).  ISET is
+    Fortran ISET(3,10,nsets) as a C array of shape (nsets, 10, 3); DNX, DNY (nelem, 3)."""
+    L = abi.lib()
+    fvx, fvy = np.zeros(10), np.zeros(10)
+    ne = int(np.sum(np.asarray(IELEM_SETS)[:NSET_NUMB]))
+    sk = np.zeros((max(ne, 1), 3)) if skin else None
+    rho = _f64(np.zeros(npoin) if RHO is None else RHO)
+    check(L.cfd_force_visc(_ci(NELEM), _ci(npoin), _ci(nsets), iptr(_i32(IELEM_SETS)),
+                           iptr(_i32(ISET)), iptr(_i32(inpoel)), _ci(NSET_NUMB),
+                           C.byref(C.c_double(U_inf)), C.byref(C.c_double(V_inf)),
+                           C.byref(C.c_double(RHO_inf)), C.byref(C.c_double(T_inf)),
+                           dptr(_f64(X)), dptr(_f64(Y)), dptr(_f64(P)), dptr(_f64(T)),
+                           dptr(_f64(VEL_X)), dptr(_f64(VEL_Y)), dptr(_f64(DNX)),
+                           dptr(_f64(DNY)), C.byref(C.c_double(RMU)), dptr(rho), dptr(fvx),
+                           dptr(fvy), dptr(sk)), "cfd_force_visc")
+    return (fvx, fvy, sk[:ne]) if skin else (fvx, fvy)
+
+
 def MASAS(area, inpoel, npoin):
     L = abi.lib()
     inp = _i32(inpoel)
@@ -225,6 +245,21 @@ class Solver:
         out = (C.c_longlong * 4)()
         check(abi.lib().cfd_ctx_guess_stats(self.h, out), "cfd_ctx_guess_stats")
         return tuple(int(v) for v in out)
+
+    def set_force_visc(self, each_step):
+        """each_step: every step computes FORCE_VISC where the reference's print block does."""
+        check(abi.lib().cfd_ctx_set_force_visc(self.h, 1 if each_step else 0),
+              "cfd_ctx_set_force_visc")
+
+    def force_visc(self):
+        """(F_VX[nset_numb], F_VY[nset_numb], SKIN.DAT rows (nedges, 3))."""
+        fvx, fvy = np.zeros(10), np.zeros(10)
+        iset, ielem_sets, n = self.case.iset_array()
+        ne = int(ielem_sets[:n].sum())
+        skin = np.zeros((max(ne, 1), 3))
+        check(abi.lib().cfd_ctx_force_visc(self.h, dptr(fvx), dptr(fvy), dptr(skin)),
+              "cfd_ctx_force_visc")
+        return fvx[:n], fvy[:n], skin[:ne]
 
     def graph_state(self):
         """(1 if steps replay a captured CUDA graph, replays so far, kernels per replay)."""

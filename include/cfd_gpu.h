@@ -55,7 +55,10 @@ enum {
 /* motion_law: the prescribed body motion (reference hard-codes law 0) */
 enum {
     CFD_MOTION_REFERENCE = 0, /* pitch pi/8*sin(10 t), no heave (meshMove.f90:55-71)    */
-    CFD_MOTION_HARMONIC = 1   /* heave A_h*sin(2 pi f t), pitch A_p*sin(2 pi f t)       */
+    CFD_MOTION_HARMONIC = 1,  /* heave A_h*sin(2 pi f t), pitch A_p*sin(2 pi f t)       */
+    CFD_MOTION_NEWMARK = 2    /* heave and pitch from the 2-DOF Newmark structural model
+                                 under set 1's pressure force and moment
+                                 (meshMove.f90:61-62, :196-367, enabled)              */
 };
 
 /* guess_mode: initial guess of the two mesh-motion solves */
@@ -165,6 +168,17 @@ int cfd_deltat(const double* T, const double* VEL_X, const double* VEL_Y,
                const double* W_X, const double* W_Y, const double* area,
                const int* inpoel, const int* nelem, const int* npoin,
                const double* scal4, double* DT, double* DTMIN);
+
+/* FORCE_VISC (ns2DComp.ALE.f90:819-893), drop-in: the reference's argument list (RMU and
+ * RHO are unused by its body), F_VX/F_VY 10 each; skin: NULL, or 3 doubles per set edge
+ * (the SKIN.DAT rows the reference writes instead). */
+int cfd_force_visc(const int* NELEM, const int* npoin, const int* nsets, const int* IELEM_SETS,
+                   const int* ISET, const int* inpoel, const int* NSET_NUMB, const double* U_inf,
+                   const double* V_inf, const double* RHO_inf, const double* T_inf,
+                   const double* X, const double* Y, const double* P, const double* T,
+                   const double* VEL_X, const double* VEL_Y, const double* DNX,
+                   const double* DNY, const double* RMU, const double* RHO, double* F_VX,
+                   double* F_VY, double* skin);
 
 /* deriv (subrutinas.f90:88-126) -> area, dNx(3,nelem), dNy, HH, HHX, HHY, hmin. */
 int cfd_deriv(const double* X, const double* Y, const int* inpoel, const int* nelem,
@@ -345,6 +359,16 @@ int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate);
 /* counters since attach: steps with the network evaluated, solves 1 (x) and 2 (y) that
  * took the network's guess, steps */
 int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4);
+
+/* FORCE_VISC (ns2DComp.ALE.f90:819-893): viscous force per force set on its wall edges
+ * (F_VX, F_VY: 10 each) and, when skin is not NULL, the SKIN.DAT row of every set edge in
+ * set and edge order (3 doubles: skin friction, the edge's mean x, element-mean pressure /
+ * 82713.27).  With each_step set (cfd_ctx_set_force_visc) every cfd_step computes it where
+ * the reference's print block does (after the mesh moved, before its dNx are recomputed)
+ * and cfd_ctx_force_visc returns the last step's values; otherwise cfd_ctx_force_visc
+ * computes it on the context's current state, mesh and dNx. */
+int cfd_ctx_set_force_visc(cfd_ctx* ctx, int each_step);
+int cfd_ctx_force_visc(cfd_ctx* ctx, double* F_VX, double* F_VY, double* skin);
 
 /* Mixed form: out3 = (1 if steps replay a captured CUDA graph, steps replayed so far,
  * kernels in one replay).  The first step of a context, and steps that run the learned

@@ -635,6 +635,69 @@ void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
 }
 
 // normales: subrutinas.f90:7-64 (wall-edge order).  Returns m.
+// FORCE_VISC (ns2DComp.ALE.f90:819-893): per set and wall edge, the stress of the owning
+// element (Sutherland mu at the edge's mean T, hard-coded 0.017, :838-840; velocity
+// gradients through dNx, dNy; element-mean pressure) on the edge's outward normal.  F_VX,
+// F_VY summed in edge order; skin (nullable) gets per edge, in set and edge order, the
+// SKIN.DAT row (:887): SKIN, the edge's mean x, press/82713.27.  RMU and RHO of the
+// reference's argument list are unused by its body and left out.
+void or_force_visc(int nelem, int npoin, int nsets, const int* ielem_sets, const int* iset,
+                   const int* inpoel, int nset_numb, double u_inf, double v_inf, double rho_inf,
+                   double t_inf, const double* X, const double* Y, const double* P,
+                   const double* T, const double* VEL_X, const double* VEL_Y, const double* dNx,
+                   const double* dNy, double* F_VX, double* F_VY, double* skin) {
+    (void)nelem;
+    (void)npoin;
+    (void)nsets;
+    for (int s = 0; s < 10; ++s) {
+        F_VX[s] = 0.0;
+        F_VY[s] = 0.0;
+    }
+    long row = 0;
+    for (int sn = 0; sn < nset_numb; ++sn)
+        for (int ii = 0; ii < ielem_sets[sn]; ++ii) {
+            const int* e = iset + 3 * (sn + 10 * (size_t)ii);
+            const int nn1 = e[0] - 1, nn2 = e[1] - 1, ielem = e[2] - 1;
+            const double temp = (T[nn1] + T[nn2]) / 2.0;
+            const double smu = 110.0;
+            const double r = temp / t_inf;
+            const double fmu = 0.017 * (r * std::sqrt(r)) * (t_inf + smu) / (temp + smu);
+            double rly = -(X[nn2] - X[nn1]);
+            double rlx = Y[nn2] - Y[nn1];
+            const double rmod = std::sqrt(rlx * rlx + rly * rly);
+            rlx = rlx / rmod;
+            rly = rly / rmod;
+            double dux = 0.0, duy = 0.0, dvx = 0.0, dvy = 0.0, press = 0.0;
+            for (int jj = 0; jj < 3; ++jj) {
+                const int nn = inpoel[3 * (size_t)ielem + jj] - 1;
+                const double nx = dNx[3 * (size_t)ielem + jj], ny = dNy[3 * (size_t)ielem + jj];
+                dux = dux + nx * VEL_X[nn];
+                duy = duy + ny * VEL_X[nn];
+                dvx = dvx + nx * VEL_Y[nn];
+                dvy = dvy + ny * VEL_Y[nn];
+                press = press + P[nn];
+            }
+            press = press / 3.0;
+            const double txx = -press - fmu * (2.0 / 3.0 * (dux + dvy) - 2.0 * dux);
+            const double txy = fmu * (duy + dvx);
+            const double tyx = txy;
+            const double tyy = -press - fmu * (2.0 / 3.0 * (dux + dvy) - 2.0 * dvy);
+            const double ttx = txx * rlx + txy * rly;
+            const double tty = tyx * rlx + tyy * rly;
+            const double tmod = -ttx * rly + tty * rlx;
+            const double uu = u_inf * u_inf + v_inf * v_inf;
+            const double sk = tmod / (.5 * rho_inf * uu);
+            F_VX[sn] = F_VX[sn] + ttx * rmod;
+            F_VY[sn] = F_VY[sn] + tty * rmod;
+            if (skin) {
+                skin[3 * row] = sk;
+                skin[3 * row + 1] = (X[nn2] + X[nn1]) / 2.0;
+                skin[3 * row + 2] = press / 82713.27;
+            }
+            ++row;
+        }
+}
+
 int or_normales(int npoin, int nwall, const int* wall, const double* X, const double* Y,
                 int* n_ipoin, double* n_x, double* n_y) {
     std::vector<double> nlx(npoin, 0.0), nly(npoin, 0.0), den(npoin, 0.0);
@@ -912,6 +975,10 @@ struct or_case {
     int m = 0; std::vector<int> n_ipoin; std::vector<double> n_x, n_y;
     int iter = 0, bandera = 1;
     double time = 0.0, dtmin = 0.0, dtmin1 = 0.0, disn[2] = {0.0, 0.0};
+    double veln[2] = {0.0, 0.0}, accn[2] = {0.0, 0.0};  // setNewmarkCondition (meshMove.f90:14-25)
+    bool fv_each = false;  // FORCE_VISC every step at the print block's point
+    double fvx[10] = {0}, fvy[10] = {0};
+    std::vector<double> skin;
     double fx[10], fy[10], rm[10];
     cfd_solve_info sx{}, sy{};
     double timers[TM_N] = {0};
@@ -1034,6 +1101,54 @@ void forces(or_case* c) {
 }
 
 // fluidStructure: meshMove.f90:28-142 with the motion law as an option
+// NEWMARK_METHOD(H) (meshMove.f90:196-310) with MATVEC (:312-324) and GAUSS (:326-346) for
+// NDIM = 2, statement by statement; DISN, VELN, ACCN and the load F are the module arrays.
+void newmark_method(double H, const double F[2], double DISN[2], double VELN[2], double ACCN[2]) {
+    const double GR = 1.0;                                       // :239
+    const double GAMA = .5, BETA = .25;                          // :246
+    const double A1 = 1.0 / (BETA * H * H), A2 = 1.0 / (BETA * H), A3 = 1.0 / (2.0 * BETA) - 1.0,
+                 A4 = (1.0 - GAMA) * H, A5 = GAMA * H;            // :248
+    const double A1D = GAMA / (BETA * H), A2D = GAMA / BETA - 1.0,
+                 A3D = 0.5 * H * (GAMA / BETA - 2.0);            // :249
+    double MASA[2][2], C[2][2], K[2][2], CTEN[2] = {0.0, 0.0};
+    MASA[0][0] = 51.5; MASA[0][1] = -51.5 * .0429;               // :258-259
+    MASA[1][0] = -51.5 * .0429; MASA[1][1] = 2.275;
+    C[0][0] = 32.358 / GR; C[0][1] = 0.0;                        // :262-263
+    C[1][0] = 0.0; C[1][1] = 5.718 / GR;
+    K[0][0] = 50828.463 / GR; K[0][1] = 0.0;                     // :266-267
+    K[1][0] = 0.0; K[1][1] = 35923.241 / GR;
+    for (int i = 0; i < 2; ++i)                                  // :280 K=K+A1*MASA+A1D*C
+        for (int j = 0; j < 2; ++j) K[i][j] = K[i][j] + A1 * MASA[i][j] + A1D * C[i][j];
+    for (int I = 0; I < 1; ++I)                                  // :283-290
+        for (int J = I + 1; J < 2; ++J) {
+            CTEN[J] = K[J][I] / K[I][I];
+            for (int l = I + 1; l < 2; ++l) K[J][l] = K[J][l] - CTEN[J] * K[I][l];
+        }
+    double DISS[2], VELS[2], ACCS[2], R[2], G[2], G1[2];
+    for (int i = 0; i < 2; ++i) { DISS[i] = DISN[i]; VELS[i] = VELN[i]; ACCS[i] = ACCN[i]; }
+    auto matvec = [](const double A[2][2], const double* X, double* AUX) {
+        for (int i = 0; i < 2; ++i) {
+            AUX[i] = 0.0;
+            for (int j = 0; j < 2; ++j) AUX[i] = AUX[i] + A[i][j] * X[j];
+        }
+    };
+    for (int i = 0; i < 2; ++i) G[i] = A1 * DISN[i] + A2 * VELN[i] + A3 * ACCN[i];  // :303
+    matvec(MASA, G, G1);
+    for (int i = 0; i < 2; ++i) R[i] = F[i] + G1[i];
+    for (int i = 0; i < 2; ++i) G[i] = A1D * DISN[i] + A2D * VELN[i] + A3D * ACCN[i];  // :308
+    matvec(C, G, G1);
+    for (int i = 0; i < 2; ++i) R[i] = R[i] + G1[i];
+    for (int I = 0; I < 1; ++I)                                  // GAUSS :333-337
+        for (int J = I + 1; J < 2; ++J) R[J] = R[J] - CTEN[J] * R[I];
+    for (int I = 1; I >= 0; --I) {                               // :340-346
+        double S = 0.0;
+        for (int J = I + 1; J < 2; ++J) S = S + K[I][J] * DISN[J];
+        DISN[I] = (R[I] - S) / K[I][I];
+    }
+    for (int i = 0; i < 2; ++i) ACCN[i] = A1 * (DISN[i] - DISS[i]) - A2 * VELS[i] - A3 * ACCS[i];
+    for (int i = 0; i < 2; ++i) VELN[i] = VELS[i] + A4 * ACCS[i] + A5 * ACCN[i];
+}
+
 void fluid_structure(or_case* c, double dtmin, double time) {
     const int N = c->npoin;
     std::vector<double> dxpos(N, 0.0), dypos(N, 0.0);
@@ -1048,6 +1163,12 @@ void fluid_structure(or_case* c, double dtmin, double time) {
         double ph = 2.0 * PI * c->p.motion_freq * time;
         c->disn[0] = c->p.heave_amp * std::sin(ph);
         c->disn[1] = c->p.pitch_amp * std::sin(ph);
+    } else if (c->p.motion_law == CFD_MOTION_NEWMARK) {
+        // the load lines :61-62 and the NEWMARK_METHOD call :67, enabled
+        double F[2];
+        F[0] = std::cos(c->disn[1]) * c->fy[0] - std::sin(c->disn[1]) * c->fx[0];
+        F[1] = c->rm[0] + 0.1 * std::sin(c->disn[1]) * c->fx[0] - std::cos(c->disn[1]) * 0.1 * c->fy[0];
+        newmark_method(dtmin, F, c->disn, c->veln, c->accn);
     } else {
         const double ampli = PI / 8.0;
         c->disn[1] = ampli * std::sin(10.0 * time);  // :70
@@ -1107,6 +1228,13 @@ void mass_update(or_case* c, double dt) {
 }  // namespace
 
 extern "C" {
+
+static void or_case_force_visc_now(or_case* c) {
+    or_force_visc(c->nelem, c->npoin, c->nsets, c->ielem_sets, c->iset.data(), c->inpoel.data(),
+                  c->nset_numb, c->p.u_inf, c->p.v_inf, c->p.rho_inf, c->p.t_inf, c->X.data(),
+                  c->Y.data(), c->P.data(), c->T.data(), c->VEL_X.data(), c->VEL_Y.data(),
+                  c->dNx.data(), c->dNy.data(), c->fvx, c->fvy, c->skin.data());
+}
 
 or_case* or_case_create(const cfd_mesh* mesh, const cfd_params* prm, int do_smoothing) {
     or_case* c = new or_case();
@@ -1221,6 +1349,10 @@ int or_case_step(or_case* c, int nsteps, cfd_step_report* rep) {
         c->U1 = c->U;
         rk(c, dtmin);
         fluid_structure(c, dtmin, c->time);
+        if (c->fv_each) {  // the print block (:224-230): after the move, before deriv
+            c->skin.assign(3 * (size_t)std::max(1, (int)(c->iset.size() / 3)), 0.0);
+            or_case_force_visc_now(c);
+        }
         c->bandera += 1;
         if (c->p.moving == 1) {  // :259-275
             geometry(c);
@@ -1267,6 +1399,24 @@ void or_case_get_fields(or_case* c, double* RHO, double* VEL_X, double* VEL_Y, d
     if (RMACH) std::memcpy(RMACH, c->RMACH.data(), n);
     if (W_X) std::memcpy(W_X, c->W_X.data(), n);
     if (W_Y) std::memcpy(W_Y, c->W_Y.data(), n);
+}
+
+void or_case_set_force_visc(or_case* c, int each_step) { c->fv_each = each_step != 0; }
+
+void or_case_force_visc(or_case* c, double* F_VX, double* F_VY, double* skin) {
+    if (!c->fv_each) {
+        c->skin.assign(3 * (size_t)std::max(1, (int)(c->iset.size() / 3)), 0.0);
+        or_case_force_visc_now(c);
+    }
+    for (int s = 0; s < 10; ++s) {
+        F_VX[s] = c->fvx[s];
+        F_VY[s] = c->fvy[s];
+    }
+    if (skin) {
+        int ne = 0;
+        for (int s = 0; s < c->nset_numb; ++s) ne += c->ielem_sets[s];
+        std::memcpy(skin, c->skin.data(), sizeof(double) * 3 * (size_t)ne);
+    }
 }
 
 void or_case_get_motion(or_case* c, double* xpos, double* ypos) {
@@ -1322,6 +1472,11 @@ void or_case_timers(or_case* c, double* seconds, int max, int* n) {
     int k = max < TM_N ? max : TM_N;
     for (int i = 0; i < k; ++i) seconds[i] = c->timers[i];
     if (n) *n = k;
+}
+
+// one NEWMARK_METHOD step on a state (dis, vel, acc: 2 each), for unit tests
+void or_newmark_step(double H, const double* F, double* dis, double* vel, double* acc) {
+    newmark_method(H, F, dis, vel, acc);
 }
 
 }  // extern "C"

@@ -81,6 +81,15 @@ int or_normales(int npoin, int nwall, const int* wall, const double* X, const do
 void or_smoothing(double* X, double* Y, const int* inpoel, const int* fixed, int npoin,
                   int nelem, int* iters_out, double* min_quality_out);
 
+void or_force_visc(int nelem, int npoin, int nsets, const int* ielem_sets, const int* iset,
+                   const int* inpoel, int nset_numb, double u_inf, double v_inf, double rho_inf,
+                   double t_inf, const double* X, const double* Y, const double* P,
+                   const double* T, const double* VEL_X, const double* VEL_Y, const double* dNx,
+                   const double* dNy, double* F_VX, double* F_VY, double* skin);
+
+/* One NEWMARK_METHOD step (meshMove.f90:196-310) on dis, vel, acc (2 each) under load F. */
+void or_newmark_step(double H, const double* F, double* dis, double* vel, double* acc);
+
 /* Whole-driver restatement (ns2DComp.ALE.f90:8-282) over a cfd_mesh/cfd_params. */
 typedef struct or_case or_case;
 or_case* or_case_create(const cfd_mesh* mesh, const cfd_params* p, int do_smoothing);
@@ -90,6 +99,11 @@ void or_case_get(or_case* c, double* U, double* T, double* X, double* Y);
 void or_case_get_fields(or_case* c, double* RHO, double* VEL_X, double* VEL_Y, double* E,
                         double* P, double* RMACH, double* W_X, double* W_Y);
 void or_case_get_motion(or_case* c, double* xpos, double* ypos);
+/* FORCE_VISC: each_step = 1 computes it in every step at the print block's point (after
+ * the move, before deriv) and or_case_force_visc returns the last step's values; 0 makes
+ * or_case_force_visc compute it on the current state and mesh.  skin: 3 per set edge. */
+void or_case_set_force_visc(or_case* c, int each_step);
+void or_case_force_visc(or_case* c, double* F_VX, double* F_VY, double* skin);
 void or_case_get_geometry(or_case* c, double* area, double* dNx, double* dNy, double* M);
 void or_case_set_state(or_case* c, const double* U, const double* T, const double* VEL_X,
                        const double* VEL_Y);

@@ -44,6 +44,12 @@ _SIG = {
                        C.POINTER(abi.CfdSolveInfo)]),
     "or_normales": (_i, [_i, _i, _ip, _dp, _dp, _ip, _dp, _dp]),
     "or_smoothing": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _dp]),
+    "or_newmark_step": (None, [C.c_double, _dp, _dp, _dp, _dp]),
+    "or_force_visc": (None, [_i, _i, _i, _ip, _ip, _ip, _i, C.c_double, C.c_double, C.c_double,
+                             C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                             _dp]),
+    "or_case_force_visc": (None, [_vp, _dp, _dp, _dp]),
+    "or_case_set_force_visc": (None, [_vp, _i]),
     "or_case_create": (_vp, [C.POINTER(abi.CfdMesh), C.POINTER(abi.CfdParams), _i]),
     "or_case_destroy": (None, [_vp]),
     "or_case_step": (_i, [_vp, _i, C.POINTER(abi.CfdStepReport)]),
@@ -231,6 +237,13 @@ def smoothing(x, y, inpoel, fixed):
     return x, y, it.value, q.value
 
 
+def newmark_step(H, F, dis, vel, acc):
+    """meshMove.f90 NEWMARK_METHOD(H) with load F; returns the new (dis, vel, acc)."""
+    d, v, a = f64(dis).copy(), f64(vel).copy(), f64(acc).copy()
+    lib().or_newmark_step(float(H), dp(f64(F)), dp(d), dp(v), dp(a))
+    return d, v, a
+
+
 # ------------------------------------------------------------------ whole driver
 class OracleCase:
     """PROGRAM NSComp2D (ns2DComp.ALE.f90:8-282) over a cfd_gb300.case.Case."""
@@ -276,6 +289,18 @@ class OracleCase:
         xp, yp = np.zeros(self.n), np.zeros(self.n)
         lib().or_case_get_motion(self.h, dp(xp), dp(yp))
         return xp, yp
+
+    def set_force_visc(self, each_step):
+        lib().or_case_set_force_visc(self.h, 1 if each_step else 0)
+
+    def force_visc(self):
+        """FORCE_VISC now: (F_VX[nset_numb], F_VY[nset_numb], skin rows (nedges, 3))."""
+        fvx, fvy = np.zeros(10), np.zeros(10)
+        ne = int(sum(self.case.iset_array()[1]))
+        skin = np.zeros((max(ne, 1), 3))
+        lib().or_case_force_visc(self.h, dp(fvx), dp(fvy), dp(skin))
+        n = self.case.iset_array()[2]
+        return fvx[:n], fvy[:n], skin[:ne]
 
     def geometry(self):
         a = np.zeros(self.ne)
