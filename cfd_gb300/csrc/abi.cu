@@ -276,6 +276,7 @@ int cfd_ctx_set_clock(cfd_ctx* ctx, int iter, double time, double dtmin1, int ba
     CFD_CUDA(cudaStreamSynchronize(c.stream));
     sc.dtmin1 = dtmin1;
     sc.bandera = bandera;
+    sc.iter = iter;
     CFD_CUDA(cudaMemcpyAsync(c.d_scal, &sc, sizeof(sc), cudaMemcpyHostToDevice, c.stream));
     if (c.d_motion) {  // the structural model's velocities and accelerations are kept
         MotionScal ms{};

@@ -89,6 +89,7 @@ struct Ctx {
     double* d_invdiag = nullptr;
     float *d_shocf = nullptr, *d_ts1f = nullptr, *d_ts2f = nullptr, *d_ts3f = nullptr;
     float* d_valf = nullptr;
+    float* d_dtef = nullptr;  // mixed form, ITLOCAL != 0: FP32 DT per element
     float* d_pf[2][2] = {};
     float* d_zf[2] = {};
     float* d_posf[2] = {};  // (float) of d_pos, kept by the mixed BiCG kernels

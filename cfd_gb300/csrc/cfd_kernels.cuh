@@ -16,11 +16,13 @@ struct StepScal {
     double dtmin1;                  // hysteresis memory (ns2DComp.ALE.f90:146-156)
     double cota;                    // 10*DTMIN of deltat
     int bandera;
-    int pad;
+    int iter;                       // mixed form: ITER, advanced on the device
     double fx[10], fy[10], rm[10];  // FORCES per set
     double inv_dtmin;               // 1/DTMIN (mixed form: W = XPOS*(1/DTMIN))
     float dtmin_f;                  // (float)DTMIN for the FP32 kernels
     float pad_f;
+    float dtfact_f, cota_f;         // mixed form, ITLOCAL != 0: DTFACT and COTA of DTL
+    float pad2_f[2];
 };
 
 // DTMIN from the minimum DTELEM (b: its bit pattern, +inf for none) with the 1% hysteresis
@@ -118,18 +120,18 @@ __global__ void k_deltat_estab(int nelem, const int4* elem, const float4* Uhi, c
                                float TINF, int estab_mode, float eps_dir, float dirx, float diry,
                                float fsafe, unsigned long long* dtmin_bits,
                                unsigned long long* block_min, float* SHOC, float* ES1,
-                               float* ES2, float* ES3);
+                               float* ES2, float* ES3, float* DTE);
 __global__ void k_deltat_refine(int nelem, const int4* elem, const float* T, const float* VX,
                                 const float* VY, const float2* W, const float* areaf,
                                 const unsigned long long* block_min, int nchunk, float fsafe,
-                                float t_inf, StepScal* sc, unsigned* count);
+                                float t_inf, StepScal* sc, unsigned* count, int itlocal);
 cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, const int4* elem,
                                      const float4* Uhi, const float4* Ulo, const float4* geo,
                                      const float* shoc, const StepScal* sc,
                                      const float* ts1, const float* ts2, const float* ts3,
                                      GasConstF gc, const float2* W, const int* slot_pos,
                                      const float* T, float4* recInv, float4* recVisc,
-                                     float2* mulam);
+                                     float2* mulam, const float* dte);
 __global__ void k_elem_mulam(int nelem, const int4* elem, const float* T, GasConstF gc,
                              float2* mulam);
 cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, const int* esup_slot,

@@ -610,10 +610,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     for (double* q : {d_WX, d_WY, d_Wxo, d_Wyo, d_RHO, d_E, d_P, d_RMACH})
         CFD_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * N, stream));
     if (prec == CFD_PREC_MIXED) {
-        if (prm.itlocal != 0) {
-            set_last_message("the mixed-precision form runs with a global time step (ITLOCAL = 0)");
-            return CFD_ERR_ARG;
-        }
+        if (prm.itlocal != 0 && (st = dalloc(&d_dtef, E))) return st;  // DT per element
         if ((st = dalloc(&d_invdiag, N))) return st;
         for (float** q : {&d_Tf, &d_VXf, &d_VYf, &d_RHOf, &d_Ef, &d_Pf, &d_RMACHf,
                           &d_invMf})
@@ -732,12 +729,12 @@ int Ctx::enqueue_mixed(bool learned) {
                (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VXf, d_VYf, d_Wf,
                (const float4*)d_geo8, (float)prm.fr, (float)prm.rho_inf, (float)prm.t_inf,
                prm.estab_mode, (float)estab_eps, (float)dir[0], (float)dir[1], (float)prm.fsafe,
-               &d_scal->dtmin32_bits, d_blockmin, d_shocf, d_ts1f, d_ts2f, d_ts3f);
+               &d_scal->dtmin32_bits, d_blockmin, d_shocf, d_ts1f, d_ts2f, d_ts3f, d_dtef);
     {
         const int nchunk = (int)blocks_for(E, TB);
         CFD_LAUNCH(k_deltat_refine, blocks_for(nchunk, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf,
                    d_VYf, d_Wf, d_areaf, (const unsigned long long*)d_blockmin, nchunk,
-                   (float)prm.fsafe, (float)prm.t_inf, d_scal, d_tcount);
+                   (float)prm.fsafe, (float)prm.t_inf, d_scal, d_tcount, prm.itlocal);
     }
     tstop(TM_DELTAT);
     GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte, prm.fr};
@@ -746,7 +743,7 @@ int Ctx::enqueue_mixed(bool learned) {
     tstart(TM_CALCRHS);
     CFD_CUDA(launch_elem_stage1_mixed(viscous, stream, E, d_elem, d_Uhi, d_Ulo, d_geo8, d_shocf,
                                       d_scal, d_ts1f, d_ts2f, d_ts3f, gf, d_Wf, d_slot_pos, d_Tf,
-                                      d_recInv, d_recVisc, d_mulam));
+                                      d_recInv, d_recVisc, d_mulam, (const float*)d_dtef));
     tstop(TM_CALCRHS);
     // stage s uses mu, lambda from the T of stage s-1 (the reference's module T): stage 1's
     // come from the element kernel above, the others from k_elem_mulam before the node pass.

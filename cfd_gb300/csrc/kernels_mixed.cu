@@ -150,7 +150,7 @@ __global__ void k_deltat_refine(int nelem, const int4* __restrict__ elem, const 
                                 const float2* __restrict__ W, const float* __restrict__ areaf,
                                 const unsigned long long* __restrict__ block_min, int nchunk,
                                 float fsafe, float t_inf, StepScal* __restrict__ sc,
-                                unsigned* __restrict__ count) {
+                                unsigned* __restrict__ count, int itlocal) {
     // thread t tests chunk blockIdx.x*256 + t; the block then refines the listed chunks
     __shared__ int list[256];
     __shared__ int nlist;
@@ -176,6 +176,11 @@ __global__ void k_deltat_refine(int nelem, const int4* __restrict__ elem, const 
         __threadfence();
         *count = 0u;
         dt_finalize_from(sc, atomicExch(&sc->dtmin_bits, 0x7ff0000000000000ull));
+        sc->iter += 1;
+        if (itlocal) {  // DTFACT of ns2DComp.ALE.f90:160 for this ITER; COTA = 10*DTMIN raw
+            sc->dtfact_f = (float)(1.0 - exp(-(sc->iter * 4.6 / itlocal)));
+            sc->cota_f = (float)sc->cota;
+        }
     }
 }
 
@@ -271,7 +276,8 @@ k_deltat_estab(int nelem, const int4* __restrict__ elem, const float4* __restric
                float RHOINF, float TINF, int estab_mode, float eps_dir, float dirx, float diry,
                float fsafe, unsigned long long* __restrict__ dtmin_bits,
                unsigned long long* __restrict__ block_min, float* __restrict__ SHOC,
-               float* __restrict__ ES1, float* __restrict__ ES2, float* __restrict__ ES3) {
+               float* __restrict__ ES1, float* __restrict__ ES2, float* __restrict__ ES3,
+               float* __restrict__ DTE) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long mybits = 0x7ff0000000000000ull;
     if (e < nelem) {
@@ -296,8 +302,10 @@ k_deltat_estab(int nelem, const int4* __restrict__ elem, const float4* __restric
             const float et = 0.017f * pow15f(fdiv(T_iel, TINF)) * fdiv(TINF + 110.f, T_iel + 110.f);
             const float alpha = fminf(fdiv(vel * hh, 2.f * et) * (1.f / 3.f), 1.f);
             const float a = fdiv(4.f * et, hh * hh);
-            const double d = f2d_bits(fdiv(fsafe, a + (a + fdiv(alpha * vel, hh))));
+            const float d32 = fdiv(fsafe, a + (a + fdiv(alpha * vel, hh)));
+            const double d = f2d_bits(d32);
             if (d < 1.0e20 && d > 0.0) mybits = (unsigned long long)__double_as_longlong(d);
+            if (DTE) DTE[e] = d32;  // DT of the element, for ITLOCAL's DTL
         }
         const float vx = ((vx1 + vx2 + vx3) - (w1.x + w2.x + w3.x)) * (1.f / 3.f);
         const float vy = ((vy1 + vy2 + vy3) - (w1.y + w2.y + w3.y)) * (1.f / 3.f);
@@ -358,7 +366,8 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
                     const float* __restrict__ ts2, const float* __restrict__ ts3, GasConstF gc,
                     const float2* __restrict__ W, const int* __restrict__ slot_pos,
                     const float* __restrict__ T, float4* __restrict__ recInv,
-                    float4* __restrict__ recVisc, float2* __restrict__ mulam) {
+                    float4* __restrict__ recVisc, float2* __restrict__ mulam,
+                    const float* __restrict__ dte) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nelem) return;
     const float g = gc.gamma, Cv = gc.cv;
@@ -394,7 +403,14 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
         tau[2] = (v3 >= 0.f) ? rsqrtf(resumen + v3) : 0.f;
     }
     const float nu = shoc[e] * gc.cte;
-    const float scale = gb.z * sc->dtmin_f * (1.f / 3.f);
+    // area*dtl/3 with dtl = DTMIN, or under ITLOCAL DTL = DTMIN*DTFACT + min(DT, COTA)*(1-DTFACT)
+    // (ns2DComp.ALE.f90:159-162, subrutinas.f90:211-215)
+    float dtl = sc->dtmin_f;
+    if (dte) {
+        const float f = sc->dtfact_f;
+        dtl = sc->dtmin_f * f + fminf(dte[e], sc->cota_f) * (1.f - f);
+    }
+    const float scale = gb.z * dtl * (1.f / 3.f);
     // Over the three edge-midpoint quadrature points k, only A (the Galerkin flux
     // divergence, to the two nodes other than k), B1, B2 and the viscous coefficients
     // depend on k; the test-function gradients and tau do not.  So the k-loop sums A per
@@ -974,16 +990,16 @@ cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, c
                                      const float* ts1, const float* ts2, const float* ts3,
                                      GasConstF gc, const float2* W, const int* slot_pos,
                                      const float* T, float4* recInv, float4* recVisc,
-                                     float2* mulam) {
+                                     float2* mulam, const float* dte) {
     const unsigned grid = blocks_for(nelem, 128);
     if (viscous)
         k_elem_stage1_mixed<true><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, shoc, sc, ts1,
                                                          ts2, ts3, gc, W, slot_pos, T, recInv,
-                                                         recVisc, mulam);
+                                                         recVisc, mulam, dte);
     else
         k_elem_stage1_mixed<false><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, shoc, sc, ts1,
                                                           ts2, ts3, gc, W, slot_pos, T, recInv,
-                                                          recVisc, mulam);
+                                                          recVisc, mulam, dte);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }

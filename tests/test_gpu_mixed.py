@@ -125,3 +125,14 @@ def test_graph_replay_matches_launches(gpu_lib, monkeypatch):
     assert on == 1 and replays == 5 and kernels > 10
     a.close()
     b.close()
+
+
+def test_mixed_local_time_step(gpu_lib):
+    """ITLOCAL != 0 (ns2DComp.ALE.f90:159-162): the element time step DTL enters calcRHS and
+    FUENTE through area*dtl/3; the mixed form forms it from its FP32 DT per element."""
+    k = small_case(1, scale=16, seed=21, estab_mode=2, itlocal=5)
+    k.params.fsafe = min(k.params.fsafe, 0.25)
+    worst, fworst = run_mixed_vs_oracle(k, 8)
+    print("worst rel L2 per variable", worst, "force", fworst)
+    assert max(worst) <= REL_TOL_STATE
+    assert fworst <= REL_TOL_FORCE
