@@ -28,6 +28,7 @@ UNITS = [
     ("noalloc.cu", ["--fmad=false"]),
     ("kernels_mpnn.cu", []),
     ("mpnn.cu", []),
+    ("smooth.cu", ["--fmad=false"]),
     ("host_prep.cpp", []),
 ]
 

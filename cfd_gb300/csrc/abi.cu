@@ -337,6 +337,11 @@ int cfd_ctx_force_visc(cfd_ctx* ctx, double* F_VX, double* F_VY, double* skin) {
     return CFD_OK;
 }
 
+int cfd_ctx_smooth(cfd_ctx* ctx, int* iters, double* min_quality) {
+    if (!ctx) return arg_error("ctx");
+    return ctx->impl.smooth(iters, min_quality);
+}
+
 int cfd_ctx_graph_state(cfd_ctx* ctx, long long* out3) {
     if (!ctx || !out3) return arg_error("null pointer");
     const Ctx& c = ctx->impl;
@@ -694,6 +699,58 @@ int cfd_force_visc(const int* NELEM, const int* npoin, const int* nsets, const i
         F_VY[k] = fv[10 + k];
     }
     return CFD_OK;
+}
+
+int cfd_smoothing(double* X, double* Y, const int* inpoel, const int* fixed, const int* npoin,
+                  const int* nelem, const double* dX, const double* dY, int* iters,
+                  double* min_quality) {
+    if (!X || !Y || !inpoel || !fixed || bad_sizes(nelem, npoin) || (!dX != !dY))
+        return arg_error("cfd_smoothing");
+    const int E = *nelem, N = *npoin;
+    std::vector<int4> el;
+    TRY(make_elems(inpoel, E, N, el));
+    Adjacency adj;
+    std::string why;
+    if (int st = build_adjacency(N, E, inpoel, adj, &why)) {
+        set_last_message(why);
+        return st;
+    }
+    std::vector<int> order, offs;
+    smoothing_colours(adj, N, order, offs);
+    std::vector<unsigned char> fx(N);
+    for (int p = 0; p < N; ++p) fx[p] = fixed[p] ? 1 : 0;
+    std::vector<double> tol;
+    if (dX) {  // setTol_move (smoothing.f90:372-386)
+        tol.resize(N);
+        for (int p = 0; p < N; ++p) tol[p] = std::fabs(dX[p]) + std::fabs(dY[p]);
+    }
+    int max_star = 0;
+    for (int p = 0; p < N; ++p) max_star = std::max(max_star, adj.esup_ptr[p + 1] - adj.esup_ptr[p]);
+    Scratch s;
+    TRY(s.init());
+    int4* d_el;
+    int *d_ep, *d_es, *d_pp, *d_ps, *d_ord, *d_flags;
+    unsigned char *d_fx, *d_sm;
+    double *d_X, *d_Y, *d_tol = nullptr;
+    unsigned long long* d_scal;
+    TRY(s.put(&d_el, el.data(), E));
+    TRY(s.put(&d_ep, adj.esup_ptr.data(), adj.esup_ptr.size()));
+    TRY(s.put(&d_es, adj.esup_slot.data(), adj.esup_slot.size()));
+    TRY(s.put(&d_pp, adj.psup_ptr.data(), adj.psup_ptr.size()));
+    TRY(s.put(&d_ps, adj.psup.data(), adj.psup.size()));
+    TRY(s.put(&d_ord, order.data(), order.size()));
+    TRY(s.put(&d_fx, fx.data(), fx.size()));
+    TRY(s.put(&d_X, X, N));
+    TRY(s.put(&d_Y, Y, N));
+    if (dX) TRY(s.put(&d_tol, tol.data(), tol.size()));
+    TRY(s.alloc(&d_sm, N));
+    TRY(s.alloc(&d_scal, 3));
+    TRY(s.alloc(&d_flags, 2));
+    TRY(smooth_on_device(s.stream, N, E, d_el, d_ep, d_es, d_pp, d_ps, d_fx, d_X, d_Y, d_tol,
+                         offs, d_ord, d_sm, d_scal, d_flags, iters, min_quality, max_star));
+    TRY(s.get(X, d_X, N));
+    TRY(s.get(Y, d_Y, N));
+    return s.sync();
 }
 
 int cfd_deriv(const double* X, const double* Y, const int* inpoel, const int* nelem,

@@ -22,6 +22,16 @@ int guess_on_stream(cfd_mpnn* net, cfd_mpnn_graph* g, cudaStream_t st, const dou
 void graph_free(cfd_mpnn_graph* g);
 }  // namespace mpnn
 
+// mesh smoothing (smooth.cu)
+void smoothing_colours(const Adjacency& adj, int npoin, std::vector<int>& order,
+                       std::vector<int>& offs);
+int smooth_on_device(cudaStream_t st, int npoin, int nelem, const int4* elem,
+                     const int* esup_ptr, const int* esup_slot, const int* psup_ptr,
+                     const int* psup, const unsigned char* fixed, double* X, double* Y,
+                     const double* tol_move, const std::vector<int>& offs, const int* order,
+                     unsigned char* smoothable, unsigned long long* scal, int* flags,
+                     int* iters_out, double* min_quality_out, int max_star);
+
 enum { TM_DELTAT, TM_ESTAB, TM_CALCRHS, TM_FUENTE, TM_UPDATE, TM_FORCES, TM_TRANSF, TM_GRAD,
        TM_NORMALES, TM_DERIV, TM_MASAS, TM_LAPLACE, TM_N };
 
@@ -64,6 +74,11 @@ struct Ctx {
     // FORCE_VISC: [F_VX(10), F_VY(10)], per-edge terms (scratch) and SKIN.DAT rows
     double *d_fv = nullptr, *d_fv_terms = nullptr, *d_fv_skin = nullptr;
     bool fv_each = false;
+    // mesh smoothing: point neighbours, fixed nodes, colour order, scratch
+    int *d_psup_ptr = nullptr, *d_psup = nullptr, *d_sm_order = nullptr, *d_sm_flags = nullptr;
+    unsigned char *d_sm_fixed = nullptr, *d_sm_flag = nullptr;
+    unsigned long long* d_sm_scal = nullptr;
+    std::vector<int> sm_offs;
     double *d_xref = nullptr, *d_yref = nullptr;
     int *d_fix_node = nullptr, *d_fix_set = nullptr, *d_ufix_node = nullptr, *d_ufix_src = nullptr;
     unsigned char* d_isfix = nullptr;
@@ -161,6 +176,7 @@ struct Ctx {
     int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);
     int force_visc_now();
+    int smooth(int* iters, double* min_quality);
     int set_force_visc_each_step(bool on);
     int step_once();
     int step_once_mixed();

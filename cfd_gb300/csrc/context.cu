@@ -274,6 +274,43 @@ int Ctx::force_visc_now() {
     return CFD_OK;
 }
 
+// The setup smoothing of the resident mesh (ns2DComp.ALE.f90:62-72: the moving and the
+// fixed mesh-motion nodes stay), then the mesh's geometry again (normales, deriv, masses,
+// Laplacian) as at setup
+int Ctx::smooth(int* iters, double* min_quality) {
+    const int N = npoin;
+    int st;
+    if (!d_psup_ptr) {
+        if ((st = upload(&d_psup_ptr, adj.psup_ptr.data(), adj.psup_ptr.size()))) return st;
+        if ((st = upload(&d_psup, adj.psup.data(), adj.psup.size()))) return st;
+        std::vector<int> order;
+        smoothing_colours(adj, N, order, sm_offs);
+        if ((st = upload(&d_sm_order, order.data(), order.size()))) return st;
+        std::vector<unsigned char> fx(N, 0);
+        for (int p : bc.fix_node) fx[p] = 1;
+        if ((st = upload(&d_sm_fixed, fx.data(), fx.size()))) return st;
+        if ((st = dalloc(&d_sm_flag, N))) return st;
+        if ((st = dalloc(&d_sm_scal, 3))) return st;
+        if ((st = dalloc(&d_sm_flags, 2))) return st;
+    }
+    int max_star = 0;
+    for (int p = 0; p < N; ++p) max_star = std::max(max_star, adj.esup_ptr[p + 1] - adj.esup_ptr[p]);
+    st = smooth_on_device(stream, N, nelem, d_elem, d_esup_ptr, d_esup_slot, d_psup_ptr, d_psup,
+                          d_sm_fixed, d_X, d_Y, nullptr, sm_offs, d_sm_order, d_sm_flag, d_sm_scal,
+                          d_sm_flags, iters, min_quality, max_star);
+    if (st) return st;
+    if (prec == CFD_PREC_MIXED) {
+        if ((st = narrow_mixed(false, false, false, false, true, false))) return st;
+        if ((st = geometry_mixed(true, true))) return st;
+    } else {
+        if ((st = geometry(true, true))) return st;
+        CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * nelem,
+                                 cudaMemcpyDeviceToDevice, stream));
+    }
+    CFD_CUDA(cudaStreamSynchronize(stream));
+    return tcollect();
+}
+
 // Every step computes FORCE_VISC at the reference's print-block point (on), or only
 // cfd_ctx_force_visc computes it, on the state and mesh of the call (off).  The captured
 // step is captured again.

@@ -169,6 +169,13 @@ int cfd_deltat(const double* T, const double* VEL_X, const double* VEL_Y,
                const int* inpoel, const int* nelem, const int* npoin,
                const double* scal4, double* DT, double* DTMIN);
 
+/* smoothing (smoothing.f90:21-72), drop-in: X, Y in/out; fixed: per node, nonzero = does
+ * not move (the reference's logical array); dX, dY: both NULL, or the step's displacement
+ * for the setTol_move path (:372-386).  GPU colour-by-colour order (cfd_ctx_smooth). */
+int cfd_smoothing(double* X, double* Y, const int* inpoel, const int* fixed, const int* npoin,
+                  const int* nelem, const double* dX, const double* dY, int* iters,
+                  double* min_quality);
+
 /* FORCE_VISC (ns2DComp.ALE.f90:819-893), drop-in: the reference's argument list (RMU and
  * RHO are unused by its body), F_VX/F_VY 10 each; skin: NULL, or 3 doubles per set edge
  * (the SKIN.DAT rows the reference writes instead). */
@@ -376,6 +383,16 @@ int cfd_ctx_force_visc(cfd_ctx* ctx, double* F_VX, double* F_VY, double* skin);
  * graph off.  No counterpart in the reference (its time loop calls the routines of
  * ns2DComp.ALE.f90:114-283 one by one). */
 int cfd_ctx_graph_state(cfd_ctx* ctx, long long* out3);
+
+/* Smooth the context's mesh as the reference does at setup (ns2DComp.ALE.f90:62-72,
+ * smoothing.f90; the mesh-motion boundary nodes stay), then recompute its geometry (normals,
+ * dNx/dNy/area, lumped mass, Laplacian).  The GPU colours the nodes so that no two nodes
+ * of a colour share an element and moves one colour at a time (the reference moves one
+ * node at a time, in node order), so the result is a nearby smoothed mesh, not the
+ * reference's.  iters: the sweeps run (NITER + 1 when they did not settle, 0 when no
+ * element is below the quality threshold 0.85); min_quality: the worst element's mu
+ * afterwards.  Either may be NULL. */
+int cfd_ctx_smooth(cfd_ctx* ctx, int* iters, double* min_quality);
 
 /* Number of kernels this library launched since process start (all contexts). */
 long long cfd_kernel_launches(void);
