@@ -167,16 +167,6 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done) {
         // learned guess (decided by the caller): the judge keeps, per solve, the network's
         // guess or the previous step's, whichever has the smaller r.z
         a.gflag = learned ? d_gflag : nullptr;
-        if (fix_done && nsolve == 2) {  // the step's mesh update rides on the last pass
-            a.mX = d_X;
-            a.mY = d_Y;
-            a.mWX = d_WX;
-            a.mWY = d_WY;
-            a.mXhi = d_Xhi;
-            a.mXlo = d_Xlo;
-            a.mWf = d_Wf;
-            a.msc = d_scal;
-        }
         a.gate = 0.0;
         a.only_if = nullptr;
         if (nufix > 0 && !fix_done)
@@ -745,14 +735,16 @@ int Ctx::widen_mixed() {
 int Ctx::geometry_mixed(bool setup, bool put_area) {
     const int N = npoin, E = nelem;
     const int TB = 256;
+    tstart(TM_NORMALES);
+    if (nwn > 0)
+        CFD_LAUNCH(k_normales, blocks_for(nwn, TB), TB, 0, stream, nwn, d_wnode, d_wptr, d_wedge,
+                   d_walls, d_X, d_Y, d_bcflag, d_nrm);
+    tstop(TM_NORMALES);
     const bool gcl = !setup && prm.mass_mode != CFD_MASS_MASAS;
-    // normales rides on the element pass (its own blocks after the elements')
     tstart(TM_DERIV);
-    const NormalsArgs nv{nwn, d_wnode, d_wptr, d_wedge, d_walls, d_X, d_Y, d_bcflag, d_nrm};
-    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB) + (nwn > 0 ? blocks_for(nwn, TB) : 0), TB, 0,
-               stream, E, d_elem, d_Xhi, d_Xlo, gcl ? 1 : 0,
-               prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_Wf, d_Wof,
-               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, d_geo8, d_gterms, nv);
+    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Xhi, d_Xlo,
+               gcl ? 1 : 0, prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_Wf, d_Wof,
+               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, d_geo8, d_gterms);
     tstop(TM_DERIV);
     tstart(TM_LAPLACE);
     CFD_LAUNCH(k_node_geometry, blocks_for(N, kGeoNodeBlock), kGeoNodeBlock, 0, stream, N,
@@ -849,10 +841,11 @@ int Ctx::enqueue_mixed(bool learned) {
     }
     tstop(TM_FORCES);
     tstart(TM_GRAD);
-    // the BiCG kernel's last pass also moves the mesh (X += XPOS, W = XPOS/DTMIN)
     int st = run_pcg(2, learned, true);
     if (st) return st;
     tstop(TM_GRAD);
+    CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1],
+               d_scal, d_X, d_Y, d_WX, d_WY, d_Xhi, d_Xlo, d_Wf);
     if (fv_each) {  // FORCE_VISC at the print block's point: moved mesh, previous dNx
         st = force_visc_now();
         if (st) return st;

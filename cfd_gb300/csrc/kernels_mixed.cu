@@ -675,15 +675,7 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
                                 int gcl, int literal, const float2* __restrict__ W,
                                 const float2* __restrict__ Wold, int put_area,
                                 float* __restrict__ area_old, float* __restrict__ areaf,
-                                float4* __restrict__ geo, float2* __restrict__ terms,
-                                NormalsArgs nv) {
-    // the blocks after the elements' do normales (one wall node per thread)
-    const int eblocks = (nelem + blockDim.x - 1) / blockDim.x;
-    if ((int)blockIdx.x >= eblocks) {
-        const int k = ((int)blockIdx.x - eblocks) * blockDim.x + threadIdx.x;
-        if (k < nv.nwn) normales_node(nv, k);
-        return;
-    }
+                                float4* __restrict__ geo, float2* __restrict__ terms) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nelem) return;
     const int4 n = elem[e];
@@ -750,49 +742,28 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     Acc m1, m2;
     m1.init();
     m2.init();
-    // four slots per pass: their loads are issued together (the element records are
-    // gathers), the sums stay in slot order
-    const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
-    for (int sb = s0; sb < s1; sb += 4) {
-        int slot[4];
-        uchar4 pos[4];
-        float4 ga[4], gb[4];
-        float2 tm[4];
+    for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) {
+        const int slot = esup_slot[s];
+        const int e = slot / 3, i = slot - 3 * e;
+        const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
+        const uchar4 pos = lap_pos[s];
+        if (gcl) {
+            const float2 t = terms[e];
+            m1.add(t.x);
+            m2.add(t.y);
+        } else {
+            m1.add(gb.z);
+        }
+        const float gx[3] = {ga.x, ga.y, ga.z}, gy[3] = {ga.w, gb.x, gb.y};
+        const float q = gb.w;
+        const float dxi = (i == 0) ? gx[0] : (i == 1 ? gx[1] : gx[2]);
+        const float dyi = (i == 0) ? gy[0] : (i == 1 ? gy[1] : gy[2]);
+        const unsigned char pj[3] = {pos.x, pos.y, pos.z};
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (sb + u < s1) {
-                slot[u] = esup_slot[sb + u];
-                pos[u] = lap_pos[sb + u];
-            }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (sb + u < s1) {
-                const int e = slot[u] / 3;
-                ga[u] = geo[2 * (size_t)e];
-                gb[u] = geo[2 * (size_t)e + 1];
-                if (gcl) tm[u] = terms[e];
-            }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (sb + u >= s1) break;
-            const int i = slot[u] - 3 * (slot[u] / 3);
-            if (gcl) {
-                m1.add(tm[u].x);
-                m2.add(tm[u].y);
-            } else {
-                m1.add(gb[u].z);
-            }
-            const float gx[3] = {ga[u].x, ga[u].y, ga[u].z}, gy[3] = {ga[u].w, gb[u].x, gb[u].y};
-            const float q = gb[u].w;
-            const float dxi = (i == 0) ? gx[0] : (i == 1 ? gx[1] : gx[2]);
-            const float dyi = (i == 0) ? gy[0] : (i == 1 ? gy[1] : gy[2]);
-            const unsigned char pj[3] = {pos[u].x, pos[u].y, pos[u].z};
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const float v = (dxi * gx[j] + dyi * gy[j]) * q;
-                if (in_smem) acc[pj[j]] += v;
-                else valf[r0 + pj[j]] += v;  // long rows (rare)
-            }
+        for (int j = 0; j < 3; ++j) {
+            const float v = (dxi * gx[j] + dyi * gy[j]) * q;
+            if (in_smem) acc[pj[j]] += v;
+            else valf[r0 + pj[j]] += v;  // long rows (rare)
         }
     }
     float diag;
@@ -830,6 +801,32 @@ __global__ void k_widen_geo(int nelem, const float4* __restrict__ geo, double* _
     dN[4 * E + e] = gb.x;
     dN[5 * E + e] = gb.y;
     area[e] = gb.z;
+}
+
+// meshMove.f90:99-126: X += XPOS, W = XPOS/DTMIN (as XPOS*(1/DTMIN), the reciprocal formed
+// once by k_dt_finalize), with the float shadows of (X, Y) and W
+__global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos,
+                                      const double* __restrict__ ypos, const StepScal* __restrict__ sc,
+                                      double* __restrict__ X, double* __restrict__ Y,
+                                      double* __restrict__ WX, double* __restrict__ WY,
+                                      float2* __restrict__ Xhi, float2* __restrict__ Xlo,
+                                      float2* __restrict__ Wf) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npoin) return;
+    const double idt = sc->inv_dtmin;
+    const double xp = xpos[p], yp = ypos[p];
+    const double x = X[p] + xp, y = Y[p] + yp;
+    X[p] = x;
+    Y[p] = y;
+    const double wx = xp * idt, wy = yp * idt;
+    WX[p] = wx;
+    WY[p] = wy;
+    Wf[p] = make_float2(d2f_trunc(wx), d2f_trunc(wy));
+    float hx, lx, hy, ly;
+    split(x, hx, lx);
+    split(y, hy, ly);
+    Xhi[p] = make_float2(hx, hy);
+    Xlo[p] = make_float2(lx, ly);
 }
 
 // ------------------------------------------------------------------ end of the flow part

@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
                 pend[s] = true;
             }
         }
-    if (done[0] && done[1] && !a.mX) return;
+    if (done[0] && done[1]) return;
 
     int k = 0;
     int last_iter[2] = {0, 0};
@@ -437,42 +437,20 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
             last_iter[s] = k;
         }
     }
-    // last deferred x update; the shadow follows x for the solves that iterated; with
-    // the mesh update fused (a.mX), X += XPOS, Y += YPOS, W = (XPOS, YPOS)/DTMIN and the float
-    // shadows: meshMove.f90:99-126 with W = XPOS*(1/DTMIN), the reciprocal formed once
-    const double idt = a.mX ? a.msc->inv_dtmin : 0.0;
+    // last deferred x update; the shadow follows x for the solves that iterated
     for (long c = blockIdx.x; c < nc; c += gridDim.x)
         for (int kk = 0; kk < 4; ++kk) {
             const long i = c * kChunk + t + 256L * kk;
             if (i >= n) break;
-            double xs[2];
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
-                if (done[s]) {
-                    if (a.mX) xs[s] = a.x[s][i];
-                    continue;
-                }
+                if (done[s]) continue;
                 double xi = a.x[s][i];
                 if (pend[s]) {
                     xi += alfa[s] * a.p[s][cur[s]][i];
                     a.x[s][i] = xi;
                 }
                 a.xf[s][i] = d2f_trunc(xi);
-                xs[s] = xi;
-            }
-            if (a.mX) {
-                const double x = a.mX[i] + xs[0], y = a.mY[i] + xs[1];
-                a.mX[i] = x;
-                a.mY[i] = y;
-                const double wx = xs[0] * idt, wy = xs[1] * idt;
-                a.mWX[i] = wx;
-                a.mWY[i] = wy;
-                a.mWf[i] = make_float2(d2f_trunc(wx), d2f_trunc(wy));
-                float hx, lx, hy, ly;
-                split_bits(x, hx, lx);
-                split_bits(y, hy, ly);
-                a.mXhi[i] = make_float2(hx, hy);
-                a.mXlo[i] = make_float2(lx, ly);
             }
         }
     if (blockIdx.x == 0 && t == 0)
