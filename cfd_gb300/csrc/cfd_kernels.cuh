@@ -49,6 +49,40 @@ __device__ __forceinline__ void dt_finalize_from(StepScal* sc, unsigned long lon
     sc->dtmin_f = (float)dtmin;
 }
 
+// normales (subrutinas.f90:21-63) of wall node k: the wall edges touching it in edge order;
+// the nodes the reference's compaction keeps (den > 1d-6 and |l| > 0.2) get BC_NORMAL
+struct NormalsArgs {
+    int nwn;
+    const int *wnode, *wptr;
+    const int2 *wedge_of, *walls;
+    const double *X, *Y;
+    unsigned char* bcflag;
+    double2* nrm;
+};
+__device__ __forceinline__ void normales_node(const NormalsArgs& a, int k) {
+    const int p = a.wnode[k];
+    double nx = 0.0, ny = 0.0, den = 0.0;
+    for (int s = a.wptr[k]; s < a.wptr[k + 1]; ++s) {
+        const int2 w = a.walls[a.wedge_of[s].x];
+        const double lex = a.Y[w.y] - a.Y[w.x];
+        const double ley = -(a.X[w.y] - a.X[w.x]);
+        const double le = sqrt(lex * lex + ley * ley);
+        nx = nx + lex;
+        ny = ny + ley;
+        den = den + le;
+    }
+    unsigned char fl = a.bcflag[p] & (unsigned char)~BC_NORMAL;
+    if (den > 1.0e-6) {
+        const double lx = nx / den, ly = ny / den;
+        const double nrmv = sqrt(lx * lx + ly * ly);
+        if (nrmv > 0.2) {
+            a.nrm[p] = make_double2(lx / nrmv, ly / nrmv);
+            fl |= BC_NORMAL;
+        }
+    }
+    a.bcflag[p] = fl;
+}
+
 // calcRHS.f90:5 imports: Cv => FCV, lambda_ref => FK, mu_ref => FMU, gamma0 => GAMA, T_inf, CTE
 struct GasConst {
     double cv, lambda_ref, mu_ref, gamma, t_inf, cte;
@@ -145,7 +179,7 @@ cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, c
 __global__ void k_elem_geometry(int nelem, const int4* elem, const float2* Xhi, const float2* Xlo,
                                 int gcl, int literal, const float2* W, const float2* Wold,
                                 int put_area, float* area_old, float* areaf, float4* geo,
-                                float2* terms);
+                                float2* terms, NormalsArgs nv);
 constexpr int kGeoNodeBlock = 128;  // block size of k_node_geometry
 __global__ void k_node_geometry(int npoin, const int* esup_ptr, const int* esup_slot,
                                 const uchar4* lap_pos, const float4* geo, const float2* terms,

@@ -735,16 +735,14 @@ int Ctx::widen_mixed() {
 int Ctx::geometry_mixed(bool setup, bool put_area) {
     const int N = npoin, E = nelem;
     const int TB = 256;
-    tstart(TM_NORMALES);
-    if (nwn > 0)
-        CFD_LAUNCH(k_normales, blocks_for(nwn, TB), TB, 0, stream, nwn, d_wnode, d_wptr, d_wedge,
-                   d_walls, d_X, d_Y, d_bcflag, d_nrm);
-    tstop(TM_NORMALES);
     const bool gcl = !setup && prm.mass_mode != CFD_MASS_MASAS;
+    // normales rides on the element pass (its own blocks after the elements')
     tstart(TM_DERIV);
-    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Xhi, d_Xlo,
-               gcl ? 1 : 0, prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_Wf, d_Wof,
-               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, d_geo8, d_gterms);
+    const NormalsArgs nv{nwn, d_wnode, d_wptr, d_wedge, d_walls, d_X, d_Y, d_bcflag, d_nrm};
+    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB) + (nwn > 0 ? blocks_for(nwn, TB) : 0), TB, 0,
+               stream, E, d_elem, d_Xhi, d_Xlo, gcl ? 1 : 0,
+               prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_Wf, d_Wof,
+               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, d_geo8, d_gterms, nv);
     tstop(TM_DERIV);
     tstart(TM_LAPLACE);
     CFD_LAUNCH(k_node_geometry, blocks_for(N, kGeoNodeBlock), kGeoNodeBlock, 0, stream, N,

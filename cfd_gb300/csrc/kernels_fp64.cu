@@ -538,25 +538,7 @@ __global__ void k_normales(int nwn, const int* __restrict__ wnode, const int* __
                            unsigned char* __restrict__ bcflag, double2* __restrict__ nrm) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nwn) return;
-    const int p = wnode[k];
-    double nx = 0.0, ny = 0.0, den = 0.0;
-    for (int s = wptr[k]; s < wptr[k + 1]; ++s) {
-        int2 w = walls[wedge_of[s].x];
-        double lex = Y[w.y] - Y[w.x];
-        double ley = -(X[w.y] - X[w.x]);
-        double le = sqrt(lex * lex + ley * ley);
-        nx = nx + lex; ny = ny + ley; den = den + le;
-    }
-    unsigned char fl = bcflag[p] & (unsigned char)~BC_NORMAL;
-    if (den > 1.0e-6) {
-        double lx = nx / den, ly = ny / den;
-        double nrmv = sqrt(lx * lx + ly * ly);
-        if (nrmv > 0.2) {
-            nrm[p] = make_double2(lx / nrmv, ly / nrmv);
-            fl |= BC_NORMAL;
-        }
-    }
-    bcflag[p] = fl;
+    normales_node(NormalsArgs{nwn, wnode, wptr, wedge_of, walls, X, Y, bcflag, nrm}, k);
 }
 
 // ------------------------------------------------------------------ laplace values

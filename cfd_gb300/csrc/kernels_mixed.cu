@@ -675,7 +675,15 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
                                 int gcl, int literal, const float2* __restrict__ W,
                                 const float2* __restrict__ Wold, int put_area,
                                 float* __restrict__ area_old, float* __restrict__ areaf,
-                                float4* __restrict__ geo, float2* __restrict__ terms) {
+                                float4* __restrict__ geo, float2* __restrict__ terms,
+                                NormalsArgs nv) {
+    // the blocks after the elements' do normales (one wall node per thread)
+    const int eblocks = (nelem + blockDim.x - 1) / blockDim.x;
+    if ((int)blockIdx.x >= eblocks) {
+        const int k = ((int)blockIdx.x - eblocks) * blockDim.x + threadIdx.x;
+        if (k < nv.nwn) normales_node(nv, k);
+        return;
+    }
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nelem) return;
     const int4 n = elem[e];
