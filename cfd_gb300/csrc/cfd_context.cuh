@@ -44,6 +44,9 @@ struct Ctx {
     Adjacency adj;
     BcTables bc;
     cudaStream_t stream = nullptr;
+    // mixed form: the mesh-motion solve's stream, forked from and joined to `stream`
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_scal = nullptr;
     StepScal* h_scal = nullptr;  // pinned
     std::vector<void*> allocs;
@@ -171,7 +174,8 @@ struct Ctx {
     int geometry_mixed(bool setup, bool put_area = false);
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
     int widen_mixed();
-    int run_pcg(int nsolve, bool learned = false, bool fix_done = false);
+    int run_pcg(int nsolve, bool learned = false, bool fix_done = false,
+                cudaStream_t sv = nullptr);
     int enqueue_mixed(bool learned);
     int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);

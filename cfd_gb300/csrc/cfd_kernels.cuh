@@ -108,6 +108,7 @@ struct MotionScal {
     double veln0, veln1, accn0, accn1;  // CFD_MOTION_NEWMARK: VELN, ACCN
 };
 struct MotionTailArgs {
+    int do_motion, do_forces;  // the parts this launch runs (Newmark: both)
     int nset;  // FORCES
     const int* set_ptr;
     const int2* set_edges;

@@ -85,10 +85,13 @@ Ctx::~Ctx() {
     if (step_exec) cudaGraphExecDestroy(step_exec);
     if (step_graph) cudaGraphDestroy(step_graph);
     if (ev_iters) cudaEventDestroy(ev_iters);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     if (ev_scal) cudaEventDestroy(ev_scal);
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (auto& m : mark)
         if (m) cudaEventDestroy(m);
+    if (stream2) cudaStreamDestroy(stream2);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -120,7 +123,8 @@ int Ctx::geometry(bool masas, bool with_laplace) {
 }
 
 // ------------------------------------------------------------------ PCG launch
-int Ctx::run_pcg(int nsolve, bool learned, bool fix_done) {
+int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
+    const cudaStream_t stream = sv ? sv : this->stream;  // the solve's stream
     PcgArgs a{};
     a.n = npoin;
     a.nsolve = nsolve;
@@ -536,6 +540,9 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     CFD_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CFD_CUDA(cudaEventCreateWithFlags(&ev_scal, cudaEventDisableTiming));
     CFD_CUDA(cudaEventCreateWithFlags(&ev_iters, cudaEventDisableTiming));
+    CFD_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CFD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    CFD_CUDA(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
     CFD_CUDA(cudaMallocHost((void**)&h_scal, sizeof(StepScal)));
     // mesh
     std::vector<int4> el(E);
@@ -772,6 +779,66 @@ int Ctx::enqueue_mixed(bool learned) {
                    (float)prm.fsafe, (float)prm.t_inf, d_scal, d_tcount, prm.itlocal);
     }
     tstop(TM_DELTAT);
+    // The mesh-motion solve of a prescribed motion needs DTMIN and the current mesh only:
+    // it runs on its own stream, beside the RK stages (forked here, joined before the
+    // forces).  The Newmark model needs this step's forces, so its solve follows them.
+    const bool structural = prm.motion_law == CFD_MOTION_NEWMARK;
+    const bool fork = !timers_on && !structural;
+    MotionTailArgs t{};
+    t.nset = bc.nset_numb;
+    t.set_ptr = d_set_ptr;
+    t.set_edges = d_set_edges;
+    t.P = d_Pf;
+    t.X = d_X;
+    t.Y = d_Y;
+    t.xref = d_xref;
+    t.yref = d_yref;
+    t.law = prm.motion_law;
+    t.heave_amp = prm.heave_amp;
+    t.pitch_amp = prm.pitch_amp;
+    t.freq = prm.motion_freq;
+    t.m = d_motion;
+    t.nnmove = nnmove;
+    t.fix_node = d_fix_node;
+    t.fix_set = d_fix_set;
+    t.xfix_x = d_xfix[0];
+    t.xfix_y = d_xfix[1];
+    t.nufix = nufix;
+    t.ufix_node = d_ufix_node;
+    t.ufix_src = d_ufix_src;
+    t.x0 = d_pos[0];
+    t.x1 = d_pos[1];
+    t.xf0 = d_posf[0];
+    t.xf1 = d_posf[1];
+    t.part = d_tpart;
+    t.sc = d_scal;
+    // clock and motion law, TRANSF, the solves' Dirichlet values, and the two solves
+    auto motion_solve = [&](cudaStream_t s, bool with_forces) -> int {
+        if (prm.guess_mode == CFD_GUESS_ZERO)
+            for (int c = 0; c < 2; ++c) {
+                CFD_CUDA(cudaMemsetAsync(d_pos[c], 0, sizeof(double) * N, s));
+                CFD_CUDA(cudaMemsetAsync(d_posf[c], 0, sizeof(float) * N, s));
+            }
+        MotionTailArgs m = t;
+        m.do_motion = 1;
+        m.do_forces = with_forces ? 1 : 0;
+        m.count = d_tcount + 1;
+        tstart(TM_FORCES);
+        CFD_LAUNCH(k_motion_tail, (unsigned)tail_blocks, 256, 0, s, m);
+        tstop(TM_FORCES);
+        tstart(TM_GRAD);
+        int st = run_pcg(2, learned, true, s);
+        if (st) return st;
+        tstop(TM_GRAD);
+        return CFD_OK;
+    };
+    if (fork) {
+        CFD_CUDA(cudaEventRecord(ev_fork, stream));
+        CFD_CUDA(cudaStreamWaitEvent(stream2, ev_fork, 0));
+        int st = motion_solve(stream2, false);
+        if (st) return st;
+        CFD_CUDA(cudaEventRecord(ev_join, stream2));
+    }
     GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte, prm.fr};
     const GasConstF gf = to_float(gc);
     const bool viscous = prm.fmu > 2.2250738585072014e-308;
@@ -797,51 +864,20 @@ int Ctx::enqueue_mixed(bool learned) {
                                    d_RMACHf));
         tstop(TM_UPDATE);
     }
-    if (prm.guess_mode == CFD_GUESS_ZERO) {
-        for (int c = 0; c < 2; ++c) {
-            CFD_CUDA(cudaMemsetAsync(d_pos[c], 0, sizeof(double) * N, stream));
-            CFD_CUDA(cudaMemsetAsync(d_posf[c], 0, sizeof(float) * N, stream));
-        }
+    int st = CFD_OK;
+    if (fork) {
+        // FORCES on the step's pressure, after the solves joined
+        CFD_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+        MotionTailArgs f = t;
+        f.do_motion = 0;
+        f.do_forces = 1;
+        f.count = d_tcount + 2;
+        tstart(TM_FORCES);
+        CFD_LAUNCH(k_motion_tail, (unsigned)tail_blocks, 256, 0, stream, f);
+        tstop(TM_FORCES);
+    } else {
+        if ((st = motion_solve(stream, true))) return st;
     }
-    // FORCES, clock and motion law, TRANSF and the solves' Dirichlet values: one launch
-    tstart(TM_FORCES);
-    {
-        MotionTailArgs t{};
-        t.nset = bc.nset_numb;
-        t.set_ptr = d_set_ptr;
-        t.set_edges = d_set_edges;
-        t.P = d_Pf;
-        t.X = d_X;
-        t.Y = d_Y;
-        t.xref = d_xref;
-        t.yref = d_yref;
-        t.law = prm.motion_law;
-        t.heave_amp = prm.heave_amp;
-        t.pitch_amp = prm.pitch_amp;
-        t.freq = prm.motion_freq;
-        t.m = d_motion;
-        t.nnmove = nnmove;
-        t.fix_node = d_fix_node;
-        t.fix_set = d_fix_set;
-        t.xfix_x = d_xfix[0];
-        t.xfix_y = d_xfix[1];
-        t.nufix = nufix;
-        t.ufix_node = d_ufix_node;
-        t.ufix_src = d_ufix_src;
-        t.x0 = d_pos[0];
-        t.x1 = d_pos[1];
-        t.xf0 = d_posf[0];
-        t.xf1 = d_posf[1];
-        t.part = d_tpart;
-        t.count = d_tcount + 1;
-        t.sc = d_scal;
-        CFD_LAUNCH(k_motion_tail, (unsigned)tail_blocks, 256, 0, stream, t);
-    }
-    tstop(TM_FORCES);
-    tstart(TM_GRAD);
-    int st = run_pcg(2, learned, true);
-    if (st) return st;
-    tstop(TM_GRAD);
     CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1],
                d_scal, d_X, d_Y, d_WX, d_WY, d_Xhi, d_Xlo, d_Wf);
     if (fv_each) {  // FORCE_VISC at the print block's point: moved mesh, previous dNx

@@ -893,22 +893,23 @@ __device__ __forceinline__ double2 transf_one(const MotionTailArgs& a, const Mot
                         -(mv.sa * distx) + mv.ca * disty - disty + mv.yposr);
 }
 
-// One launch of a few blocks after the RK stages: FORCES (meshMove.f90:167-192; per-block
-// trees of the edge terms, folded in block order by the last block), the clock and the
-// motion law, TRANSF into x_fix, and the Dirichlet values of the two BiCG solves
-// (biconjGrad.f90:28: x(fix) = x_fix, in x and in its float shadow).  Every block forms
-// the motion from the step-start MotionScal; the last block stores the new one.
+// One launch of a few blocks for FORCES (meshMove.f90:167-192; per-block trees of the edge
+// terms, folded in block order by the last block) and/or the clock and the motion law,
+// TRANSF into x_fix, and the Dirichlet values of the two BiCG solves (biconjGrad.f90:28:
+// x(fix) = x_fix, in x and in its float shadow).  Every block forms the motion from the
+// step-start MotionScal; the last block stores the new one.  The Newmark law runs both
+// parts in one launch: its motion needs the forces.
 __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
     __shared__ MotionScal mv;
     __shared__ double red[9];
     __shared__ bool last;
-    if (threadIdx.x == 0) mv = motion_step(*a.m, a.sc->dtmin, a.law, a.heave_amp, a.pitch_amp,
-                                           a.freq);
+    if (a.do_motion && threadIdx.x == 0)
+        mv = motion_step(*a.m, a.sc->dtmin, a.law, a.heave_amp, a.pitch_amp, a.freq);
     __syncthreads();
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
     const bool structural = a.law == CFD_MOTION_NEWMARK;
-    if (!structural) tail_transf(a, mv, gt, gs);
-    for (int s = 0; s < a.nset; ++s) {
+    if (a.do_motion && !structural) tail_transf(a, mv, gt, gs);
+    for (int s = 0; a.do_forces && s < a.nset; ++s) {
         double fx = 0.0, fy = 0.0, rm = 0.0;
         const double xr = a.xref[s], yr = a.yref[s];
         for (int k = a.set_ptr[s] + gt; k < a.set_ptr[s + 1]; k += gs) {
@@ -935,13 +936,13 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if ((int)threadIdx.x < 3 * a.nset) {
+    if (a.do_forces && (int)threadIdx.x < 3 * a.nset) {
         double v = 0.0;
         for (unsigned b = 0; b < gridDim.x; ++b) v += __ldcg(a.part + threadIdx.x * gridDim.x + b);
         const int s = threadIdx.x / 3, q = threadIdx.x % 3;
         (q == 0 ? a.sc->fx : q == 1 ? a.sc->fy : a.sc->rm)[s] = v;
     }
-    if (structural) {  // the Newmark step under set 1's load, then TRANSF by this block
+    if (a.do_motion && structural) {  // the Newmark step under set 1's load, then TRANSF
         __syncthreads();
         if (threadIdx.x == 0) {
             NewmarkState ns;
@@ -969,7 +970,7 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
         tail_transf(a, mv, threadIdx.x, blockDim.x);
     }
     if (threadIdx.x == 0) {
-        *a.m = mv;
+        if (a.do_motion) *a.m = mv;
         *a.count = 0u;
     }
 }
