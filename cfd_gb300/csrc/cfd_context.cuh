@@ -137,8 +137,16 @@ struct Ctx {
     // mixed form: one step (the network not run) captured as a CUDA graph and replayed;
     // off with the timers or CFD_GRAPHS=0, or when the capture fails
     bool graphs_on = false, capturing = false;
-    cudaGraph_t step_graph = nullptr;
-    cudaGraphExec_t step_exec = nullptr;
+    cudaGraph_t step_graph[2] = {nullptr, nullptr};   // per buffer parity (below)
+    cudaGraphExec_t step_exec[2] = {nullptr, nullptr};
+    // mixed form: what the mesh-motion branch writes for the next step while the RK stages
+    // read the current values; swapped after every step (parity `buf`)
+    float4* d_geo8_n = nullptr;
+    float* d_invMf_n = nullptr;
+    double *d_WX_n = nullptr, *d_WY_n = nullptr;
+    float2* d_Wf_n = nullptr;
+    double4* d_fgeo = nullptr;  // per force-set edge: the step-start edge geometry
+    int buf = 0;
     long long graph_kernels = 0;  // kernels of one replay
     long long mixed_steps = 0;    // steps of this context (the first runs uncaptured)
     long long graph_replays = 0;
@@ -171,7 +179,10 @@ struct Ctx {
     ~Ctx();
     int create(const cfd_mesh* m, const cfd_params* p, int precision_mode);
     int geometry(bool masas, bool with_laplace);
-    int geometry_mixed(bool setup, bool put_area = false);
+    int geometry_mixed(bool setup, bool put_area = false, bool to_next = false,
+                       cudaStream_t sv = nullptr);
+    void swap_mixed_buffers();
+    void drop_graphs();
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
     int widen_mixed();
     int run_pcg(int nsolve, bool learned = false, bool fix_done = false,

@@ -82,8 +82,7 @@ Ctx::~Ctx() {
     for (void* p : allocs) cudaFree(p);
     if (h_scal) cudaFreeHost(h_scal);
     if (h_iters) cudaFreeHost(h_iters);
-    if (step_exec) cudaGraphExecDestroy(step_exec);
-    if (step_graph) cudaGraphDestroy(step_graph);
+    drop_graphs();
     if (ev_iters) cudaEventDestroy(ev_iters);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -247,8 +246,7 @@ int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
         CFD_CUDA(cudaMallocHost((void**)&h_iters, 2 * sizeof(int)));
         h_iters[0] = h_iters[1] = 0;
         // the captured step has no copy of the counts yet: capture it again
-        if (step_exec) { cudaGraphExecDestroy(step_exec); step_exec = nullptr; }
-        if (step_graph) { cudaGraphDestroy(step_graph); step_graph = nullptr; }
+        drop_graphs();
         CFD_CUDA(cudaMemsetAsync(d_gflag, 0, 2 * sizeof(int), stream));
         CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 4 * sizeof(long long), stream));
         CFD_CUDA(cudaStreamSynchronize(stream));
@@ -321,8 +319,7 @@ int Ctx::smooth(int* iters, double* min_quality) {
 int Ctx::set_force_visc_each_step(bool on) {
     if (on == fv_each) return CFD_OK;
     fv_each = on;
-    if (step_exec) { cudaGraphExecDestroy(step_exec); step_exec = nullptr; }
-    if (step_graph) { cudaGraphDestroy(step_graph); step_graph = nullptr; }
+    drop_graphs();
     if (on && !d_fv) return force_visc_now();  // buffers, and a defined first readout
     return CFD_OK;
 }
@@ -692,6 +689,12 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_recVisc, 3 * (size_t)E))) return st;
         if ((st = dalloc(&d_invSum, N))) return st;
         if ((st = dalloc(&d_motion, 1))) return st;
+        if ((st = dalloc(&d_geo8_n, 2 * (size_t)E))) return st;
+        if ((st = dalloc(&d_invMf_n, N))) return st;
+        if ((st = dalloc(&d_WX_n, N))) return st;
+        if ((st = dalloc(&d_WY_n, N))) return st;
+        if ((st = dalloc(&d_Wf_n, N))) return st;
+        if ((st = dalloc(&d_fgeo, std::max<size_t>(1, bc.set_elem.size())))) return st;
         if ((st = dalloc(&d_tcount, 4))) return st;
         {  // blocks of the motion tail: a block per 256 edges, moving nodes or fixed values
             int w = std::max(nnmove, nufix);
@@ -739,22 +742,32 @@ int Ctx::widen_mixed() {
 // Geometry of the current mesh for the mixed form: normales, then one element pass
 // (deriv, Laplacian weights, gcl element terms, putArea) and one node pass (Laplacian rows,
 // 1/diag, MASAS at setup or per step, or the gcl mass update and putW).
-int Ctx::geometry_mixed(bool setup, bool put_area) {
+int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv) {
+    const cudaStream_t stream = sv ? sv : this->stream;
     const int N = npoin, E = nelem;
     const int TB = 256;
     const bool gcl = !setup && prm.mass_mode != CFD_MASS_MASAS;
-    // normales rides on the element pass (its own blocks after the elements')
+    // to_next (the step's mesh-motion branch): the next step's geo8, 1/M, with W the next
+    // and W_old the current W (putW by the buffer swap); normales are left to the caller
+    // (the RK stages still read this step's).  Otherwise normales ride on the element pass
+    // (its own blocks after the elements').
+    float4* geo8 = to_next ? d_geo8_n : d_geo8;
+    float* invMf = to_next ? d_invMf_n : d_invMf;
+    const float2* Wn = to_next ? d_Wf_n : d_Wf;
+    const float2* Wo = to_next ? d_Wf : d_Wof;
     tstart(TM_DERIV);
-    const NormalsArgs nv{nwn, d_wnode, d_wptr, d_wedge, d_walls, d_X, d_Y, d_bcflag, d_nrm};
-    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB) + (nwn > 0 ? blocks_for(nwn, TB) : 0), TB, 0,
-               stream, E, d_elem, d_Xhi, d_Xlo, gcl ? 1 : 0,
-               prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_Wf, d_Wof,
-               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, d_geo8, d_gterms, nv);
+    const NormalsArgs nv{to_next ? 0 : nwn, d_wnode, d_wptr, d_wedge, d_walls, d_X, d_Y, d_bcflag,
+                         d_nrm};
+    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB) + (nv.nwn > 0 ? blocks_for(nv.nwn, TB) : 0), TB,
+               0, stream, E, d_elem, d_Xhi, d_Xlo, gcl ? 1 : 0,
+               prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, Wn, Wo,
+               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, geo8, d_gterms, nv);
     tstop(TM_DERIV);
     tstart(TM_LAPLACE);
     CFD_LAUNCH(k_node_geometry, blocks_for(N, kGeoNodeBlock), kGeoNodeBlock, 0, stream, N,
-               d_esup_ptr, d_esup_slot, d_lap_pos, d_geo8, d_gterms, &d_scal->dtmin, gcl ? 1 : 0,
-               d_rowptr, d_valf, d_invdiag, d_invdiagf, d_M, d_invMf, d_Wf, d_Wof);
+               d_esup_ptr, d_esup_slot, d_lap_pos, geo8, d_gterms, &d_scal->dtmin, gcl ? 1 : 0,
+               d_rowptr, d_valf, d_invdiag, d_invdiagf, d_M, invMf, Wn,
+               to_next ? (float2*)nullptr : d_Wof);
     tstop(TM_LAPLACE);
     return CFD_OK;
 }
@@ -779,9 +792,11 @@ int Ctx::enqueue_mixed(bool learned) {
                    (float)prm.fsafe, (float)prm.t_inf, d_scal, d_tcount, prm.itlocal);
     }
     tstop(TM_DELTAT);
-    // The mesh-motion solve of a prescribed motion needs DTMIN and the current mesh only:
-    // it runs on its own stream, beside the RK stages (forked here, joined before the
-    // forces).  The Newmark model needs this step's forces, so its solve follows them.
+    // The mesh motion of a prescribed law needs DTMIN and the step-start mesh only, and
+    // what it produces (the moved mesh, W, the new geometry) is the next step's: it runs
+    // on its own stream beside the RK stages, writing the next-step buffers (swapped after
+    // the step), and joins before FORCES.  The Newmark law needs this step's forces: its
+    // motion follows them on the main stream.
     const bool structural = prm.motion_law == CFD_MOTION_NEWMARK;
     const bool fork = !timers_on && !structural;
     MotionTailArgs t{};
@@ -812,8 +827,10 @@ int Ctx::enqueue_mixed(bool learned) {
     t.xf1 = d_posf[1];
     t.part = d_tpart;
     t.sc = d_scal;
-    // clock and motion law, TRANSF, the solves' Dirichlet values, and the two solves
-    auto motion_solve = [&](cudaStream_t s, bool with_forces) -> int {
+    t.fgeo = structural ? nullptr : d_fgeo;
+    // clock and motion law, TRANSF, the solves' Dirichlet values (and with the Newmark law
+    // FORCES first), the two solves, the mesh update and the next step's geometry
+    auto motion = [&](cudaStream_t s) -> int {
         if (prm.guess_mode == CFD_GUESS_ZERO)
             for (int c = 0; c < 2; ++c) {
                 CFD_CUDA(cudaMemsetAsync(d_pos[c], 0, sizeof(double) * N, s));
@@ -821,7 +838,7 @@ int Ctx::enqueue_mixed(bool learned) {
             }
         MotionTailArgs m = t;
         m.do_motion = 1;
-        m.do_forces = with_forces ? 1 : 0;
+        m.do_forces = structural ? 1 : 0;
         m.count = d_tcount + 1;
         tstart(TM_FORCES);
         CFD_LAUNCH(k_motion_tail, (unsigned)tail_blocks, 256, 0, s, m);
@@ -830,14 +847,20 @@ int Ctx::enqueue_mixed(bool learned) {
         int st = run_pcg(2, learned, true, s);
         if (st) return st;
         tstop(TM_GRAD);
+        CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, s, N, d_pos[0], d_pos[1],
+                   d_scal, d_X, d_Y, d_WX_n, d_WY_n, d_Xhi, d_Xlo, d_Wf_n);
+        if (prm.moving == 1 && (st = geometry_mixed(false, false, true, s))) return st;
         return CFD_OK;
     };
     if (fork) {
         CFD_CUDA(cudaEventRecord(ev_fork, stream));
         CFD_CUDA(cudaStreamWaitEvent(stream2, ev_fork, 0));
-        int st = motion_solve(stream2, false);
+        int st = motion(stream2);
         if (st) return st;
         CFD_CUDA(cudaEventRecord(ev_join, stream2));
+    } else if (!structural) {
+        int st = motion(stream);
+        if (st) return st;
     }
     GasConst gc{prm.fcv, prm.fk, prm.fmu, prm.gama, prm.t_inf, prm.cte, prm.fr};
     const GasConstF gf = to_float(gc);
@@ -865,9 +888,11 @@ int Ctx::enqueue_mixed(bool learned) {
         tstop(TM_UPDATE);
     }
     int st = CFD_OK;
-    if (fork) {
-        // FORCES on the step's pressure, after the solves joined
-        CFD_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+    if (structural) {
+        if ((st = motion(stream))) return st;
+    } else {
+        // FORCES on the step's pressure and the step-start edge geometry
+        if (fork) CFD_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
         MotionTailArgs f = t;
         f.do_motion = 0;
         f.do_forces = 1;
@@ -875,26 +900,49 @@ int Ctx::enqueue_mixed(bool learned) {
         tstart(TM_FORCES);
         CFD_LAUNCH(k_motion_tail, (unsigned)tail_blocks, 256, 0, stream, f);
         tstop(TM_FORCES);
-    } else {
-        if ((st = motion_solve(stream, true))) return st;
     }
-    CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1],
-               d_scal, d_X, d_Y, d_WX, d_WY, d_Xhi, d_Xlo, d_Wf);
-    if (fv_each) {  // FORCE_VISC at the print block's point: moved mesh, previous dNx
+    if (prm.moving == 1) {  // normales of the moved mesh, for the next step's wall BC
+        tstart(TM_NORMALES);
+        if (nwn > 0)
+            CFD_LAUNCH(k_normales, blocks_for(nwn, TB), TB, 0, stream, nwn, d_wnode, d_wptr, d_wedge,
+                       d_walls, d_X, d_Y, d_bcflag, d_nrm);
+        tstop(TM_NORMALES);
+    }
+    if (fv_each) {  // FORCE_VISC at the print block's point: moved mesh, this step's dNx
         st = force_visc_now();
         if (st) return st;
     }
-    if (prm.moving == 1) {
-        st = geometry_mixed(false);
-        if (st) return st;
-    }
     return CFD_OK;
+}
+
+// The next-step buffers become the current ones (after each mixed step)
+void Ctx::swap_mixed_buffers() {
+    std::swap(d_WX, d_WX_n);
+    std::swap(d_WY, d_WY_n);
+    std::swap(d_Wf, d_Wf_n);
+    if (prm.moving == 1) {
+        std::swap(d_geo8, d_geo8_n);
+        std::swap(d_invMf, d_invMf_n);
+    }
+    buf ^= 1;
+}
+
+void Ctx::drop_graphs() {
+    for (int p = 0; p < 2; ++p) {
+        if (step_exec[p]) cudaGraphExecDestroy(step_exec[p]);
+        if (step_graph[p]) cudaGraphDestroy(step_graph[p]);
+        step_exec[p] = nullptr;
+        step_graph[p] = nullptr;
+    }
 }
 
 // Replay the captured step, capturing it first.  *launched = false when the capture is
 // not possible here (the caller then enqueues the step launch by launch, and stays so).
 int Ctx::launch_step_graph(bool* launched) {
     *launched = false;
+    // one graph per buffer parity: the captured pointers are the parity's
+    cudaGraph_t& step_graph = this->step_graph[buf];
+    cudaGraphExec_t& step_exec = this->step_exec[buf];
     if (!step_exec) {
         const long long k0 = g_launches.load();
         CFD_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -947,12 +995,14 @@ int Ctx::step_once_mixed() {
         if (st) return st;
         if (launched) {
             mixed_steps += 1;
+            swap_mixed_buffers();
             return CFD_OK;
         }
     }
     int st = enqueue_mixed(learned);
     if (st) return st;
     mixed_steps += 1;
+    swap_mixed_buffers();
     return tcollect();
 }
 

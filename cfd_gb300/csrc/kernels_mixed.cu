@@ -787,7 +787,7 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     double m;
     if (gcl) {
         m = M[p] + (*dtp) * (f2d_bits(m1.value()) + f2d_bits(m2.value())) * 0.5;
-        Wold[p] = W[p];
+        if (Wold) Wold[p] = W[p];  // putW (null: the caller swaps W buffers instead)
     } else {
         m = f2d_bits(m1.value()) * (1.0 / 3.0);
     }
@@ -909,17 +909,30 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
     const bool structural = a.law == CFD_MOTION_NEWMARK;
     if (a.do_motion && !structural) tail_transf(a, mv, gt, gs);
+    if (a.do_motion && a.fgeo)  // the edge geometry FORCES will need, before the mesh moves
+        for (int k = gt; k < a.set_ptr[a.nset]; k += gs) {
+            const int2 ed = a.set_edges[k];
+            a.fgeo[k] = make_double4(a.Y[ed.y] - a.Y[ed.x], a.X[ed.x] - a.X[ed.y],
+                                     (a.X[ed.x] + a.X[ed.y]) * 0.5, (a.Y[ed.y] + a.Y[ed.x]) * 0.5);
+        }
     for (int s = 0; a.do_forces && s < a.nset; ++s) {
         double fx = 0.0, fy = 0.0, rm = 0.0;
         const double xr = a.xref[s], yr = a.yref[s];
         for (int k = a.set_ptr[s] + gt; k < a.set_ptr[s + 1]; k += gs) {
             const int2 ed = a.set_edges[k];
             const double d_press = ((double)a.P[ed.x] + (double)a.P[ed.y]) * 0.5;
-            const double fa = d_press * (a.Y[ed.y] - a.Y[ed.x]);
-            const double fb = d_press * (a.X[ed.x] - a.X[ed.y]);
+            double4 g;  // Y(N2)-Y(N1), X(N1)-X(N2), the edge's midpoint
+            if (a.fgeo) {
+                g = a.fgeo[k];
+            } else {
+                g = make_double4(a.Y[ed.y] - a.Y[ed.x], a.X[ed.x] - a.X[ed.y],
+                                 (a.X[ed.x] + a.X[ed.y]) * 0.5, (a.Y[ed.y] + a.Y[ed.x]) * 0.5);
+            }
+            const double fa = d_press * g.x;
+            const double fb = d_press * g.y;
             fx += fa;
             fy += fb;
-            rm += fb * ((a.X[ed.x] + a.X[ed.y]) * 0.5 - xr) - fa * ((a.Y[ed.y] + a.Y[ed.x]) * 0.5 - yr);
+            rm += fb * (g.z - xr) - fa * (g.w - yr);
         }
         fx = block_tree256(fx, red);
         fy = block_tree256(fy, red);
