@@ -145,7 +145,7 @@ struct Ctx {
     float* d_invMf_n = nullptr;
     double *d_WX_n = nullptr, *d_WY_n = nullptr;
     float2* d_Wf_n = nullptr;
-    double4* d_fgeo = nullptr;  // per force-set edge: the step-start edge geometry
+    double4_32a* d_fgeo = nullptr;  // per force-set edge: the step-start edge geometry
     int buf = 0;
     long long graph_kernels = 0;  // kernels of one replay
     long long mixed_steps = 0;    // steps of this context (the first runs uncaptured)
@@ -182,6 +182,8 @@ struct Ctx {
     int geometry_mixed(bool setup, bool put_area = false, bool to_next = false,
                        cudaStream_t sv = nullptr);
     void swap_mixed_buffers();
+    unsigned branch_grid(long n, int threads, cudaStream_t s) const;
+    int branch_bpsm = 0;  // mesh-motion branch: blocks per SM of its grid-stride kernels
     void drop_graphs();
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
     int widen_mixed();

@@ -125,7 +125,7 @@ struct MotionTailArgs {
     double *x0, *x1;
     float *xf0, *xf1;
     double* part;  // [3 * nset][gridDim.x] per-block force sums
-    double4* fgeo; // null, or per set edge the step-start geometry (the motion part writes,
+    double4_32a* fgeo; // null, or per set edge the step-start geometry (the motion part writes,
                    // the forces part reads: the mesh may have moved in between)
     unsigned* count;
     StepScal* sc;

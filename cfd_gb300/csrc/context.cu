@@ -174,7 +174,11 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         a.only_if = nullptr;
         if (nufix > 0 && !fix_done)
             CFD_LAUNCH(k_bicg_fix_mixed, blocks_for(nufix, 256), 256, 0, stream, a);
-        CFD_LAUNCH(k_bicg_resid_mixed, (unsigned)a.nblk_r, 256, 0, stream, a);
+        // beside the RK stages (sv: the branch stream) the row kernels take a smaller grid
+        const unsigned rgrid = (sv && branch_bpsm > 0)
+                                   ? (unsigned)std::min<long>(a.nblk_r, (long)branch_bpsm * nsm)
+                                   : (unsigned)a.nblk_r;
+        CFD_LAUNCH(k_bicg_resid_mixed, rgrid, 256, 0, stream, a);
         if (learned) {
             // the network runs only when the previous-step guess leaves r.z >= gate; its
             // guess replaces it, per solve, when its r.z is the smaller; the first pass is
@@ -192,7 +196,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
             b.only_if = d_gflag + 1;
             CFD_LAUNCH(k_bicg_resid_mixed, gsz, 256, 0, stream, b);
         }
-        CFD_LAUNCH(k_bicg_dir_mixed, (unsigned)a.nblk_r, 256, 0, stream, a);
+        CFD_LAUNCH(k_bicg_dir_mixed, rgrid, 256, 0, stream, a);
     }
     CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
     void* args[] = {&a};
@@ -705,6 +709,10 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         CFD_CUDA(cudaMemsetAsync(d_tcount, 0, 4 * sizeof(unsigned), stream));
         CFD_CUDA(cudaMemsetAsync(d_motion, 0, sizeof(MotionScal), stream));
         graphs_on = !timers_on && !(getenv("CFD_GRAPHS") && atoi(getenv("CFD_GRAPHS")) == 0);
+        // 8 blocks per SM measured best at 1M nodes (0.640 ms vs 0.671 with full grids, 0.69
+        // at 6, 0.65 at 16); 0 = full grids
+        branch_bpsm = getenv("CFD_BRANCH_BLOCKS_PER_SM") ? atoi(getenv("CFD_BRANCH_BLOCKS_PER_SM"))
+                                                         : 8;
         if ((st = narrow_mixed(true, true, true, true, true, true))) return st;
     }
     // setup geometry: NORMALES, DERIV, MASAS, laplace (ns2DComp.ALE.f90:88-100)
@@ -758,13 +766,14 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
     tstart(TM_DERIV);
     const NormalsArgs nv{to_next ? 0 : nwn, d_wnode, d_wptr, d_wedge, d_walls, d_X, d_Y, d_bcflag,
                          d_nrm};
-    CFD_LAUNCH(k_elem_geometry, blocks_for(E, TB) + (nv.nwn > 0 ? blocks_for(nv.nwn, TB) : 0), TB,
+    CFD_LAUNCH(k_elem_geometry,
+               nv.nwn > 0 ? blocks_for(E, TB) + blocks_for(nv.nwn, TB) : branch_grid(E, TB, sv), TB,
                0, stream, E, d_elem, d_Xhi, d_Xlo, gcl ? 1 : 0,
                prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, Wn, Wo,
                (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, geo8, d_gterms, nv);
     tstop(TM_DERIV);
     tstart(TM_LAPLACE);
-    CFD_LAUNCH(k_node_geometry, blocks_for(N, kGeoNodeBlock), kGeoNodeBlock, 0, stream, N,
+    CFD_LAUNCH(k_node_geometry, branch_grid(N, kGeoNodeBlock, sv), kGeoNodeBlock, 0, stream, N,
                d_esup_ptr, d_esup_slot, d_lap_pos, geo8, d_gterms, &d_scal->dtmin, gcl ? 1 : 0,
                d_rowptr, d_valf, d_invdiag, d_invdiagf, d_M, invMf, Wn,
                to_next ? (float2*)nullptr : d_Wof);
@@ -847,7 +856,7 @@ int Ctx::enqueue_mixed(bool learned) {
         int st = run_pcg(2, learned, true, s);
         if (st) return st;
         tstop(TM_GRAD);
-        CFD_LAUNCH(k_motion_update_mixed, blocks_for(N, TB), TB, 0, s, N, d_pos[0], d_pos[1],
+        CFD_LAUNCH(k_motion_update_mixed, branch_grid(N, TB, s), TB, 0, s, N, d_pos[0], d_pos[1],
                    d_scal, d_X, d_Y, d_WX_n, d_WY_n, d_Xhi, d_Xlo, d_Wf_n);
         if (prm.moving == 1 && (st = geometry_mixed(false, false, true, s))) return st;
         return CFD_OK;
@@ -913,6 +922,14 @@ int Ctx::enqueue_mixed(bool learned) {
         if (st) return st;
     }
     return CFD_OK;
+}
+
+// Grid of a kernel over n items with `threads` per block: full, or on the mesh-motion
+// branch's stream (running beside the RK stages) at most branch_bpsm blocks per SM
+unsigned Ctx::branch_grid(long n, int threads, cudaStream_t s) const {
+    const unsigned full = blocks_for(n, threads);
+    if (!s || s != stream2 || branch_bpsm <= 0) return full;
+    return std::min<unsigned>(full, (unsigned)(branch_bpsm * nsm));
 }
 
 // The next-step buffers become the current ones (after each mixed step)

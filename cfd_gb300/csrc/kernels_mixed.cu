@@ -679,13 +679,14 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
                                 NormalsArgs nv) {
     // the blocks after the elements' do normales (one wall node per thread)
     const int eblocks = (nelem + blockDim.x - 1) / blockDim.x;
-    if ((int)blockIdx.x >= eblocks) {
+    if (nv.nwn > 0 && (int)blockIdx.x >= eblocks) {
         const int k = ((int)blockIdx.x - eblocks) * blockDim.x + threadIdx.x;
         if (k < nv.nwn) normales_node(nv, k);
         return;
     }
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nelem) return;
+    // grid-stride over the elements (the normales blocks, when any, follow eblocks blocks)
+    const int estride = (nv.nwn > 0 ? eblocks : (int)gridDim.x) * blockDim.x;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += estride) {
     const int4 n = elem[e];
     const float2 h0 = Xhi[n.x], h1 = Xhi[n.y], h2 = Xhi[n.z];
     const float2 l0 = Xlo[n.x], l1 = Xlo[n.y], l2 = Xlo[n.z];
@@ -716,6 +717,7 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
         terms[e] = make_float2(divW * area * (1.f / 3.f), divWo * area_old[e] * (1.f / 3.f));
     }
     if (put_area) area_old[e] = area;
+    }
 }
 
 // Node pass: the row of the mesh Laplacian (mLaplace.f90:28-56; rows of up to 16 entries
@@ -735,8 +737,8 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
                 double* __restrict__ M, float* __restrict__ invM,
                 const float2* __restrict__ W, float2* __restrict__ Wold) {
     __shared__ float row[kGeoBlock][kLapRow + 1];
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npoin) return;
+    // grid-stride (a smaller grid leaves room for kernels running beside it)
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npoin; p += gridDim.x * blockDim.x) {
     float* acc = row[threadIdx.x];
     const int r0 = rowptr[p], r1 = rowptr[p + 1];
     const int len = r1 - r0;
@@ -793,6 +795,7 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     }
     M[p] = m;
     invM[p] = 1.f / d2f_trunc(m);
+    }
 }
 
 // geo -> the FP64 dNx/dNy (column-major [6][nelem]) and area the download entries read
@@ -819,8 +822,7 @@ __global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos
                                       double* __restrict__ WX, double* __restrict__ WY,
                                       float2* __restrict__ Xhi, float2* __restrict__ Xlo,
                                       float2* __restrict__ Wf) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npoin) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npoin; p += gridDim.x * blockDim.x) {
     const double idt = sc->inv_dtmin;
     const double xp = xpos[p], yp = ypos[p];
     const double x = X[p] + xp, y = Y[p] + yp;
@@ -835,6 +837,7 @@ __global__ void k_motion_update_mixed(int npoin, const double* __restrict__ xpos
     split(y, hy, ly);
     Xhi[p] = make_float2(hx, hy);
     Xlo[p] = make_float2(lx, ly);
+    }
 }
 
 // ------------------------------------------------------------------ end of the flow part
@@ -912,7 +915,7 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
     if (a.do_motion && a.fgeo)  // the edge geometry FORCES will need, before the mesh moves
         for (int k = gt; k < a.set_ptr[a.nset]; k += gs) {
             const int2 ed = a.set_edges[k];
-            a.fgeo[k] = make_double4(a.Y[ed.y] - a.Y[ed.x], a.X[ed.x] - a.X[ed.y],
+            a.fgeo[k] = make_double4_32a(a.Y[ed.y] - a.Y[ed.x], a.X[ed.x] - a.X[ed.y],
                                      (a.X[ed.x] + a.X[ed.y]) * 0.5, (a.Y[ed.y] + a.Y[ed.x]) * 0.5);
         }
     for (int s = 0; a.do_forces && s < a.nset; ++s) {
@@ -921,11 +924,11 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
         for (int k = a.set_ptr[s] + gt; k < a.set_ptr[s + 1]; k += gs) {
             const int2 ed = a.set_edges[k];
             const double d_press = ((double)a.P[ed.x] + (double)a.P[ed.y]) * 0.5;
-            double4 g;  // Y(N2)-Y(N1), X(N1)-X(N2), the edge's midpoint
+            double4_32a g;  // Y(N2)-Y(N1), X(N1)-X(N2), the edge's midpoint
             if (a.fgeo) {
                 g = a.fgeo[k];
             } else {
-                g = make_double4(a.Y[ed.y] - a.Y[ed.x], a.X[ed.x] - a.X[ed.y],
+                g = make_double4_32a(a.Y[ed.y] - a.Y[ed.x], a.X[ed.x] - a.X[ed.y],
                                  (a.X[ed.x] + a.X[ed.y]) * 0.5, (a.Y[ed.y] + a.Y[ed.x]) * 0.5);
             }
             const double fa = d_press * g.x;

@@ -285,9 +285,11 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
 #pragma unroll
     for (int s = 0; s < 2; ++s) act[s] = s < a.nsolve && !(a.bscal[4 * s] < a.tol);
     if (!act[0] && !act[1]) return;  // the same in every block
-    const long i = blockIdx.x * (long)blockDim.x + t;
+    // 256-row groups blockIdx.x, blockIdx.x + gridDim.x, ...; one partial per block
     double py[2] = {0.0, 0.0};
-    if (i < a.n) {
+    for (long rb = blockIdx.x; rb < a.nblk_r; rb += gridDim.x) {
+        const long i = rb * 256 + t;
+        if (i >= a.n) continue;
         const bool fx = a.isfix[i];
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
@@ -296,7 +298,7 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
             const double yi =
                 fx ? 1.0e30 * pi : f2d_bits(spmv_row_dir_f<8>(a, (int)i, a.pf[s][0], a.pf[s][0], 0.f));
             a.y[s][i] = yi;
-            py[s] = pi * yi;
+            py[s] += pi * yi;
         }
     }
     sh[0][t] = py[0];
@@ -304,9 +306,9 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
     __syncthreads();
     if ((t >> 5) < 2) {
         const double v = warp_sum256(sh[t >> 5]);
-        if ((t & 31) == 0) a.part_r[(t >> 5) * a.nblk_r + blockIdx.x] = v;
+        if ((t & 31) == 0) a.part_r[(t >> 5) * gridDim.x + blockIdx.x] = v;
     }
-    if (last_block_fold(&a.bcount[1], a.part_r, a.nblk_r, 2, sh, out) && t == 0)
+    if (last_block_fold(&a.bcount[1], a.part_r, gridDim.x, 2, sh, out) && t == 0)
         for (int s = 0; s < 2; ++s)
             if (act[s]) {
                 a.bscal[4 * s + 2] = out[s];
