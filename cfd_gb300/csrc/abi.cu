@@ -360,7 +360,7 @@ int cfd_ctx_download_state(cfd_ctx* ctx, double* U, double* T, double* X, double
     if (!ctx) return arg_error("ctx");
     Ctx& c = ctx->impl;
     const size_t N = c.npoin;
-    if (T && c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed());
+    if (T && c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed(1));
     if (U) CFD_CUDA(cudaMemcpyAsync(U, c.d_U, 32 * N, cudaMemcpyDeviceToHost, c.stream));
     if (T) CFD_CUDA(cudaMemcpyAsync(T, c.d_T, 8 * N, cudaMemcpyDeviceToHost, c.stream));
     if (X) CFD_CUDA(cudaMemcpyAsync(X, c.d_X, 8 * N, cudaMemcpyDeviceToHost, c.stream));
@@ -374,7 +374,7 @@ int cfd_ctx_download_fields(cfd_ctx* ctx, double* RHO, double* VEL_X, double* VE
     if (!ctx) return arg_error("ctx");
     Ctx& c = ctx->impl;
     const size_t n8 = 8 * (size_t)c.npoin;
-    if (c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed());
+    if (c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed(2));
     const double* src[8] = {c.d_RHO, c.d_VX, c.d_VY, c.d_E, c.d_P, c.d_RMACH, c.d_WX, c.d_WY};
     double* dst[8] = {RHO, VEL_X, VEL_Y, E, P, RMACH, W_X, W_Y};
     for (int i = 0; i < 8; ++i)
@@ -397,7 +397,7 @@ int cfd_ctx_download_geometry(cfd_ctx* ctx, double* area, double* dNx, double* d
     if (!ctx) return arg_error("ctx");
     Ctx& c = ctx->impl;
     const size_t E = c.nelem;
-    if ((dNx || dNy || area) && c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed());
+    if ((dNx || dNy || area) && c.prec == CFD_PREC_MIXED) TRY(c.widen_mixed(4));
     if (area) CFD_CUDA(cudaMemcpyAsync(area, c.d_area, 8 * E, cudaMemcpyDeviceToHost, c.stream));
     if (M) CFD_CUDA(cudaMemcpyAsync(M, c.d_M, 8 * (size_t)c.npoin, cudaMemcpyDeviceToHost, c.stream));
     std::vector<double> g;

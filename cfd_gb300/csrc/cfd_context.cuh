@@ -49,6 +49,8 @@ struct Ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_scal = nullptr;
     StepScal* h_scal = nullptr;  // pinned
+    StepOut* h_out = nullptr;    // pinned step report
+    StepOut* d_out = nullptr;
     std::vector<void*> allocs;
     // time-loop scalars kept on the host
     int iter = 0;
@@ -186,7 +188,7 @@ struct Ctx {
     int branch_bpsm = 0;  // mesh-motion branch: blocks per SM of its grid-stride kernels
     void drop_graphs();
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
-    int widen_mixed();
+    int widen_mixed(int what);
     int run_pcg(int nsolve, bool learned = false, bool fix_done = false,
                 cudaStream_t sv = nullptr);
     int enqueue_mixed(bool learned);

@@ -107,6 +107,17 @@ struct MotionScal {
     double dtmin;               // DTMIN of the step
     double veln0, veln1, accn0, accn1;  // CFD_MOTION_NEWMARK: VELN, ACCN
 };
+// What cfd_step reports, gathered on the device into one record for one copy
+struct StepOut {
+    StepScal sc;
+    MotionScal ms;
+    double rz[2];
+    int it[2], cv[2];
+    int bar_err, has_motion;
+};
+__global__ void k_pack_report(const StepScal* sc, const MotionScal* ms, const int* it,
+                              const int* cv, const double* rz, const GridBar* bar, StepOut* out);
+
 struct MotionTailArgs {
     int do_motion, do_forces;  // the parts this launch runs (Newmark: both)
     int nset;  // FORCES

@@ -81,6 +81,7 @@ Ctx::~Ctx() {
     if (lgraph) mpnn::graph_free(lgraph);
     for (void* p : allocs) cudaFree(p);
     if (h_scal) cudaFreeHost(h_scal);
+    if (h_out) cudaFreeHost(h_out);
     if (h_iters) cudaFreeHost(h_iters);
     drop_graphs();
     if (ev_iters) cudaEventDestroy(ev_iters);
@@ -455,18 +456,19 @@ int Ctx::step(int nsteps, cfd_step_report* rep) {
         int st = (prec == CFD_PREC_MIXED) ? step_once_mixed() : step_once();
         if (st) return st;
     }
-    CFD_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(StepScal), cudaMemcpyDeviceToHost, stream));
-    int it[2] = {0, 0}, cv[2] = {0, 0};
-    double rz[2] = {0, 0};
-    GridBar gb{};
-    CFD_CUDA(cudaMemcpyAsync(it, d_pcg_iters, sizeof(it), cudaMemcpyDeviceToHost, stream));
-    CFD_CUDA(cudaMemcpyAsync(cv, d_pcg_conv, sizeof(cv), cudaMemcpyDeviceToHost, stream));
-    CFD_CUDA(cudaMemcpyAsync(rz, d_pcg_rz, sizeof(rz), cudaMemcpyDeviceToHost, stream));
-    CFD_CUDA(cudaMemcpyAsync(&gb, d_bar, sizeof(gb), cudaMemcpyDeviceToHost, stream));
-    MotionScal ms{};
-    if (d_motion)
-        CFD_CUDA(cudaMemcpyAsync(&ms, d_motion, sizeof(ms), cudaMemcpyDeviceToHost, stream));
+    // the report: one gather on the device, one copy into pinned memory
+    CFD_LAUNCH(k_pack_report, 1, 32, 0, stream, (const StepScal*)d_scal,
+               (const MotionScal*)d_motion, (const int*)d_pcg_iters, (const int*)d_pcg_conv,
+               (const double*)d_pcg_rz, (const GridBar*)d_bar, d_out);
+    CFD_CUDA(cudaMemcpyAsync(h_out, d_out, sizeof(StepOut), cudaMemcpyDeviceToHost, stream));
     CFD_CUDA(cudaStreamSynchronize(stream));
+    *h_scal = h_out->sc;
+    const MotionScal ms = h_out->ms;
+    const int* it = h_out->it;
+    const int* cv = h_out->cv;
+    const double* rz = h_out->rz;
+    GridBar gb{};
+    gb.err = h_out->bar_err;
     if (d_motion && nsteps > 0) {  // the mixed form's clock is kept on the device
         time = ms.time;
         last_dtmin = ms.dtmin;
@@ -545,6 +547,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     CFD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     CFD_CUDA(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
     CFD_CUDA(cudaMallocHost((void**)&h_scal, sizeof(StepScal)));
+    CFD_CUDA(cudaMallocHost((void**)&h_out, sizeof(StepOut)));
     // mesh
     std::vector<int4> el(E);
     for (int e = 0; e < E; ++e)
@@ -618,6 +621,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     CFD_CUDA(cudaMemsetAsync(d_pcg_conv, 0, 2 * sizeof(int), stream));
     CFD_CUDA(cudaMemsetAsync(d_pcg_rz, 0, 2 * sizeof(double), stream));
     if ((st = dalloc(&d_scal, 1))) return st;
+    if ((st = dalloc(&d_out, 1))) return st;
     StepScal sc0{};
     sc0.dtmin_bits = 0x7ff0000000000000ull;
     sc0.dtmin32_bits = 0x7ff0000000000000ull;
@@ -736,14 +740,17 @@ int Ctx::narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W) {
 }
 
 // float fields -> the FP64 arrays the download entries read
-int Ctx::widen_mixed() {
+// what: 1 = T only, 2 = the seven node fields, 4 = the geometry (bits may combine)
+int Ctx::widen_mixed(int what) {
     const long N = npoin, E = nelem;
     const float* src[7] = {d_Tf, d_VXf, d_VYf, d_RHOf, d_Ef, d_Pf, d_RMACHf};
     double* dst[7] = {d_T, d_VX, d_VY, d_RHO, d_E, d_P, d_RMACH};
-    for (int i = 0; i < 7; ++i)
+    const int nf = (what & 2) ? 7 : ((what & 1) ? 1 : 0);
+    for (int i = 0; i < nf; ++i)
         CFD_LAUNCH(k_widen, blocks_for(N, 256), 256, 0, stream, N, src[i], dst[i]);
-    CFD_LAUNCH(k_widen_geo, blocks_for(E, 256), 256, 0, stream, (int)E, (const float4*)d_geo8, d_geo,
-               d_area);
+    if (what & 4)
+        CFD_LAUNCH(k_widen_geo, blocks_for(E, 256), 256, 0, stream, (int)E, (const float4*)d_geo8,
+                   d_geo, d_area);
     return CFD_OK;
 }
 

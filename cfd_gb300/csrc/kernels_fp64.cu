@@ -815,4 +815,21 @@ cudaError_t launch_force_visc(cudaStream_t st, int form, int nset, const int* se
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ step report
+__global__ void k_pack_report(const StepScal* __restrict__ sc, const MotionScal* __restrict__ ms,
+                              const int* __restrict__ it, const int* __restrict__ cv,
+                              const double* __restrict__ rz, const GridBar* __restrict__ bar,
+                              StepOut* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    out->sc = *sc;
+    out->has_motion = ms != nullptr;
+    if (ms) out->ms = *ms;
+    for (int s = 0; s < 2; ++s) {
+        out->it[s] = it[s];
+        out->cv[s] = cv[s];
+        out->rz[s] = rz[s];
+    }
+    out->bar_err = bar->err;
+}
+
 }  // namespace cfd
