@@ -358,7 +358,7 @@ __global__ void k_elem_mulam(int nelem, const int4* __restrict__ elem, const flo
 // Vlam(3).
 
 template <bool VISCOUS>
-__global__ void __launch_bounds__(128, 5)
+__global__ void __launch_bounds__(128, 6)
 k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
                     const float4* __restrict__ Ulo, const float4* __restrict__ geo,
                     const float* __restrict__ shoc,
@@ -534,8 +534,9 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 // a boundary condition.  The last stage writes U1, every primitive and the hi/lo split of
 // U1 (the next step's U).  Node p alone reads U[p] and writes U1[p], so U1 may be U (the
 // update in place, U = U1 of ns2DComp.ALE.f90:277-281 without a copy).
+constexpr int kNodeTB = 256;  // threads per block of the node passes
 template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kNodeTB)
 k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
              const float2* __restrict__ mulam, const float4* __restrict__ recInv,
              const float4* __restrict__ recVisc, float4* __restrict__ invSum, GasConst gc,
@@ -1037,16 +1038,16 @@ cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, c
                               const unsigned char* bcflag, const double* bcval, const double2* nrm,
                               const double* WX, const double* WY, double* U1, float* RHO,
                               float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH) {
-    const unsigned grid = blocks_for(npoin, 256);
+    const unsigned grid = blocks_for(npoin, kNodeTB);
 #define CFD_NODE_ARGS                                                                          \
     npoin, esup_ptr, esup_slot, mulam, recInv, recVisc, invSum, gc, gf, viscous, U, Uhi, Ulo, invM, \
         rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH
     if (first_stage)
-        k_node_mixed<true, false><<<grid, 256, 0, st>>>(CFD_NODE_ARGS);
+        k_node_mixed<true, false><<<grid, kNodeTB, 0, st>>>(CFD_NODE_ARGS);
     else if (last_stage)
-        k_node_mixed<false, true><<<grid, 256, 0, st>>>(CFD_NODE_ARGS);
+        k_node_mixed<false, true><<<grid, kNodeTB, 0, st>>>(CFD_NODE_ARGS);
     else
-        k_node_mixed<false, false><<<grid, 256, 0, st>>>(CFD_NODE_ARGS);
+        k_node_mixed<false, false><<<grid, kNodeTB, 0, st>>>(CFD_NODE_ARGS);
 #undef CFD_NODE_ARGS
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
