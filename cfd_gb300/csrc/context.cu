@@ -894,8 +894,8 @@ int Ctx::enqueue_mixed(bool learned) {
         const float rk_fact = 1.f / (float)(NRK + 1 - irk);
         tstart(TM_UPDATE);
         if (irk > 1 && viscous)
-            CFD_LAUNCH(k_elem_mulam, blocks_for(E, TB), TB, 0, stream, E, d_elem, (const float*)d_Tf,
-                       gf, d_mulam);
+            CFD_LAUNCH(k_elem_mulam, blocks_for(E, kMulamTB), kMulamTB, 0, stream, E, d_elem,
+                       (const float*)d_Tf, gf, d_mulam);
         CFD_CUDA(launch_node_mixed(stream, N, d_esup_ptr, d_esup_slot, d_mulam, d_recInv, d_recVisc,
                                    d_invSum, irk == 1 ? 1 : 0, gc, gf, viscous ? 1 : 0, d_U, d_Uhi,
                                    d_Ulo, d_invMf, rk_fact, irk == NRK ? 1 : 0, d_bcflag, d_bcval,

@@ -534,7 +534,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 // a boundary condition.  The last stage writes U1, every primitive and the hi/lo split of
 // U1 (the next step's U).  Node p alone reads U[p] and writes U1[p], so U1 may be U (the
 // update in place, U = U1 of ns2DComp.ALE.f90:277-281 without a copy).
-constexpr int kNodeTB = 256;  // threads per block of the node passes
+constexpr int kNodeTB = 128;  // threads per block of the node passes
 template <bool FIRST, bool LAST>
 __global__ void __launch_bounds__(kNodeTB)
 k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
