@@ -535,6 +535,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 // U1 (the next step's U).  Node p alone reads U[p] and writes U1[p], so U1 may be U (the
 // update in place, U = U1 of ns2DComp.ALE.f90:277-281 without a copy).
 constexpr int kNodeTB = 128;  // threads per block of the node passes
+constexpr int kSlotBatch = 4, kSlotBatchFirst = 4;  // slots whose loads go out together
 template <bool FIRST, bool LAST>
 __global__ void __launch_bounds__(kNodeTB)
 k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
@@ -554,13 +555,14 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
     a0.init(); a1.init(); a2.init(); a3.init();
     v1.init(); v2.init(); v3.init();
     const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
-    // four slots per pass: their loads are issued together, the sums stay in slot order
-    for (int s = s0; s < s1; s += 4) {
-        float4 ri[4], rv[4];
-        int e[4];
-        float2 ml[4];
+    // B slots per pass: their loads are issued together, the sums stay in slot order
+    constexpr int B = FIRST ? kSlotBatchFirst : kSlotBatch;
+    for (int s = s0; s < s1; s += B) {
+        float4 ri[B], rv[B];
+        int e[B];
+        float2 ml[B];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < B; ++j) {
             if (s + j < s1) {
                 if (FIRST) ri[j] = recInv[s + j];
                 if (viscous) {
@@ -571,11 +573,11 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
         }
         if (viscous) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+            for (int j = 0; j < B; ++j)
                 if (s + j < s1) ml[j] = mulam[e[j]];
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < B; ++j) {
             if (s + j < s1) {
                 if (FIRST) {
                     a0.add(ri[j].x);
