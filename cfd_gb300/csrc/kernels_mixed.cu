@@ -25,10 +25,9 @@ namespace cfd {
 
 __device__ __forceinline__ float pow15f(float x) { return x * sqrtf(x); }
 
-// FP32 quotients of the stabilisation, time-step and Sutherland kernels: __fdividef
-// (within 2 ulp), several times fewer instructions than the IEEE quotient in kernels that
-// are instruction-issue bound.  The RHS element kernel and the node update keep IEEE
-// quotients.
+// FP32 quotients of the stabilisation, time-step, Sutherland and RHS element kernels:
+// __fdividef (within 2 ulp), several times fewer instructions than the IEEE quotient in
+// kernels that are instruction-issue bound.  The node update keeps IEEE quotients.
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
 // Neumaier-compensated float accumulator
@@ -434,7 +433,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 #pragma unroll
         for (int q = 0; q < 4; ++q) Uk[q] = 0.5f * (Un[ia][q] + Un[ib][q]);
         const float rho = Uk[0];
-        const float irho = 1.f / rho;
+        const float irho = fdiv(1.f, rho);
         const float v1 = Uk[1] * irho, v2 = Uk[2] * irho, ev = Uk[3] * irho;
         const float V_sq = v1 * v1 + v2 * v2;
         const float W0 = V_sq * gm1 - ev * g;
@@ -466,7 +465,7 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
         }
         if (VISCOUS) {
             // K1, K2 of calcRHS.f90:121-132 split as mu*(...) + lambda*(...)
-            const float icv = 1.f / (Cv * rho);
+            const float icv = irho * fdiv(1.f, Cv);
             const float m11 = (2.f / 3.f) * (-2.f * Ux[0] * v1 + 2.f * Ux[1] + Uy[0] * v2 - Uy[2]) * irho;
             const float m12 = (-Ux[0] * v2 + Ux[2] - Uy[0] * v1 + Uy[1]) * irho;
             const float m22 = (2.f / 3.f) * (Ux[0] * v1 - Ux[1] - 2.f * Uy[0] * v2 + 2.f * Uy[2]) * irho;
