@@ -524,7 +524,9 @@ def main_ours(args):
                 "launches_per_step": calls_per_step[dom],
                 "algorithmic_bytes_per_launch": (ab[dom] / calls_per_step[dom]) if dom in ab else None}
     kernels = {n_: {"ms_per_launch": per_launch[n_] * 1e3, "launches_per_step": calls_per_step[n_],
-                    "GBps_algorithmic": (ab[n_] / per_step[n_] / 1e9) if n_ in ab else None}
+                    "GBps_algorithmic": (ab[n_] / per_step[n_] / 1e9) if n_ in ab else None,
+                    "frac_of_hbm_peak": (ab[n_] / per_step[n_] / 1e9 / hbm_peak)
+                    if n_ in ab else None}
                for n_ in per_launch}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
