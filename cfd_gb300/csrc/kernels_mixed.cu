@@ -728,6 +728,7 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
 // M += dt*(tot1+tot2)/2 in FP64 from compensated FP32 sums of the element terms, followed
 // by putW (W_old = W).
 constexpr int kLapRow = 16;
+constexpr int kGeoBatch = 1;  // slots per pass of k_node_geometry
 constexpr int kGeoBlock = kGeoNodeBlock;
 
 __global__ void __launch_bounds__(kGeoBlock)
@@ -754,28 +755,48 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     Acc m1, m2;
     m1.init();
     m2.init();
-    for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) {
-        const int slot = esup_slot[s];
-        const int e = slot / 3, i = slot - 3 * e;
-        const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
-        const uchar4 pos = lap_pos[s];
-        if (gcl) {
-            const float2 t = terms[e];
-            m1.add(t.x);
-            m2.add(t.y);
-        } else {
-            m1.add(gb.z);
-        }
-        const float gx[3] = {ga.x, ga.y, ga.z}, gy[3] = {ga.w, gb.x, gb.y};
-        const float q = gb.w;
-        const float dxi = (i == 0) ? gx[0] : (i == 1 ? gx[1] : gx[2]);
-        const float dyi = (i == 0) ? gy[0] : (i == 1 ? gy[1] : gy[2]);
-        const unsigned char pj[3] = {pos.x, pos.y, pos.z};
+    // kGeoBatch slots per pass: their loads go out together, the sums stay in slot order
+    const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
+    for (int sb = s0; sb < s1; sb += kGeoBatch) {
+        int slot[kGeoBatch];
+        uchar4 pos[kGeoBatch];
+        float4 ga[kGeoBatch], gb[kGeoBatch];
+        float2 tm[kGeoBatch];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const float v = (dxi * gx[j] + dyi * gy[j]) * q;
-            if (in_smem) acc[pj[j]] += v;
-            else valf[r0 + pj[j]] += v;  // long rows (rare)
+        for (int u = 0; u < kGeoBatch; ++u)
+            if (sb + u < s1) {
+                slot[u] = esup_slot[sb + u];
+                pos[u] = lap_pos[sb + u];
+            }
+#pragma unroll
+        for (int u = 0; u < kGeoBatch; ++u)
+            if (sb + u < s1) {
+                const int e = slot[u] / 3;
+                ga[u] = geo[2 * (size_t)e];
+                gb[u] = geo[2 * (size_t)e + 1];
+                if (gcl) tm[u] = terms[e];
+            }
+#pragma unroll
+        for (int u = 0; u < kGeoBatch; ++u) {
+            if (sb + u >= s1) break;
+            const int i = slot[u] - 3 * (slot[u] / 3);
+            if (gcl) {
+                m1.add(tm[u].x);
+                m2.add(tm[u].y);
+            } else {
+                m1.add(gb[u].z);
+            }
+            const float gx[3] = {ga[u].x, ga[u].y, ga[u].z}, gy[3] = {ga[u].w, gb[u].x, gb[u].y};
+            const float q = gb[u].w;
+            const float dxi = (i == 0) ? gx[0] : (i == 1 ? gx[1] : gx[2]);
+            const float dyi = (i == 0) ? gy[0] : (i == 1 ? gy[1] : gy[2]);
+            const unsigned char pj[3] = {pos[u].x, pos[u].y, pos[u].z};
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float v = (dxi * gx[j] + dyi * gy[j]) * q;
+                if (in_smem) acc[pj[j]] += v;
+                else valf[r0 + pj[j]] += v;  // long rows (rare)
+            }
         }
     }
     float diag;
