@@ -728,7 +728,7 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
 // M += dt*(tot1+tot2)/2 in FP64 from compensated FP32 sums of the element terms, followed
 // by putW (W_old = W).
 constexpr int kLapRow = 16;
-constexpr int kGeoBatch = 1;  // slots per pass of k_node_geometry
+constexpr int kGeoBatch = 2;  // slots per pass of k_node_geometry
 constexpr int kGeoBlock = kGeoNodeBlock;
 
 __global__ void __launch_bounds__(kGeoBlock)
