@@ -181,10 +181,10 @@ def config_dict(k, args, ws):
 # profiles/step_mixed_1M_launches.md (the full-size workload fits the capture rules: ~2.5 GB
 # on the device, kernels of 13-130 us).
 NCU_TRAFFIC_PER_STEP = {
-    "update_t": 1063.7e6,   # 4 node passes + 3 mu/lambda passes
-    "calcrhs_t": 374.8e6,
-    "estab_t": 174.2e6,
-    "laplace_t": 198.0e6,
+    "update_t": 1059.5e6,   # 4 node passes (946.4 MB) + 3 mu/lambda passes (113.1 MB)
+    "calcrhs_t": 381.8e6,
+    "deltat_t": 174.5e6,    # k_deltat_estab (the FP64 refinement reads a few chunks)
+    "laplace_t": 181.8e6,
 }
 
 
@@ -209,8 +209,9 @@ def algorithmic_bytes(k, iters, precision):
             # stage 1 adds recInv (16 B/slot); stage 4 adds U 32, U1 32, six primitives 24,
             # U hi/lo 32 B/N; stages 2-4 recompute mu/lambda (elem 16 + 8 B/E, T 4 B/N)
             "update_t": 4 * node_common + S * 16 + N * 120 + 3 * (E * 24 + N * 4),
-            "estab_t": E * (16 + 32 + 16) + N * 52,
-            "deltat_t": E * 20 + N * 20,
+            # deltat + the DTMIN-free ESTAB in one pass: elem 16, geo 32, SHOC and the three
+            # ESTAB terms 16 B/E; T, VX, VY 12 + W 8 + rho hi/lo 8 B/N
+            "deltat_t": E * (16 + 32 + 16) + N * 28,
             "deriv_t": E * (16 + 32 + 4 + 8 + 8) + N * 32,
             "laplace_t": S * 8 + E * 40 + N * 52 + nnz * 4,
             "grad_t": bicg,
