@@ -138,6 +138,7 @@ struct MotionTailArgs {
     double* part;  // [3 * nset][gridDim.x] per-block force sums
     double4_32a* fgeo; // null, or per set edge the step-start geometry (the motion part writes,
                    // the forces part reads: the mesh may have moved in between)
+    NormalsArgs nv;    // the forces part also runs normales (nv.nwn = 0: not)
     unsigned* count;
     StepScal* sc;
 };

@@ -705,7 +705,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_fgeo, std::max<size_t>(1, bc.set_elem.size())))) return st;
         if ((st = dalloc(&d_tcount, 4))) return st;
         {  // blocks of the motion tail: a block per 256 edges, moving nodes or fixed values
-            int w = std::max(nnmove, nufix);
+            int w = std::max(std::max(nnmove, nufix), nwn);
             for (int s = 0; s < bc.nset_numb; ++s) w = std::max(w, bc.set_ptr[s + 1] - bc.set_ptr[s]);
             tail_blocks = std::min(64, std::max(1, (int)blocks_for(w, 256)));
         }
@@ -913,11 +913,13 @@ int Ctx::enqueue_mixed(bool learned) {
         f.do_motion = 0;
         f.do_forces = 1;
         f.count = d_tcount + 2;
+        if (prm.moving == 1)  // normales of the moved mesh ride on this launch
+            f.nv = NormalsArgs{nwn, d_wnode, d_wptr, d_wedge, d_walls, d_X, d_Y, d_bcflag, d_nrm};
         tstart(TM_FORCES);
         CFD_LAUNCH(k_motion_tail, (unsigned)tail_blocks, 256, 0, stream, f);
         tstop(TM_FORCES);
     }
-    if (prm.moving == 1) {  // normales of the moved mesh, for the next step's wall BC
+    if (prm.moving == 1 && structural) {  // normales of the moved mesh (the Newmark path)
         tstart(TM_NORMALES);
         if (nwn > 0)
             CFD_LAUNCH(k_normales, blocks_for(nwn, TB), TB, 0, stream, nwn, d_wnode, d_wptr, d_wedge,

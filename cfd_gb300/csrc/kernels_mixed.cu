@@ -935,6 +935,8 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
     const bool structural = a.law == CFD_MOTION_NEWMARK;
     if (a.do_motion && !structural) tail_transf(a, mv, gt, gs);
+    if (a.do_forces)  // normales of the moved mesh, for the next step's wall condition
+        for (int k = gt; k < a.nv.nwn; k += gs) normales_node(a.nv, k);
     if (a.do_motion && a.fgeo)  // the edge geometry FORCES will need, before the mesh moves
         for (int k = gt; k < a.set_ptr[a.nset]; k += gs) {
             const int2 ed = a.set_edges[k];
