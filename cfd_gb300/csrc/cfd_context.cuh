@@ -185,7 +185,9 @@ struct Ctx {
                        cudaStream_t sv = nullptr);
     void swap_mixed_buffers();
     unsigned branch_grid(long n, int threads, cudaStream_t s) const;
-    int branch_bpsm = 0;  // mesh-motion branch: blocks per SM of its grid-stride kernels
+    int branch_bpsm = 0;
+    int node_bulk = 0;          // dynamic smem of the bulk-copy node pass (0: not used)
+    int* d_node_err = nullptr;  // its bounded wait's error flag  // mesh-motion branch: blocks per SM of its grid-stride kernels
     void drop_graphs();
     int narrow_mixed(bool U, bool T, bool VX, bool VY, bool XY, bool W);
     int widen_mixed(int what);

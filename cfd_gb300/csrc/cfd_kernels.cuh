@@ -116,7 +116,8 @@ struct StepOut {
     int bar_err, has_motion;
 };
 __global__ void k_pack_report(const StepScal* sc, const MotionScal* ms, const int* it,
-                              const int* cv, const double* rz, const GridBar* bar, StepOut* out);
+                              const int* cv, const double* rz, const GridBar* bar,
+                              const int* wait_err, StepOut* out);
 
 struct MotionTailArgs {
     int do_motion, do_forces;  // the parts this launch runs (Newmark: both)
@@ -191,7 +192,11 @@ cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, c
                               const float* invM, float rk_fact, int last_stage,
                               const unsigned char* bcflag, const double* bcval, const double2* nrm,
                               const double* WX, const double* WY, double* U1, float* RHO,
-                              float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH);
+                              float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH,
+                              int bulk_smem = 0, int* bulk_err = nullptr);
+// dynamic shared memory of the bulk-copy node pass for blocks of `block` nodes (0: the
+// variant is not used: its staged slots would not fit)
+int node_bulk_smem(const int* esup_ptr_host, int npoin);
 __global__ void k_elem_geometry(int nelem, const int4* elem, const float2* Xhi, const float2* Xlo,
                                 int gcl, int literal, const float2* W, const float2* Wold,
                                 int put_area, float* area_old, float* areaf, float4* geo,

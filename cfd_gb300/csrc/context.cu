@@ -459,7 +459,7 @@ int Ctx::step(int nsteps, cfd_step_report* rep) {
     // the report: one gather on the device, one copy into pinned memory
     CFD_LAUNCH(k_pack_report, 1, 32, 0, stream, (const StepScal*)d_scal,
                (const MotionScal*)d_motion, (const int*)d_pcg_iters, (const int*)d_pcg_conv,
-               (const double*)d_pcg_rz, (const GridBar*)d_bar, d_out);
+               (const double*)d_pcg_rz, (const GridBar*)d_bar, (const int*)d_node_err, d_out);
     CFD_CUDA(cudaMemcpyAsync(h_out, d_out, sizeof(StepOut), cudaMemcpyDeviceToHost, stream));
     CFD_CUDA(cudaStreamSynchronize(stream));
     *h_scal = h_out->sc;
@@ -476,7 +476,7 @@ int Ctx::step(int nsteps, cfd_step_report* rep) {
         disn[1] = ms.disn1;
     }
     if (gb.err) {
-        set_last_message("a grid barrier of the BiCG kernel gave up waiting");
+        set_last_message("a bounded device wait gave up (BiCG grid barrier or node-pass copy)");
         return CFD_ERR_BARRIER;
     }
     if (rep) {
@@ -556,7 +556,11 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if ((st = upload(&d_X, m->x, N))) return st;
     if ((st = upload(&d_Y, m->y, N))) return st;
     if ((st = upload(&d_esup_ptr, adj.esup_ptr.data(), N + 1))) return st;
-    if ((st = upload(&d_esup_slot, adj.esup_slot.data(), 3 * (size_t)E))) return st;
+    {  // padded by 4 ids: the bulk-copy node pass reads whole 16-byte groups of slot ids
+        std::vector<int> es(adj.esup_slot);
+        es.resize(3 * (size_t)E + 4, 0);
+        if ((st = upload(&d_esup_slot, es.data(), es.size()))) return st;
+    }
     if ((st = upload(&d_lap_pos, (const uchar4*)adj.lap_pos.data(), 3 * (size_t)E))) return st;
     if ((st = upload(&d_rowptr, adj.rowptr.data(), N + 1))) return st;
     if ((st = upload(&d_col, adj.col.data(), adj.col.size()))) return st;
@@ -704,6 +708,10 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_Wf_n, N))) return st;
         if ((st = dalloc(&d_fgeo, std::max<size_t>(1, bc.set_elem.size())))) return st;
         if ((st = dalloc(&d_tcount, 4))) return st;
+        if ((st = dalloc(&d_node_err, 1))) return st;
+        CFD_CUDA(cudaMemsetAsync(d_node_err, 0, sizeof(int), stream));
+        if (!(getenv("CFD_NODE_BULK") && atoi(getenv("CFD_NODE_BULK")) == 0))
+            node_bulk = node_bulk_smem(adj.esup_ptr.data(), N);
         {  // blocks of the motion tail: a block per 256 edges, moving nodes or fixed values
             int w = std::max(std::max(nnmove, nufix), nwn);
             for (int s = 0; s < bc.nset_numb; ++s) w = std::max(w, bc.set_ptr[s + 1] - bc.set_ptr[s]);
@@ -900,7 +908,7 @@ int Ctx::enqueue_mixed(bool learned) {
                                    d_invSum, irk == 1 ? 1 : 0, gc, gf, viscous ? 1 : 0, d_U, d_Uhi,
                                    d_Ulo, d_invMf, rk_fact, irk == NRK ? 1 : 0, d_bcflag, d_bcval,
                                    d_nrm, d_WX, d_WY, d_U, d_RHOf, d_VXf, d_VYf, d_Ef, d_Pf, d_Tf,
-                                   d_RMACHf));
+                                   d_RMACHf, node_bulk, d_node_err));
         tstop(TM_UPDATE);
     }
     int st = CFD_OK;

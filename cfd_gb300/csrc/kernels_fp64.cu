@@ -819,7 +819,7 @@ cudaError_t launch_force_visc(cudaStream_t st, int form, int nset, const int* se
 __global__ void k_pack_report(const StepScal* __restrict__ sc, const MotionScal* __restrict__ ms,
                               const int* __restrict__ it, const int* __restrict__ cv,
                               const double* __restrict__ rz, const GridBar* __restrict__ bar,
-                              StepOut* __restrict__ out) {
+                              const int* __restrict__ wait_err, StepOut* __restrict__ out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     out->sc = *sc;
     out->has_motion = ms != nullptr;
@@ -829,7 +829,7 @@ __global__ void k_pack_report(const StepScal* __restrict__ sc, const MotionScal*
         out->cv[s] = cv[s];
         out->rz[s] = rz[s];
     }
-    out->bar_err = bar->err;
+    out->bar_err = bar->err | (wait_err ? *wait_err : 0);
 }
 
 }  // namespace cfd

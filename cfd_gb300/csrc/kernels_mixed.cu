@@ -534,74 +534,23 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 // U1 (the next step's U).  Node p alone reads U[p] and writes U1[p], so U1 may be U (the
 // update in place, U = U1 of ns2DComp.ALE.f90:277-281 without a copy).
 constexpr int kNodeTB = 128;  // threads per block of the node passes
-constexpr int kSlotBatch = 4, kSlotBatchFirst = 4;  // slots whose loads go out together
+// The node's update once its slot sums are known (inv: the stage-invariant sum in the first
+// stage, read back from invSum in the others; sv1..3: the viscous sums)
 template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(kNodeTB)
-k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
-             const float2* __restrict__ mulam, const float4* __restrict__ recInv,
-             const float4* __restrict__ recVisc, float4* __restrict__ invSum, GasConst gc,
-             GasConstF gf, int viscous,
-             const double* U, float4* __restrict__ Uhi, float4* __restrict__ Ulo,
-             const float* __restrict__ invM, float rk_fact,
-             const unsigned char* __restrict__ bcflag, const double* __restrict__ bcval,
-             const double2* __restrict__ nrm, const double* __restrict__ WX,
-             const double* __restrict__ WY, double* U1, float* __restrict__ RHO, float* __restrict__ VX,
-             float* __restrict__ VY, float* __restrict__ Eo, float* __restrict__ Po,
-             float* __restrict__ Tout, float* __restrict__ RMACH) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npoin) return;
-    Acc a0, a1, a2, a3, v1, v2, v3;
-    a0.init(); a1.init(); a2.init(); a3.init();
-    v1.init(); v2.init(); v3.init();
-    const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
-    // B slots per pass: their loads are issued together, the sums stay in slot order
-    constexpr int B = FIRST ? kSlotBatchFirst : kSlotBatch;
-    for (int s = s0; s < s1; s += B) {
-        float4 ri[B], rv[B];
-        int e[B];
-        float2 ml[B];
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            if (s + j < s1) {
-                if (FIRST) ri[j] = recInv[s + j];
-                if (viscous) {
-                    rv[j] = recVisc[s + j];
-                    e[j] = esup_slot[s + j] / 3;
-                }
-            }
-        }
-        if (viscous) {
-#pragma unroll
-            for (int j = 0; j < B; ++j)
-                if (s + j < s1) ml[j] = mulam[e[j]];
-        }
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            if (s + j < s1) {
-                if (FIRST) {
-                    a0.add(ri[j].x);
-                    a1.add(ri[j].y);
-                    a2.add(ri[j].z);
-                    a3.add(ri[j].w);
-                }
-                if (viscous) {
-                    v1.add(ml[j].x * rv[j].x);
-                    v2.add(ml[j].x * rv[j].y);
-                    v3.add(ml[j].x * rv[j].z + ml[j].y * rv[j].w);
-                }
-            }
-        }
-    }
-    float4 inv;
-    if (FIRST) {
-        inv = make_float4(a0.value(), a1.value(), a2.value(), a3.value());
-        invSum[p] = inv;
-    } else {
-        inv = invSum[p];
-    }
+__device__ __forceinline__ void node_finish(
+    int p, float4 inv, float sv1, float sv2, float sv3, float4* __restrict__ invSum, GasConst gc,
+    GasConstF gf, const double* U, float4* __restrict__ Uhi, float4* __restrict__ Ulo,
+    const float* __restrict__ invM, float rk_fact, const unsigned char* __restrict__ bcflag,
+    const double* __restrict__ bcval, const double2* __restrict__ nrm,
+    const double* __restrict__ WX, const double* __restrict__ WY, double* U1,
+    float* __restrict__ RHO, float* __restrict__ VX, float* __restrict__ VY,
+    float* __restrict__ Eo, float* __restrict__ Po, float* __restrict__ Tout,
+    float* __restrict__ RMACH) {
+    if (FIRST) invSum[p] = inv;
+    else inv = invSum[p];
     const float f = rk_fact * invM[p];
-    const float d0 = f * inv.x, d1 = f * (inv.y + v1.value()), d2 = f * (inv.z + v2.value()),
-                d3 = f * (inv.w + v3.value());
+    const float d0 = f * inv.x, d1 = f * (inv.y + sv1), d2 = f * (inv.z + sv2),
+                d3 = f * (inv.w + sv3);
     const float g = gf.gamma;
     const unsigned char fl = bcflag[p];
     if (!fl) {
@@ -660,6 +609,71 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
         Uhi[p] = make_float4(h[0], h[1], h[2], h[3]);
         Ulo[p] = make_float4(l[0], l[1], l[2], l[3]);
     }
+}
+
+constexpr int kSlotBatch = 4, kSlotBatchFirst = 4;  // slots whose loads go out together
+template <bool FIRST, bool LAST>
+__global__ void __launch_bounds__(kNodeTB)
+k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
+             const float2* __restrict__ mulam, const float4* __restrict__ recInv,
+             const float4* __restrict__ recVisc, float4* __restrict__ invSum, GasConst gc,
+             GasConstF gf, int viscous,
+             const double* U, float4* __restrict__ Uhi, float4* __restrict__ Ulo,
+             const float* __restrict__ invM, float rk_fact,
+             const unsigned char* __restrict__ bcflag, const double* __restrict__ bcval,
+             const double2* __restrict__ nrm, const double* __restrict__ WX,
+             const double* __restrict__ WY, double* U1, float* __restrict__ RHO, float* __restrict__ VX,
+             float* __restrict__ VY, float* __restrict__ Eo, float* __restrict__ Po,
+             float* __restrict__ Tout, float* __restrict__ RMACH) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npoin) return;
+    Acc a0, a1, a2, a3, v1, v2, v3;
+    a0.init(); a1.init(); a2.init(); a3.init();
+    v1.init(); v2.init(); v3.init();
+    const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
+    // B slots per pass: their loads are issued together, the sums stay in slot order
+    constexpr int B = FIRST ? kSlotBatchFirst : kSlotBatch;
+    for (int s = s0; s < s1; s += B) {
+        float4 ri[B], rv[B];
+        int e[B];
+        float2 ml[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (s + j < s1) {
+                if (FIRST) ri[j] = recInv[s + j];
+                if (viscous) {
+                    rv[j] = recVisc[s + j];
+                    e[j] = esup_slot[s + j] / 3;
+                }
+            }
+        }
+        if (viscous) {
+#pragma unroll
+            for (int j = 0; j < B; ++j)
+                if (s + j < s1) ml[j] = mulam[e[j]];
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (s + j < s1) {
+                if (FIRST) {
+                    a0.add(ri[j].x);
+                    a1.add(ri[j].y);
+                    a2.add(ri[j].z);
+                    a3.add(ri[j].w);
+                }
+                if (viscous) {
+                    v1.add(ml[j].x * rv[j].x);
+                    v2.add(ml[j].x * rv[j].y);
+                    v3.add(ml[j].x * rv[j].z + ml[j].y * rv[j].w);
+                }
+            }
+        }
+    }
+    const float4 inv =
+        FIRST ? make_float4(a0.value(), a1.value(), a2.value(), a3.value()) : make_float4(0.f, 0.f, 0.f, 0.f);
+    node_finish<FIRST, LAST>(p, inv, v1.value(), v2.value(), v3.value(), invSum, gc, gf, U, Uhi, Ulo,
+                             invM, rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, Eo, Po,
+                             Tout, RMACH);
 }
 
 // ------------------------------------------------------------------ geometry (mixed)
@@ -1054,6 +1068,99 @@ cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, c
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ node pass, bulk-copy variant
+// The viscous stages 2-4 with the block's slot records staged by the bulk-copy engine: a
+// block's 128 nodes own one contiguous range of slots (element-around-point order), so one
+// thread issues two cp.async.bulk copies (the recVisc records and the slot ids) into shared
+// memory, completing on an mbarrier, while every thread loads its node's own data; the
+// threads then gather the slots' mu, lambda (all of a node's gathers in flight at once) and
+// sum from shared memory in slot order.  The wait is bounded: past kSpinLimit polls the
+// block sets *err and leaves.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+template <bool LAST>
+__global__ void __launch_bounds__(kNodeTB)
+k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
+                  const float2* __restrict__ mulam, const float4* __restrict__ recVisc,
+                  float4* __restrict__ invSum, GasConst gc, GasConstF gf, const double* U,
+                  float4* __restrict__ Uhi, float4* __restrict__ Ulo, const float* __restrict__ invM,
+                  float rk_fact, const unsigned char* __restrict__ bcflag,
+                  const double* __restrict__ bcval, const double2* __restrict__ nrm,
+                  const double* __restrict__ WX, const double* __restrict__ WY, double* U1,
+                  float* __restrict__ RHO, float* __restrict__ VX, float* __restrict__ VY,
+                  float* __restrict__ Eo, float* __restrict__ Po, float* __restrict__ Tout,
+                  float* __restrict__ RMACH, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char stage_raw[];
+    __shared__ __align__(8) unsigned long long bar;
+    const int p0 = blockIdx.x * kNodeTB;
+    const int p1 = min(p0 + kNodeTB, npoin);
+    const int S0 = esup_ptr[p0], S1 = esup_ptr[p1];
+    const int S0a = S0 & ~3, S1a = (S1 + 3) & ~3;  // 16-byte aligned range of slot ids
+    const unsigned bytesV = 16u * (unsigned)(S1 - S0), bytesE = 4u * (unsigned)(S1a - S0a);
+    const float4* sv = reinterpret_cast<const float4*>(stage_raw);
+    const int* se = reinterpret_cast<const int*>(stage_raw + bytesV);
+    const unsigned ubar = smem_u32(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar),
+                     "r"(bytesV + bytesE)
+                     : "memory");
+        if (bytesV)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                    "r"(smem_u32(stage_raw)), "l"(recVisc + S0), "r"(bytesV), "r"(ubar)
+                : "memory");
+        if (bytesE)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                    "r"(smem_u32(stage_raw + bytesV)), "l"(esup_slot + S0a), "r"(bytesE), "r"(ubar)
+                : "memory");
+    }
+    const int p = p0 + threadIdx.x;
+    const bool live = p < npoin;
+    const int s0 = live ? esup_ptr[p] : 0, s1 = live ? esup_ptr[p + 1] : 0;
+    // bounded wait for the copies (phase 0)
+    unsigned done = 0;
+    for (long long k = 0; k < kSpinLimit && !done; ++k)
+        asm volatile(
+            "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0; selp.u32 %0, 1, 0, q; }"
+            : "=r"(done)
+            : "r"(ubar)
+            : "memory");
+    if (!done) {
+        if (threadIdx.x == 0) atomicExch(err, (int)CFD_ERR_BARRIER);
+        return;
+    }
+    if (!live) return;
+    Acc v1, v2, v3;
+    v1.init();
+    v2.init();
+    v3.init();
+    for (int s = s0; s < s1; s += 8) {
+        float2 ml[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (s + j < s1) ml[j] = mulam[se[s + j - S0a] / 3];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (s + j < s1) {
+                const float4 rv = sv[s + j - S0];
+                v1.add(ml[j].x * rv.x);
+                v2.add(ml[j].x * rv.y);
+                v3.add(ml[j].x * rv.z + ml[j].y * rv.w);
+            }
+    }
+    node_finish<false, LAST>(p, make_float4(0.f, 0.f, 0.f, 0.f), v1.value(), v2.value(), v3.value(),
+                             invSum, gc, gf, U, Uhi, Ulo, invM, rk_fact, bcflag, bcval, nrm, WX,
+                             WY, U1, RHO, VX, VY, Eo, Po, Tout, RMACH);
+}
+
 cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, const int* esup_slot,
                               const float2* mulam, const float4* recInv, const float4* recVisc,
                               float4* invSum, int first_stage, GasConst gc, GasConstF gf,
@@ -1061,8 +1168,21 @@ cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, c
                               const float* invM, float rk_fact, int last_stage,
                               const unsigned char* bcflag, const double* bcval, const double2* nrm,
                               const double* WX, const double* WY, double* U1, float* RHO,
-                              float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH) {
+                              float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH,
+                              int bulk_smem, int* bulk_err) {
     const unsigned grid = blocks_for(npoin, kNodeTB);
+    if (bulk_smem > 0 && viscous && !first_stage) {  // the bulk-copy variant
+        if (last_stage)
+            k_node_mixed_bulk<true><<<grid, kNodeTB, bulk_smem, st>>>(
+                npoin, esup_ptr, esup_slot, mulam, recVisc, invSum, gc, gf, U, Uhi, Ulo, invM,
+                rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH, bulk_err);
+        else
+            k_node_mixed_bulk<false><<<grid, kNodeTB, bulk_smem, st>>>(
+                npoin, esup_ptr, esup_slot, mulam, recVisc, invSum, gc, gf, U, Uhi, Ulo, invM,
+                rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH, bulk_err);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        return cudaGetLastError();
+    }
 #define CFD_NODE_ARGS                                                                          \
     npoin, esup_ptr, esup_slot, mulam, recInv, recVisc, invSum, gc, gf, viscous, U, Uhi, Ulo, invM, \
         rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH
@@ -1077,5 +1197,26 @@ cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, c
     return cudaGetLastError();
 }
 
+
+// Shared memory the bulk-copy node pass needs for the largest block of this mesh (0: more
+// than the variant takes), with the kernel attributes set for it
+int node_bulk_smem(const int* esup_ptr, int npoin) {
+    long worst = 0;
+    for (int p0 = 0; p0 < npoin; p0 += kNodeTB) {
+        const int S0 = esup_ptr[p0], S1 = esup_ptr[std::min(p0 + kNodeTB, npoin)];
+        const long b = 16L * (S1 - S0) + 4L * (((S1 + 3) & ~3) - (S0 & ~3));
+        worst = std::max(worst, b);
+    }
+    if (worst > 200 * 1024) return 0;
+    const int smem = (int)std::max(worst, 16L);
+    if (cudaFuncSetAttribute(k_node_mixed_bulk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_node_mixed_bulk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    return smem;
+}
 
 }  // namespace cfd
