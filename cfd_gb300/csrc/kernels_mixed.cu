@@ -1069,22 +1069,21 @@ cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, c
 }
 
 // ------------------------------------------------------------------ node pass, bulk-copy variant
-// The viscous RK stages with the block's slot records staged by the bulk-copy engine: a
+// The viscous stages 2-4 with the block's slot records staged by the bulk-copy engine: a
 // block's 128 nodes own one contiguous range of slots (element-around-point order), so one
-// thread issues the cp.async.bulk copies (the recVisc records, the slot ids, and in the
-// first stage the recInv records) into shared memory, completing on an mbarrier; the
-// threads then gather the slots' mu, lambda (up to eight of a node's gathers in flight at
-// once) and sum from shared memory in slot order.  The wait is bounded: past kSpinLimit
-// polls the block sets *err and leaves.
+// thread issues two cp.async.bulk copies (the recVisc records and the slot ids) into shared
+// memory, completing on an mbarrier, while every thread loads its node's own data; the
+// threads then gather the slots' mu, lambda (all of a node's gathers in flight at once) and
+// sum from shared memory in slot order.  The wait is bounded: past kSpinLimit polls the
+// block sets *err and leaves.
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
 }
 
-template <bool FIRST, bool LAST>
+template <bool LAST>
 __global__ void __launch_bounds__(kNodeTB)
 k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
-                  const float2* __restrict__ mulam, const float4* __restrict__ recInv,
-                  const float4* __restrict__ recVisc,
+                  const float2* __restrict__ mulam, const float4* __restrict__ recVisc,
                   float4* __restrict__ invSum, GasConst gc, GasConstF gf, const double* U,
                   float4* __restrict__ Uhi, float4* __restrict__ Ulo, const float* __restrict__ invM,
                   float rk_fact, const unsigned char* __restrict__ bcflag,
@@ -1100,10 +1099,8 @@ k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __rest
     const int S0 = esup_ptr[p0], S1 = esup_ptr[p1];
     const int S0a = S0 & ~3, S1a = (S1 + 3) & ~3;  // 16-byte aligned range of slot ids
     const unsigned bytesV = 16u * (unsigned)(S1 - S0), bytesE = 4u * (unsigned)(S1a - S0a);
-    const unsigned bytesI = FIRST ? bytesV : 0u;
     const float4* sv = reinterpret_cast<const float4*>(stage_raw);
-    const float4* si = reinterpret_cast<const float4*>(stage_raw + bytesV);
-    const int* se = reinterpret_cast<const int*>(stage_raw + bytesV + bytesI);
+    const int* se = reinterpret_cast<const int*>(stage_raw + bytesV);
     const unsigned ubar = smem_u32(&bar);
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar) : "memory");
@@ -1112,23 +1109,17 @@ k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __rest
     __syncthreads();
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar),
-                     "r"(bytesV + bytesI + bytesE)
+                     "r"(bytesV + bytesE)
                      : "memory");
         if (bytesV)
             asm volatile(
                 "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
                     "r"(smem_u32(stage_raw)), "l"(recVisc + S0), "r"(bytesV), "r"(ubar)
                 : "memory");
-        if (bytesI)
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-                    "r"(smem_u32(stage_raw + bytesV)), "l"(recInv + S0), "r"(bytesI), "r"(ubar)
-                : "memory");
         if (bytesE)
             asm volatile(
                 "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-                    "r"(smem_u32(stage_raw + bytesV + bytesI)), "l"(esup_slot + S0a), "r"(bytesE),
-                    "r"(ubar)
+                    "r"(smem_u32(stage_raw + bytesV)), "l"(esup_slot + S0a), "r"(bytesE), "r"(ubar)
                 : "memory");
     }
     const int p = p0 + threadIdx.x;
@@ -1147,19 +1138,10 @@ k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __rest
         return;
     }
     if (!live) return;
-    Acc a0, a1, a2, a3, v1, v2, v3;
-    a0.init(); a1.init(); a2.init(); a3.init();
+    Acc v1, v2, v3;
     v1.init();
     v2.init();
     v3.init();
-    if (FIRST)
-        for (int s = s0; s < s1; ++s) {
-            const float4 ri = si[s - S0];
-            a0.add(ri.x);
-            a1.add(ri.y);
-            a2.add(ri.z);
-            a3.add(ri.w);
-        }
     for (int s = s0; s < s1; s += 8) {
         float2 ml[8];
 #pragma unroll
@@ -1174,11 +1156,9 @@ k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __rest
                 v3.add(ml[j].x * rv.z + ml[j].y * rv.w);
             }
     }
-    const float4 inv =
-        FIRST ? make_float4(a0.value(), a1.value(), a2.value(), a3.value()) : make_float4(0.f, 0.f, 0.f, 0.f);
-    node_finish<FIRST, LAST>(p, inv, v1.value(), v2.value(), v3.value(), invSum, gc, gf, U, Uhi,
-                             Ulo, invM, rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, Eo,
-                             Po, Tout, RMACH);
+    node_finish<false, LAST>(p, make_float4(0.f, 0.f, 0.f, 0.f), v1.value(), v2.value(), v3.value(),
+                             invSum, gc, gf, U, Uhi, Ulo, invM, rk_fact, bcflag, bcval, nrm, WX,
+                             WY, U1, RHO, VX, VY, Eo, Po, Tout, RMACH);
 }
 
 cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, const int* esup_slot,
@@ -1191,17 +1171,15 @@ cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, c
                               float* VX, float* VY, float* E, float* P, float* Tout, float* RMACH,
                               int bulk_smem, int* bulk_err) {
     const unsigned grid = blocks_for(npoin, kNodeTB);
-    if (bulk_smem > 0 && viscous) {  // the bulk-copy variant
-#define CFD_BULK_ARGS                                                                            \
-    npoin, esup_ptr, esup_slot, mulam, recInv, recVisc, invSum, gc, gf, U, Uhi, Ulo, invM, rk_fact, \
-        bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH, bulk_err
-        if (first_stage)
-            k_node_mixed_bulk<true, false><<<grid, kNodeTB, bulk_smem, st>>>(CFD_BULK_ARGS);
-        else if (last_stage)
-            k_node_mixed_bulk<false, true><<<grid, kNodeTB, bulk_smem, st>>>(CFD_BULK_ARGS);
+    if (bulk_smem > 0 && viscous && !first_stage) {  // the bulk-copy variant
+        if (last_stage)
+            k_node_mixed_bulk<true><<<grid, kNodeTB, bulk_smem, st>>>(
+                npoin, esup_ptr, esup_slot, mulam, recVisc, invSum, gc, gf, U, Uhi, Ulo, invM,
+                rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH, bulk_err);
         else
-            k_node_mixed_bulk<false, false><<<grid, kNodeTB, bulk_smem, st>>>(CFD_BULK_ARGS);
-#undef CFD_BULK_ARGS
+            k_node_mixed_bulk<false><<<grid, kNodeTB, bulk_smem, st>>>(
+                npoin, esup_ptr, esup_slot, mulam, recVisc, invSum, gc, gf, U, Uhi, Ulo, invM,
+                rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, E, P, Tout, RMACH, bulk_err);
         g_launches.fetch_add(1, std::memory_order_relaxed);
         return cudaGetLastError();
     }
@@ -1226,17 +1204,15 @@ int node_bulk_smem(const int* esup_ptr, int npoin) {
     long worst = 0;
     for (int p0 = 0; p0 < npoin; p0 += kNodeTB) {
         const int S0 = esup_ptr[p0], S1 = esup_ptr[std::min(p0 + kNodeTB, npoin)];
-        const long b = 32L * (S1 - S0) + 4L * (((S1 + 3) & ~3) - (S0 & ~3));  // first stage
+        const long b = 16L * (S1 - S0) + 4L * (((S1 + 3) & ~3) - (S0 & ~3));
         worst = std::max(worst, b);
     }
     if (worst > 200 * 1024) return 0;
     const int smem = (int)std::max(worst, 16L);
-    if (cudaFuncSetAttribute(k_node_mixed_bulk<true, false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_node_mixed_bulk<false, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_node_mixed_bulk<false, false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
+    if (cudaFuncSetAttribute(k_node_mixed_bulk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_node_mixed_bulk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess) {
         (void)cudaGetLastError();
         return 0;
     }
