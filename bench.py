@@ -465,7 +465,12 @@ def main_ours(args):
         Sm.close()
         forms["mixed_vs_fp64"] = {
             "steps": NC, "estab_mode": "regularized", "guess": "previous",
+            # the whole conserved state; per variable against its own norm; rho*v (small at
+            # 2 degrees) also against the momentum scale max(|rho*u|, |rho*v|)
+            "state_rel_l2": rel_l2(Um, Ur),
             "rel_l2": [rel_l2(Um[:, q], Ur[:, q]) for q in range(4)],
+            "rho_v_rel_l2_momentum_scale": float(np.linalg.norm(Um[:, 2] - Ur[:, 2]) / max(
+                np.linalg.norm(Ur[:, 1]), np.linalg.norm(Ur[:, 2]))),
             "force_rel_err": float(np.hypot(repm.fx[0] - repr_.fx[0], repm.fy[0] - repr_.fy[0])
                                    / np.hypot(repr_.fx[0], repr_.fy[0]))}
         if net is not None:
