@@ -202,7 +202,10 @@ def _geometric_ratio(n_int: int, span: float, first: float) -> float:
     lo, hi = 1.0 + 1e-12, 2.0
     for _ in range(200):
         mid = 0.5 * (lo + hi)
-        s = first * (mid ** n_int - 1.0) / (mid - 1.0)
+        try:
+            s = first * (mid ** n_int - 1.0) / (mid - 1.0)
+        except OverflowError:  # mid^n beyond the double range: far above the span
+            s = float("inf")
         if s > span:
             hi = mid
         else:
