@@ -136,3 +136,20 @@ def test_mixed_local_time_step(gpu_lib):
     print("worst rel L2 per variable", worst, "force", fworst)
     assert max(worst) <= REL_TOL_STATE
     assert fworst <= REL_TOL_FORCE
+
+
+def test_bulk_copy_node_pass_matches_plain_loads(gpu_lib, monkeypatch):
+    """The node passes that stage their slot records with bulk copies (the default) sum the
+    same products in the same order as the plain-load passes (CFD_NODE_BULK=0)."""
+    from cfd_gb300 import abi, solver
+    k = small_case(3, scale=32, seed=8, estab_mode=2)
+    monkeypatch.setenv("CFD_NODE_BULK", "0")
+    a = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    monkeypatch.delenv("CFD_NODE_BULK")
+    b = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    a.step(4)
+    b.step(4)
+    ua, ub = a.state()["U"], b.state()["U"]
+    assert np.abs(ua - ub).max() <= 1e-14 * np.abs(ua).max()
+    a.close()
+    b.close()
