@@ -135,6 +135,8 @@ SIGNATURES = {
     "cfd_ctx_graph_state": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_set_force_visc": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smooth": (C.c_int, [_P, _ip, _dp]),
+    "cfd_ctx_set_smoothing": (C.c_int, [_P, C.c_int]),
+    "cfd_ctx_smoothing_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_smoothing": (C.c_int, [_dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _ip, _dp]),
     "cfd_ctx_force_visc": (C.c_int, [_P, _dp, _dp, _dp]),
     "cfd_force_visc": (C.c_int, [_ip] * 7 + [_dp] * 4 + [_dp] * 10 + [_dp, _dp, _dp]),

@@ -319,6 +319,19 @@ int cfd_ctx_set_force_visc(cfd_ctx* ctx, int each_step) {
     return CFD_OK;
 }
 
+int cfd_ctx_set_smoothing(cfd_ctx* ctx, int every) {
+    if (!ctx) return arg_error("ctx");
+    TRY(ctx->impl.set_smoothing(every));
+    return CFD_OK;
+}
+
+int cfd_ctx_smoothing_stats(cfd_ctx* ctx, long long* out2) {
+    if (!ctx || !out2) return arg_error("null pointer");
+    out2[0] = ctx->impl.smooth_steps;
+    out2[1] = ctx->impl.smooth_sweeps;
+    return CFD_OK;
+}
+
 int cfd_ctx_force_visc(cfd_ctx* ctx, double* F_VX, double* F_VY, double* skin) {
     if (!ctx || !F_VX || !F_VY) return arg_error("null pointer");
     Ctx& c = ctx->impl;

@@ -23,6 +23,12 @@ void graph_free(cfd_mpnn_graph* g);
 }  // namespace mpnn
 
 // mesh smoothing (smooth.cu)
+__global__ void k_smooth_prep(int n, const double* xpos, const double* ypos, const double* X,
+                              const double* Y, double* tol, double* xb, double* yb);
+__global__ void k_smooth_w(int n, const double* xpos, const double* ypos, const double* X,
+                           const double* Y, const double* xb, const double* yb,
+                           const StepScal* sc, double* WX, double* WY, float2* Wf, float2* Xhi,
+                           float2* Xlo);
 void smoothing_colours(const Adjacency& adj, int npoin, std::vector<int>& order,
                        std::vector<int>& offs);
 int smooth_on_device(cudaStream_t st, int npoin, int nelem, const int4* elem,
@@ -198,6 +204,14 @@ struct Ctx {
     int set_guess_net(cfd_mpnn* n, double gate);
     int force_visc_now();
     int smooth(int* iters, double* min_quality);
+    int smooth_setup();
+    int set_smoothing(int every);
+    int smooth_in_step(cudaStream_t s, double* WX, double* WY, float2* Wf);
+    int smooth_every = 0;  // smooth the moved mesh every this many steps (0: never)
+    double *d_sm_tol = nullptr, *d_sm_xb = nullptr, *d_sm_yb = nullptr;
+    long long smooth_steps = 0, smooth_sweeps = 0;
+    int smooth_max_star = -1;
+    bool smoothing_now = false;
     int set_force_visc_each_step(bool on);
     int step_once();
     int step_once_mixed();

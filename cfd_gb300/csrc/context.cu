@@ -281,10 +281,9 @@ int Ctx::force_visc_now() {
     return CFD_OK;
 }
 
-// The setup smoothing of the resident mesh (ns2DComp.ALE.f90:62-72: the moving and the
-// fixed mesh-motion nodes stay), then the mesh's geometry again (normales, deriv, masses,
-// Laplacian) as at setup
-int Ctx::smooth(int* iters, double* min_quality) {
+// The smoothing's adjacency, node colours and fixed nodes (the moving and the fixed
+// mesh-motion nodes stay), uploaded once
+int Ctx::smooth_setup() {
     const int N = npoin;
     int st;
     if (!d_psup_ptr) {
@@ -300,6 +299,15 @@ int Ctx::smooth(int* iters, double* min_quality) {
         if ((st = dalloc(&d_sm_scal, 3))) return st;
         if ((st = dalloc(&d_sm_flags, 2))) return st;
     }
+    return CFD_OK;
+}
+
+// The setup smoothing of the resident mesh (ns2DComp.ALE.f90:62-72), then the mesh's
+// geometry again (normales, deriv, masses, Laplacian) as at setup
+int Ctx::smooth(int* iters, double* min_quality) {
+    const int N = npoin;
+    int st = smooth_setup();
+    if (st) return st;
     int max_star = 0;
     for (int p = 0; p < N; ++p) max_star = std::max(max_star, adj.esup_ptr[p + 1] - adj.esup_ptr[p]);
     st = smooth_on_device(stream, N, nelem, d_elem, d_esup_ptr, d_esup_slot, d_psup_ptr, d_psup,
@@ -316,6 +324,54 @@ int Ctx::smooth(int* iters, double* min_quality) {
     }
     CFD_CUDA(cudaStreamSynchronize(stream));
     return tcollect();
+}
+
+// The per-step smoothing of the moved mesh (before its geometry): the setTol_move path of
+// smoothing.f90:372-386 with the step's displacement, then W of the whole move
+int Ctx::set_smoothing(int every) {
+    if (every < 0) {
+        set_last_message("smoothing interval below 0");
+        return CFD_ERR_ARG;
+    }
+    int st;
+    if (every > 0) {
+        if ((st = smooth_setup())) return st;
+        if (!d_sm_tol) {
+            if ((st = dalloc(&d_sm_tol, npoin))) return st;
+            if ((st = dalloc(&d_sm_xb, npoin))) return st;
+            if ((st = dalloc(&d_sm_yb, npoin))) return st;
+        }
+        CFD_CUDA(cudaStreamSynchronize(stream));
+    }
+    smooth_every = every;
+    return CFD_OK;
+}
+
+int Ctx::smooth_in_step(cudaStream_t s, double* WX, double* WY, float2* Wf) {
+    const int N = npoin;
+    int st;
+    const unsigned g = blocks_for(N, 256);
+    CFD_LAUNCH(k_smooth_prep, g, 256, 0, s, N, d_pos[0], d_pos[1], d_X, d_Y, d_sm_tol, d_sm_xb,
+               d_sm_yb);
+    if (smooth_max_star < 0) {
+        smooth_max_star = 0;
+        for (int p = 0; p < N; ++p)
+            smooth_max_star = std::max(smooth_max_star, adj.esup_ptr[p + 1] - adj.esup_ptr[p]);
+    }
+    const int max_star = smooth_max_star;
+    int iters = 0;
+    st = smooth_on_device(s, N, nelem, d_elem, d_esup_ptr, d_esup_slot, d_psup_ptr, d_psup,
+                          d_sm_fixed, d_X, d_Y, d_sm_tol, sm_offs, d_sm_order, d_sm_flag,
+                          d_sm_scal, d_sm_flags, &iters, nullptr, max_star);
+    if (st) return st;
+    smooth_steps += 1;
+    smooth_sweeps += iters;
+    const bool mixed = prec == CFD_PREC_MIXED;
+    CFD_LAUNCH(k_smooth_w, g, 256, 0, s, N, d_pos[0], d_pos[1], d_X, d_Y, d_sm_xb, d_sm_yb,
+               (const StepScal*)d_scal,
+               WX, WY, mixed ? Wf : (float2*)nullptr, mixed ? d_Xhi : (float2*)nullptr,
+               mixed ? d_Xlo : (float2*)nullptr);
+    return CFD_OK;
 }
 
 // Every step computes FORCE_VISC at the reference's print-block point (on), or only
@@ -423,6 +479,10 @@ int Ctx::step_once() {
     tstop(TM_GRAD);
     CFD_LAUNCH(k_motion_update, blocks_for(N, TB), TB, 0, stream, N, d_pos[0], d_pos[1], d_scal,
                d_X, d_Y, d_WX, d_WY);
+    if (smooth_every > 0 && iter % smooth_every == 0) {
+        st = smooth_in_step(stream, d_WX, d_WY, nullptr);
+        if (st) return st;
+    }
     if (fv_each) {  // FORCE_VISC at the print block's point: moved mesh, previous dNx
         st = force_visc_now();
         if (st) return st;
@@ -873,6 +933,7 @@ int Ctx::enqueue_mixed(bool learned) {
         tstop(TM_GRAD);
         CFD_LAUNCH(k_motion_update_mixed, branch_grid(N, TB, s), TB, 0, s, N, d_pos[0], d_pos[1],
                    d_scal, d_X, d_Y, d_WX_n, d_WY_n, d_Xhi, d_Xlo, d_Wf_n);
+        if (smoothing_now && (st = smooth_in_step(s, d_WX_n, d_WY_n, d_Wf_n))) return st;
         if (prm.moving == 1 && (st = geometry_mixed(false, false, true, s))) return st;
         return CFD_OK;
     };
@@ -1023,7 +1084,10 @@ int Ctx::step_once_mixed() {
         guess_first = false;
     }
     bandera_host += 1;
-    if (graphs_on && !learned && mixed_steps > 0) {
+    // a step that smooths its moved mesh waits on the host for the sweeps' convergence
+    // flags: it is enqueued launch by launch
+    smoothing_now = smooth_every > 0 && iter % smooth_every == 0;
+    if (graphs_on && !learned && !smoothing_now && mixed_steps > 0) {
         bool launched = false;
         int st = launch_step_graph(&launched);
         if (st) return st;

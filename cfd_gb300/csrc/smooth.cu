@@ -249,6 +249,50 @@ __global__ void k_sm_quality(SmArgs a, unsigned long long* qbits) {
 
 }  // namespace
 
+// Per-step smoothing inside the time loop (the setTol_move path): tol = |xpos| + |ypos|,
+// the step's displacement, and the mesh before smoothing
+__global__ void k_smooth_prep(int n, const double* __restrict__ xpos,
+                              const double* __restrict__ ypos, const double* __restrict__ X,
+                              const double* __restrict__ Y, double* __restrict__ tol,
+                              double* __restrict__ xb, double* __restrict__ yb) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        tol[p] = fabs(xpos[p]) + fabs(ypos[p]);
+        xb[p] = X[p];
+        yb[p] = Y[p];
+    }
+}
+
+// ... and after it: W is the whole move of the step over DTMIN (the prescribed displacement
+// plus the smoothing's), so that the geometric conservation law sees the mesh that is
+// used; the mixed form also refreshes its float shadows of W and of (X, Y)
+__global__ void k_smooth_w(int n, const double* __restrict__ xpos, const double* __restrict__ ypos,
+                           const double* __restrict__ X, const double* __restrict__ Y,
+                           const double* __restrict__ xb, const double* __restrict__ yb,
+                           const StepScal* __restrict__ sc, double* __restrict__ WX,
+                           double* __restrict__ WY, float2* __restrict__ Wf,
+                           float2* __restrict__ Xhi, float2* __restrict__ Xlo) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const double x = X[p], y = Y[p];
+        const double dx = x - xb[p], dy = y - yb[p];
+        if (dx == 0.0 && dy == 0.0) continue;
+        const double mx = xpos[p] + dx, my = ypos[p] + dy;
+        if (Wf) {
+            const double wx = mx * sc->inv_dtmin, wy = my * sc->inv_dtmin;
+            WX[p] = wx;
+            WY[p] = wy;
+            Wf[p] = make_float2(d2f_trunc(wx), d2f_trunc(wy));
+            float hx, lx, hy, ly;
+            split_bits(x, hx, lx);
+            split_bits(y, hy, ly);
+            Xhi[p] = make_float2(hx, hy);
+            Xlo[p] = make_float2(lx, ly);
+        } else {
+            WX[p] = mx / sc->dtmin;
+            WY[p] = my / sc->dtmin;
+        }
+    }
+}
+
 // Greedy colouring of the point-neighbour graph in node order; returns the nodes grouped by
 // colour (node order within a colour) and the colour offsets.
 void smoothing_colours(const Adjacency& adj, int npoin, std::vector<int>& order,

@@ -121,9 +121,11 @@ def residuals(U_old, U_new):
 
 
 def run_case(directory, out_dir=None, precision=abi.CFD_PREC_FP64, maxiter=None, engine=None,
-             smoothing=None, verbose=False):
+             smoothing=None, smooth_every=0, verbose=False):
     """Run the case in `directory` for MAXITER (or `maxiter`) iterations and write the
-    reference's files into `out_dir` (default: the case directory).  Returns a summary."""
+    reference's files into `out_dir` (default: the case directory).  `smooth_every` > 0
+    smooths the moved mesh every that many steps (the commented-out per-step smoothing,
+    meshMove.f90:133, on the setTol_move path).  Returns a summary."""
     case = read_case(directory)
     out_dir = out_dir or directory
     os.makedirs(out_dir, exist_ok=True)
@@ -139,6 +141,8 @@ def run_case(directory, out_dir=None, precision=abi.CFD_PREC_FP64, maxiter=None,
     if p.irestart == 1:
         _, _, U, T, _ = read_restart(os.path.join(directory, name + ".RST"), case.npoin)
         engine.set_state(U, T, U[:, 1] / U[:, 0], U[:, 2] / U[:, 0])
+    if smooth_every > 0:
+        engine.set_smoothing(smooth_every)
     viscous = p.fmu != 0.0
     if viscous:
         engine.set_force_visc(True)

@@ -272,6 +272,16 @@ class Solver:
         check(abi.lib().cfd_ctx_set_force_visc(self.h, 1 if each_step else 0),
               "cfd_ctx_set_force_visc")
 
+    def set_smoothing(self, every):
+        """Smooth the moved mesh every `every` steps inside the time loop (0: never)."""
+        check(abi.lib().cfd_ctx_set_smoothing(self.h, int(every)), "cfd_ctx_set_smoothing")
+
+    def smoothing_stats(self):
+        """(steps smoothed, smoothing sweeps) so far."""
+        out = (C.c_longlong * 2)()
+        check(abi.lib().cfd_ctx_smoothing_stats(self.h, out), "cfd_ctx_smoothing_stats")
+        return int(out[0]), int(out[1])
+
     def force_visc(self):
         """(F_VX[nset_numb], F_VY[nset_numb], SKIN.DAT rows (nedges, 3))."""
         fvx, fvy = np.zeros(10), np.zeros(10)

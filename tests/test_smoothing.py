@@ -87,3 +87,82 @@ def test_resident_smoothing_then_step(gpu_lib):
     rep = s.step(2)
     assert np.isfinite(s.state()["U"]).all() and rep.iter == 2
     s.close()
+
+
+def _pair(prec, every, **over):
+    """Two contexts of the jittered moving cylinder, the second smoothing its moved mesh
+    every `every` steps."""
+    from cfd_gb300 import abi, solver
+    k = small_case(2, scale=16, seed=1, **over)
+    P = abi.CFD_PREC_FP64 if prec == "fp64" else abi.CFD_PREC_MIXED
+    a, b = solver.Solver(k, precision=P), solver.Solver(k, precision=P)
+    b.set_smoothing(every)
+    return k, a, b
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_smoothing_in_time_loop_step(gpu_lib, oracle, prec):
+    """One step with the moved mesh smoothed (the setTol_move path with the step's
+    displacement) against the same step without: no node moves further than the two
+    Laplace passes and NITER sweeps allow (1.5 + 1.5 + 1 times |XPOS| + |YPOS|), a node
+    that the motion did not move stays, the worst element does not get worse, W is the
+    whole move over DTMIN, and the next step's geometry is the smoothed mesh's."""
+    k, a, b = _pair(prec, 1)
+    x0, y0 = k.x.copy(), k.y.copy()
+    ra, rb = a.step(1), b.step(1)
+    assert ra.dtmin == rb.dtmin
+    sa, sb = a.state(), b.state()
+    xp, yp = a.motion()
+    tol = np.abs(xp) + np.abs(yp)
+    assert tol.max() > 0
+    move = np.abs(sb["X"] - sa["X"]) + np.abs(sb["Y"] - sa["Y"])
+    scale = np.abs(x0).max()
+    assert (move <= 4.0 * tol * (1 + 1e-9) + 1e-15 * scale).all()
+    assert move.max() > 0
+    assert (move[tol == 0] == 0).all()
+    assert quality(sb["X"], sb["Y"], k.inpoel).min() >= quality(sa["X"], sa["Y"], k.inpoel).min()
+    fb = b.fields()
+    dt = rb.dtmin
+    for w, xn, xs in (("W_X", "X", x0), ("W_Y", "Y", y0)):
+        whole = sb[xn] - xs
+        assert np.abs(fb[w] * dt - whole).max() <= 1e-9 * np.abs(whole).max()
+    # the geometry of the smoothed mesh (the mixed form keeps it in FP32)
+    area_b = oracle.deriv(sb["X"], sb["Y"], k.inpoel)["area"]
+    area_a = oracle.deriv(sa["X"], sa["Y"], k.inpoel)["area"]
+    rtol = 1e-12 if prec == "fp64" else 2e-6
+    assert np.allclose(b.geometry()["area"], area_b, rtol=rtol, atol=0)
+    assert (np.abs(area_a - area_b) > 10 * rtol * np.abs(area_b)).any()
+    assert b.smoothing_stats()[0] == 1 and b.smoothing_stats()[1] >= 0
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_gpu_smoothing_in_time_loop_mixed_matches_fp64(gpu_lib):
+    """The mixed form with per-step smoothing against the FP64 form with it, over 12 steps
+    smoothing every 2nd: the same state within the mixed form's tolerance; the graph replays
+    the steps in between."""
+    from cfd_gb300 import abi, solver
+    k = small_case(2, scale=16, seed=1, estab_mode=2)
+    k.params.fsafe = min(k.params.fsafe, 0.25)
+    f = solver.Solver(k, precision=abi.CFD_PREC_FP64)
+    m = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    for s in (f, m):
+        s.set_smoothing(2)
+    worst = 0.0
+    for _ in range(12):
+        rf, rm = f.step(1), m.step(1)
+        assert abs(rm.dtmin - rf.dtmin) <= 1e-6 * rf.dtmin
+        uf, um = f.state()["U"], m.state()["U"]
+        worst = max(worst, max(np.linalg.norm(um[:, q] - uf[:, q]) / np.linalg.norm(uf[:, q])
+                               for q in (0, 1, 3)))
+    xf, xm = f.state()["X"], m.state()["X"]
+    print("worst rel L2", worst, "mesh", np.abs(xf - xm).max())
+    assert worst <= 1e-6
+    assert np.abs(xf - xm).max() <= 1e-6 * np.abs(xf).max()
+    assert f.smoothing_stats()[0] == 6 and m.smoothing_stats()[0] == 6
+    assert m.graph_state()[1] > 0
+    f.close()
+    m.close()
+
