@@ -747,12 +747,461 @@ __global__ void __launch_bounds__(32 * IW, 2) k_infer_layer(
     }
 }
 
+// ------------------------------------------------------------------ BF16 inference, tcgen05
+// The same passes with the GEMMs on the 5th-generation tensor cores.  A block of 8 warps
+// owns a tile of 128 nodes (the MMA's M): the warps gather the tile's [h; agg] rows (16
+// nodes each, the arithmetic of the mma.sync pass) into shared memory, one thread issues
+// tcgen05.mma (BF16 operands from shared memory, FP32 accumulators in tensor memory) and
+// commits it to an mbarrier, and after the bounded wait every warp reads its 32 rows of
+// the accumulator with tcgen05.ld for the epilogue.  The update GEMM (N = 64, K = 128) and
+// the next layer's P|Q GEMM (N = 128, K = 64) use the same 128 tensor-memory columns one
+// after the other.
+namespace tc {
+constexpr int TM = 128;          // nodes per tile
+constexpr int NTHR = 256;        // 8 warps
+constexpr unsigned TMEM_COLS = 128;
+// K-major operands in the no-swizzle core-matrix layout: a core matrix is 8 rows x 16
+// bytes (128 contiguous bytes); the core matrices of one 8-row group lie along K, 128 B
+// apart (the descriptor's leading byte offset); the 8-row groups lie SBO bytes apart.
+constexpr int LBO = 128;
+constexpr int SBO_X = 16 * 2 * HID;  // the tile, 128 rows x K = 128 (h, then agg)
+constexpr int SBO_U = 16 * 2 * HID;  // U: N = 64 rows x K = 128
+constexpr int SBO_W = 16 * HID;      // [A; B]: N = 128 rows x K = 64
+constexpr int X_BYTES = TM * 2 * HID * 2;
+constexpr int U_BYTES = HID * 2 * HID * 2;
+constexpr int W_BYTES = 2 * HID * HID * 2;
+constexpr int F_FLOATS = HID * F_IN + HID;  // the largest float table (W_in, b_in)
+static_assert(HID * E_F + 2 * HID + OUT * HID + OUT <= F_FLOATS, "float tables");
+constexpr int SMEM = X_BYTES + U_BYTES + W_BYTES + 4 * F_FLOATS + 16;
+
+__host__ __device__ constexpr int cm_off(int r, int k, int sbo) {
+    return (r >> 3) * sbo + (k >> 3) * LBO + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// shared-memory matrix descriptor: start address, leading and stride byte offsets (all
+// >> 4), the descriptor version 1 at bit 46, base offset 0, no swizzle
+__device__ __forceinline__ unsigned long long sdesc(unsigned saddr, unsigned sbo) {
+    return (unsigned long long)((saddr & 0x3FFFFu) >> 4) |
+           ((unsigned long long)(LBO >> 4) << 16) | ((unsigned long long)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator (bit 4), A and B BF16 (bits 7,
+// 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr unsigned idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) |
+           ((unsigned)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ unsigned su32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// this thread's st.shared become visible to the tensor cores' reads
+__device__ __forceinline__ void fence_smem_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mma(unsigned d, unsigned long long a, unsigned long long b,
+                                    unsigned idesc, unsigned accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        :
+        : "r"(d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void commit(unsigned mbar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+        : "memory");
+}
+
+// bounded wait on the mbarrier's phase of the given parity
+__device__ __forceinline__ bool wait_parity(unsigned mbar, unsigned parity) {
+    unsigned done = 0;
+    for (long long k = 0; k < kSpinLimit && !done; ++k)
+        asm volatile(
+            "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; "
+            "selp.u32 %0, 1, 0, q; }"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
+// 16 consecutive FP32 columns of this thread's tensor-memory lane; the wait is tied to
+// the registers so that no use moves above it
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                   "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                   "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// rows x cols of a row-major BF16 matrix into the core-matrix layout (16-byte chunks)
+__device__ __forceinline__ void load_cm(unsigned char* dst, int sbo, const bf16* src, int rows,
+                                        int cols) {
+    const int per_row = cols / 8;
+    for (int q = threadIdx.x; q < rows * per_row; q += blockDim.x) {
+        const int r = q / per_row, k = (q - r * per_row) * 8;
+        *reinterpret_cast<uint4*>(dst + cm_off(r, k, sbo)) =
+            *reinterpret_cast<const uint4*>(src + (size_t)r * cols + k);
+    }
+}
+
+__device__ __forceinline__ unsigned pack2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const unsigned*>(&h);
+}
+
+// ENC: h0 = relu(W_in f + b_in), then P|Q of layer 0.  Otherwise layer l: aggregation,
+// update GEMM, residual, then P|Q of layer l+1 (has_next) or the decoder.
+template <bool ENC>
+__global__ void __launch_bounds__(NTHR, 2) k_infer_tc(
+    int n, int l, const int* __restrict__ ptr, const int* __restrict__ nbr,
+    const float* __restrict__ e, const float* __restrict__ f, const float* __restrict__ w,
+    const bf16* __restrict__ wb, int has_next, const bf16* __restrict__ pq_in,
+    bf16* __restrict__ hb, bf16* __restrict__ pq_out, float* __restrict__ y,
+    const int* __restrict__ gate, int* __restrict__ err) {
+    if (gate && !*gate) return;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* Xs = smem_raw;
+    unsigned char* Us = Xs + X_BYTES;
+    unsigned char* Ws = Us + U_BYTES;
+    float* fl = reinterpret_cast<float*>(Ws + W_BYTES);
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(fl + F_FLOATS);
+    unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 1);
+    int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // float tables: ENC W_in, b_in; layers C, c, u, W_out, b_out
+    float *Cs = fl, *cs = fl + HID * E_F, *us = cs + HID, *wo = us + HID;
+    const int has_pq = ENC || has_next;
+    if (ENC) {
+        for (int q = tid; q < F_FLOATS; q += NTHR) fl[q] = w[OFF_W_IN + q];
+    } else {
+        const float* W = w + layer_off(l);
+        load_cm(Us, SBO_U, wb + layer_off(l) + L_U, HID, 2 * HID);
+        for (int q = tid; q < HID * E_F; q += NTHR) Cs[q] = W[L_C + q];
+        for (int q = tid; q < HID; q += NTHR) {
+            cs[q] = W[L_c + q];
+            us[q] = W[L_u + q];
+        }
+        if (!has_next)
+            for (int q = tid; q < OUT * HID + OUT; q += NTHR) wo[q] = w[OFF_W_OUT + q];
+    }
+    if (has_pq) load_cm(Ws, SBO_W, wb + layer_off(ENC ? 0 : l + 1) + L_A, 2 * HID, HID);
+    const unsigned ubar = su32(mbar);
+    if (tid == 0) {
+        *abort_flag = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        __syncwarp();
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         su32(tslot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_smem_async();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const unsigned tbase = *tslot;
+    const unsigned xa = su32(Xs), ua = su32(Us), wa = su32(Ws);
+    // epilogue geometry: warp w reads tensor-memory lanes 32 (w % 4) .. (its 32 rows) and
+    // half w / 4 of the accumulator's columns
+    const int q4 = warp & 3, half = warp >> 2;
+    const int erow = 32 * q4 + lane;
+    const unsigned tlane = tbase + ((unsigned)(32 * q4) << 16);
+    unsigned phase = 0;
+    bool pending = false;  // a commit that this block has not seen arrive
+    float acc_hi[8];
+    const int ntile = (n + TM - 1) / TM;
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int tb = tile * TM;
+        if (ENC) {
+            // lane l of warp w owns row 16 w + l / 2 and the outputs [32 (l % 2), +32)
+            const int r = 16 * warp + (lane >> 1), o0 = 32 * (lane & 1), node = tb + r;
+            float fi[F_IN];
+#pragma unroll
+            for (int k = 0; k < F_IN; ++k) fi[k] = node < n ? f[(size_t)node * F_IN + k] : 0.f;
+            unsigned w16[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                float hv[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int o = o0 + 2 * q + u;
+                    float a = fl[HID * F_IN + o];
+#pragma unroll
+                    for (int k = 0; k < F_IN; ++k) a += fl[o * F_IN + k] * fi[k];
+                    hv[u] = node < n ? fmaxf(a, 0.f) : 0.f;
+                }
+                w16[q] = pack2(hv[0], hv[1]);
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const uint4 wv = make_uint4(w16[4 * v], w16[4 * v + 1], w16[4 * v + 2], w16[4 * v + 3]);
+                *reinterpret_cast<uint4*>(Xs + cm_off(r, o0 + 8 * v, SBO_X)) = wv;
+                if (node < n)
+                    *reinterpret_cast<uint4*>(hb + (size_t)node * HID + o0 + 8 * v) = wv;
+            }
+        } else {
+            // [h; agg] rows, 8 nodes per pass: lane l owns row 16 w + l / 4 (+8) and the 16
+            // features [16 (l % 4), +16)
+            for (int pass = 0; pass < 2; ++pass) {
+                const int r = 16 * warp + (lane >> 2) + 8 * pass, f0 = 16 * (lane & 3),
+                          node = tb + r;
+                float acc16[16], pz[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc16[q] = 0.f;
+                uint4 hv4[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+                if (node < n) {
+                    const uint4* hp = reinterpret_cast<const uint4*>(hb + (size_t)node * HID + f0);
+                    const uint4* pp =
+                        reinterpret_cast<const uint4*>(pq_in + (size_t)node * 2 * HID + f0);
+#pragma unroll
+                    for (int v = 0; v < 2; ++v) {
+                        hv4[v] = hp[v];
+                        const uint4 pv = pp[v];
+                        const unsigned w4[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float2 f2 =
+                                __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w4[u]));
+                            pz[8 * v + 2 * u] = f2.x + cs[f0 + 8 * v + 2 * u];
+                            pz[8 * v + 2 * u + 1] = f2.y + cs[f0 + 8 * v + 2 * u + 1];
+                        }
+                    }
+                    const int k0 = ptr[node], k1 = ptr[node + 1];
+                    for (int k = k0; k < k1; ++k) {
+                        const int j = nbr[k];
+                        const float e0 = e[3 * (size_t)k], e1 = e[3 * (size_t)k + 1],
+                                    e2 = e[3 * (size_t)k + 2];
+                        const uint4* qp = reinterpret_cast<const uint4*>(
+                            pq_in + (size_t)j * 2 * HID + HID + f0);
+                        const uint4 qa = qp[0], qb = qp[1];
+                        const unsigned w8[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const float2 q2 = __bfloat1622float2(
+                                *reinterpret_cast<const __nv_bfloat162*>(&w8[u]));
+                            const int o = f0 + 2 * u;
+                            const float z0 = pz[2 * u] + q2.x +
+                                             (Cs[o * 3] * e0 + Cs[o * 3 + 1] * e1 + Cs[o * 3 + 2] * e2);
+                            const float z1 =
+                                pz[2 * u + 1] + q2.y +
+                                (Cs[o * 3 + 3] * e0 + Cs[o * 3 + 4] * e1 + Cs[o * 3 + 5] * e2);
+                            acc16[2 * u] += fmaxf(z0, 0.f);
+                            acc16[2 * u + 1] += fmaxf(z1, 0.f);
+                        }
+                    }
+                    const float inv = 1.f / (float)max(k1 - k0, 1);
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) acc16[q] *= inv;
+                }
+#pragma unroll
+                for (int v = 0; v < 2; ++v) {
+                    *reinterpret_cast<uint4*>(Xs + cm_off(r, f0 + 8 * v, SBO_X)) = hv4[v];
+                    *reinterpret_cast<uint4*>(Xs + cm_off(r, HID + f0 + 8 * v, SBO_X)) =
+                        make_uint4(pack2(acc16[8 * v], acc16[8 * v + 1]),
+                                   pack2(acc16[8 * v + 2], acc16[8 * v + 3]),
+                                   pack2(acc16[8 * v + 4], acc16[8 * v + 5]),
+                                   pack2(acc16[8 * v + 6], acc16[8 * v + 7]));
+                }
+            }
+        }
+        fence_smem_async();
+        fence_before();
+        __syncthreads();
+        if (*abort_flag) break;
+        if (!ENC) {
+            // v = U [h; agg]: 8 MMAs of K = 16 into columns 0..63
+            if (tid == 0) {
+                fence_after();
+#pragma unroll
+                for (int kk = 0; kk < 2 * HID / 16; ++kk)
+                    mma(tbase, sdesc(xa + kk * 2 * LBO, SBO_X), sdesc(ua + kk * 2 * LBO, SBO_U),
+                        idesc_bf16(TM, HID), kk > 0 ? 1u : 0u);
+                commit(ubar);
+            }
+            pending = true;
+            // the warp goes on only as a whole (tcgen05.ld is warp-collective)
+            if (!__all_sync(0xffffffffu, wait_parity(ubar, phase & 1))) {
+                atomicExch(err, (int)CFD_ERR_BARRIER);
+                *abort_flag = 1;
+            } else {
+                pending = false;
+                phase += 1;
+                fence_after();
+                // h <- h + relu(v + u) on this thread's row, columns [32 half, +32)
+                const int node = tb + erow;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float acc[8];
+                    if (c % 2 == 0) {
+                        float a16[16];
+                        tmem_ld16(tlane + 32 * half + 8 * c, a16);
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            acc[i] = a16[i];
+                            acc_hi[i] = a16[8 + i];
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) acc[i] = acc_hi[i];
+                    }
+                    const int k0 = 32 * half + 8 * c;
+                    uint4* xp = reinterpret_cast<uint4*>(Xs + cm_off(erow, k0, SBO_X));
+                    const uint4 hv = *xp;
+                    const unsigned hw[4] = {hv.x, hv.y, hv.z, hv.w};
+                    unsigned nw[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float2 h2 =
+                            __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&hw[u]));
+                        const int col = k0 + 2 * u;
+                        nw[u] = pack2(h2.x + fmaxf(acc[2 * u] + us[col], 0.f),
+                                      h2.y + fmaxf(acc[2 * u + 1] + us[col + 1], 0.f));
+                    }
+                    const uint4 nv = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+                    *xp = nv;
+                    if (node < n) *reinterpret_cast<uint4*>(hb + (size_t)node * HID + k0) = nv;
+                }
+            }
+            fence_smem_async();
+            fence_before();
+            __syncthreads();
+            if (*abort_flag) break;
+        }
+        if (has_pq) {
+            // P|Q = [A; B] h: 4 MMAs of K = 16 into columns 0..127
+            if (tid == 0) {
+                fence_after();
+#pragma unroll
+                for (int kk = 0; kk < HID / 16; ++kk)
+                    mma(tbase, sdesc(xa + kk * 2 * LBO, SBO_X), sdesc(wa + kk * 2 * LBO, SBO_W),
+                        idesc_bf16(TM, 2 * HID), kk > 0 ? 1u : 0u);
+                commit(ubar);
+            }
+            pending = true;
+            if (!__all_sync(0xffffffffu, wait_parity(ubar, phase & 1))) {
+                atomicExch(err, (int)CFD_ERR_BARRIER);
+                *abort_flag = 1;
+            } else {
+                pending = false;
+                phase += 1;
+                fence_after();
+                const int node = tb + erow;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float v[16];
+                    tmem_ld16(tlane + 64 * half + 16 * c, v);
+                    if (node < n) {
+                        uint4* op = reinterpret_cast<uint4*>(pq_out + (size_t)node * 2 * HID +
+                                                             64 * half + 16 * c);
+                        op[0] = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]),
+                                           pack2(v[4], v[5]), pack2(v[6], v[7]));
+                        op[1] = make_uint4(pack2(v[8], v[9]), pack2(v[10], v[11]),
+                                           pack2(v[12], v[13]), pack2(v[14], v[15]));
+                    }
+                }
+            }
+        } else if (half == 0) {
+            // decoder: y = W_out h + b_out on this thread's row
+            const int node = tb + erow;
+            float hrow[HID];
+#pragma unroll
+            for (int c = 0; c < HID / 8; ++c) {
+                const uint4 hv = *reinterpret_cast<const uint4*>(Xs + cm_off(erow, 8 * c, SBO_X));
+                const unsigned hw[4] = {hv.x, hv.y, hv.z, hv.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float2 h2 =
+                        __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&hw[u]));
+                    hrow[8 * c + 2 * u] = h2.x;
+                    hrow[8 * c + 2 * u + 1] = h2.y;
+                }
+            }
+            if (node < n)
+                for (int o = 0; o < OUT; ++o) {
+                    float a = wo[OUT * HID + o];
+                    for (int k = 0; k < HID; ++k) a += wo[o * HID + k] * hrow[k];
+                    y[(size_t)OUT * node + o] = a;
+                }
+        }
+        fence_before();
+        __syncthreads();
+        if (*abort_flag) break;
+    }
+    // a commit that timed out may still land: wait for it (bounded) before the columns go
+    if (tid == 0 && pending) wait_parity(ubar, phase & 1);
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                     "r"(TMEM_COLS)
+                     : "memory");
+    }
+}
+}  // namespace tc
+
 int infer_bf16(cudaStream_t st, const float* w, bf16* wb, bool* wb_valid, int n, const int* ptr,
                const int* nbr, const float* f, const float* e, bf16* hb, bf16* pqb, float* y,
-               const int* gate) {
+               const int* gate, int* err) {
     if (!*wb_valid) {
         CFD_LAUNCH(k_to_bf16, blocks_for(N_PARAMS, 256), 256, 0, st, N_PARAMS, w, wb);
         *wb_valid = true;
+    }
+    int dev = 0, nsm = 1;
+    CFD_CUDA(cudaGetDevice(&dev));
+    CFD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    bf16* pq[2] = {pqb, pqb + (size_t)n * 2 * HID};
+    // tensor-core generation: tcgen05 unless CFD_MPNN_TC=0 (the mma.sync passes)
+    const char* tce = getenv("CFD_MPNN_TC");
+    if (!(tce && atoi(tce) == 0)) {
+        static bool tc_attr = false;
+        if (!tc_attr) {
+            CFD_CUDA(cudaFuncSetAttribute(tc::k_infer_tc<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
+            CFD_CUDA(cudaFuncSetAttribute(tc::k_infer_tc<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
+            tc_attr = true;
+        }
+        const int ntile = (n + tc::TM - 1) / tc::TM;
+        const int grid = std::max(1, std::min(ntile, 2 * nsm));
+        CFD_LAUNCH(tc::k_infer_tc<true>, grid, tc::NTHR, tc::SMEM, st, n, 0, ptr, nbr, e, f, w,
+                   (const bf16*)wb, 1, (const bf16*)nullptr, hb, pq[0], y, gate, err);
+        for (int l = 0; l < LAYERS; ++l) {
+            const int next = l + 1 < LAYERS ? 1 : 0;
+            CFD_LAUNCH(tc::k_infer_tc<false>, grid, tc::NTHR, tc::SMEM, st, n, l, ptr, nbr, e, f,
+                       w, (const bf16*)wb, next, (const bf16*)pq[l & 1], hb, pq[(l + 1) & 1], y,
+                       gate, err);
+        }
+        return CFD_OK;
     }
     const size_t smem_enc = sizeof(bf16) * (2 * HID * HS + IW * 16 * HS) +
                             sizeof(float) * (HID * F_IN + HID);
@@ -766,12 +1215,8 @@ int infer_bf16(cudaStream_t st, const float* w, bf16* wb, bool* wb_valid, int n,
                                       (int)smem_layer));
         attr_set = true;
     }
-    int dev = 0, nsm = 1;
-    CFD_CUDA(cudaGetDevice(&dev));
-    CFD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int ntile = (n + TILE - 1) / TILE;
     const int grid = std::min(ntile, 2 * nsm);  // resident blocks (registers, shared memory)
-    bf16* pq[2] = {pqb, pqb + (size_t)n * 2 * HID};
     CFD_LAUNCH(k_infer_encode, grid, 32 * IW, smem_enc, st, n, f, w, (const bf16*)wb, hb, pq[0],
                gate);
     for (int l = 0; l < LAYERS; ++l) {

@@ -68,6 +68,7 @@ struct cfd_mpnn_graph {
     // inference (BF16)
     __nv_bfloat16 *hb = nullptr, *pqb = nullptr;
     float* yb = nullptr;
+    int* tc_err = nullptr;  // set when a tensor-core pass's bounded wait gave up
     double *ux = nullptr, *uy = nullptr, *uz = nullptr;
     bool training = false;
     ~cfd_mpnn_graph() {
@@ -288,6 +289,8 @@ int graph_build(cfd_mpnn_graph** out, int npoin, const std::vector<int>& rowptr,
     if ((rc = dev_alloc(o, &g->hb, n * HID))) return rc;
     if ((rc = dev_alloc(o, &g->pqb, 2 * n * 2 * HID))) return rc;  // two P|Q buffers
     if ((rc = dev_alloc(o, &g->yb, n * OUT))) return rc;
+    if ((rc = dev_alloc(o, &g->tc_err, 1))) return rc;
+    CFD_CUDA(cudaMemsetAsync(g->tc_err, 0, sizeof(int), st));
     // geometry globals (zero displacement), node and edge features
     const int* ng = nullptr;
     CFD_LAUNCH(k_globals, 1, 256, 0, st, g->nb, g->bnode, g->bkind, (const double*)g->bgx,
@@ -317,7 +320,7 @@ int guess_on_stream(cfd_mpnn* net, cfd_mpnn_graph* g, cudaStream_t st, const dou
     CFD_LAUNCH(k_edge_features, std::min(blocks_for(g->m, 256), gs), 256, 0, st, g->m, g->src,
                g->nbr, X, Y, (const Globals*)g->G, g->e, gate);
     int rc = infer_bf16(st, net->w, net->wb, &net->wb_valid, g->n, g->ptr, g->nbr, g->f, g->e,
-                        g->hb, g->pqb, g->yb, gate);
+                        g->hb, g->pqb, g->yb, gate, g->tc_err);
     if (rc) return rc;
     CFD_LAUNCH(k_guess, std::min(blocks_for(g->n, 256), gs), 256, 0, st, g->n,
                (const float*)g->yb, g->kind, (const double*)g->gnx, (const double*)g->gny,
@@ -476,7 +479,7 @@ int cfd_mpnn_forward(cfd_mpnn* net, cfd_mpnn_graph* g, int bf16, double* ux, dou
     const float* y = nullptr;
     if (bf16) {
         if ((rc = infer_bf16(g->stream, net->w, net->wb, &net->wb_valid, g->n, g->ptr, g->nbr, g->f,
-                             g->e, g->hb, g->pqb, g->yb, nullptr)))
+                             g->e, g->hb, g->pqb, g->yb, nullptr, g->tc_err)))
             return rc;
         y = g->yb;
     } else {
@@ -488,7 +491,14 @@ int cfd_mpnn_forward(cfd_mpnn* net, cfd_mpnn_graph* g, int bf16, double* ux, dou
                (const int*)nullptr);
     if (ux) CFD_CUDA(cudaMemcpyAsync(ux, g->ux, sizeof(double) * g->n, cudaMemcpyDeviceToHost, g->stream));
     if (uy) CFD_CUDA(cudaMemcpyAsync(uy, g->uy, sizeof(double) * g->n, cudaMemcpyDeviceToHost, g->stream));
+    int tc_err = 0;
+    CFD_CUDA(cudaMemcpyAsync(&tc_err, g->tc_err, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
     CFD_CUDA(cudaStreamSynchronize(g->stream));
+    if (tc_err) {
+        CFD_CUDA(cudaMemsetAsync(g->tc_err, 0, sizeof(int), g->stream));
+        set_last_message("a tensor-core inference pass timed out on its mbarrier");
+        return tc_err;
+    }
     return CFD_OK;
 }
 

@@ -48,7 +48,7 @@ __global__ void k_guess(int n, const float* y, const int* kind, const double* gn
 // when *wb_valid is false
 int infer_bf16(cudaStream_t st, const float* w, __nv_bfloat16* wb, bool* wb_valid, int n,
                const int* ptr, const int* nbr, const float* f, const float* e,
-               __nv_bfloat16* hb, __nv_bfloat16* pqb, float* y, const int* gate);
+               __nv_bfloat16* hb, __nv_bfloat16* pqb, float* y, const int* gate, int* err);
 
 }  // namespace mpnn
 }  // namespace cfd

@@ -301,16 +301,52 @@ def guess_gain(net, case, heave, pitch_deg, bf16=True):
             "guess_rel_l2": rel_guess}
 
 
+def time_inference(reps=20, nr=1024):
+    """BF16 inference on the nr x nr ellipse O-grid workload with the shipped weights: ms per
+    forward (the guess and its download included) of the tcgen05 passes and of the mma.sync
+    passes (CFD_MPNN_TC=0), and whether the two guesses are identical."""
+    k = cs.config_case(3, scale=nr)
+    G = Graph(k)
+    net = Net.load()
+    G.set_bc(*rigid_bc(k, 0.05, 2.0))
+    out, guess = {}, {}
+    prev = os.environ.get("CFD_MPNN_TC")
+    try:
+        for mode in ("1", "0"):
+            os.environ["CFD_MPNN_TC"] = mode
+            for _ in range(3):
+                guess[mode] = net.forward(G, bf16=True)
+            t = time.perf_counter()
+            for _ in range(reps):
+                net.forward(G, bf16=True)
+            out["tcgen05" if mode == "1" else "mma.sync"] = (time.perf_counter() - t) / reps * 1e3
+    finally:
+        if prev is None:
+            os.environ.pop("CFD_MPNN_TC", None)
+        else:
+            os.environ["CFD_MPNN_TC"] = prev
+    out["identical"] = bool(all(np.array_equal(a, b) for a, b in zip(guess["1"], guess["0"])))
+    out["nodes"] = k.npoin
+    G.close()
+    net.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", metavar="OUT", help="train and write the weights (.npz)")
+    ap.add_argument("--time-inference", type=int, metavar="REPS",
+                    help="time the BF16 inference passes on the 1M-node workload")
     ap.add_argument("--meshes", type=int, default=24)
     ap.add_argument("--steps", type=int, default=8000)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     a = ap.parse_args()
+    if a.time_inference:
+        print(time_inference(a.time_inference), flush=True)
+        return
     if not a.train:
-        ap.error("--train OUT is required")
+        ap.error("--train OUT or --time-inference REPS is required")
 
     def log(m):
         print(m, flush=True)

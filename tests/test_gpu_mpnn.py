@@ -104,6 +104,33 @@ def test_bf16_inference_matches_fp32(gpu_lib):
     assert np.array_equal(bx[~free], fx[~free]) and np.array_equal(by[~free], fy[~free])
 
 
+def test_tcgen05_inference_matches_mma_sync(gpu_lib, monkeypatch):
+    """The tcgen05 passes (the default: accumulators in tensor memory) and the mma.sync
+    passes (CFD_MPNN_TC=0) take the same BF16 operands and round the same FP32 sums to
+    BF16; only the order of the FP32 sums differs.  968 nodes: a ragged last tile."""
+    from cfd_gb300 import learned
+    k = small_case(1, scale=22, seed=6)
+    assert k.npoin % 128 != 0
+    G, kind, gfull, Gr, _ = setup(k, -0.15, 5.0)
+    rng = np.random.default_rng(4)
+    net = learned.Net((learned.init_weights(3) + 0.02 * rng.normal(size=learned.n_params()))
+                      .astype(np.float32))
+    monkeypatch.setenv("CFD_MPNN_TC", "0")
+    mx, my = net.forward(G, bf16=True)
+    monkeypatch.delenv("CFD_MPNN_TC")
+    tx, ty = net.forward(G, bf16=True)
+    tx2, ty2 = net.forward(G, bf16=True)
+    fx, fy = net.forward(G, bf16=False)
+    assert np.array_equal(tx, tx2) and np.array_equal(ty, ty2)
+    free = kind == 0
+    nrm = np.linalg.norm(np.hypot(fx, fy)[free])
+    d_mma = np.linalg.norm(np.hypot(tx - mx, ty - my)[free]) / nrm
+    d_f32 = np.linalg.norm(np.hypot(tx - fx, ty - fy)[free]) / nrm
+    print("tcgen05 vs mma.sync", d_mma, "vs FP32", d_f32)
+    assert d_mma <= 5e-3
+    assert d_f32 <= 3e-2
+
+
 def test_trained_guess_beats_zero_guess(gpu_lib):
     """The shipped weights: on a mesh and motions not in the training set, BiCG from the
     network's guess reaches the same solution (to the solve tolerance) in fewer
