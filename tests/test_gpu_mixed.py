@@ -153,3 +153,31 @@ def test_bulk_copy_node_pass_matches_plain_loads(gpu_lib, monkeypatch):
     assert np.abs(ua - ub).max() <= 1e-14 * np.abs(ua).max()
     a.close()
     b.close()
+
+
+def test_full_size_mixed_learned_matches_fp64(gpu_lib):
+    """The 1M-node ellipse O-grid (1024 x 1024) with the regularized ESTAB: the mixed form
+    with the learned guess attached (it runs on the cold first solve) against the FP64
+    form over 4 steps (the later ones replayed from the captured graph): the state within
+    the mixed form's tolerance, DTMIN to 1e-6, the mesh to the BiCG tolerance."""
+    from cfd_gb300 import abi, case as C, learned, solver
+    k = C.config_case(3)
+    k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
+    f = solver.Solver(k, precision=abi.CFD_PREC_FP64)
+    k.params.guess_mode = abi.CFD_GUESS_LEARNED
+    m = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    net = learned.Net.load()
+    m.set_guess_net(net)
+    for _ in range(4):
+        rf, rm = f.step(1), m.step(1)
+        assert abs(rm.dtmin - rf.dtmin) <= 1e-6 * rf.dtmin
+    sf, sm = f.state(), m.state()
+    err = state_errors(sm["U"], sf["U"])
+    print("1M mixed+learned vs FP64, rel L2 per variable", err)
+    assert max(err) <= REL_TOL_STATE
+    for key in ("X", "Y"):
+        assert np.abs(sm[key] - sf[key]).max() <= 1e-9 * np.abs(sf[key]).max()
+    assert m.guess_stats()[0] >= 1 and m.graph_state()[1] >= 2
+    f.close()
+    m.close()
+    net.close()
