@@ -336,14 +336,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", metavar="OUT", help="train and write the weights (.npz)")
     ap.add_argument("--time-inference", type=int, metavar="REPS",
-                    help="time the BF16 inference passes on the 1M-node workload")
+                    help="time the BF16 inference passes on the ellipse O-grid workload")
+    ap.add_argument("--nr", type=int, default=1024,
+                    help="--time-inference: nodes per direction of the O-grid (default 1024)")
     ap.add_argument("--meshes", type=int, default=24)
     ap.add_argument("--steps", type=int, default=8000)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     a = ap.parse_args()
     if a.time_inference:
-        print(time_inference(a.time_inference), flush=True)
+        print(time_inference(a.time_inference, a.nr), flush=True)
         return
     if not a.train:
         ap.error("--train OUT or --time-inference REPS is required")

@@ -159,7 +159,7 @@ def test_full_size_mixed_learned_matches_fp64(gpu_lib):
     """The 1M-node ellipse O-grid (1024 x 1024) with the regularized ESTAB: the mixed form
     with the learned guess attached (it runs on the cold first solve) against the FP64
     form over 4 steps (the later ones replayed from the captured graph): the state within
-    the mixed form's tolerance, DTMIN to 1e-6, the mesh to the BiCG tolerance."""
+    the mixed form's tolerance, DTMIN to 1e-6, the mesh to 1e-8 of the domain's size."""
     from cfd_gb300 import abi, case as C, learned, solver
     k = C.config_case(3)
     k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
@@ -175,8 +175,8 @@ def test_full_size_mixed_learned_matches_fp64(gpu_lib):
     err = state_errors(sm["U"], sf["U"])
     print("1M mixed+learned vs FP64, rel L2 per variable", err)
     assert max(err) <= REL_TOL_STATE
-    for key in ("X", "Y"):
-        assert np.abs(sm[key] - sf[key]).max() <= 1e-9 * np.abs(sf[key]).max()
+    for key in ("X", "Y"):  # two BiCG solves per step, each stopped at |r.z| <= 1e-10
+        assert np.abs(sm[key] - sf[key]).max() <= 1e-8 * np.abs(sf[key]).max()
     assert m.guess_stats()[0] >= 1 and m.graph_state()[1] >= 2
     f.close()
     m.close()
