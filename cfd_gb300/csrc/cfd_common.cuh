@@ -68,10 +68,35 @@ __device__ __forceinline__ float d2f_trunc(double v) {
     return __uint_as_float(sign | ((unsigned)fe << 23) | frac);
 }
 
+// lo is formed from the bits as well: v - hd (hd = v with the low 29 significand bits
+// cleared) is exactly m * 2^(e - 1075), m those 29 bits, so its float truncation takes the
+// 24 bits from m's leading one; m = 0 gives +0 (as the FP64 difference v - v does).  Only
+// infinities and NaNs take the FP64 subtraction.
 __device__ __forceinline__ void split_bits(double v, float& hi, float& lo) {
     hi = d2f_trunc(v);
-    const double hd = __longlong_as_double(__double_as_longlong(v) & ~0x1fffffffLL);
-    lo = d2f_trunc(v - hd);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ffull);
+    if (e == 0x7ff) {
+        const double hd = __longlong_as_double((long long)(b & ~0x1fffffffull));
+        lo = d2f_trunc(v - hd);
+        return;
+    }
+    const unsigned m = (unsigned)(b & 0x1fffffffull);
+    if (m == 0u) {
+        lo = 0.f;
+        return;
+    }
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int k = 31 - __clz((int)m);  // leading one of m
+    const int fe = k + e - 948;        // the float exponent field of m * 2^(e - 1075)
+    if (fe <= 0) {
+        lo = __uint_as_float(sign);
+    } else if (fe >= 0xff) {
+        lo = __uint_as_float(sign | 0x7f800000u);
+    } else {
+        const unsigned mant = (k >= 23 ? (m >> (k - 23)) : (m << (23 - k))) & 0x7fffffu;
+        lo = __uint_as_float(sign | ((unsigned)fe << 23) | mant);
+    }
 }
 
 // ------------------------------------------------------------------ fixed-order sums

@@ -302,8 +302,11 @@ k_deltat_estab(int nelem, const int4* __restrict__ elem, const float4* __restric
             const float alpha = fminf(fdiv(vel * hh, 2.f * et) * (1.f / 3.f), 1.f);
             const float a = fdiv(4.f * et, hh * hh);
             const float d32 = fdiv(fsafe, a + (a + fdiv(alpha * vel, hh)));
-            const double d = f2d_bits(d32);
-            if (d < 1.0e20 && d > 0.0) mybits = (unsigned long long)__double_as_longlong(d);
+            // 0 < d < 1e20 in FP64 as integer tests on the float's bits (positive normal,
+            // below 0x60ad78ec = 1e20f, the least float >= 1e20): no FP64 compare per element
+            const unsigned ub = __float_as_uint(d32);
+            if (ub >= 0x00800000u && ub < 0x60ad78ecu)
+                mybits = (unsigned long long)__double_as_longlong(f2d_bits(d32));
             if (DTE) DTE[e] = d32;  // DT of the element, for ITLOCAL's DTL
         }
         const float vx = ((vx1 + vx2 + vx3) - (w1.x + w2.x + w3.x)) * (1.f / 3.f);
