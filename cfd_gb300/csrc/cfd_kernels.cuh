@@ -144,6 +144,7 @@ struct MotionTailArgs {
     StepScal* sc;
 };
 __global__ void k_motion_tail(MotionTailArgs a);
+constexpr int kTailBlocks = 64;  // blocks of k_motion_tail at most (<= 256: the fold)
 
 // FORCE_VISC over the force sets' edges: form 0 reads FP64 fields and dNx(j,e) =
 // dnx[e*se + j*sj]; form 1 reads float fields and the mixed form's geo8.  terms: 2 per

@@ -936,8 +936,9 @@ __device__ __forceinline__ double2 transf_one(const MotionTailArgs& a, const Mot
                         -(mv.sa * distx) + mv.ca * disty - disty + mv.yposr);
 }
 
-// One launch of a few blocks for FORCES (meshMove.f90:167-192; per-block trees of the edge
-// terms, folded in block order by the last block) and/or the clock and the motion law,
+// One launch of up to kTailBlocks blocks for FORCES (meshMove.f90:167-192; per-block trees of the
+// edge terms, folded by a tree in block order by the last block) and/or the clock and the
+// motion law,
 // TRANSF into x_fix, and the Dirichlet values of the two BiCG solves (biconjGrad.f90:28:
 // x(fix) = x_fix, in x and in its float shadow).  Every block forms the motion from the
 // step-start MotionScal; the last block stores the new one.  The Newmark law runs both
@@ -949,7 +950,9 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
     if (a.do_motion && threadIdx.x == 0)
         mv = motion_step(*a.m, a.sc->dtmin, a.law, a.heave_amp, a.pitch_amp, a.freq);
     __syncthreads();
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    // items interleaved over the blocks (item k in block k % gridDim.x): the FP64 work of a
+    // few thousand items spreads over as many SMs as there are blocks
+    const int gt = threadIdx.x * gridDim.x + blockIdx.x, gs = gridDim.x * blockDim.x;
     const bool structural = a.law == CFD_MOTION_NEWMARK;
     if (a.do_motion && !structural) tail_transf(a, mv, gt, gs);
     if (a.do_forces)  // normales of the moved mesh, for the next step's wall condition
@@ -994,12 +997,15 @@ __global__ void __launch_bounds__(256) k_motion_tail(MotionTailArgs a) {
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if (a.do_forces && (int)threadIdx.x < 3 * a.nset) {
-        double v = 0.0;
-        for (unsigned b = 0; b < gridDim.x; ++b) v += __ldcg(a.part + threadIdx.x * gridDim.x + b);
-        const int s = threadIdx.x / 3, q = threadIdx.x % 3;
-        (q == 0 ? a.sc->fx : q == 1 ? a.sc->fy : a.sc->rm)[s] = v;
-    }
+    if (a.do_forces)  // the blocks' partials of each sum, folded by a tree in block order
+        for (int j = 0; j < 3 * a.nset; ++j) {
+            double v = (threadIdx.x < gridDim.x) ? __ldcg(a.part + j * gridDim.x + threadIdx.x) : 0.0;
+            v = block_tree256(v, red);
+            if (threadIdx.x == 0) {
+                const int s = j / 3, q = j % 3;
+                (q == 0 ? a.sc->fx : q == 1 ? a.sc->fy : a.sc->rm)[s] = v;
+            }
+        }
     if (a.do_motion && structural) {  // the Newmark step under set 1's load, then TRANSF
         __syncthreads();
         if (threadIdx.x == 0) {
