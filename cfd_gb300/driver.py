@@ -124,8 +124,8 @@ def run_case(directory, out_dir=None, precision=abi.CFD_PREC_FP64, maxiter=None,
              smoothing=None, smooth_every=0, verbose=False):
     """Run the case in `directory` for MAXITER (or `maxiter`) iterations and write the
     reference's files into `out_dir` (default: the case directory).  `smooth_every` > 0
-    smooths the moved mesh every that many steps (the commented-out per-step smoothing,
-    meshMove.f90:133, on the setTol_move path).  Returns a summary."""
+    smooths the moved mesh every that many steps (the smoothing module's setTol_move path,
+    smoothing.f90:372-386, which the reference's loop never calls).  Returns a summary."""
     case = read_case(directory)
     out_dir = out_dir or directory
     os.makedirs(out_dir, exist_ok=True)

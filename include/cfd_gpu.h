@@ -398,9 +398,11 @@ int cfd_ctx_smooth(cfd_ctx* ctx, int* iters, double* min_quality);
  * after the step's mesh update, the smoothing moves each node at most |XPOS| + |YPOS| (the
  * setTol_move path, smoothing.f90:372-386, with the step's displacement), W becomes the
  * whole move over DTMIN, and the new mesh's geometry is computed from the smoothed nodes.
- * The reference has this call in its loop commented out (meshMove.f90:133,
- * subrutinas.f90:795); a step that smooths runs launch by launch and waits on the host for
- * the sweeps' convergence.  cfd_ctx_smoothing_stats: out2 = (steps smoothed, sweeps). */
+ * The reference's time loop smooths nothing: its per-step calls of the older SMOOTH_MESH
+ * are commented out (meshMove.f90:133, subrutinas.f90:795) and the smoothing module's
+ * setTol_move, made for a moved mesh, has no caller.  A step that smooths runs launch by
+ * launch and waits on the host for the sweeps' convergence.  cfd_ctx_smoothing_stats:
+ * out2 = (steps smoothed, sweeps). */
 int cfd_ctx_set_smoothing(cfd_ctx* ctx, int every);
 int cfd_ctx_smoothing_stats(cfd_ctx* ctx, long long* out2);
 
