@@ -182,8 +182,8 @@ def config_dict(k, args, ws):
 # on the device, kernels of 13-130 us).
 NCU_TRAFFIC_PER_STEP = {
     "update_t": 1059.5e6,   # 4 node passes (946.4 MB) + 3 mu/lambda passes (113.1 MB)
-    "calcrhs_t": 381.8e6,
-    "deltat_t": 174.5e6,    # k_deltat_estab (the FP64 refinement reads a few chunks)
+    "calcrhs_t": 350.1e6,   # k_elem_stage1_mixed (ESTAB's DTMIN-free part included)
+    "deltat_t": 63.3e6,     # k_deltat_mixed (the FP64 refinement reads a few chunks)
     "laplace_t": 181.8e6,
 }
 
@@ -203,15 +203,14 @@ def algorithmic_bytes(k, iters, precision):
         # slot pointers 4, stage-invariant sums 16, 1/M 4, BC flags 1, U hi 16, T 4 B/N
         node_common = S * (16 + 4) + E * 8 + N * (4 + 16 + 4 + 1 + 16 + 4)
         return {
-            # elem 16, slot_pos 12, geo 32, shoc/tau 16 B/E; recInv + recVisc 96 B/E;
-            # mu/lambda 8 B/E; U hi/lo 32 + W 8 + T 4 B/N
-            "calcrhs_t": E * (16 + 12 + 32 + 16 + 96 + 8) + N * 44,
+            # ESTAB + calcRHS + FUENTE: elem 16, slot_pos 12, geo 32 B/E; recInv + recVisc
+            # 96 B/E; mu/lambda 8 B/E; U hi/lo 32 + W 8 + T 4 + VX, VY 8 B/N
+            "calcrhs_t": E * (16 + 12 + 32 + 96 + 8) + N * 52,
             # stage 1 adds recInv (16 B/slot); stage 4 adds U 32, U1 32, six primitives 24,
             # U hi/lo 32 B/N; stages 2-4 recompute mu/lambda (elem 16 + 8 B/E, T 4 B/N)
             "update_t": 4 * node_common + S * 16 + N * 120 + 3 * (E * 24 + N * 4),
-            # deltat + the DTMIN-free ESTAB in one pass: elem 16, geo 32, SHOC and the three
-            # ESTAB terms 16 B/E; T, VX, VY 12 + W 8 + rho hi/lo 8 B/N
-            "deltat_t": E * (16 + 32 + 16) + N * 28,
+            # deltat: elem 16, area 4 B/E; T, VX, VY 12 + W 8 B/N
+            "deltat_t": E * (16 + 4) + N * 20,
             "deriv_t": E * (16 + 32 + 4 + 8 + 8) + N * 32,
             "laplace_t": S * 8 + E * 40 + N * 52 + nnz * 4,
             "grad_t": bicg,

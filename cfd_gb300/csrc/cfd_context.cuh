@@ -113,7 +113,6 @@ struct Ctx {
     float4* d_geo8 = nullptr;  // per element: dNx(1:3), dNy(1:3), area, Laplacian weight
     unsigned long long* d_blockmin = nullptr;  // per-block FP32 DTELEM minima
     double* d_invdiag = nullptr;
-    float *d_shocf = nullptr, *d_ts1f = nullptr, *d_ts2f = nullptr, *d_ts3f = nullptr;
     float* d_valf = nullptr;
     float* d_dtef = nullptr;  // mixed form, ITLOCAL != 0: FP32 DT per element
     float* d_pf[2][2] = {};

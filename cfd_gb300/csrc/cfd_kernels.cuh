@@ -165,24 +165,26 @@ __global__ void k_narrow_state(int npoin, const double* U, const double* T, cons
                                float2* Wf);
 __global__ void k_widen(long n, const float* a, double* b);
 __global__ void k_narrow(long n, const double* a, float* b);
-__global__ void k_deltat_estab(int nelem, const int4* elem, const float4* Uhi, const float4* Ulo,
-                               const float* T, float gm, const float* VX, const float* VY,
-                               const float2* W, const float4* geo, float FR, float RHOINF,
-                               float TINF, int estab_mode, float eps_dir, float dirx, float diry,
+__global__ void k_deltat_mixed(int nelem, const int4* elem, const float* T, const float* VX,
+                               const float* VY, const float2* W, const float* areaf, float TINF,
                                float fsafe, unsigned long long* dtmin_bits,
-                               unsigned long long* block_min, float* SHOC, float* ES1,
-                               float* ES2, float* ES3, float* DTE);
+                               unsigned long long* block_min, float* DTE);
+// ESTAB's constants for the mixed form's stage-1 element kernel (estab_mode as CFD_ESTAB_*)
+struct EstabConst {
+    float gm, fr, rho_inf, t_inf;
+    int mode;
+    float eps, dirx, diry;
+};
 __global__ void k_deltat_refine(int nelem, const int4* elem, const float* T, const float* VX,
                                 const float* VY, const float2* W, const float* areaf,
                                 const unsigned long long* block_min, int nchunk, float fsafe,
                                 float t_inf, StepScal* sc, unsigned* count, int itlocal);
 cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, const int4* elem,
                                      const float4* Uhi, const float4* Ulo, const float4* geo,
-                                     const float* shoc, const StepScal* sc,
-                                     const float* ts1, const float* ts2, const float* ts3,
-                                     GasConstF gc, const float2* W, const int* slot_pos,
-                                     const float* T, float4* recInv, float4* recVisc,
-                                     float2* mulam, const float* dte);
+                                     const float* VX, const float* VY, EstabConst ec,
+                                     const StepScal* sc, GasConstF gc, const float2* W,
+                                     const int* slot_pos, const float* T, float4* recInv,
+                                     float4* recVisc, float2* mulam, const float* dte);
 constexpr int kMulamTB = 256;  // threads per block of k_elem_mulam
 __global__ void k_elem_mulam(int nelem, const int4* elem, const float* T, GasConstF gc,
                              float2* mulam);

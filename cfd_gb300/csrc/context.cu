@@ -732,7 +732,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
             if ((st = dalloc(q, N))) return st;
         for (float4** q : {&d_Uhi, &d_Ulo})
             if ((st = dalloc(q, N))) return st;
-        for (float** q : {&d_shocf, &d_ts1f, &d_ts2f, &d_ts3f, &d_areaf, &d_areaf_old})
+        for (float** q : {&d_areaf, &d_areaf_old})
             if ((st = dalloc(q, E))) return st;
         if ((st = dalloc(&d_blockmin, blocks_for(E, 256)))) return st;
         if ((st = dalloc(&d_geo8, 2 * (size_t)E))) return st;
@@ -863,14 +863,13 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
 int Ctx::enqueue_mixed(bool learned) {
     const int N = npoin, E = nelem;
     const int TB = 256;
-    // deltat and the DTMIN-free part of ESTAB in one element pass; the FP64 refinement of
-    // the elements near the FP32 minimum, whose last block forms DTMIN
+    // deltat alone (a light pass, so that the mesh motion forks early); the FP64 refinement
+    // of the elements near the FP32 minimum, whose last block forms DTMIN.  ESTAB is formed
+    // in the stage-1 element pass.
     tstart(TM_DELTAT);
-    CFD_LAUNCH(k_deltat_estab, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Uhi, d_Ulo, d_Tf,
-               (float)((prm.gama + prm.gama + prm.gama) / 3.0), d_VXf, d_VYf, d_Wf,
-               (const float4*)d_geo8, (float)prm.fr, (float)prm.rho_inf, (float)prm.t_inf,
-               prm.estab_mode, (float)estab_eps, (float)dir[0], (float)dir[1], (float)prm.fsafe,
-               &d_scal->dtmin32_bits, d_blockmin, d_shocf, d_ts1f, d_ts2f, d_ts3f, d_dtef);
+    CFD_LAUNCH(k_deltat_mixed, blocks_for(E, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf, d_VYf,
+               d_Wf, d_areaf, (float)prm.t_inf, (float)prm.fsafe, &d_scal->dtmin32_bits,
+               d_blockmin, d_dtef);
     {
         const int nchunk = (int)blocks_for(E, TB);
         CFD_LAUNCH(k_deltat_refine, blocks_for(nchunk, TB), TB, 0, stream, E, d_elem, d_Tf, d_VXf,
@@ -953,9 +952,12 @@ int Ctx::enqueue_mixed(bool learned) {
     const GasConstF gf = to_float(gc);
     const bool viscous = prm.fmu > 2.2250738585072014e-308;
     tstart(TM_CALCRHS);
-    CFD_CUDA(launch_elem_stage1_mixed(viscous, stream, E, d_elem, d_Uhi, d_Ulo, d_geo8, d_shocf,
-                                      d_scal, d_ts1f, d_ts2f, d_ts3f, gf, d_Wf, d_slot_pos, d_Tf,
-                                      d_recInv, d_recVisc, d_mulam, (const float*)d_dtef));
+    const EstabConst ec{(float)((prm.gama + prm.gama + prm.gama) / 3.0), (float)prm.fr,
+                        (float)prm.rho_inf, (float)prm.t_inf, prm.estab_mode, (float)estab_eps,
+                        (float)dir[0], (float)dir[1]};
+    CFD_CUDA(launch_elem_stage1_mixed(viscous, stream, E, d_elem, d_Uhi, d_Ulo, d_geo8, d_VXf,
+                                      d_VYf, ec, d_scal, gf, d_Wf, d_slot_pos, d_Tf, d_recInv,
+                                      d_recVisc, d_mulam, (const float*)d_dtef));
     tstop(TM_CALCRHS);
     // stage s uses mu, lambda from the T of stage s-1 (the reference's module T): stage 1's
     // come from the element kernel above, the others from k_elem_mulam before the node pass.

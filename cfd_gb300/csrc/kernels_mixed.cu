@@ -264,59 +264,27 @@ __device__ __forceinline__ EstabPre estab_pre(const float DX[3], const float DY[
     return o;
 }
 
-// One element pass for deltat (subrutinas.f90:170-210, FP32 DTELEM; per-block minima and
-// the FP32 minimum as the bit pattern of a positive double) and for the DTMIN-free part of
-// ESTAB: the two routines gather the same node data.
+// The step's first pass: deltat (subrutinas.f90:170-210) per element in FP32, per-block
+// minima and the FP32 minimum as the bit pattern of a positive double, for the FP64
+// refinement that forms DTMIN.  It gathers T, the velocities and W only, so that the mesh
+// motion, which needs DTMIN, can start early; ESTAB's DTMIN-free part is formed by the
+// stage-1 element kernel from the node data it gathers anyway.
 __global__ void __launch_bounds__(256)
-k_deltat_estab(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
-               const float4* __restrict__ Ulo, const float* __restrict__ T, float gm,
+k_deltat_mixed(int nelem, const int4* __restrict__ elem, const float* __restrict__ T,
                const float* __restrict__ VX, const float* __restrict__ VY,
-               const float2* __restrict__ W, const float4* __restrict__ geo, float FR,
-               float RHOINF, float TINF, int estab_mode, float eps_dir, float dirx, float diry,
+               const float2* __restrict__ W, const float* __restrict__ areaf, float TINF,
                float fsafe, unsigned long long* __restrict__ dtmin_bits,
-               unsigned long long* __restrict__ block_min, float* __restrict__ SHOC,
-               float* __restrict__ ES1, float* __restrict__ ES2, float* __restrict__ ES3,
-               float* __restrict__ DTE) {
+               unsigned long long* __restrict__ block_min, float* __restrict__ DTE) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long mybits = 0x7ff0000000000000ull;
     if (e < nelem) {
-        const int4 n = elem[e];
-        const int n1 = n.x, n2 = n.y, n3 = n.z;
-        const float4 ga = geo[2 * (size_t)e], gb = geo[2 * (size_t)e + 1];
-        const float DX[3] = {ga.x, ga.y, ga.z};
-        const float DY[3] = {ga.w, gb.x, gb.y};
-        const float rh1 = Uhi[n1].x, rh2 = Uhi[n2].x, rh3 = Uhi[n3].x;
-        const float rl1 = Ulo[n1].x, rl2 = Ulo[n2].x, rl3 = Ulo[n3].x;
-        const float2 w1 = W[n1], w2 = W[n2], w3 = W[n3];
-        const float vx1 = VX[n1], vx2 = VX[n2], vx3 = VX[n3];
-        const float vy1 = VY[n1], vy2 = VY[n2], vy3 = VY[n3];
-        const float t1 = T[n1], t2 = T[n2], t3 = T[n3];
-        // deltat: dtelem_f32 on the gathered values (area = the element's FP32 area)
-        {
-            float vumax = fmaxf(fmaxf(fabsf(vx1 - w1.x), fabsf(vx2 - w2.x)), fabsf(vx3 - w3.x));
-            float vvmax = fmaxf(fmaxf(fabsf(vy1 - w1.y), fabsf(vy2 - w2.y)), fabsf(vy3 - w3.y));
-            const float T_iel = (t1 + t2 + t3) * (1.f / 3.f);
-            const float hh = sqrtf(2.f * gb.z);
-            const float vel = sqrtf(vumax * vumax + vvmax * vvmax);
-            const float et = 0.017f * pow15f(fdiv(T_iel, TINF)) * fdiv(TINF + 110.f, T_iel + 110.f);
-            const float alpha = fminf(fdiv(vel * hh, 2.f * et) * (1.f / 3.f), 1.f);
-            const float a = fdiv(4.f * et, hh * hh);
-            const float d32 = fdiv(fsafe, a + (a + fdiv(alpha * vel, hh)));
-            // 0 < d < 1e20 in FP64 as integer tests on the float's bits (positive normal,
-            // below 0x60ad78ec = 1e20f, the least float >= 1e20): no FP64 compare per element
-            const unsigned ub = __float_as_uint(d32);
-            if (ub >= 0x00800000u && ub < 0x60ad78ecu)
-                mybits = (unsigned long long)__double_as_longlong(f2d_bits(d32));
-            if (DTE) DTE[e] = d32;  // DT of the element, for ITLOCAL's DTL
-        }
-        const float vx = ((vx1 + vx2 + vx3) - (w1.x + w2.x + w3.x)) * (1.f / 3.f);
-        const float vy = ((vy1 + vy2 + vy3) - (w1.y + w2.y + w3.y)) * (1.f / 3.f);
-        const EstabPre o = estab_pre(DX, DY, rh1, rh2, rh3, rl1, rl2, rl3, vx, vy, t1, t2, t3, gm,
-                                     FR, RHOINF, TINF, estab_mode, eps_dir, dirx, diry);
-        SHOC[e] = o.shoc;
-        ES1[e] = o.inv_tau2;
-        ES2[e] = o.v_rgn;
-        ES3[e] = o.v_rgne;
+        const float d32 = dtelem_f32(elem[e], T, VX, VY, W, areaf[e], fsafe, TINF);
+        // 0 < d < 1e20 in FP64 as integer tests on the float's bits (positive normal,
+        // below 0x60ad78ec = 1e20f, the least float >= 1e20): no FP64 compare per element
+        const unsigned ub = __float_as_uint(d32);
+        if (ub >= 0x00800000u && ub < 0x60ad78ecu)
+            mybits = (unsigned long long)__double_as_longlong(f2d_bits(d32));
+        if (DTE) DTE[e] = d32;  // DT of the element, for ITLOCAL's DTL
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -354,18 +322,18 @@ __global__ void k_elem_mulam(int nelem, const int4* __restrict__ elem, const flo
 }
 
 // ------------------------------------------------------------------ stage-1 element kernel
-// calcRHS.f90:36-141 + FUENTE (subrutinas.f90:1060-1078) in FP32, folded with the
-// step's area*dtl/3, written as slot records in element-around-point order: recInv holds
-// the stage-invariant contributions to the 4 equations, recVisc Vmu(1), Vmu(2), Vmu(3),
-// Vlam(3).
+// ESTAB (subrutinas.f90:346-443, its DTMIN-free part by estab_pre, then TS1-3 with the step's
+// DTMIN) and calcRHS.f90:36-141 + FUENTE (subrutinas.f90:1060-1078) in FP32, folded with
+// the step's area*dtl/3, written as slot records in element-around-point order: recInv
+// holds the stage-invariant contributions to the 4 equations, recVisc Vmu(1), Vmu(2),
+// Vmu(3), Vlam(3).
 
 template <bool VISCOUS>
 __global__ void __launch_bounds__(128, 6)
 k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __restrict__ Uhi,
                     const float4* __restrict__ Ulo, const float4* __restrict__ geo,
-                    const float* __restrict__ shoc,
-                    const StepScal* __restrict__ sc, const float* __restrict__ ts1,
-                    const float* __restrict__ ts2, const float* __restrict__ ts3, GasConstF gc,
+                    const float* __restrict__ VX, const float* __restrict__ VY, EstabConst ec,
+                    const StepScal* __restrict__ sc, GasConstF gc,
                     const float2* __restrict__ W, const int* __restrict__ slot_pos,
                     const float* __restrict__ T, float4* __restrict__ recInv,
                     float4* __restrict__ recVisc, float2* __restrict__ mulam,
@@ -394,17 +362,24 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
         Ux[q] = d1 * Nx[1] + d2 * Nx[2];
         Uy[q] = d1 * Ny[1] + d2 * Ny[2];
     }
-    // TS1-3 of ESTAB from its DTMIN-free part (k_deltat_estab) and this step's DTMIN
-    float tau[3];
+    const float2 w0 = W[p[0]], w1 = W[p[1]], w2 = W[p[2]];
+    // ESTAB: the DTMIN-free part from the gathered rho (hi, lo), relative velocity and T,
+    // then TS1-3 with this step's DTMIN
+    float tau[3], nu;
     {
+        const float t1 = T[p[0]], t2 = T[p[1]], t3 = T[p[2]];
+        const float vx = ((VX[p[0]] + VX[p[1]] + VX[p[2]]) - (w0.x + w1.x + w2.x)) * (1.f / 3.f);
+        const float vy = ((VY[p[0]] + VY[p[1]] + VY[p[2]]) - (w0.y + w1.y + w2.y)) * (1.f / 3.f);
+        const EstabPre o = estab_pre(Nx, Ny, Un[0][0], Un[1][0], Un[2][0], Ul[0][0], Ul[1][0],
+                                     Ul[2][0], vx, vy, t1, t2, t3, ec.gm, ec.fr, ec.rho_inf,
+                                     ec.t_inf, ec.mode, ec.eps, ec.dirx, ec.diry);
         const float two_dt = fdiv(2.f, sc->dtmin_f);
-        const float resumen = ts1[e] + two_dt * two_dt;
-        const float v2 = ts2[e], v3 = ts3[e];
+        const float resumen = o.inv_tau2 + two_dt * two_dt;
         tau[0] = rsqrtf(resumen);
-        tau[1] = (v2 >= 0.f) ? rsqrtf(resumen + v2) : 0.f;
-        tau[2] = (v3 >= 0.f) ? rsqrtf(resumen + v3) : 0.f;
+        tau[1] = (o.v_rgn >= 0.f) ? rsqrtf(resumen + o.v_rgn) : 0.f;
+        tau[2] = (o.v_rgne >= 0.f) ? rsqrtf(resumen + o.v_rgne) : 0.f;
+        nu = o.shoc * gc.cte;
     }
-    const float nu = shoc[e] * gc.cte;
     // area*dtl/3 with dtl = DTMIN, or under ITLOCAL DTL = DTMIN*DTFACT + min(DT, COTA)*(1-DTFACT)
     // (ns2DComp.ALE.f90:159-162, subrutinas.f90:211-215)
     float dtl = sc->dtmin_f;
@@ -499,7 +474,6 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
             r[i][q] += tau[i] * (Nx[i] * SB1[q] + Ny[i] * SB2[q]) +
                        3.f * nu * (Nx[i] * Ux[q] + Ny[i] * Uy[q]);
     {  // FUENTE: -AR*sum_k sp(i,k)*(Ux*wx_k + Uy*wy_k), AR = area*dtl/3 = scale
-        const float2 w0 = W[p[0]], w1 = W[p[1]], w2 = W[p[2]];
         const float wx[3] = {0.5f * (w0.x + w1.x), 0.5f * (w1.x + w2.x), 0.5f * (w0.x + w2.x)};
         const float wy[3] = {0.5f * (w0.y + w1.y), 0.5f * (w1.y + w2.y), 0.5f * (w0.y + w2.y)};
 #pragma unroll
@@ -1059,19 +1033,18 @@ __device__ __forceinline__ void tail_transf(const MotionTailArgs& a, const Motio
 // ------------------------------------------------------------------ host launchers
 cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, const int4* elem,
                                      const float4* Uhi, const float4* Ulo, const float4* geo,
-                                     const float* shoc, const StepScal* sc,
-                                     const float* ts1, const float* ts2, const float* ts3,
-                                     GasConstF gc, const float2* W, const int* slot_pos,
-                                     const float* T, float4* recInv, float4* recVisc,
-                                     float2* mulam, const float* dte) {
+                                     const float* VX, const float* VY, EstabConst ec,
+                                     const StepScal* sc, GasConstF gc, const float2* W,
+                                     const int* slot_pos, const float* T, float4* recInv,
+                                     float4* recVisc, float2* mulam, const float* dte) {
     const unsigned grid = blocks_for(nelem, 128);
     if (viscous)
-        k_elem_stage1_mixed<true><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, shoc, sc, ts1,
-                                                         ts2, ts3, gc, W, slot_pos, T, recInv,
-                                                         recVisc, mulam, dte);
+        k_elem_stage1_mixed<true><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, VX, VY, ec, sc,
+                                                         gc, W, slot_pos, T, recInv, recVisc,
+                                                         mulam, dte);
     else
-        k_elem_stage1_mixed<false><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, shoc, sc, ts1,
-                                                          ts2, ts3, gc, W, slot_pos, T, recInv,
+        k_elem_stage1_mixed<false><<<grid, 128, 0, st>>>(nelem, elem, Uhi, Ulo, geo, VX, VY, ec,
+                                                          sc, gc, W, slot_pos, T, recInv,
                                                           recVisc, mulam, dte);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
