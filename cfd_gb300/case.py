@@ -539,3 +539,29 @@ def read_case(directory: str) -> Case:
                 rfixv_valuey=rvy, ifixt_node=ifixt, rfixt_value=rfixt, wall=wall,
                 iset_entries=sets, i_m=i_m, ifm=ifm, nfixvi=nfixvi, nfixt_file=nfixt,
                 meta=meta)
+
+
+def main(argv=None):
+    """Command line: write one of the synthetic workloads as a case directory in the
+    reference's input formats."""
+    import argparse
+    ap = argparse.ArgumentParser(description="Write a synthetic workload as a case directory "
+                                 "(EULER.DAT, <name>-1.dat, <name>.dat).")
+    ap.add_argument("directory")
+    ap.add_argument("--config", type=int, default=3, choices=(1, 2, 3, 5),
+                    help="1: cylinder 64x128 fixed; 2: cylinder 512x512 heave; 3: ellipse "
+                         "1024x1024 Mach 0.8 heave; 5: ellipse 2048x2048 heave + pitch")
+    ap.add_argument("--scale", type=int, default=None,
+                    help="nodes per direction instead of the workload's")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--maxiter", type=int, default=None)
+    a = ap.parse_args(argv)
+    c = config_case(a.config, scale=a.scale, seed=a.seed)
+    if a.maxiter is not None:
+        c.params.maxiter = a.maxiter
+    write_case(c, a.directory)
+    print(f"{a.directory}: {c.name}, {c.npoin} nodes, {c.nelem} triangles")
+
+
+if __name__ == "__main__":
+    main()

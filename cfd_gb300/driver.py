@@ -202,3 +202,27 @@ def run_case(directory, out_dir=None, precision=abi.CFD_PREC_FP64, maxiter=None,
         cnv.close()
         desp.close()
     return last
+
+
+def main(argv=None):
+    """Command line: run a case directory as the reference's executable does."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="Run a case directory (EULER.DAT, <name>-1.dat, "
+                                 "<name>.dat) and write the reference's output files.")
+    ap.add_argument("directory")
+    ap.add_argument("--out", default=None, help="output directory (default: the case's)")
+    ap.add_argument("--precision", choices=("fp64", "mixed"), default="fp64")
+    ap.add_argument("--maxiter", type=int, default=None, help="steps (default: MAXITER)")
+    ap.add_argument("--smooth-every", type=int, default=0,
+                    help="smooth the moved mesh every this many steps (0: never)")
+    ap.add_argument("--verbose", action="store_true")
+    a = ap.parse_args(argv)
+    prec = abi.CFD_PREC_FP64 if a.precision == "fp64" else abi.CFD_PREC_MIXED
+    last = run_case(a.directory, a.out, precision=prec, maxiter=a.maxiter,
+                    smooth_every=a.smooth_every, verbose=a.verbose)
+    print(json.dumps(last))
+
+
+if __name__ == "__main__":
+    main()

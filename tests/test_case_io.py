@@ -39,3 +39,16 @@ def test_derived_parameters():
     assert p.u_inf ** 2 + p.v_inf ** 2 == pytest.approx((5000 * 0.017) ** 2)
     assert p.c_inf == pytest.approx(np.hypot(p.u_inf, p.v_inf) / 0.8)
     assert p.p_inf == pytest.approx(p.rho_inf * p.fr * p.t_inf)
+
+
+def test_case_cli_writes_a_readable_case(tmp_path):
+    """`python -m cfd_gb300.case DIR --config 3 --scale 16` writes the reference's three
+    input files; reading them back gives the same mesh and parameters."""
+    from cfd_gb300 import case as C
+    d = str(tmp_path / "c3")
+    C.main([d, "--config", "3", "--scale", "16", "--maxiter", "7"])
+    k = C.read_case(d)
+    ref = C.config_case(3, scale=16)
+    assert k.npoin == ref.npoin and k.nelem == ref.nelem and k.params.maxiter == 7
+    assert np.array_equal(k.inpoel, ref.inpoel)
+    np.testing.assert_allclose(k.x, ref.x, rtol=0, atol=1e-12 * np.abs(ref.x).max())
