@@ -135,6 +135,7 @@ SIGNATURES = {
     "cfd_ctx_graph_state": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_set_force_visc": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smooth": (C.c_int, [_P, _ip, _dp]),
+    "cfd_selftest_waits": (C.c_int, [C.c_longlong, _ip, _ip]),
     "cfd_ctx_set_smoothing": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smoothing_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_smoothing": (C.c_int, [_dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _ip, _dp]),

@@ -145,6 +145,34 @@ int cfd_device_available(void) {
 
 long long cfd_kernel_launches(void) { return g_launches.load(); }
 
+int cfd_selftest_waits(long long polls, int* barrier_status, int* mbarrier_status) {
+    if (polls < 1 || polls > (1LL << 24) || !barrier_status || !mbarrier_status)
+        return arg_error("polls in [1, 2^24] and two status pointers");
+    GridBar* gb = nullptr;
+    int* out = nullptr;
+    CFD_CUDA(cudaMalloc(&gb, sizeof(GridBar)));
+    const cudaError_t e1 = cudaMalloc(&out, 2 * sizeof(int));
+    if (e1 != cudaSuccess) {
+        cudaFree(gb);
+        CFD_CUDA(e1);
+    }
+    int h[2] = {-1, -1};
+    cudaError_t e = cudaMemset(gb, 0, sizeof(GridBar));
+    if (e == cudaSuccess) e = cudaMemset(out, 0xff, 2 * sizeof(int));
+    if (e == cudaSuccess) {
+        k_selftest_waits<<<1, 32>>>(gb, out, polls);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h, out, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(gb);
+    cudaFree(out);
+    CFD_CUDA(e);
+    *barrier_status = h[0];
+    *mbarrier_status = h[1];
+    return CFD_OK;
+}
+
 void* cfd_ctx_stream(cfd_ctx* ctx) { return ctx ? (void*)ctx->impl.stream : nullptr; }
 
 int cfd_ctx_mark(cfd_ctx* ctx, int slot) {

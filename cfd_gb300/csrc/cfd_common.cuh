@@ -152,7 +152,8 @@ struct GridBar {
     int pad;
 };
 
-__device__ __forceinline__ void grid_barrier(GridBar* gb, unsigned nblocks) {
+__device__ __forceinline__ void grid_barrier(GridBar* gb, unsigned nblocks,
+                                             long long limit = kSpinLimit) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int* vgen = &gb->gen;
@@ -166,7 +167,7 @@ __device__ __forceinline__ void grid_barrier(GridBar* gb, unsigned nblocks) {
         } else {
             long long spins = 0;
             while (*vgen == g) {
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     atomicExch(&gb->err, (int)CFD_ERR_BARRIER);
                     break;
                 }
@@ -176,6 +177,21 @@ __device__ __forceinline__ void grid_barrier(GridBar* gb, unsigned nblocks) {
         __threadfence();
     }
     __syncthreads();
+}
+
+// Bounded wait on the phase of the given parity of a shared-memory mbarrier (an mbarrier
+// completed by bulk copies or by tcgen05.commit): false after `limit` polls
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned ubar, unsigned parity,
+                                                  long long limit = kSpinLimit) {
+    unsigned done = 0;
+    for (long long k = 0; k < limit && !done; ++k)
+        asm volatile(
+            "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; "
+            "selp.u32 %0, 1, 0, q; }"
+            : "=r"(done)
+            : "r"(ubar), "r"(parity)
+            : "memory");
+    return done != 0;
 }
 
 }  // namespace cfd

@@ -325,6 +325,7 @@ struct PcgArgs {
 
 __global__ void k_pcg_fp64(PcgArgs a);
 __global__ void k_pcg_mixed(PcgArgs a);
+__global__ void k_selftest_waits(GridBar* gb, int* out, long long limit);
 __global__ void k_bicg_fix_mixed(PcgArgs a);
 __global__ void k_bicg_resid_mixed(PcgArgs a);
 __global__ void k_bicg_dir_mixed(PcgArgs a);

@@ -1108,14 +1108,7 @@ k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __rest
     const bool live = p < npoin;
     const int s0 = live ? esup_ptr[p] : 0, s1 = live ? esup_ptr[p + 1] : 0;
     // bounded wait for the copies (phase 0)
-    unsigned done = 0;
-    for (long long k = 0; k < kSpinLimit && !done; ++k)
-        asm volatile(
-            "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0; selp.u32 %0, 1, 0, q; }"
-            : "=r"(done)
-            : "r"(ubar)
-            : "memory");
-    if (!done) {
+    if (!mbar_wait_bounded(ubar, 0u)) {
         if (threadIdx.x == 0) atomicExch(err, (int)CFD_ERR_BARRIER);
         return;
     }

@@ -823,17 +823,9 @@ __device__ __forceinline__ void commit(unsigned mbar) {
         : "memory");
 }
 
-// bounded wait on the mbarrier's phase of the given parity
+// bounded wait on the mbarrier's phase of the given parity (mbar_wait_bounded)
 __device__ __forceinline__ bool wait_parity(unsigned mbar, unsigned parity) {
-    unsigned done = 0;
-    for (long long k = 0; k < kSpinLimit && !done; ++k)
-        asm volatile(
-            "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; "
-            "selp.u32 %0, 1, 0, q; }"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-    return done != 0;
+    return mbar_wait_bounded(mbar, parity);
 }
 
 // 16 consecutive FP32 columns of this thread's tensor-memory lane; the wait is tied to

@@ -242,4 +242,20 @@ __global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
         }
 }
 
+// Failure-detection self-test of the two bounded waits (one block): a grid barrier that
+// expects a second block that never comes, and an mbarrier nothing arrives on.  Both give
+// up after `limit` polls; out[0] = the barrier's error word, out[1] = CFD_ERR_BARRIER when
+// the mbarrier wait gave up (0 if it completed).
+__global__ void k_selftest_waits(GridBar* gb, int* out, long long limit) {
+    __shared__ __align__(8) unsigned long long bar;
+    grid_barrier(gb, 2u, limit);
+    if (threadIdx.x == 0) {
+        const unsigned ubar = (unsigned)__cvta_generic_to_shared(&bar);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        out[1] = mbar_wait_bounded(ubar, 0u, limit) ? 0 : (int)CFD_ERR_BARRIER;
+        out[0] = gb->err;
+    }
+}
+
 }  // namespace cfd

@@ -409,6 +409,13 @@ int cfd_ctx_smoothing_stats(cfd_ctx* ctx, long long* out2);
 /* Number of kernels this library launched since process start (all contexts). */
 long long cfd_kernel_launches(void);
 
+/* Failure-detection self-test (no counterpart in the reference): runs, in one block, the
+ * library's two bounded device waits on conditions that never come true (a grid barrier
+ * that a second block never reaches; an mbarrier nothing arrives on), each giving up after
+ * `polls` polls (1 .. 2^24; the library's kernels use 2^24).  Both statuses come back as
+ * CFD_ERR_BARRIER and the device stays usable. */
+int cfd_selftest_waits(long long polls, int* barrier_status, int* mbarrier_status);
+
 const char* cfd_strerror(int status);
 /* 1 if a CUDA device is usable by this library. */
 int cfd_device_available(void);

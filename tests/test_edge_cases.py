@@ -5,6 +5,8 @@ captured graph included)."""
 import numpy as np
 import pytest
 
+from conftest import small_case
+
 
 def square(n, perturbed=True):
     from cfd_gb300 import case as C
@@ -97,3 +99,21 @@ def test_single_triangle(gpu_lib, precision):
         assert abs(rg.dtmin - ro.dtmin) <= 1e-6 * ro.dtmin
     g.close()
     o.close()
+
+
+@pytest.mark.gpu
+def test_bounded_waits_give_up_and_the_device_stays_usable(gpu_lib):
+    """Failure detection without a fault: the library's grid barrier (a second block that
+    never arrives) and its mbarrier wait (nothing arrives) give up after their poll limit
+    and report CFD_ERR_BARRIER; a full step runs afterwards in the same process."""
+    import ctypes as C
+    from cfd_gb300 import abi, solver
+    b, m = C.c_int(-1), C.c_int(-1)
+    abi.check(abi.lib().cfd_selftest_waits(100000, C.byref(b), C.byref(m)), "selftest")
+    assert b.value == abi.CFD_ERR_BARRIER and m.value == abi.CFD_ERR_BARRIER
+    assert abi.lib().cfd_selftest_waits(0, C.byref(b), C.byref(m)) == abi.CFD_ERR_ARG
+    k = small_case(3, scale=16, seed=3, estab_mode=2)
+    s = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    rep = s.step(2)
+    assert rep.iter == 2 and np.isfinite(s.state()["U"]).all()
+    s.close()
