@@ -44,6 +44,10 @@ def parse():
                     help="skip the plain-FP64 timing and the mixed-vs-FP64 error")
     ap.add_argument("--scale", type=int, default=None, help="nr = ntheta (reduced-size runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--large-nr", type=int, default=None,
+                    help="nodes per direction of the large heave + pitch O-grid report "
+                         "(default 2048, the 4,194,304-node workload; given, it also runs "
+                         "under --no-compare)")
     ap.add_argument("--guess", choices=["learned", "previous", "zero"], default="learned",
                     help="initial guess of the mesh-motion solve in the mixed form")
     ap.add_argument("--guess-gate", type=float, default=20.0,
@@ -328,12 +332,13 @@ def main_accuracy(args):
     print(json.dumps(line), flush=True)
 
 
-def large_mesh_report(W, net, gate, hbm_peak):
-    """The 4,194,304-node ellipse O-grid (config 5: heave + pitch, Re 10000) in the mixed
-    form with the learned guess: node-steps/s over 200 event-timed steps, and the update_t
-    group's algorithmic bandwidth and roofline fraction (timers on, own context)."""
+def large_mesh_report(W, net, gate, hbm_peak, nr=2048):
+    """The nr x nr ellipse O-grid of config 5 (heave + pitch, Re 10000; nr = 2048: 4,194,304
+    nodes) in the mixed form with the learned guess: node-steps/s over 200 event-timed
+    steps, and the update_t group's algorithmic bandwidth and roofline fraction (timers on,
+    own context)."""
     from cfd_gb300 import abi, case as C, solver
-    k = C.config_case(5)
+    k = C.config_case(5, scale=None if nr == 2048 else nr)
     k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
     if net is not None:
         k.params.guess_mode = abi.CFD_GUESS_LEARNED
@@ -567,8 +572,12 @@ def main_ours(args):
                 "launch_ms": per_launch[dom] * 1e3,
                 "launches_per_step": calls_per_step[dom],
                 "algorithmic_bytes_per_launch": (ab[dom] / calls_per_step[dom]) if dom in ab else None}
-    if mixed and not args.no_compare and args.scale is None and ws == 1:
-        forms["config5_4M"] = large_mesh_report(W, net, gate, hbm_peak)
+    if mixed and args.scale is None and ws == 1:
+        if args.large_nr is not None and args.large_nr != 2048:
+            forms[f"config5_nr{args.large_nr}"] = large_mesh_report(W, net, gate, hbm_peak,
+                                                                    args.large_nr)
+        elif not args.no_compare or args.large_nr is not None:
+            forms["config5_4M"] = large_mesh_report(W, net, gate, hbm_peak)
     kernels = {n_: {"ms_per_launch": per_launch[n_] * 1e3, "launches_per_step": calls_per_step[n_],
                     "GBps_algorithmic": (ab[n_] / per_step[n_] / 1e9) if n_ in ab else None,
                     "frac_of_hbm_peak": (ab[n_] / per_step[n_] / 1e9 / hbm_peak)
