@@ -216,7 +216,7 @@ struct Ctx {
     int step_once_mixed();
     int step(int nsteps, cfd_step_report* rep);
     int tstart(int slot);
-    int tstop(int slot);
+    int tstop(int slot, int ncalls = 1);
     int tcollect();
     template <class T>
     int dalloc(T** p, size_t n);

@@ -56,11 +56,12 @@ int Ctx::tstart(int slot) {
     CFD_CUDA(cudaEventRecord(pool[2 * open_pair[slot]], stream));
     return CFD_OK;
 }
-int Ctx::tstop(int slot) {
+// ncalls: launches of the group the interval covers (one event pair around several)
+int Ctx::tstop(int slot, int ncalls) {
     if (!timers_on) return CFD_OK;
     CFD_CUDA(cudaEventRecord(pool[2 * open_pair[slot] + 1], stream));
     pending.push_back(std::make_pair(slot, open_pair[slot]));
-    calls[slot] += 1;
+    calls[slot] += ncalls;
     return CFD_OK;
 }
 int Ctx::tcollect() {
@@ -963,9 +964,11 @@ int Ctx::enqueue_mixed(bool learned) {
     // come from the element kernel above, the others from k_elem_mulam before the node pass.
     // The last stage updates U in place.
     const int NRK = 4;
+    // one event pair around the four stages (no event between their kernels), counted as
+    // four launches of the group
+    tstart(TM_UPDATE);
     for (int irk = 1; irk <= NRK; ++irk) {
         const float rk_fact = 1.f / (float)(NRK + 1 - irk);
-        tstart(TM_UPDATE);
         if (irk > 1 && viscous)
             CFD_LAUNCH(k_elem_mulam, blocks_for(E, kMulamTB), kMulamTB, 0, stream, E, d_elem,
                        (const float*)d_Tf, gf, d_mulam);
@@ -974,8 +977,8 @@ int Ctx::enqueue_mixed(bool learned) {
                                    d_Ulo, d_invMf, rk_fact, irk == NRK ? 1 : 0, d_bcflag, d_bcval,
                                    d_nrm, d_WX, d_WY, d_U, d_RHOf, d_VXf, d_VYf, d_Ef, d_Pf, d_Tf,
                                    d_RMACHf, node_bulk, d_node_err));
-        tstop(TM_UPDATE);
     }
+    tstop(TM_UPDATE, NRK);
     int st = CFD_OK;
     if (structural) {
         if ((st = motion(stream))) return st;
