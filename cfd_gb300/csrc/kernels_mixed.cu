@@ -513,9 +513,31 @@ k_elem_stage1_mixed(int nelem, const int4* __restrict__ elem, const float4* __re
 constexpr int kNodeTB = 128;  // threads per block of the node passes
 // The node's update once its slot sums are known (inv: the stage-invariant sum in the first
 // stage, read back from invSum in the others; sv1..3: the viscous sums)
+// The node's own inputs of node_finish, loaded ahead of its slot sums so that they are in
+// flight together with the slot loads (the stage-invariant sum of the first stage is formed
+// from the slots, not loaded)
+struct NodePre {
+    float4 inv, h;
+    float im;
+    unsigned char fl;
+};
+template <bool FIRST>
+__device__ __forceinline__ NodePre node_pre(int p, const float4* __restrict__ invSum,
+                                            const float* __restrict__ invM,
+                                            const unsigned char* __restrict__ bcflag,
+                                            const float4* __restrict__ Uhi) {
+    NodePre q;
+    q.inv = FIRST ? make_float4(0.f, 0.f, 0.f, 0.f) : invSum[p];
+    q.im = invM[p];
+    q.fl = bcflag[p];
+    q.h = Uhi[p];
+    return q;
+}
+
 template <bool FIRST, bool LAST>
 __device__ __forceinline__ void node_finish(
-    int p, float4 inv, float sv1, float sv2, float sv3, float4* __restrict__ invSum, GasConst gc,
+    int p, const NodePre& pre, float4 inv, float sv1, float sv2, float sv3,
+    float4* __restrict__ invSum, GasConst gc,
     GasConstF gf, const double* U, float4* __restrict__ Uhi, float4* __restrict__ Ulo,
     const float* __restrict__ invM, float rk_fact, const unsigned char* __restrict__ bcflag,
     const double* __restrict__ bcval, const double2* __restrict__ nrm,
@@ -524,14 +546,14 @@ __device__ __forceinline__ void node_finish(
     float* __restrict__ Eo, float* __restrict__ Po, float* __restrict__ Tout,
     float* __restrict__ RMACH) {
     if (FIRST) invSum[p] = inv;
-    else inv = invSum[p];
-    const float f = rk_fact * invM[p];
+    else inv = pre.inv;
+    const float f = rk_fact * pre.im;
     const float d0 = f * inv.x, d1 = f * (inv.y + sv1), d2 = f * (inv.z + sv2),
                 d3 = f * (inv.w + sv3);
     const float g = gf.gamma;
-    const unsigned char fl = bcflag[p];
+    const unsigned char fl = pre.fl;
     if (!fl) {
-        const float4 h = Uhi[p];
+        const float4 h = pre.h;
         const float rho = h.x - d0, ir = 1.f / rho;
         const float vx = (h.y - d1) * ir, vy = (h.z - d2) * ir, ee = (h.w - d3) * ir;
         const float vel2 = vx * vx + vy * vy;
@@ -604,6 +626,7 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
              float* __restrict__ Tout, float* __restrict__ RMACH) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npoin) return;
+    const NodePre pre = node_pre<FIRST>(p, invSum, invM, bcflag, Uhi);
     Acc a0, a1, a2, a3, v1, v2, v3;
     a0.init(); a1.init(); a2.init(); a3.init();
     v1.init(); v2.init(); v3.init();
@@ -648,7 +671,7 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
     }
     const float4 inv =
         FIRST ? make_float4(a0.value(), a1.value(), a2.value(), a3.value()) : make_float4(0.f, 0.f, 0.f, 0.f);
-    node_finish<FIRST, LAST>(p, inv, v1.value(), v2.value(), v3.value(), invSum, gc, gf, U, Uhi, Ulo,
+    node_finish<FIRST, LAST>(p, pre, inv, v1.value(), v2.value(), v3.value(), invSum, gc, gf, U, Uhi, Ulo,
                              invM, rk_fact, bcflag, bcval, nrm, WX, WY, U1, RHO, VX, VY, Eo, Po,
                              Tout, RMACH);
 }
@@ -1107,6 +1130,8 @@ k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __rest
     const int p = p0 + threadIdx.x;
     const bool live = p < npoin;
     const int s0 = live ? esup_ptr[p] : 0, s1 = live ? esup_ptr[p + 1] : 0;
+    NodePre pre{};
+    if (live) pre = node_pre<false>(p, invSum, invM, bcflag, Uhi);
     // bounded wait for the copies (phase 0)
     if (!mbar_wait_bounded(ubar, 0u)) {
         if (threadIdx.x == 0) atomicExch(err, (int)CFD_ERR_BARRIER);
@@ -1131,7 +1156,7 @@ k_node_mixed_bulk(int npoin, const int* __restrict__ esup_ptr, const int* __rest
                 v3.add(ml[j].x * rv.z + ml[j].y * rv.w);
             }
     }
-    node_finish<false, LAST>(p, make_float4(0.f, 0.f, 0.f, 0.f), v1.value(), v2.value(), v3.value(),
+    node_finish<false, LAST>(p, pre, make_float4(0.f, 0.f, 0.f, 0.f), v1.value(), v2.value(), v3.value(),
                              invSum, gc, gf, U, Uhi, Ulo, invM, rk_fact, bcflag, bcval, nrm, WX,
                              WY, U1, RHO, VX, VY, Eo, Po, Tout, RMACH);
 }
