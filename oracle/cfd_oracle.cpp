@@ -858,8 +858,11 @@ struct Smoother {
         if (d_move > d_max) d_max = d_move;
         if (d_move > 2.2250738585072014e-308) update_list(ip);
     }
+    const int* order = nullptr;  // 0-based visiting order of the nodes (null: 1..npoin)
+    int node_at(int k) const { return (order ? order[k] : k) + 1; }
     void laplacianSmoothing(const int* fixed) {  // :74-114
-        for (int ip = 1; ip <= npoin; ++ip) {
+        for (int k = 0; k < npoin; ++k) {
+            const int ip = node_at(k);
             if (!(smoothable[ip - 1] && !fixed[ip - 1])) continue;
             double xn = 0.0, yn = 0.0;
             double mu_old = getMu_min(ip);
@@ -912,7 +915,8 @@ struct Smoother {
         int iter;
         for (iter = 1; iter <= NITER; ++iter) {
             double d_max = 0.0;
-            for (int ip = 1; ip <= npoin; ++ip) {
+            for (int k = 0; k < npoin; ++k) {
+                const int ip = node_at(k);
                 if (smoothable[ip - 1] && !fixed[ip - 1]) {
                     smoothable[ip - 1] = 0;
                     int min_idx = getMu_vec(mu_vec, ip);
@@ -927,9 +931,26 @@ struct Smoother {
 
 }  // namespace
 
+// The same algorithm visiting the nodes in `order` (0-based, a permutation) instead of node
+// order in its Laplacian passes and sweeps: the reference's sequential semantics (each node
+// sees every move made before it) in another order.  Test infrastructure for the GPU
+// smoothing, which moves one colour of mutually non-adjacent nodes at a time: with its
+// colour order here the two must agree exactly.
+extern "C" void or_smoothing_ordered(double* X, double* Y, const int* inpoel, const int* fixed,
+                                     int npoin, int nelem, const int* order, int* iters_out,
+                                     double* min_quality_out);
+
 extern "C" void or_smoothing(double* X, double* Y, const int* inpoel, const int* fixed,
                              int npoin, int nelem, int* iters_out, double* min_quality_out) {
+    or_smoothing_ordered(X, Y, inpoel, fixed, npoin, nelem, nullptr, iters_out,
+                         min_quality_out);
+}
+
+extern "C" void or_smoothing_ordered(double* X, double* Y, const int* inpoel, const int* fixed,
+                                     int npoin, int nelem, const int* order, int* iters_out,
+                                     double* min_quality_out) {
     Smoother s;
+    s.order = order;
     s.npoin = npoin;
     s.nelem = nelem;
     s.inpoel = inpoel;

@@ -44,6 +44,7 @@ _SIG = {
                        C.POINTER(abi.CfdSolveInfo)]),
     "or_normales": (_i, [_i, _i, _ip, _dp, _dp, _ip, _dp, _dp]),
     "or_smoothing": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _dp]),
+    "or_smoothing_ordered": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _ip, _dp]),
     "or_newmark_step": (None, [C.c_double, _dp, _dp, _dp, _dp]),
     "or_force_visc": (None, [_i, _i, _i, _ip, _ip, _ip, _i, C.c_double, C.c_double, C.c_double,
                              C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -227,14 +228,35 @@ def normales(wall, x, y):
     return ni[:m], nx[:m], ny[:m]
 
 
-def smoothing(x, y, inpoel, fixed):
+def smoothing(x, y, inpoel, fixed, order=None):
+    """smoothing.f90:21-72 -> (X, Y, iterations, min quality); `order` (0-based node
+    permutation) replaces node order in the Laplacian passes and the sweeps."""
     x, y = f64(x).copy(), f64(y).copy()
     inp = i32(inpoel)
     it = C.c_int(0)
     q = C.c_double(0)
-    lib().or_smoothing(dp(x), dp(y), ip(inp), ip(i32(fixed)), len(x), inp.shape[0],
-                       C.byref(it), C.byref(q))
+    if order is None:
+        lib().or_smoothing(dp(x), dp(y), ip(inp), ip(i32(fixed)), len(x), inp.shape[0],
+                           C.byref(it), C.byref(q))
+    else:
+        lib().or_smoothing_ordered(dp(x), dp(y), ip(inp), ip(i32(fixed)), len(x), inp.shape[0],
+                                   ip(i32(order)), C.byref(it), C.byref(q))
     return x, y, it.value, q.value
+
+
+def colour_order(inpoel, npoin):
+    """Nodes by colour of a greedy colouring of the point-neighbour graph in node order (each
+    node takes the least colour none of its lower-numbered neighbours has), in node order
+    within a colour: the order in which a colour-by-colour smoothing moves them."""
+    nbr, ptr = psup(inpoel, npoin)  # 1-based neighbours, 0-based row pointers
+    col = np.full(npoin, -1, np.int64)
+    for p in range(npoin):
+        used = {int(col[q - 1]) for q in nbr[ptr[p]:ptr[p + 1]] if col[q - 1] >= 0}
+        c = 0
+        while c in used:
+            c += 1
+        col[p] = c
+    return np.argsort(col, kind="stable").astype(np.int32)
 
 
 def newmark_step(H, F, dis, vel, acc):
