@@ -811,7 +811,8 @@ struct Smoother {
                    int ip) const {  // :245-272
         double gxm = gx[min_idx - 1], gym = gy[min_idx - 1], mum = mu_vec[min_idx - 1];
         double g2 = gxm * gxm + gym * gym;
-        double st = getH_min(ip) * FACTOR_STEP / (std::fabs(gxm) + std::fabs(gym));
+        double st = tol_move ? tol_move[ip - 1] / ((std::fabs(gxm) + std::fabs(gym)) * NITER)
+                             : getH_min(ip) * FACTOR_STEP / (std::fabs(gxm) + std::fabs(gym));
         int n = esup2[ip] - esup2[ip - 1];
         for (int i = 0; i < n; ++i) {
             double gg = gxm * gx[i] + gym * gy[i];
@@ -859,6 +860,7 @@ struct Smoother {
         if (d_move > 2.2250738585072014e-308) update_list(ip);
     }
     const int* order = nullptr;  // 0-based visiting order of the nodes (null: 1..npoin)
+    const double* tol_move = nullptr;  // setTol_move (:372-386): |dX| + |dY| per node, or null
     int node_at(int k) const { return (order ? order[k] : k) + 1; }
     void laplacianSmoothing(const int* fixed) {  // :74-114
         for (int k = 0; k < npoin; ++k) {
@@ -874,6 +876,11 @@ struct Smoother {
             }
             xn = xn / n;
             yn = yn / n;
+            if (tol_move) {  // SWITCH_TOL_MOVE (:98-102)
+                const double dX = xn - xo, dY = yn - yo;
+                xn = xo + dX / (std::fabs(dX) + std::fabs(dY)) * tol_move[ip - 1] / 2 * FACTOR_STEP;
+                yn = yo + dY / (std::fabs(dX) + std::fabs(dY)) * tol_move[ip - 1] / 2 * FACTOR_STEP;
+            }
             X[ip - 1] = xn;
             Y[ip - 1] = yn;
             if (getMu_min(ip) < mu_old) {
@@ -936,21 +943,25 @@ struct Smoother {
 // sees every move made before it) in another order.  Test infrastructure for the GPU
 // smoothing, which moves one colour of mutually non-adjacent nodes at a time: with its
 // colour order here the two must agree exactly.
+// tol_move: setTol_move's |dX| + |dY| per node (:372-386), or null (SWITCH_TOL_MOVE off).
 extern "C" void or_smoothing_ordered(double* X, double* Y, const int* inpoel, const int* fixed,
-                                     int npoin, int nelem, const int* order, int* iters_out,
+                                     int npoin, int nelem, const int* order,
+                                     const double* tol_move, int* iters_out,
                                      double* min_quality_out);
 
 extern "C" void or_smoothing(double* X, double* Y, const int* inpoel, const int* fixed,
                              int npoin, int nelem, int* iters_out, double* min_quality_out) {
-    or_smoothing_ordered(X, Y, inpoel, fixed, npoin, nelem, nullptr, iters_out,
+    or_smoothing_ordered(X, Y, inpoel, fixed, npoin, nelem, nullptr, nullptr, iters_out,
                          min_quality_out);
 }
 
 extern "C" void or_smoothing_ordered(double* X, double* Y, const int* inpoel, const int* fixed,
-                                     int npoin, int nelem, const int* order, int* iters_out,
+                                     int npoin, int nelem, const int* order,
+                                     const double* tol_move, int* iters_out,
                                      double* min_quality_out) {
     Smoother s;
     s.order = order;
+    s.tol_move = tol_move;
     s.npoin = npoin;
     s.nelem = nelem;
     s.inpoel = inpoel;

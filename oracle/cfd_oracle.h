@@ -80,9 +80,11 @@ int or_normales(int npoin, int nwall, const int* wall, const double* X, const do
 
 void or_smoothing(double* X, double* Y, const int* inpoel, const int* fixed, int npoin,
                   int nelem, int* iters_out, double* min_quality_out);
-/* the same visiting the nodes in `order` (0-based permutation; NULL: node order) */
+/* the same visiting the nodes in `order` (0-based permutation; NULL: node order), with
+ * setTol_move's |dX| + |dY| per node when tol_move is not NULL */
 void or_smoothing_ordered(double* X, double* Y, const int* inpoel, const int* fixed, int npoin,
-                          int nelem, const int* order, int* iters_out, double* min_quality_out);
+                          int nelem, const int* order, const double* tol_move, int* iters_out,
+                          double* min_quality_out);
 
 void or_force_visc(int nelem, int npoin, int nsets, const int* ielem_sets, const int* iset,
                    const int* inpoel, int nset_numb, double u_inf, double v_inf, double rho_inf,

@@ -44,7 +44,7 @@ _SIG = {
                        C.POINTER(abi.CfdSolveInfo)]),
     "or_normales": (_i, [_i, _i, _ip, _dp, _dp, _ip, _dp, _dp]),
     "or_smoothing": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _dp]),
-    "or_smoothing_ordered": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _ip, _dp]),
+    "or_smoothing_ordered": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _dp, _ip, _dp]),
     "or_newmark_step": (None, [C.c_double, _dp, _dp, _dp, _dp]),
     "or_force_visc": (None, [_i, _i, _i, _ip, _ip, _ip, _i, C.c_double, C.c_double, C.c_double,
                              C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -228,19 +228,22 @@ def normales(wall, x, y):
     return ni[:m], nx[:m], ny[:m]
 
 
-def smoothing(x, y, inpoel, fixed, order=None):
+def smoothing(x, y, inpoel, fixed, order=None, dX=None, dY=None):
     """smoothing.f90:21-72 -> (X, Y, iterations, min quality); `order` (0-based node
-    permutation) replaces node order in the Laplacian passes and the sweeps."""
+    permutation) replaces node order in the Laplacian passes and the sweeps; dX, dY turn on
+    the setTol_move path (:372-386) with tol = |dX| + |dY|."""
     x, y = f64(x).copy(), f64(y).copy()
     inp = i32(inpoel)
     it = C.c_int(0)
     q = C.c_double(0)
-    if order is None:
+    if order is None and dX is None:
         lib().or_smoothing(dp(x), dp(y), ip(inp), ip(i32(fixed)), len(x), inp.shape[0],
                            C.byref(it), C.byref(q))
     else:
+        tol = None if dX is None else f64(np.abs(f64(dX)) + np.abs(f64(dY)))
         lib().or_smoothing_ordered(dp(x), dp(y), ip(inp), ip(i32(fixed)), len(x), inp.shape[0],
-                                   ip(i32(order)), C.byref(it), C.byref(q))
+                                   None if order is None else ip(i32(order)),
+                                   None if tol is None else dp(tol), C.byref(it), C.byref(q))
     return x, y, it.value, q.value
 
 

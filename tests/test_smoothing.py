@@ -192,3 +192,36 @@ def test_gpu_smoothing_is_the_reference_in_colour_order(gpu_lib, oracle):
     assert it == ito
     assert np.array_equal(xs, xo) and np.array_equal(ys, yo)
     assert q == qo
+
+
+def _displacement(k, seed=5):
+    rng = np.random.default_rng(seed)
+    scale = 0.02 * np.abs(k.x).max() / np.sqrt(k.npoin)
+    return scale * rng.normal(size=k.npoin), scale * rng.normal(size=k.npoin)
+
+
+def test_oracle_tol_move_bounds_the_moves(oracle):
+    """The setTol_move path: a node moves at most 1.5 + 1.5 + 1 times |dX| + |dY| (two
+    Laplacian passes of tol/2 * FACTOR_STEP, NITER sweeps of tol / NITER)."""
+    k, x, y, fixed = jittered()
+    dX, dY = _displacement(k)
+    xs, ys, it, q = oracle.smoothing(x, y, k.inpoel, fixed, dX=dX, dY=dY)
+    tol = np.abs(dX) + np.abs(dY)
+    move = np.abs(xs - x) + np.abs(ys - y)
+    assert it >= 1 and move.max() > 0
+    assert (move <= 4.0 * tol * (1 + 1e-12)).all()
+
+
+@pytest.mark.gpu
+def test_gpu_tol_move_smoothing_is_the_reference_in_colour_order(gpu_lib, oracle):
+    """cfd_smoothing's setTol_move path (dX, dY given) against the oracle's, both visiting
+    the nodes in the GPU's colour order: the same mesh bit for bit."""
+    from cfd_gb300 import solver
+    k, x, y, fixed = jittered()
+    dX, dY = _displacement(k)
+    order = oracle.colour_order(k.inpoel, k.npoin)
+    xs, ys, it, q = solver.smoothing(x, y, k.inpoel, fixed, dX, dY)
+    xo, yo, ito, qo = oracle.smoothing(x, y, k.inpoel, fixed, order=order, dX=dX, dY=dY)
+    print("iterations", it, ito, "max |dx|", np.abs(xs - xo).max(), np.abs(ys - yo).max())
+    assert it == ito
+    assert np.array_equal(xs, xo) and np.array_equal(ys, yo)
