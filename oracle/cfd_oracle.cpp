@@ -1009,6 +1009,8 @@ struct or_case {
     double time = 0.0, dtmin = 0.0, dtmin1 = 0.0, disn[2] = {0.0, 0.0};
     double veln[2] = {0.0, 0.0}, accn[2] = {0.0, 0.0};  // setNewmarkCondition (meshMove.f90:14-25)
     bool fv_each = false;  // FORCE_VISC every step at the print block's point
+    int smooth_every = 0;    // smooth the moved mesh every this many steps (0: never)
+    std::vector<int> sm_order;  // the visiting order of that smoothing (0-based)
     double fvx[10] = {0}, fvy[10] = {0};
     std::vector<double> skin;
     double fx[10], fy[10], rm[10];
@@ -1179,6 +1181,28 @@ void newmark_method(double H, const double F[2], double DISN[2], double VELN[2],
     }
     for (int i = 0; i < 2; ++i) ACCN[i] = A1 * (DISN[i] - DISS[i]) - A2 * VELS[i] - A3 * ACCS[i];
     for (int i = 0; i < 2; ++i) VELN[i] = VELS[i] + A4 * ACCS[i] + A5 * ACCN[i];
+}
+
+// The moved mesh smoothed on the setTol_move path (smoothing.f90:372-386) with this step's
+// displacement, the mesh-motion nodes fixed, in c->sm_order; W becomes the whole move over
+// DTMIN at the nodes the smoothing moved.  The reference's loop has no such call (its calls
+// of the older SMOOTH_MESH are commented out, meshMove.f90:133): this restates the GPU
+// context's per-step smoothing option for its tests.
+void smooth_moved_mesh(or_case* c, double dtmin) {
+    const int N = c->npoin;
+    std::vector<double> tol(N), xb(c->X), yb(c->Y);
+    for (int i = 0; i < N; ++i) tol[i] = std::fabs(c->xpos[i]) + std::fabs(c->ypos[i]);
+    std::vector<int> fixed(N, 0);
+    for (int v : c->ilaux) fixed[v - 1] = 1;
+    or_smoothing_ordered(c->X.data(), c->Y.data(), c->inpoel.data(), fixed.data(), N, c->nelem,
+                         c->sm_order.empty() ? nullptr : c->sm_order.data(), tol.data(),
+                         nullptr, nullptr);
+    for (int i = 0; i < N; ++i) {
+        const double dx = c->X[i] - xb[i], dy = c->Y[i] - yb[i];
+        if (dx == 0.0 && dy == 0.0) continue;
+        c->W_X[i] = (c->xpos[i] + dx) / dtmin;
+        c->W_Y[i] = (c->ypos[i] + dy) / dtmin;
+    }
 }
 
 void fluid_structure(or_case* c, double dtmin, double time) {
@@ -1381,6 +1405,7 @@ int or_case_step(or_case* c, int nsteps, cfd_step_report* rep) {
         c->U1 = c->U;
         rk(c, dtmin);
         fluid_structure(c, dtmin, c->time);
+        if (c->smooth_every > 0 && c->iter % c->smooth_every == 0) smooth_moved_mesh(c, dtmin);
         if (c->fv_each) {  // the print block (:224-230): after the move, before deriv
             c->skin.assign(3 * (size_t)std::max(1, (int)(c->iset.size() / 3)), 0.0);
             or_case_force_visc_now(c);
@@ -1434,6 +1459,12 @@ void or_case_get_fields(or_case* c, double* RHO, double* VEL_X, double* VEL_Y, d
 }
 
 void or_case_set_force_visc(or_case* c, int each_step) { c->fv_each = each_step != 0; }
+
+void or_case_set_smoothing(or_case* c, int every, const int* order) {
+    c->smooth_every = every;
+    if (order) c->sm_order.assign(order, order + c->npoin);
+    else c->sm_order.clear();
+}
 
 void or_case_force_visc(or_case* c, double* F_VX, double* F_VY, double* skin) {
     if (!c->fv_each) {

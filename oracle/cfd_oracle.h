@@ -108,6 +108,9 @@ void or_case_get_motion(or_case* c, double* xpos, double* ypos);
  * the move, before deriv) and or_case_force_visc returns the last step's values; 0 makes
  * or_case_force_visc compute it on the current state and mesh.  skin: 3 per set edge. */
 void or_case_set_force_visc(or_case* c, int each_step);
+/* smooth the moved mesh every `every` steps on the setTol_move path, visiting the nodes in
+ * `order` (0-based; NULL: node order); W the whole move over DTMIN */
+void or_case_set_smoothing(or_case* c, int every, const int* order);
 void or_case_force_visc(or_case* c, double* F_VX, double* F_VY, double* skin);
 void or_case_get_geometry(or_case* c, double* area, double* dNx, double* dNy, double* M);
 void or_case_set_state(or_case* c, const double* U, const double* T, const double* VEL_X,

@@ -51,6 +51,7 @@ _SIG = {
                              _dp]),
     "or_case_force_visc": (None, [_vp, _dp, _dp, _dp]),
     "or_case_set_force_visc": (None, [_vp, _i]),
+    "or_case_set_smoothing": (None, [_vp, _i, _ip]),
     "or_case_create": (_vp, [C.POINTER(abi.CfdMesh), C.POINTER(abi.CfdParams), _i]),
     "or_case_destroy": (None, [_vp]),
     "or_case_step": (_i, [_vp, _i, C.POINTER(abi.CfdStepReport)]),
@@ -317,6 +318,15 @@ class OracleCase:
 
     def set_force_visc(self, each_step):
         lib().or_case_set_force_visc(self.h, 1 if each_step else 0)
+
+    def set_smoothing(self, every, order="colour"):
+        """Smooth the moved mesh every `every` steps (setTol_move path); order "colour": the
+        GPU's colour order, None: node order, or a 0-based permutation."""
+        if isinstance(order, str):
+            order = colour_order(self.case.inpoel, self.case.npoin)
+        self._sm_order = None if order is None else i32(order)
+        lib().or_case_set_smoothing(self.h, int(every),
+                                    None if self._sm_order is None else ip(self._sm_order))
 
     def force_visc(self):
         """FORCE_VISC now: (F_VX[nset_numb], F_VY[nset_numb], skin rows (nedges, 3))."""

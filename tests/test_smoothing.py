@@ -225,3 +225,40 @@ def test_gpu_tol_move_smoothing_is_the_reference_in_colour_order(gpu_lib, oracle
     print("iterations", it, ito, "max |dx|", np.abs(xs - xo).max(), np.abs(ys - yo).max())
     assert it == ito
     assert np.array_equal(xs, xo) and np.array_equal(ys, yo)
+
+
+def test_oracle_case_smooths_in_the_loop(oracle):
+    """The oracle's time loop with the per-step smoothing: the state stays finite and the
+    mesh differs from the unsmoothed run's."""
+    k = small_case(2, scale=16, seed=1)
+    a, b = oracle.OracleCase(k), oracle.OracleCase(k)
+    b.set_smoothing(1)
+    a.step(2)
+    b.step(2)
+    sa, sb = a.state(), b.state()
+    assert np.isfinite(sb["U"]).all()
+    assert not np.array_equal(sa["X"], sb["X"])
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_gpu_fp64_smoothing_in_the_loop_bit_exact(gpu_lib, oracle):
+    """The FP64 form with the moved mesh smoothed every 2nd step against the oracle's loop
+    with the same smoothing in the GPU's colour order: state, mesh, DTMIN and BiCG counts
+    equal bit for bit over 6 steps."""
+    from cfd_gb300 import abi, solver
+    k = small_case(2, scale=16, seed=1)
+    g = solver.Solver(k, precision=abi.CFD_PREC_FP64)
+    o = oracle.OracleCase(k)
+    g.set_smoothing(2)
+    o.set_smoothing(2)
+    for s in range(6):
+        rg, ro = g.step(1), o.step(1)
+        assert rg.dtmin == ro.dtmin and tuple(rg.bicg_iters) == tuple(ro.bicg_iters), s
+        sg, so = g.state(), o.state()
+        for key in ("U", "T", "X", "Y"):
+            assert np.array_equal(sg[key], so[key]), (s, key, np.abs(sg[key] - so[key]).max())
+    assert g.smoothing_stats()[0] == 3
+    g.close()
+    o.close()
