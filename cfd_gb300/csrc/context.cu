@@ -169,8 +169,8 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         a.nblk_r = blocks_for(npoin, 256);
         a.bscal = d_bscal;
         a.bcount = d_bcount;
-        // learned guess (decided by the caller): the judge keeps, per solve, the network's
-        // guess or the previous step's, whichever has the smaller r.z
+        // learned guess (decided by the caller): k_guess_judge keeps, per solve, the
+        // network's guess or the previous step's, whichever has the smaller r.z
         a.gflag = learned ? d_gflag : nullptr;
         a.gate = 0.0;
         a.only_if = nullptr;

@@ -359,7 +359,7 @@ int cfd_mpnn_forward(cfd_mpnn* net, cfd_mpnn_graph* g, int bf16, double* ux, dou
  * the network's guess is formed on the first mesh-motion solve after attaching, and then
  * whenever the previous step's solve took more than `gate` iterations (every step when
  * gate = 0); per solve it replaces the previous-step guess if its r.z (the solve's measure
- * of convergence) is the smaller, so the plain guess stays the fallback and the judge.
+ * of convergence) is the smaller, so the plain guess stays the fallback and the yardstick.
  * net = NULL detaches it (previous-step guess).  The network must outlive its use by the
  * context. */
 int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate);
