@@ -102,3 +102,20 @@ def test_fp64_run_files_identical_to_oracle(gpu_lib, tmp_path):
     for f in FILES:
         f = f.format(name=name)
         assert (tmp_path / "gpu" / f).read_bytes() == (tmp_path / "cpu" / f).read_bytes(), f
+
+
+@pytest.mark.gpu
+def test_command_lines_write_and_run_a_case(gpu_lib, tmp_path, capsys):
+    """`python -m cfd_gb300.case DIR` then `python -m cfd_gb300.driver DIR`: the mixed form
+    with per-step smoothing runs the written case and writes the reference's files."""
+    import json
+    import os
+    from cfd_gb300 import case as C, driver
+    d, out = str(tmp_path / "c3"), str(tmp_path / "out")
+    C.main([d, "--config", "3", "--scale", "24", "--maxiter", "4"])
+    driver.main([d, "--out", out, "--precision", "mixed", "--smooth-every", "2"])
+    last = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert last["iter"] == 4 and all(np.isfinite(last["residuals"]))
+    names = set(os.listdir(out))
+    assert {"FORCES", "DESPLAZAMIENTO", "FORCES_HISTORY"} <= names
+    assert any(n.endswith(".RST") for n in names) and any(n.endswith(".cnv") for n in names)
