@@ -784,10 +784,10 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         CFD_CUDA(cudaMemsetAsync(d_tcount, 0, 4 * sizeof(unsigned), stream));
         CFD_CUDA(cudaMemsetAsync(d_motion, 0, sizeof(MotionScal), stream));
         graphs_on = !timers_on && !(getenv("CFD_GRAPHS") && atoi(getenv("CFD_GRAPHS")) == 0);
-        // 8 blocks per SM measured best at 1M nodes (0.640 ms vs 0.671 with full grids, 0.69
-        // at 6, 0.65 at 16); 0 = full grids
+        // 6 blocks per SM measured best at 1M nodes with the current passes (0.535 ms; 3, 4,
+        // 5, 7, 8, 10, 12: 0.606, 0.568, 0.539, 0.538, 0.550, 0.561, 0.563); 0 = full grids
         branch_bpsm = getenv("CFD_BRANCH_BLOCKS_PER_SM") ? atoi(getenv("CFD_BRANCH_BLOCKS_PER_SM"))
-                                                         : 8;
+                                                         : 6;
         if ((st = narrow_mixed(true, true, true, true, true, true))) return st;
     }
     // setup geometry: NORMALES, DERIV, MASAS, laplace (ns2DComp.ALE.f90:88-100)
