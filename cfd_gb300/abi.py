@@ -23,6 +23,7 @@ CFD_MASS_MASAS, CFD_MASS_GCL_LITERAL, CFD_MASS_GCL_CORRECTED = 0, 1, 2
 CFD_MOTION_REFERENCE, CFD_MOTION_HARMONIC, CFD_MOTION_NEWMARK = 0, 1, 2
 CFD_GUESS_PREVIOUS, CFD_GUESS_ZERO, CFD_GUESS_LEARNED = 0, 1, 2
 CFD_ESTAB_REFERENCE, CFD_ESTAB_EXACT, CFD_ESTAB_REGULARIZED = 0, 1, 2
+CFD_BICG_TOL_ABS, CFD_BICG_TOL_REL, CFD_BICG_TOL_REL_R0 = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -44,7 +45,7 @@ class CfdParams(C.Structure):
         ("heave_amp", C.c_double), ("pitch_amp", C.c_double), ("motion_freq", C.c_double),
         ("mass_mode", C.c_int), ("guess_mode", C.c_int),
         ("bicg_tol", C.c_double), ("bicg_maxit", C.c_int), ("estab_mode", C.c_int),
-        ("reserved", C.c_int * 6),
+        ("bicg_tol_mode", C.c_int), ("reserved", C.c_int * 5),
     ]
 
 
@@ -67,12 +68,14 @@ class CfdStepReport(C.Structure):
         ("bicg_iters", C.c_int * 2), ("bicg_rz", C.c_double * 2),
         ("bicg_converged", C.c_int * 2),
         ("fx", C.c_double * 10), ("fy", C.c_double * 10), ("rm", C.c_double * 10),
-        ("nset_numb", C.c_int), ("reserved", C.c_int * 5),
+        ("nset_numb", C.c_int), ("reserved0", C.c_int),
+        ("bicg_relres", C.c_double * 2), ("reserved", C.c_int * 4),
     ]
 
 
 class CfdSolveInfo(C.Structure):
-    _fields_ = [("iters", C.c_int), ("converged", C.c_int), ("rz", C.c_double)]
+    _fields_ = [("iters", C.c_int), ("converged", C.c_int), ("rz", C.c_double),
+                ("relres", C.c_double)]
 
 
 def dptr(a):
@@ -111,6 +114,8 @@ SIGNATURES = {
                            C.POINTER(CfdSolveInfo)]),
     "cfd_bicg_ex": (C.c_int, [_dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _ip, C.c_double,
                               C.c_int, C.POINTER(CfdSolveInfo)]),
+    "cfd_bicg_mode": (C.c_int, [_dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _ip, C.c_double,
+                                C.c_int, C.c_int, C.POINTER(CfdSolveInfo)]),
     "cfd_bicg_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                           C.c_double, C.c_int, C.c_void_p,

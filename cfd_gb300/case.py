@@ -63,6 +63,7 @@ class Params:
     bicg_tol: float = 1.0e-10
     bicg_maxit: int = 1000
     estab_mode: int = abi.CFD_ESTAB_REFERENCE
+    bicg_tol_mode: int = abi.CFD_BICG_TOL_ABS
 
     def to_c(self) -> abi.CfdParams:
         p = abi.CfdParams()
@@ -344,7 +345,7 @@ def config_case(which: int, scale: Optional[int] = None, seed: int = 0) -> Case:
 
 # ----------------------------------------------------------------------------- file I/O
 _BUILD_KEYS = ("motion_law", "heave_amp", "pitch_amp", "motion_freq", "mass_mode",
-               "guess_mode", "bicg_tol", "bicg_maxit", "estab_mode")
+               "guess_mode", "bicg_tol", "bicg_maxit", "estab_mode", "bicg_tol_mode")
 
 
 def _fmt(v):

@@ -221,6 +221,8 @@ int cfd_ctx_create(cfd_ctx** out, const cfd_mesh* mesh, const cfd_params* p, int
         return arg_error("precision_mode");
     if (p->estab_mode < CFD_ESTAB_REFERENCE || p->estab_mode > CFD_ESTAB_REGULARIZED)
         return arg_error("estab_mode");
+    if (p->bicg_tol_mode < CFD_BICG_TOL_ABS || p->bicg_tol_mode > CFD_BICG_TOL_REL_R0)
+        return arg_error("bicg_tol_mode");
     if (p->ngas != 0) {
         set_last_message("only the perfect-gas path (NGAS = 0) is implemented");
         return CFD_ERR_ARG;
@@ -955,11 +957,13 @@ int cfd_laplace(const int* inpoel, const double* area, const double* dNx, const 
     return s.sync();
 }
 
-int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr, const double* diagMtx,
-                double* x, const double* b, const double* x_fix, const int* x_fixIdx,
-                const int* npoin, const int* nfix, double tol, int maxit, cfd_solve_info* info) {
+int cfd_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
+                  const double* diagMtx, double* x, const double* b, const double* x_fix,
+                  const int* x_fixIdx, const int* npoin, const int* nfix, double tol, int maxit,
+                  int tol_mode, cfd_solve_info* info) {
     if (!spMtx || !spIdx || !spRowptr || !diagMtx || !x || !b || !npoin || !nfix || *npoin <= 0 ||
-        *nfix < 0 || (*nfix > 0 && (!x_fix || !x_fixIdx)) || maxit < 0)
+        *nfix < 0 || (*nfix > 0 && (!x_fix || !x_fixIdx)) || maxit < 0 ||
+        tol_mode < CFD_BICG_TOL_ABS || tol_mode > CFD_BICG_TOL_REL_R0)
         return arg_error("cfd_bicg");
     const int N = *npoin, NF = *nfix;
     const int nnz = spRowptr[N];
@@ -1006,11 +1010,11 @@ int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr, cons
     TRY(s.put(&d_b, b, N));
     for (double** q : {&d_r, &d_z, &d_y, &d_p0, &d_p1}) TRY(s.alloc(q, N));
     const long nc = ((long)N + kChunk - 1) / kChunk;
-    TRY(s.alloc(&d_part, 4 * (size_t)nc));
+    TRY(s.alloc(&d_part, 6 * (size_t)nc));
     TRY(s.alloc(&d_bar, 1));
     TRY(s.alloc(&d_it, 2));
     TRY(s.alloc(&d_cv, 2));
-    TRY(s.alloc(&d_rz, 2));
+    TRY(s.alloc(&d_rz, 4));
     CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), s.stream));
     PcgArgs a{};
     a.n = N;
@@ -1035,8 +1039,10 @@ int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr, cons
     a.bar = d_bar;
     a.tol = tol;
     a.maxit = maxit;
+    a.tol_mode = tol_mode;
     a.iters_out = d_it;
     a.rz_out = d_rz;
+    a.relres_out = d_rz + 2;
     a.conv_out = d_cv;
     int dev = 0, nsm = 0, per_sm = 0;
     CFD_CUDA(cudaGetDevice(&dev));
@@ -1049,12 +1055,12 @@ int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr, cons
     CFD_CUDA(cudaLaunchCooperativeKernel((void*)k_pcg_fp64, dim3((unsigned)g), dim3(256), args, 0, s.stream));
     g_launches.fetch_add(1, std::memory_order_relaxed);
     int it = 0, cv = 0;
-    double rz = 0.0;
+    double rz[4] = {0.0, 0.0, 0.0, 0.0};
     GridBar gb{};
     TRY(s.get(x, d_x, N));
     TRY(s.get(&it, d_it, 1));
     TRY(s.get(&cv, d_cv, 1));
-    TRY(s.get(&rz, d_rz, 1));
+    TRY(s.get(rz, d_rz, 4));
     TRY(s.get(&gb, d_bar, 1));
     TRY(s.sync());
     if (gb.err) {
@@ -1064,9 +1070,17 @@ int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr, cons
     if (info) {
         info->iters = it;
         info->converged = cv;
-        info->rz = rz;
+        info->rz = rz[0];
+        info->relres = rz[2];
     }
     return CFD_OK;
+}
+
+int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr, const double* diagMtx,
+                double* x, const double* b, const double* x_fix, const int* x_fixIdx,
+                const int* npoin, const int* nfix, double tol, int maxit, cfd_solve_info* info) {
+    return cfd_bicg_mode(spMtx, spIdx, spRowptr, diagMtx, x, b, x_fix, x_fixIdx, npoin, nfix, tol,
+                         maxit, CFD_BICG_TOL_ABS, info);
 }
 
 int cfd_bicg(const double* spMtx, const int* spIdx, const int* spRowptr, const double* diagMtx,

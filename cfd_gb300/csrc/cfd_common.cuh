@@ -140,10 +140,21 @@ __device__ __forceinline__ double fold_partials(const double* part, long nc, dou
     return block_tree256(acc, red);
 }
 
-// ------------------------------------------------------------------ bounded grid barrier
-// Sense-free generation barrier for cooperative launches.  Every wait is bounded: after
-// kSpinLimit polls the block sets *err = CFD_ERR_BARRIER and leaves; callers check err.
+// ------------------------------------------------------------------ bounded waits
+// Every device-side wait of the library is bounded twice: by a number of polls and by the
+// elapsed time on the GPU's global nanosecond timer (a poll may suspend the thread for a
+// system-dependent time, so the count alone does not bound the time).
 constexpr long long kSpinLimit = 1LL << 24;
+constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Sense-free generation barrier for cooperative launches.  A block that waits longer than
+// the bounds above sets *err = CFD_ERR_BARRIER and leaves; callers check err.
 
 struct GridBar {
     unsigned int arrive;
@@ -166,8 +177,10 @@ __device__ __forceinline__ void grid_barrier(GridBar* gb, unsigned nblocks,
             atomicAdd(&gb->gen, 1u);
         } else {
             long long spins = 0;
+            const unsigned long long t0 = globaltimer_ns();
             while (*vgen == g) {
-                if (++spins > limit) {
+                if (++spins > limit ||
+                    ((spins & 63) == 0 && globaltimer_ns() - t0 > kWaitNs)) {
                     atomicExch(&gb->err, (int)CFD_ERR_BARRIER);
                     break;
                 }
@@ -180,17 +193,20 @@ __device__ __forceinline__ void grid_barrier(GridBar* gb, unsigned nblocks,
 }
 
 // Bounded wait on the phase of the given parity of a shared-memory mbarrier (an mbarrier
-// completed by bulk copies or by tcgen05.commit): false after `limit` polls
+// completed by bulk copies or by tcgen05.commit): false after `limit` polls or kWaitNs
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned ubar, unsigned parity,
                                                   long long limit = kSpinLimit) {
     unsigned done = 0;
-    for (long long k = 0; k < limit && !done; ++k)
+    const unsigned long long t0 = globaltimer_ns();
+    for (long long k = 0; k < limit && !done; ++k) {
         asm volatile(
             "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; "
             "selp.u32 %0, 1, 0, q; }"
             : "=r"(done)
             : "r"(ubar), "r"(parity)
             : "memory");
+        if (!done && (k & 63) == 63 && globaltimer_ns() - t0 > kWaitNs) break;
+    }
     return done != 0;
 }
 

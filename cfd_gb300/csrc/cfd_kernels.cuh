@@ -111,10 +111,11 @@ struct MotionScal {
 struct StepOut {
     StepScal sc;
     MotionScal ms;
-    double rz[2];
+    double rz[2], relres[2];
     int it[2], cv[2];
     int bar_err, has_motion;
 };
+// rz: [|r.z| x 2, ||r||/||ref|| x 2]
 __global__ void k_pack_report(const StepScal* sc, const MotionScal* ms, const int* it,
                               const int* cv, const double* rz, const GridBar* bar,
                               const int* wait_err, StepOut* out);
@@ -308,7 +309,8 @@ struct PcgArgs {
     const float* invdiagf;       // (float)(1/diag), with invdiag = (double)invdiagf
     double* part_r;              // [4][nblk_r] per-block partials of the row kernels
     long nblk_r;                 // 256-row blocks of the row kernels
-    double* bscal;               // [2 solves][4]: r.r, r.p, p.y, alfa of the first direction
+    double* bscal;               // [2 solves][8]: r.r, r.p, p.y, alfa of the first direction,
+                                 // the squared reference norm and the threshold on r.r
     unsigned* bcount;            // [3] block counters of the row kernels (zero between uses)
     // learned guess (null: off): the first residual pass sets gflag[0] = (sum r.z >= gate)
     // and clears gflag[1]; a pass with only_if != null runs only when *only_if != 0
@@ -318,8 +320,11 @@ struct PcgArgs {
     GridBar* bar;
     double tol;
     int maxit;
+    int tol_mode;                // CFD_BICG_TOL_*: the relative modes also sum r.r per
+                                 // iteration, in part[2][s] (part then holds 6 x nchunks)
     int* iters_out;              // [2]
     double* rz_out;              // [2]
+    double* relres_out;          // [2] ||r||/||ref|| (relative modes), may be null
     int* conv_out;               // [2]
 };
 

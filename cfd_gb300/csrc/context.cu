@@ -151,8 +151,10 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
     a.bar = d_bar;
     a.tol = prm.bicg_tol;
     a.maxit = prm.bicg_maxit;
+    a.tol_mode = prm.bicg_tol_mode;
     a.iters_out = d_pcg_iters;
     a.rz_out = d_pcg_rz;
+    a.relres_out = d_pcg_rz + 2;
     a.conv_out = d_pcg_conv;
     const bool mixed = (prec == CFD_PREC_MIXED);
     if (mixed) {
@@ -528,6 +530,7 @@ int Ctx::step(int nsteps, cfd_step_report* rep) {
     const int* it = h_out->it;
     const int* cv = h_out->cv;
     const double* rz = h_out->rz;
+    const double* relres = h_out->relres;
     GridBar gb{};
     gb.err = h_out->bar_err;
     if (d_motion && nsteps > 0) {  // the mixed form's clock is kept on the device
@@ -548,6 +551,7 @@ int Ctx::step(int nsteps, cfd_step_report* rep) {
         for (int s = 0; s < 2; ++s) {
             rep->bicg_iters[s] = it[s];
             rep->bicg_rz[s] = rz[s];
+            rep->bicg_relres[s] = relres[s];
             rep->bicg_converged[s] = cv[s];
         }
         rep->nset_numb = bc.nset_numb;
@@ -677,14 +681,14 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         CFD_CUDA(cudaMemsetAsync(d_xfix[s], 0, sizeof(double) * (nnmove ? nnmove : 1), stream));
     }
     const long nc = ((long)N + kChunk - 1) / kChunk;
-    if ((st = dalloc(&d_part, 4 * (size_t)(nc > 0 ? nc : 1)))) return st;
+    if ((st = dalloc(&d_part, 6 * (size_t)(nc > 0 ? nc : 1)))) return st;
     if ((st = dalloc(&d_bar, 1))) return st;
     if ((st = dalloc(&d_pcg_iters, 2))) return st;
     if ((st = dalloc(&d_pcg_conv, 2))) return st;
-    if ((st = dalloc(&d_pcg_rz, 2))) return st;
+    if ((st = dalloc(&d_pcg_rz, 4))) return st;  // |r.z| and ||r||/||ref|| per solve
     CFD_CUDA(cudaMemsetAsync(d_pcg_iters, 0, 2 * sizeof(int), stream));
     CFD_CUDA(cudaMemsetAsync(d_pcg_conv, 0, 2 * sizeof(int), stream));
-    CFD_CUDA(cudaMemsetAsync(d_pcg_rz, 0, 2 * sizeof(double), stream));
+    CFD_CUDA(cudaMemsetAsync(d_pcg_rz, 0, 4 * sizeof(double), stream));
     if ((st = dalloc(&d_scal, 1))) return st;
     if ((st = dalloc(&d_out, 1))) return st;
     StepScal sc0{};
@@ -746,11 +750,11 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
                 if ((st = dalloc(q, N))) return st;
             CFD_CUDA(cudaMemsetAsync(d_posf[s], 0, sizeof(float) * N, stream));
         }
-        if ((st = dalloc(&d_part_r, 4 * (size_t)blocks_for(N, 256)))) return st;
-        if ((st = dalloc(&d_bscal, 8))) return st;
+        if ((st = dalloc(&d_part_r, 6 * (size_t)blocks_for(N, 256)))) return st;
+        if ((st = dalloc(&d_bscal, 16))) return st;
         if ((st = dalloc(&d_bcount, 3))) return st;
         if ((st = dalloc(&d_invdiagf, N))) return st;
-        CFD_CUDA(cudaMemsetAsync(d_bscal, 0, 8 * sizeof(double), stream));
+        CFD_CUDA(cudaMemsetAsync(d_bscal, 0, 16 * sizeof(double), stream));
         CFD_CUDA(cudaMemsetAsync(d_bcount, 0, 3 * sizeof(unsigned), stream));
         if ((st = dalloc(&d_valf, adj.col.size()))) return st;
         if ((st = dalloc(&d_gterms, E))) return st;

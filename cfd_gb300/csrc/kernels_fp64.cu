@@ -828,6 +828,7 @@ __global__ void k_pack_report(const StepScal* __restrict__ sc, const MotionScal*
         out->it[s] = it[s];
         out->cv[s] = cv[s];
         out->rz[s] = rz[s];
+        out->relres[s] = rz[2 + s];
     }
     out->bar_err = bar->err | (wait_err ? *wait_err : 0);
 }

@@ -1079,8 +1079,8 @@ cudaError_t launch_elem_stage1_mixed(bool viscous, cudaStream_t st, int nelem, c
 // thread issues two cp.async.bulk copies (the recVisc records and the slot ids) into shared
 // memory, completing on an mbarrier, while every thread loads its node's own data; the
 // threads then gather the slots' mu, lambda (all of a node's gathers in flight at once) and
-// sum from shared memory in slot order.  The wait is bounded: past kSpinLimit polls the
-// block sets *err and leaves.
+// sum from shared memory in slot order.  The wait is bounded (kSpinLimit polls, kWaitNs of
+// the global timer): past either the block sets *err and leaves.
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
 }

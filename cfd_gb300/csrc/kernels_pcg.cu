@@ -6,7 +6,7 @@
 // once, sharing the matrix reads) is one launch: each iteration is two grid-wide phases
 // separated by a bounded grid barrier.
 //   phase 1: x += alfa*p (deferred from the previous iteration), r -= alfa*y, z = r/diag,
-//            partial sums of r.z
+//            partial sums of r.z (and of r.r under a relative stopping test)
 //   phase 2: p_new = beta*p + z computed on the fly inside the SpMV row loop
 //            (y_i = sum_j A_ij*(beta*p_j + z_j)), y(fix) = 1e30*p_new(fix), partial p.y
 // Every block folds the chunk partials itself in the fixed order of cfd_common.cuh, so
@@ -34,18 +34,38 @@ __device__ __forceinline__ double spmv_row_dir(const PcgArgs& a, int i, const do
     return dot;
 }
 
+// Row i of A.v and, in the same column order, the sum over the Dirichlet columns only
+// (the product with x_D, the vector that is v on the Dirichlet rows and 0 elsewhere; a
+// skipped term adds +0, which leaves a sum that starts at +0 unchanged)
+__device__ __forceinline__ double spmv_row_fixcols(const PcgArgs& a, int i, const double* v,
+                                                   double& dfix) {
+    double dot = 0.0, df = 0.0;
+    const int j1 = a.rowptr[i + 1];
+    for (int j = a.rowptr[i]; j < j1; ++j) {
+        const int c = a.col[j];
+        const double t = a.val[j] * v[c];
+        dot = dot + t;
+        if (a.isfix[c]) df = df + t;
+    }
+    dfix = df;
+    return dot;
+}
+
 __device__ __forceinline__ bool bar_failed(GridBar* gb) {
     return *((volatile int*)&gb->err) != 0;
 }
 
-__global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
+__global__ void __launch_bounds__(256, 3) k_pcg_fp64(PcgArgs a) {
     __shared__ double red[9];
+    __shared__ double s_thr[2], s_ref2[2];  // relative modes: threshold on r.r, ref.ref
     const int t = threadIdx.x;
     const int n = a.n;
     const int ns = a.nsolve;
     const long nc = ((long)n + kChunk - 1) / kChunk;
     const unsigned nb = gridDim.x;
     auto part = [&](int buf, int s) { return a.part + ((long)buf * 2 + s) * nc; };
+    const bool rel = a.tol_mode != CFD_BICG_TOL_ABS;      // r.r per iteration
+    const bool relb = a.tol_mode == CFD_BICG_TOL_REL;     // ||b - A.x_D|| as reference
 
     // copy1 (biconjGrad.f90:28): x(fix) = x_fix
     for (int k = blockIdx.x * blockDim.x + t; k < a.nfix; k += gridDim.x * blockDim.x)
@@ -54,37 +74,67 @@ __global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
     if (bar_failed(a.bar)) return;
 
     // y = A.x; y(fix) = 1e30*x(fix); r = -1*y + b; r(fix) = 0; r.r   (:138-144)
+    // CFD_BICG_TOL_REL also forms b - A.x_D (0 on the Dirichlet rows) and its square sum
     for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-        double acc[2] = {0.0, 0.0};
+        double acc[2] = {0.0, 0.0}, accb[2] = {0.0, 0.0};
         for (int k = 0; k < 4; ++k) {
             const long i = c * kChunk + t + 256L * k;
             if (i >= n) break;
             const bool fx = a.isfix[i];
             for (int s = 0; s < ns; ++s) {
-                double yi = fx ? 1.0e30 * a.x[s][i] : spmv_row(a, (int)i, a.x[s]);
+                double dfix = 0.0;
+                double yi = fx ? 1.0e30 * a.x[s][i]
+                               : (relb ? spmv_row_fixcols(a, (int)i, a.x[s], dfix)
+                                       : spmv_row(a, (int)i, a.x[s]));
                 a.y[s][i] = yi;
-                double ri = -1.0 * yi + (a.b[s] ? a.b[s][i] : 0.0);
+                const double bi = a.b[s] ? a.b[s][i] : 0.0;
+                double ri = -1.0 * yi + bi;
                 if (fx) ri = 0.0;
                 a.r[s][i] = ri;
                 acc[s] = (k == 0) ? ri * ri : acc[s] + ri * ri;
+                if (relb) {
+                    double ei = -1.0 * dfix + bi;
+                    if (fx) ei = 0.0;
+                    accb[s] = (k == 0) ? ei * ei : accb[s] + ei * ei;
+                }
             }
         }
         for (int s = 0; s < ns; ++s) {
             double v = block_tree256(acc[s], red);
             if (t == 0) part(0, s)[c] = v;
+            if (relb) {
+                v = block_tree256(accb[s], red);
+                if (t == 0) part(2, s)[c] = v;
+            }
         }
     }
     grid_barrier(a.bar, nb);
     if (bar_failed(a.bar)) return;
     bool done[2] = {true, true};
     double err_old[2] = {0.0, 0.0}, alfa[2] = {0.0, 0.0};
+    // relative modes: r.r of the current residual (rrc), and in shared memory the squared
+    // reference norm and the threshold r.r <= tol^2 * ref.ref
+    double rrc[2] = {0.0, 0.0};
     for (int s = 0; s < ns; ++s) {
         double rr = fold_partials(part(0, s), nc, red);
-        done[s] = rr < a.tol;
+        if (rel) {
+            const double ref2 = relb ? fold_partials(part(2, s), nc, red) : rr;
+            if (t == 0) {
+                s_ref2[s] = ref2;
+                s_thr[s] = (a.tol * a.tol) * ref2;
+            }
+            __syncthreads();
+            rrc[s] = rr;
+            done[s] = rr <= s_thr[s];
+        } else {
+            done[s] = rr < a.tol;
+        }
         if (done[s] && blockIdx.x == 0 && t == 0) {
             a.iters_out[s] = 0;
             a.rz_out[s] = rr;
             a.conv_out[s] = 1;
+            if (a.relres_out)
+                a.relres_out[s] = (rel && s_ref2[s] > 0.0) ? sqrt(rr / s_ref2[s]) : 0.0;
         }
     }
     if (done[0] && (ns < 2 || done[1])) return;
@@ -154,12 +204,13 @@ __global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
     while (true) {  // :156-170
         bool act[2] = {false, false};
         for (int s = 0; s < ns; ++s)
-            act[s] = !done[s] && fabs(err_old[s]) > a.tol && k < a.maxit;
+            act[s] = !done[s] && (rel ? rrc[s] > s_thr[s] : fabs(err_old[s]) > a.tol) &&
+                     k < a.maxit;
         if (!act[0] && !act[1]) break;
         k = k + 1;
         // phase 1
         for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-            double acc[2] = {0.0, 0.0};
+            double acc[2] = {0.0, 0.0}, accr[2] = {0.0, 0.0};
             for (int kk = 0; kk < 4; ++kk) {
                 const long i = c * kChunk + t + 256L * kk;
                 if (i >= n) break;
@@ -172,12 +223,17 @@ __global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
                     a.r[s][i] = ri;
                     a.z[s][i] = zi;
                     acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
+                    if (rel) accr[s] = (kk == 0) ? ri * ri : accr[s] + ri * ri;
                 }
             }
             for (int s = 0; s < ns; ++s) {
                 if (!act[s]) continue;
                 double v = block_tree256(acc[s], red);
                 if (t == 0) part(1, s)[c] = v;
+                if (rel) {
+                    v = block_tree256(accr[s], red);
+                    if (t == 0) part(2, s)[c] = v;
+                }
             }
         }
         for (int s = 0; s < ns; ++s) pend[s] = false;
@@ -187,6 +243,7 @@ __global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
         for (int s = 0; s < ns; ++s) {
             if (!act[s]) continue;
             err_new[s] = fold_partials(part(1, s), nc, red);
+            if (rel) rrc[s] = fold_partials(part(2, s), nc, red);
             beta[s] = err_new[s] / err_old[s];
         }
         // phase 2
@@ -238,7 +295,9 @@ __global__ void __launch_bounds__(256) k_pcg_fp64(PcgArgs a) {
             if (done[s]) continue;
             a.iters_out[s] = last_iter[s];
             a.rz_out[s] = fabs(err_old[s]);
-            a.conv_out[s] = fabs(err_old[s]) > a.tol ? 0 : 1;
+            a.conv_out[s] = (rel ? rrc[s] > s_thr[s] : fabs(err_old[s]) > a.tol) ? 0 : 1;
+            if (a.relres_out)
+                a.relres_out[s] = (rel && s_ref2[s] > 0.0) ? sqrt(rrc[s] / s_ref2[s]) : 0.0;
         }
 }
 

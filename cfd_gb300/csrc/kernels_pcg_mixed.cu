@@ -21,15 +21,18 @@ namespace cfd {
 // together, then the gathered vector entries, so each batch costs two dependent memory
 // latencies instead of two per entry.  The products are still summed in column order.
 
-// row i of A times (v0, v1): one pass over the row's columns for both right-hand sides
-template <int NS, int kRowBatch = 8>
+// row i of A times (v0, v1): one pass over the row's columns for both right-hand sides;
+// with FIXC also the sums over the Dirichlet columns only (f0, f1: the row of A.x_D)
+template <int NS, bool FIXC = false, int kRowBatch = 8>
 __device__ __forceinline__ void spmv_row2_f(const PcgArgs& a, int i, const float* v0,
-                                            const float* v1, float& d0, float& d1) {
-    float s0 = 0.f, s1 = 0.f;
+                                            const float* v1, float& d0, float& d1,
+                                            float* f0 = nullptr, float* f1 = nullptr) {
+    float s0 = 0.f, s1 = 0.f, g0 = 0.f, g1 = 0.f;
     const int j0 = a.rowptr[i], j1 = a.rowptr[i + 1];
     for (int jb = j0; jb < j1; jb += kRowBatch) {
         int c[kRowBatch];
         float m[kRowBatch], x0[kRowBatch], x1[kRowBatch];
+        bool fx[kRowBatch];
 #pragma unroll
         for (int u = 0; u < kRowBatch; ++u)
             if (jb + u < j1) {
@@ -41,16 +44,25 @@ __device__ __forceinline__ void spmv_row2_f(const PcgArgs& a, int i, const float
             if (jb + u < j1) {
                 x0[u] = v0[c[u]];
                 if (NS == 2) x1[u] = v1[c[u]];
+                if (FIXC) fx[u] = a.isfix[c[u]] != 0;
             }
 #pragma unroll
         for (int u = 0; u < kRowBatch; ++u)
             if (jb + u < j1) {
                 s0 += m[u] * x0[u];
                 if (NS == 2) s1 += m[u] * x1[u];
+                if (FIXC && fx[u]) {
+                    g0 += m[u] * x0[u];
+                    if (NS == 2) g1 += m[u] * x1[u];
+                }
             }
     }
     d0 = s0;
     d1 = s1;
+    if (FIXC) {
+        *f0 = g0;
+        *f1 = g1;
+    }
 }
 
 template <int kRowBatch = 4>
@@ -140,24 +152,25 @@ __device__ bool last_block_fold(unsigned* count, const double* part, long nb, in
 
 // First pass of a solve, one row per thread: y = A.x (FP32 SpMV over the shadow of x),
 // r = b - y with r(fix) = 0, p = r/diag (as r*(1/diag)); per-block partials of r.r and r.p
-// (biconjGrad.f90:29-38).  y itself is not kept: the next pass overwrites it.  A block
-// visits the 256-row groups blockIdx.x, blockIdx.x + gridDim.x, ... (one group when the
-// grid has a block per group); there is one partial per block.
-template <int NS>
+// (biconjGrad.f90:29-38), and with RELB of e.e, e = b - A.x_D (0 on the Dirichlet rows),
+// the reference norm of CFD_BICG_TOL_REL.  y itself is not kept: the next pass overwrites
+// it.  A block visits the 256-row groups blockIdx.x, blockIdx.x + gridDim.x, ... (one
+// group when the grid has a block per group); there is one partial per block.
+template <int NS, bool RELB>
 __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) {
     const int t = threadIdx.x;
-    double rr[2] = {0.0, 0.0}, rp[2] = {0.0, 0.0};
+    double rr[2] = {0.0, 0.0}, rp[2] = {0.0, 0.0}, ee[2] = {0.0, 0.0};
     for (long rb = blockIdx.x; rb < a.nblk_r; rb += gridDim.x) {
     const long i = rb * 256 + t;
     if (i < a.n) {
         const bool fx = a.isfix[i];
-        float d[2] = {0.f, 0.f};
-        if (!fx) spmv_row2_f<NS>(a, (int)i, a.xf[0], a.xf[1], d[0], d[1]);
+        float d[2] = {0.f, 0.f}, f[2] = {0.f, 0.f};
+        if (!fx) spmv_row2_f<NS, RELB>(a, (int)i, a.xf[0], a.xf[1], d[0], d[1], &f[0], &f[1]);
         const double id = a.invdiag[i];
         const float idf = a.invdiagf[i];
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-            double r, p;
+            double r, p, e = 0.0;
             float pf;
             if (fx) {
                 r = 0.0;
@@ -167,16 +180,19 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
                 r = a.b[s][i] - f2d_bits(d[s]);
                 p = r * id;
                 pf = d2f_trunc(p);
+                if (RELB) e = a.b[s][i] - f2d_bits(f[s]);
             } else {
                 r = f2d_bits(-d[s]);
                 p = r * id;
                 pf = -d[s] * idf;
+                if (RELB) e = f2d_bits(-f[s]);
             }
             a.r[s][i] = r;
             a.p[s][0][i] = p;
             a.pf[s][0][i] = pf;
             rr[s] += r * r;
             rp[s] += r * p;
+            if (RELB) ee[s] += e * e;
         }
     }
     }
@@ -184,24 +200,38 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
     for (int s = 0; s < 2; ++s) {
         sh[s][t] = rr[s];
         sh[2 + s][t] = rp[s];
+        if (RELB) sh[4 + s][t] = ee[s];
     }
     __syncthreads();
-    if ((t >> 5) < 4) {
+    if ((t >> 5) < (RELB ? 6 : 4)) {
         const double v = warp_sum256(sh[t >> 5]);
         if ((t & 31) == 0) a.part_r[(t >> 5) * gridDim.x + blockIdx.x] = v;
     }
 }
 
+// The first pass's convergence test of solve s (biconjGrad.f90:35, or the relative test)
+__device__ __forceinline__ bool first_done(const PcgArgs& a, int s) {
+    const double rr = a.bscal[8 * s];
+    return a.tol_mode == CFD_BICG_TOL_ABS ? rr < a.tol : rr <= a.bscal[8 * s + 5];
+}
+
 __global__ void __launch_bounds__(256) k_bicg_resid_mixed(PcgArgs a) {
-    __shared__ double sh[4][256];
-    __shared__ double out[4];
+    __shared__ double sh[6][256];
+    __shared__ double out[6];
     if (a.only_if && !*a.only_if) return;  // the same in every block
-    if (a.nsolve == 2) first_rows<2>(a, sh);
-    else first_rows<1>(a, sh);
-    if (last_block_fold(&a.bcount[0], a.part_r, gridDim.x, 4, sh, out) && threadIdx.x == 0) {
+    const bool relb = a.tol_mode == CFD_BICG_TOL_REL;
+    if (a.nsolve == 2) relb ? first_rows<2, true>(a, sh) : first_rows<2, false>(a, sh);
+    else relb ? first_rows<1, true>(a, sh) : first_rows<1, false>(a, sh);
+    if (last_block_fold(&a.bcount[0], a.part_r, gridDim.x, relb ? 6 : 4, sh, out) &&
+        threadIdx.x == 0) {
         for (int s = 0; s < 2; ++s) {
-            a.bscal[4 * s + 0] = out[s];      // r.r
-            a.bscal[4 * s + 1] = out[2 + s];  // r.p
+            a.bscal[8 * s + 0] = out[s];      // r.r
+            a.bscal[8 * s + 1] = out[2 + s];  // r.p
+            if (a.tol_mode != CFD_BICG_TOL_ABS) {
+                const double ref2 = relb ? out[4 + s] : out[s];
+                a.bscal[8 * s + 4] = ref2;
+                a.bscal[8 * s + 5] = (a.tol * a.tol) * ref2;
+            }
         }
         if (a.gflag && !a.only_if) {  // gate on r.z, the convergence measure of the solve
             a.gflag[0] = (out[2] + out[3] >= a.gate) ? 1 : 0;
@@ -253,7 +283,7 @@ __global__ void k_guess_select(PcgArgs a, const double* __restrict__ cand0,
     bool use[2] = {false, false};
     if (open)
 #pragma unroll
-        for (int s = 0; s < 2; ++s) use[s] = s < a.nsolve && rr[s] < a.bscal[4 * s + 1];
+        for (int s = 0; s < 2; ++s) use[s] = s < a.nsolve && rr[s] < a.bscal[8 * s + 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         stats[0] += open ? 1 : 0;
         stats[1] += use[0] ? 1 : 0;
@@ -283,7 +313,7 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
     const int t = threadIdx.x;
     bool act[2];
 #pragma unroll
-    for (int s = 0; s < 2; ++s) act[s] = s < a.nsolve && !(a.bscal[4 * s] < a.tol);
+    for (int s = 0; s < 2; ++s) act[s] = s < a.nsolve && !first_done(a, s);
     if (!act[0] && !act[1]) return;  // the same in every block
     // 256-row groups blockIdx.x, blockIdx.x + gridDim.x, ...; one partial per block
     double py[2] = {0.0, 0.0};
@@ -311,13 +341,14 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
     if (last_block_fold(&a.bcount[1], a.part_r, gridDim.x, 2, sh, out) && t == 0)
         for (int s = 0; s < 2; ++s)
             if (act[s]) {
-                a.bscal[4 * s + 2] = out[s];
-                a.bscal[4 * s + 3] = a.bscal[4 * s + 1] / out[s];
+                a.bscal[8 * s + 2] = out[s];
+                a.bscal[8 * s + 3] = a.bscal[8 * s + 1] / out[s];
             }
 }
 
 __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
     __shared__ double red[9];
+    __shared__ double s_thr[2], s_ref2[2];  // relative modes: threshold on r.r, ref.ref
     const int t = threadIdx.x;
     const int n = a.n;
     const int ns = a.nsolve;
@@ -327,25 +358,35 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
 
     // x(fix), r, p, err = r.p, y = A.p and alfa come from k_bicg_fix_mixed,
     // k_bicg_resid_mixed and k_bicg_dir_mixed
+    const bool rel = a.tol_mode != CFD_BICG_TOL_ABS;  // r.r per iteration
     bool done[2] = {true, true};
     double err_old[2] = {0.0, 0.0}, alfa[2] = {0.0, 0.0};
     bool pend[2] = {false, false};
     int cur[2] = {0, 0};
     double err_new[2] = {0.0, 0.0};
+    double rrc[2] = {0.0, 0.0};
+    if (t < 2) {
+        s_ref2[t] = a.bscal[8 * t + 4];
+        s_thr[t] = a.bscal[8 * t + 5];
+    }
+    __syncthreads();
 #pragma unroll
     for (int s = 0; s < 2; ++s)
         if (s < ns) {
-            const double rr = a.bscal[4 * s];
-            done[s] = rr < a.tol;
+            const double rr = a.bscal[8 * s];
+            done[s] = first_done(a, s);
+            if (rel) rrc[s] = rr;
             if (done[s]) {
                 if (blockIdx.x == 0 && t == 0) {
                     a.iters_out[s] = 0;
                     a.rz_out[s] = rr;
                     a.conv_out[s] = 1;
+                    if (a.relres_out)
+                        a.relres_out[s] = (rel && s_ref2[s] > 0.0) ? sqrt(rr / s_ref2[s]) : 0.0;
                 }
             } else {
-                err_new[s] = a.bscal[4 * s + 1];
-                alfa[s] = a.bscal[4 * s + 3];
+                err_new[s] = a.bscal[8 * s + 1];
+                alfa[s] = a.bscal[8 * s + 3];
                 err_old[s] = err_new[s];
                 pend[s] = true;
             }
@@ -357,12 +398,14 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
     while (true) {
         bool act[2] = {false, false};
 #pragma unroll
-        for (int s = 0; s < 2; ++s) act[s] = !done[s] && fabs(err_old[s]) > a.tol && k < a.maxit;
+        for (int s = 0; s < 2; ++s)
+            act[s] = !done[s] && (rel ? rrc[s] > s_thr[s] : fabs(err_old[s]) > a.tol) &&
+                     k < a.maxit;
         if (!act[0] && !act[1]) break;
         k = k + 1;
-        // phase 1: x += alfa p; r -= alfa y; z = r/diag; r.z
+        // phase 1: x += alfa p; r -= alfa y; z = r/diag; r.z (and r.r, relative modes)
         for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-            double acc[2] = {0.0, 0.0};
+            double acc[2] = {0.0, 0.0}, accr[2] = {0.0, 0.0};
             for (int kk = 0; kk < 4; ++kk) {
                 const long i = c * kChunk + t + 256L * kk;
                 if (i >= n) break;
@@ -377,13 +420,18 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
                     a.z[s][i] = zi;
                     a.zf[s][i] = d2f_trunc(zi);
                     acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
+                    if (rel) accr[s] = (kk == 0) ? ri * ri : accr[s] + ri * ri;
                 }
             }
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
                 if (!act[s]) continue;
-                const double v = block_tree256(acc[s], red);
+                double v = block_tree256(acc[s], red);
                 if (t == 0) part(1, s)[c] = v;
+                if (rel) {
+                    v = block_tree256(accr[s], red);
+                    if (t == 0) part(2, s)[c] = v;
+                }
             }
         }
 #pragma unroll
@@ -396,6 +444,7 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
         for (int s = 0; s < 2; ++s) {
             if (!act[s]) continue;
             err_new[s] = fold_partials(part(1, s), nc, red);
+            if (rel) rrc[s] = fold_partials(part(2, s), nc, red);
             beta[s] = err_new[s] / err_old[s];
             betaf[s] = d2f_trunc(beta[s]);
         }
@@ -461,7 +510,9 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
             if (done[s]) continue;
             a.iters_out[s] = last_iter[s];
             a.rz_out[s] = fabs(err_old[s]);
-            a.conv_out[s] = fabs(err_old[s]) > a.tol ? 0 : 1;
+            a.conv_out[s] = (rel ? rrc[s] > s_thr[s] : fabs(err_old[s]) > a.tol) ? 0 : 1;
+            if (a.relres_out)
+                a.relres_out[s] = (rel && s_ref2[s] > 0.0) ? sqrt(rrc[s] / s_ref2[s]) : 0.0;
         }
 }
 

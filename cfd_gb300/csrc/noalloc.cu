@@ -5,8 +5,12 @@
 // arrays are already resident, or a framework with its own memory pool and a fixed
 // budget), or a time loop that must not allocate once it is running.  For them
 // cfd_bicg_device_noalloc solves on arrays that are already in device memory and keeps
-// its work vectors in one file-scope static device array of fixed size, set aside when
-// the library is loaded on a GPU.
+// its work vectors in one file-scope static device array of fixed size.  The CUDA runtime
+// creates that array when it loads this file's module on a device; with lazy module
+// loading (the default since CUDA 12.2, CUDA_MODULE_LOADING=LAZY) that happens inside the
+// first call on each device, at its cudaGetSymbolAddress, so a caller whose own pool will
+// take all free device memory makes that first call during its set-up.  Later calls on the
+// device use the address found then and allocate nothing.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -130,6 +134,7 @@ extern "C" int cfd_bicg_device_noalloc(const double* spMtx, const int* col, cons
         info->iters = h.iters[0];
         info->converged = h.conv[0];
         info->rz = h.rz[0];
+        info->relres = 0.0;
     }
     return CFD_OK;
 }

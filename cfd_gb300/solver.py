@@ -204,16 +204,19 @@ def laplace(inpoel, area, dNx, dNy, X, Y, lap_idx, lap_rowptr):
     return vals, diag
 
 
-def biCG(spMtx, spIdx, spRowptr, diagMtx, x, b, x_fix, x_fixIdx, tol=1.0e-10, maxit=1000):
-    """x (initial guess, copied) -> (solution, CfdSolveInfo) (biconjGrad.f90:8-62)."""
+def biCG(spMtx, spIdx, spRowptr, diagMtx, x, b, x_fix, x_fixIdx, tol=1.0e-10, maxit=1000,
+         tol_mode=abi.CFD_BICG_TOL_ABS):
+    """x (initial guess, copied) -> (solution, CfdSolveInfo) (biconjGrad.f90:8-62).
+    tol_mode CFD_BICG_TOL_ABS is the reference's absolute test on |r.z|; the relative modes
+    stop when ||r|| <= tol * ||ref|| (include/cfd_gpu.h)."""
     L = abi.lib()
     x = _f64(x).copy()
     info = abi.CfdSolveInfo()
     fi = _i32(x_fixIdx)
-    check(L.cfd_bicg_ex(dptr(_f64(spMtx)), iptr(_i32(spIdx)), iptr(_i32(spRowptr)),
-                        dptr(_f64(diagMtx)), dptr(x), dptr(_f64(b)), dptr(_f64(x_fix)),
-                        iptr(fi), _ci(len(x)), _ci(len(fi)), float(tol), int(maxit),
-                        C.byref(info)), "cfd_bicg")
+    check(L.cfd_bicg_mode(dptr(_f64(spMtx)), iptr(_i32(spIdx)), iptr(_i32(spRowptr)),
+                          dptr(_f64(diagMtx)), dptr(x), dptr(_f64(b)), dptr(_f64(x_fix)),
+                          iptr(fi), _ci(len(x)), _ci(len(fi)), float(tol), int(maxit),
+                          int(tol_mode), C.byref(info)), "cfd_bicg")
     return x, info
 
 

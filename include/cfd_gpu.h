@@ -80,6 +80,17 @@ enum {
                                  (round-off in the reference) is d                      */
 };
 
+/* bicg_tol_mode: what the BiCG stopping test measures.  The reference's test is absolute
+ * (biconjGrad.f90:26, :35, :47); the relative modes compare the 2-norm of the (Dirichlet-
+ * rows-zeroed) residual r with a reference norm:  ||r|| <= tol * ||ref||. */
+enum {
+    CFD_BICG_TOL_ABS = 0,     /* |r.z| <= tol, early exit on r.r < tol (reference)      */
+    CFD_BICG_TOL_REL = 1,     /* ref = b - A.x_D, the residual of the guess that is 0 off
+                                 the Dirichlet rows: independent of the initial guess, so
+                                 every guess solves to the same accuracy                 */
+    CFD_BICG_TOL_REL_R0 = 2   /* ref = r_0, the residual of the initial guess           */
+};
+
 /* ---------------------------------------------------------------- plain structs */
 
 /* InputData (dataLoader.f90:5-15) after readInputData's derivations (:58-64),
@@ -98,7 +109,8 @@ typedef struct cfd_params {
     double bicg_tol;          /* 1e-10 in biconjGrad.f90:26 (absolute, on r.z)         */
     int bicg_maxit;           /* 1000 in biconjGrad.f90:47                             */
     int estab_mode;           /* CFD_ESTAB_*                                           */
-    int reserved[6];
+    int bicg_tol_mode;        /* CFD_BICG_TOL_* (default 0: the reference's absolute test) */
+    int reserved[5];
 } cfd_params;
 
 /* MeshData (dataLoader.f90:68-91) as loadMeshData leaves it.  Host pointers, Fortran
@@ -127,13 +139,17 @@ typedef struct cfd_step_report {
     int bicg_converged[2];
     double fx[10], fy[10], rm[10]; /* FORCES (pressure) per set, before the mesh moves */
     int nset_numb;
-    int reserved[5];
+    int reserved0;
+    double bicg_relres[2];    /* ||r||/||ref|| of the last iteration (relative modes; 0 in
+                                 the absolute mode)                                    */
+    int reserved[4];
 } cfd_step_report;
 
 typedef struct cfd_solve_info {
     int iters;                /* k of biconjGrad.f90:47-48                             */
-    int converged;            /* 1 if |r.z| <= tol (or early exit at :144)             */
-    double rz;                /* final |r.z|                                           */
+    int converged;            /* 1 if the stopping test holds (or the early exit at :35) */
+    double rz;                /* final |r.z| (at an early exit: r.r, as the reference)  */
+    double relres;            /* relative modes: final ||r||/||ref||; absolute mode: 0  */
 } cfd_solve_info;
 
 typedef struct cfd_ctx cfd_ctx;
@@ -236,6 +252,13 @@ int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr,
                 const double* diagMtx, double* x, const double* b, const double* x_fix,
                 const int* x_fixIdx, const int* npoin, const int* nfix,
                 double tol, int maxit, cfd_solve_info* info);
+/* biCG with the stopping test chosen by tol_mode (CFD_BICG_TOL_*; tol is then the relative
+ * tolerance, e.g. 1e-10).  The iterates are those of cfd_bicg_ex, only the iteration at
+ * which the solve stops differs. */
+int cfd_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
+                  const double* diagMtx, double* x, const double* b, const double* x_fix,
+                  const int* x_fixIdx, const int* npoin, const int* nfix,
+                  double tol, int maxit, int tol_mode, cfd_solve_info* info);
 
 /* BiCG on arrays already in device memory, with no device allocation.  This entry has no
  * counterpart in the reference: it is for callers that cannot call cudaMalloc where they
@@ -249,9 +272,11 @@ int cfd_bicg_ex(const double* spMtx, const int* spIdx, const int* spRowptr,
  * Dirichlet values on those rows (the reference's copy1), b may be NULL (zero).  Same
  * arithmetic and result as cfd_bicg_ex.  Runs on `stream` (cudaStream_t, NULL = default)
  * and waits for it before returning.  The first call on a device looks up the array's
- * device address (call it once before any stream capture).  Every call shares the one
- * array: calls that overlap on the GPU (other streams or threads) race.  npoin above the
- * cap returns CFD_ERR_LIMIT. */
+ * device address; under CUDA's lazy module loading (the default, CUDA_MODULE_LOADING=LAZY)
+ * that lookup is also when the runtime creates the array on the device, so make the first
+ * call during set-up, before a memory pool takes the free device memory and before any
+ * stream capture.  Every call shares the one array: calls that overlap on the GPU (other
+ * streams or threads) race.  npoin above the cap returns CFD_ERR_LIMIT. */
 #define CFD_NOALLOC_MAX_NPOIN 65536
 int cfd_bicg_device_noalloc(const double* spMtx, const int* col, const int* rowptr,
                             const double* diag, const unsigned char* isfix, double* x,
@@ -412,8 +437,9 @@ long long cfd_kernel_launches(void);
 /* Failure-detection self-test (no counterpart in the reference): runs, in one block, the
  * library's two bounded device waits on conditions that never come true (a grid barrier
  * that a second block never reaches; an mbarrier nothing arrives on), each giving up after
- * `polls` polls (1 .. 2^24; the library's kernels use 2^24).  Both statuses come back as
- * CFD_ERR_BARRIER and the device stays usable. */
+ * `polls` polls (1 .. 2^24; the library's kernels use 2^24) or 1 s on the GPU's global
+ * timer, whichever comes first (every wait of the library has both bounds).  Both statuses
+ * come back as CFD_ERR_BARRIER and the device stays usable. */
 int cfd_selftest_waits(long long polls, int* barrier_status, int* mbarrier_status);
 
 const char* cfd_strerror(int status);

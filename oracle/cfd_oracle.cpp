@@ -18,9 +18,14 @@
 
 namespace {
 
-// x**1.5d0 and x**(-.5d0): see the header for why these compositions.
-inline double pow15(double x) { return x * std::sqrt(x); }
-inline double powm05(double x) { return 1.0 / std::sqrt(x); }
+// x**1.5d0, x**.5d0 and x**(-.5d0): see the header for why these compositions.  With
+// or_set_pow_mode(1) they are std::pow (the C library's pow), which is how a Fortran
+// compiler without unsafe-math options evaluates a real exponent: the mode measures how far
+// a build of the reference that calls pow sits from the compositions.
+int g_pow_mode = 0;
+inline double pow15(double x) { return g_pow_mode ? std::pow(x, 1.5) : x * std::sqrt(x); }
+inline double powm05(double x) { return g_pow_mode ? std::pow(x, -0.5) : 1.0 / std::sqrt(x); }
+inline double pow05(double x) { return g_pow_mode ? std::pow(x, 0.5) : std::sqrt(x); }
 
 // ESTAB's DUX/DUY evaluation (CFD_ESTAB_*), set by or_set_estab_mode / the case params
 int g_estab_mode = CFD_ESTAB_REFERENCE;
@@ -47,6 +52,23 @@ void or_set_threads(int n) {
 }
 
 void or_set_estab_mode(int mode) { g_estab_mode = mode; }
+void or_set_pow_mode(int mode) { g_pow_mode = mode; }
+int or_get_pow_mode(void) { return g_pow_mode; }
+
+// How many of x[0..n) give pow(x, 1.5) != x*sqrt(x), pow(x, -0.5) != 1/sqrt(x) and
+// pow(x, 0.5) != sqrt(x) (the three non-integer powers of the reference's step)
+void or_pow_census(int n, const double* x, long long* out3) {
+    long long c15 = 0, cm05 = 0, c05 = 0;
+    for (int i = 0; i < n; ++i) {
+        const double v = x[i];
+        if (std::pow(v, 1.5) != v * std::sqrt(v)) ++c15;
+        if (std::pow(v, -0.5) != 1.0 / std::sqrt(v)) ++cm05;
+        if (std::pow(v, 0.5) != std::sqrt(v)) ++c05;
+    }
+    out3[0] = c15;
+    out3[1] = cm05;
+    out3[2] = c05;
+}
 void or_set_estab_eps(double eps) { g_estab_eps = eps; }
 void or_set_estab_dir(double ux, double uy) {
     const double n = std::sqrt(ux * ux + uy * uy);
@@ -131,7 +153,7 @@ void or_deltat(int npoin, int nelem, const double* T, const double* VEL_X,
             if (vv > vvmax) vvmax = vv;
         }
         double hh = std::sqrt(2.0 * area[e]);
-        double vel = std::sqrt(vumax * vumax + vvmax * vvmax);
+        double vel = pow05(vumax * vumax + vvmax * vvmax);  // :194 (**.5D0)
         const double smu = 110.0;
         double fmu = 0.017 * pow15(T_iel / T_inf) * (T_inf + smu) / (T_iel + smu);
         double et = fmu;
@@ -568,11 +590,15 @@ double or_vecdot(int n, const double* x, const double* y) {
     return tree256(s);
 }
 
-// biCG: biconjGrad.f90:8-62 (+ vecdiv/vecsum/assign2/copy1/copy2/SpMV :64-190)
-void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
-             const double* diagMtx, double* x, const double* b, const double* x_fix,
-             const int* x_fixIdx, int npoin, int nfix, double tol, int maxit,
-             cfd_solve_info* info) {
+// biCG: biconjGrad.f90:8-62 (+ vecdiv/vecsum/assign2/copy1/copy2/SpMV :64-190).
+// tol_mode CFD_BICG_TOL_ABS is the reference's test (|r.z| > tol continues, :47; early exit
+// on r.r < tol, :35).  The relative modes (not in the reference) test the same iterates on
+// r.r <= tol^2 * ref.ref, with ref = b - A.x_D (x_D: the Dirichlet values, 0 elsewhere;
+// ref(fix) = 0) or ref = r_0; r.r is the vecdot of the residual after its update.
+void or_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
+                  const double* diagMtx, double* x, const double* b, const double* x_fix,
+                  const int* x_fixIdx, int npoin, int nfix, double tol, int maxit, int tol_mode,
+                  cfd_solve_info* info) {
     std::vector<double> y(npoin), p(npoin), r(npoin), z(npoin);
     auto spmv = [&](const double* v, double* out) {
 #pragma omp parallel for schedule(static)
@@ -585,16 +611,29 @@ void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
     auto copy2 = [&](const double* v, double* out) {
         for (int i = 0; i < nfix; ++i) out[x_fixIdx[i] - 1] = 1.0e30 * v[x_fixIdx[i] - 1];
     };
+    const bool rel = tol_mode != CFD_BICG_TOL_ABS;
     int k = 0;
     for (int i = 0; i < nfix; ++i) x[x_fixIdx[i] - 1] = 1.0 * x_fix[i];  // copy1
+    double ref2 = 0.0;
+    if (tol_mode == CFD_BICG_TOL_REL) {  // e = b - A.x_D, e(fix) = 0
+        std::vector<double> xd(npoin, 0.0), e(npoin);
+        for (int i = 0; i < nfix; ++i) xd[x_fixIdx[i] - 1] = x[x_fixIdx[i] - 1];
+        spmv(xd.data(), e.data());
+        for (int i = 0; i < npoin; ++i) e[i] = -1.0 * e[i] + b[i];
+        for (int i = 0; i < nfix; ++i) e[x_fixIdx[i] - 1] = 0.0;
+        ref2 = or_vecdot(npoin, e.data(), e.data());
+    }
     spmv(x, y.data());
     copy2(x, y.data());
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npoin; ++i) r[i] = -1.0 * y[i] + b[i];  // vecsum(-1, y, b, r)
     for (int i = 0; i < nfix; ++i) r[x_fixIdx[i] - 1] = 0.0;  // assign2
     double rr = or_vecdot(npoin, r.data(), r.data());
-    if (rr < tol) {
-        if (info) { info->iters = 0; info->converged = 1; info->rz = rr; }
+    if (tol_mode == CFD_BICG_TOL_REL_R0) ref2 = rr;
+    const double thr = (tol * tol) * ref2;
+    auto relres = [&](double q) { return (rel && ref2 > 0.0) ? std::sqrt(q / ref2) : 0.0; };
+    if (rel ? rr <= thr : rr < tol) {
+        if (info) { info->iters = 0; info->converged = 1; info->rz = rr; info->relres = relres(rr); }
         return;
     }
 #pragma omp parallel for schedule(static)
@@ -607,7 +646,7 @@ void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < npoin; ++i) x[i] = alfa * p[i] + x[i];
     double err_old = err_new;
-    while (std::fabs(err_old) > tol && k < maxit) {
+    while ((rel ? rr > thr : std::fabs(err_old) > tol) && k < maxit) {
         k = k + 1;
         const double malfa = -alfa;
 #pragma omp parallel for schedule(static)
@@ -616,6 +655,7 @@ void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
             z[i] = r[i] / diagMtx[i];
         }
         err_new = or_vecdot(npoin, r.data(), z.data());
+        if (rel) rr = or_vecdot(npoin, r.data(), r.data());
         double beta = err_new / err_old;
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < npoin; ++i) p[i] = beta * p[i] + z[i];
@@ -629,9 +669,18 @@ void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
     }
     if (info) {
         info->iters = k;
-        info->converged = std::fabs(err_old) > tol ? 0 : 1;
+        info->converged = (rel ? rr > thr : std::fabs(err_old) > tol) ? 0 : 1;
         info->rz = std::fabs(err_old);
+        info->relres = relres(rr);
     }
+}
+
+void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
+             const double* diagMtx, double* x, const double* b, const double* x_fix,
+             const int* x_fixIdx, int npoin, int nfix, double tol, int maxit,
+             cfd_solve_info* info) {
+    or_bicg_mode(spMtx, spIdx, spRowptr, diagMtx, x, b, x_fix, x_fixIdx, npoin, nfix, tol, maxit,
+                 CFD_BICG_TOL_ABS, info);
 }
 
 // normales: subrutinas.f90:7-64 (wall-edge order).  Returns m.
@@ -661,7 +710,7 @@ void or_force_visc(int nelem, int npoin, int nsets, const int* ielem_sets, const
             const double temp = (T[nn1] + T[nn2]) / 2.0;
             const double smu = 110.0;
             const double r = temp / t_inf;
-            const double fmu = 0.017 * (r * std::sqrt(r)) * (t_inf + smu) / (temp + smu);
+            const double fmu = 0.017 * pow15(r) * (t_inf + smu) / (temp + smu);
             double rly = -(X[nn2] - X[nn1]);
             double rlx = Y[nn2] - Y[nn1];
             const double rmod = std::sqrt(rlx * rlx + rly * rly);
@@ -1246,9 +1295,9 @@ void fluid_structure(or_case* c, double dtmin, double time) {
     std::vector<double> pos_aux(nn, 0.0), b(N, 0.0);
     for (int i = 0; i < c->nmove; ++i) pos_aux[i] = dxpos[c->ilaux[i] - 1];
     Clock tg;
-    or_bicg(c->lap_sparse.data(), c->lap_idx.data(), c->lap_rowptr.data(), c->lap_diag.data(),
+    or_bicg_mode(c->lap_sparse.data(), c->lap_idx.data(), c->lap_rowptr.data(), c->lap_diag.data(),
             c->xpos.data(), b.data(), pos_aux.data(), c->ilaux.data(), N, nn, c->p.bicg_tol,
-            c->p.bicg_maxit, &c->sx);
+            c->p.bicg_maxit, c->p.bicg_tol_mode, &c->sx);
     c->timers[TM_GRAD] += tg.sec();
     for (int i = 0; i < N; ++i) {
         c->X[i] = c->X[i] + c->xpos[i];
@@ -1256,9 +1305,9 @@ void fluid_structure(or_case* c, double dtmin, double time) {
     }
     for (int i = 0; i < c->nmove; ++i) pos_aux[i] = dypos[c->ilaux[i] - 1];
     Clock tg2;
-    or_bicg(c->lap_sparse.data(), c->lap_idx.data(), c->lap_rowptr.data(), c->lap_diag.data(),
+    or_bicg_mode(c->lap_sparse.data(), c->lap_idx.data(), c->lap_rowptr.data(), c->lap_diag.data(),
             c->ypos.data(), b.data(), pos_aux.data(), c->ilaux.data(), N, nn, c->p.bicg_tol,
-            c->p.bicg_maxit, &c->sy);
+            c->p.bicg_maxit, c->p.bicg_tol_mode, &c->sy);
     c->timers[TM_GRAD] += tg2.sec();
     for (int i = 0; i < N; ++i) {
         c->Y[i] = c->Y[i] + c->ypos[i];
@@ -1430,6 +1479,8 @@ int or_case_step(or_case* c, int nsteps, cfd_step_report* rep) {
         rep->bicg_iters[1] = c->sy.iters;
         rep->bicg_rz[0] = c->sx.rz;
         rep->bicg_rz[1] = c->sy.rz;
+        rep->bicg_relres[0] = c->sx.relres;
+        rep->bicg_relres[1] = c->sy.relres;
         rep->bicg_converged[0] = c->sx.converged;
         rep->bicg_converged[1] = c->sy.converged;
         rep->nset_numb = c->nset_numb;

@@ -31,6 +31,13 @@ extern "C" {
 
 void or_set_threads(int n);
 void or_set_estab_mode(int mode);  /* CFD_ESTAB_* for the per-routine or_estab */
+/* 0 (default): the compositions above; 1: x**1.5d0, x**.5d0 and x**(-.5d0) through the C
+ * library's pow, as a Fortran compiler without unsafe-math options evaluates them */
+void or_set_pow_mode(int mode);
+int or_get_pow_mode(void);
+/* counts over x[0..n): pow(x,1.5) != x*sqrt(x), pow(x,-0.5) != 1/sqrt(x),
+ * pow(x,0.5) != sqrt(x) */
+void or_pow_census(int n, const double* x, long long* out3);
 int or_get_threads(void);
 
 void or_deriv(int npoin, int nelem, const double* X, const double* Y, const int* inpoel,
@@ -74,6 +81,11 @@ void or_bicg(const double* spMtx, const int* spIdx, const int* spRowptr,
              const double* diagMtx, double* x, const double* b, const double* x_fix,
              const int* x_fixIdx, int npoin, int nfix, double tol, int maxit,
              cfd_solve_info* info);
+/* the same iterates with the stopping test of tol_mode (CFD_BICG_TOL_*) */
+void or_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
+                  const double* diagMtx, double* x, const double* b, const double* x_fix,
+                  const int* x_fixIdx, int npoin, int nfix, double tol, int maxit, int tol_mode,
+                  cfd_solve_info* info);
 
 int or_normales(int npoin, int nwall, const int* wall, const double* X, const double* Y,
                 int* n_ipoin, double* n_x, double* n_y);

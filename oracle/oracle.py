@@ -42,6 +42,11 @@ _SIG = {
     "or_vecdot": (_d, [_i, _dp, _dp]),
     "or_bicg": (None, [_dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _i, _i, _d, _i,
                        C.POINTER(abi.CfdSolveInfo)]),
+    "or_set_pow_mode": (None, [_i]),
+    "or_get_pow_mode": (_i, []),
+    "or_pow_census": (None, [_i, _dp, C.POINTER(C.c_longlong)]),
+    "or_bicg_mode": (None, [_dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _i, _i, _d, _i, _i,
+                            C.POINTER(abi.CfdSolveInfo)]),
     "or_normales": (_i, [_i, _i, _ip, _dp, _dp, _ip, _dp, _dp]),
     "or_smoothing": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _dp]),
     "or_smoothing_ordered": (None, [_dp, _dp, _ip, _ip, _i, _i, _ip, _dp, _ip, _dp]),
@@ -97,6 +102,24 @@ def i32(a):
 
 def set_threads(n):
     lib().or_set_threads(int(n))
+
+
+def set_pow_mode(mode):
+    """0: the compositions x*sqrt(x), 1/sqrt(x), sqrt(x) (the GPU's); 1: the C library's
+    pow for x**1.5d0, x**(-.5d0), x**.5d0 (a Fortran build without unsafe math)."""
+    lib().or_set_pow_mode(int(mode))
+
+
+def get_pow_mode():
+    return lib().or_get_pow_mode()
+
+
+def pow_census(x):
+    """(#pow(x,1.5) != x*sqrt(x), #pow(x,-0.5) != 1/sqrt(x), #pow(x,0.5) != sqrt(x))."""
+    x = f64(x)
+    out = (C.c_longlong * 3)()
+    lib().or_pow_census(len(x), dp(x), out)
+    return tuple(out)
 
 
 # ------------------------------------------------------------------ per-routine calls
@@ -211,12 +234,13 @@ def vecdot(x, y):
     return lib().or_vecdot(len(x), dp(f64(x)), dp(f64(y)))
 
 
-def bicg(vals, idx, rowptr, diag, x, b, x_fix, fix_idx, tol=1e-10, maxit=1000):
+def bicg(vals, idx, rowptr, diag, x, b, x_fix, fix_idx, tol=1e-10, maxit=1000,
+         tol_mode=abi.CFD_BICG_TOL_ABS):
     x = f64(x).copy()
     info = abi.CfdSolveInfo()
-    lib().or_bicg(dp(f64(vals)), ip(i32(idx)), ip(i32(rowptr)), dp(f64(diag)), dp(x),
-                  dp(f64(b)), dp(f64(x_fix)), ip(i32(fix_idx)), len(x), len(fix_idx), tol,
-                  maxit, C.byref(info))
+    lib().or_bicg_mode(dp(f64(vals)), ip(i32(idx)), ip(i32(rowptr)), dp(f64(diag)), dp(x),
+                       dp(f64(b)), dp(f64(x_fix)), ip(i32(fix_idx)), len(x), len(fix_idx), tol,
+                       maxit, int(tol_mode), C.byref(info))
     return x, info
 
 

@@ -132,7 +132,7 @@ def test_adjacency_laplace_bicg(S, oracle, mesh):
     eq(xg, xo, "biCG x (capped)")
 
 
-def run_pair(case, steps, check_each=True, setup=None):
+def run_pair(case, steps, check_each=True, setup=None, on_step=None):
     from cfd_gb300 import solver
     g = solver.Solver(case)
     o = None
@@ -145,6 +145,9 @@ def run_pair(case, steps, check_each=True, setup=None):
         assert rg.dtmin == ro.dtmin, f"step {s + 1}: DTMIN"
         assert rg.time == ro.time
         assert tuple(rg.bicg_iters) == tuple(ro.bicg_iters), f"step {s + 1}: BiCG iterations"
+        assert tuple(rg.bicg_relres) == tuple(ro.bicg_relres), f"step {s + 1}: BiCG ||r||"
+        if on_step:
+            on_step(rg, ro)
         for i in range(rg.nset_numb):
             assert (rg.fx[i], rg.fy[i], rg.rm[i]) == (ro.fx[i], ro.fy[i], ro.rm[i]), "FORCES"
         if check_each or s == steps - 1:

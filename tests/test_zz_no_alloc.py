@@ -2,7 +2,8 @@
 where they solve (their arrays already live on the GPU; the library keeps its work
 vectors in a fixed static device array).  Checked through the C-ABI against the existing
 cfd_bicg_ex entry on the same system, on two calls in a row (the shared work array keeps
-the previous call's contents, so the second call shows nothing stale leaks through).
+the previous call's contents, so the second call shows nothing stale leaks through); the
+second call takes b = NULL and must not change the device's free memory.
 
 This file is named to be collected last."""
 import ctypes as C
@@ -48,14 +49,21 @@ def test_noalloc_bicg_matches_bicg_twice(gpu_lib, oracle):
         t_diag = torch.from_numpy(np.ascontiguousarray(diag)).to(dev)
         t_fix = torch.from_numpy(isfix).to(dev)
         t_b = torch.zeros(n, dtype=torch.float64, device=dev)
-        for call in range(2):
-            t_x = torch.from_numpy(xd0.copy()).to(dev)
-            torch.cuda.synchronize()
+        # both calls' x buffers exist before the first call, so nothing in between allocates
+        t_xs = [torch.from_numpy(xd0.copy()).to(dev) for _ in range(2)]
+        torch.cuda.synchronize()
+        for call, t_x in enumerate(t_xs):
+            # the second call passes b = NULL (a zero right-hand side, like the zero b of the
+            # first) and must leave the device's free memory exactly as it was
+            b_ptr = t_b.data_ptr() if call == 0 else None
+            free_before = torch.cuda.mem_get_info()[0]
             info = abi.CfdSolveInfo()
             st = L.cfd_bicg_device_noalloc(t_val.data_ptr(), t_col.data_ptr(), t_rp.data_ptr(),
                                            t_diag.data_ptr(), t_fix.data_ptr(), t_x.data_ptr(),
-                                           t_b.data_ptr(), n, 1.0e-10, 1000, None, C.byref(info))
+                                           b_ptr, n, 1.0e-10, 1000, None, C.byref(info))
             assert st == abi.CFD_OK, L.cfd_strerror(st)
+            if call == 1:
+                assert torch.cuda.mem_get_info()[0] == free_before, "the call allocated"
             x = t_x.cpu().numpy()
             assert (info.iters, info.converged) == (info_ref.iters, info_ref.converged), call
             assert info.rz == info_ref.rz
