@@ -101,6 +101,7 @@ struct Ctx {
            *d_DTL = nullptr;
     double *d_SHOC = nullptr, *d_TS1 = nullptr, *d_TS2 = nullptr, *d_TS3 = nullptr;
     double *d_contrib = nullptr, *d_contribF = nullptr;
+    double* d_einv = nullptr;  // FP64 form: calcRHS's stage-invariant addends (per element)
     // mixed precision: float shadows (FP64 arrays above are widened from them on download)
     float4 *d_Uhi = nullptr, *d_Ulo = nullptr;  // U = hi + lo
     float2 *d_Xhi = nullptr, *d_Xlo = nullptr;  // (X, Y) = hi + lo

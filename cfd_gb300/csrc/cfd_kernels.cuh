@@ -245,6 +245,20 @@ __global__ void k_estab(int nelem, const int4* elem, const double* U, const doub
                         double RHOINF, double TINF, int estab_mode, double eps_dir,
                         double dirx, double diry, double* SHOC, double* TS1, double* TS2,
                         double* TS3);
+// calcRHS split into its stage-invariant part (once per step: the cached addends and
+// factors, FUENTE into contribF; with !viscous the final contributions into contrib) and
+// the per-stage viscous replay from the cache (kernels_fp64.cu); cache: kInvPlanes x nelem
+constexpr int kElemInvPlanes = 94;
+cudaError_t launch_elem_inv(bool viscous, cudaStream_t stream, int nelem, const int4* elem,
+                            const double* U, const double* geo, const double* area,
+                            const double* shoc, const double* dtl_arr, const double* dtl_scalar,
+                            const double* ts1, const double* ts2, const double* ts3, GasConst gc,
+                            double* cache, double* contrib, const double* WX, const double* WY,
+                            double* contribF);
+cudaError_t launch_elem_replay(cudaStream_t stream, int nelem, const int4* elem, const double* T,
+                               const double* geo, const double* area, const double* dtl_arr,
+                               const double* dtl_scalar, GasConst gc, const double* cache,
+                               double* contrib);
 // calcRHS (+ FUENTE when contribF != NULL) element kernel; contrib may be NULL (FUENTE only)
 cudaError_t launch_elem_rhs(bool viscous, bool with_theta, cudaStream_t stream, int nelem,
                             const int4* elem, const double* U, const double* theta,

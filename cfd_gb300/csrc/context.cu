@@ -420,13 +420,18 @@ int Ctx::step_once() {
     const int NRK = 4;
     for (int irk = 1; irk <= NRK; ++irk) {
         const double rk_fact = 1.0 / (NRK + 1 - irk);
-        // FUENTE depends on the step-start U and W only: its contributions are formed in
-        // stage 1 and re-read by stages 2-4
-        double* cF = (irk == 1) ? d_contribF : nullptr;
+        // calcRHS and FUENTE see the step-start U in every stage (subrutinas.f90:685,
+        // :1064): stage 1 forms FUENTE and calcRHS's stage-invariant addends, and every
+        // stage replays the sums with its own viscous terms (bit-identical to evaluating
+        // the whole element in each stage; without viscosity the stage-1 result is final)
         tstart(TM_CALCRHS);
-        CFD_CUDA(launch_elem_rhs(viscous, false, stream, E, d_elem, d_U, nullptr, d_T, d_geo, d_area,
-                                 d_SHOC, dtl_arr, dtl_scalar, d_TS1, d_TS2, d_TS3, gc, d_contrib,
-                                 d_WX, d_WY, cF));
+        if (irk == 1)
+            CFD_CUDA(launch_elem_inv(viscous, stream, E, d_elem, d_U, d_geo, d_area, d_SHOC,
+                                     dtl_arr, dtl_scalar, d_TS1, d_TS2, d_TS3, gc, d_einv,
+                                     d_contrib, d_WX, d_WY, d_contribF));
+        if (viscous)
+            CFD_CUDA(launch_elem_replay(stream, E, d_elem, d_T, d_geo, d_area, dtl_arr, dtl_scalar,
+                                        gc, d_einv, d_contrib));
         tstop(TM_CALCRHS);
         tstart(TM_UPDATE);
         CFD_LAUNCH(k_node_update, blocks_for(N, TB), TB, 0, stream, N, d_esup_ptr, d_esup_slot,
@@ -673,6 +678,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if ((st = dalloc(&d_geo, 6 * (size_t)E))) return st;
     if ((st = dalloc(&d_contrib, 12 * (size_t)E))) return st;
     if ((st = dalloc(&d_contribF, 12 * (size_t)E))) return st;
+    if (prec == CFD_PREC_FP64 && (st = dalloc(&d_einv, (size_t)kElemInvPlanes * E))) return st;
     for (int s = 0; s < 2; ++s) {
         for (double** q : {&d_pos[s], &d_r[s], &d_z[s], &d_y[s], &d_p[s][0], &d_p[s][1]})
             if ((st = dalloc(q, N))) return st;

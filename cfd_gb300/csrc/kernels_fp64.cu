@@ -448,6 +448,299 @@ cudaError_t launch_elem_rhs(bool viscous, bool with_theta, cudaStream_t stream, 
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ calcRHS, stage-invariant split
+// All four RK stages evaluate calcRHS at the step-start U (subrutinas.f90:685); between the
+// stages only T changes, and T enters only mu and lambda (calcRHS.f90:49-51), i.e. only
+// the viscous K-flux terms (:119-137).  The per-node sums of calcRHS.f90:109-117 and
+// :133-135 are left-associative and interleave the quadrature points: for local node i,
+// variable q and quadrature point k the running sum takes
+//     (+ 0.5*AiUi_k(q) if i != k)  + tau_i*(Nx_i*B1_k(q) + Ny_i*B2_k(q))
+//     + nu*(Nx_i*Ux(q) + Ny_i*Uy(q))  [+ Nx_i*K1_k(q) + Ny_i*K2_k(q) for q = 2..4],
+// so caching the individual addends (not their sum) and replaying the adds in the same
+// order reproduces every bit.  k_elem_inv forms, once per step, the stage-invariant addends
+// and the mu-independent factors of K1, K2; k_elem_replay forms, per stage, mu and lambda,
+// K1, K2 and the sums.  Variable 1 (continuity) has no viscous term: its contribution is
+// final after k_elem_inv.
+//
+// Cache planes (kInvPlanes, each nelem doubles, plane-major so a warp's loads coalesce):
+constexpr int kC0 = 0;    // [i]        final continuity contribution of local node i
+constexpr int kA1 = 3;    // [k][q-1]   0.5*AiUi_k(q)
+constexpr int kA2 = 12;   // [i][k][q-1] tau_i*(Nx_i*B1_k(q) + Ny_i*B2_k(q))
+constexpr int kA3 = 39;   // [i][q-1]   nu*(Nx_i*Ux(q) + Ny_i*Uy(q))
+constexpr int kV = 48;    // [k][14]    mu-independent factors of K1_k, K2_k (below)
+constexpr int kVG = 90;   // [4]        Ux(1), Uy(1), 3*Ux(4), 3*Uy(4)
+constexpr int kInvPlanes = 94;
+// kV + 14*k + m: 0 rho, 1 P11, 2 P12, 3 P13a, 4 P13b, 5 P13c, 6 Ux(2)*v1, 7 3*Ux(3)*v2,
+// 8 Cv*rho, 9 P22, 10 P23a, 11 P23b, 12 3*Uy(2)*v1, 13 Uy(3)*v2
+
+template <bool VISCOUS>
+__global__ void __launch_bounds__(128)
+k_elem_inv(int nelem, const int4* __restrict__ elem, const double* __restrict__ U,
+           const double* __restrict__ geo, const double* __restrict__ area,
+           const double* __restrict__ shoc, const double* __restrict__ dtl_arr,
+           const double* __restrict__ dtl_scalar, const double* __restrict__ ts1,
+           const double* __restrict__ ts2, const double* __restrict__ ts3, GasConst gc,
+           double* __restrict__ cache, double* __restrict__ contrib,
+           const double* __restrict__ WX, const double* __restrict__ WY,
+           double* __restrict__ contribF) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    const size_t E = (size_t)nelem;
+    const double Cv = gc.cv, g = gc.gamma, cte = gc.cte;
+    int4 n = elem[e];
+    const int p[3] = {n.x, n.y, n.z};
+    const double Nx[3] = {geo[e], geo[E + e], geo[2 * E + e]};
+    const double Ny[3] = {geo[3 * E + e], geo[4 * E + e], geo[5 * E + e]};
+    double Un[3][4];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double2* u2 = reinterpret_cast<const double2*>(U + 4 * (size_t)p[i]);
+        double2 a = u2[0], b = u2[1];
+        Un[i][0] = a.x; Un[i][1] = a.y; Un[i][2] = b.x; Un[i][3] = b.y;
+    }
+    double Ux[4], Uy[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        Ux[q] = Un[0][q] * Nx[0] + Un[1][q] * Nx[1] + Un[2][q] * Nx[2];
+        Uy[q] = Un[0][q] * Ny[0] + Un[1][q] * Ny[1] + Un[2][q] * Ny[2];
+    }
+    const double dtl = dtl_arr ? dtl_arr[e] : *dtl_scalar;
+    const double ar = area[e];
+    const double tau[3] = {ts1[e], ts2[e], ts3[e]};
+    const double nu = shoc[e] * cte;
+    auto C = [&](int plane) -> double& { return cache[(size_t)plane * E + e]; };
+    double a3[3][4];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a3[i][q] = nu * (Nx[i] * Ux[q] + Ny[i] * Uy[q]);
+    double r[3][4];  // non-viscous sums (all four variables when !VISCOUS, else continuity)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) r[i][q] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int ia = (k == 0) ? 1 : 0;
+        const int ib = (k == 2) ? 1 : 2;
+        double Uk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Uk[q] = 0.5 * Un[ia][q] + 0.5 * Un[ib][q];
+        const double rho = Uk[0];
+        const double v1 = Uk[1] / rho, v2 = Uk[2] / rho, ev = Uk[3] / rho;
+        const double V_sq = v1 * v1 + v2 * v2;
+        double A[4];
+        A[0] = Ux[1] + Uy[2];
+        A[1] = 0.5 * Ux[0] * (V_sq * (g - 1.0) - 2.0 * (v1 * v1)) - Ux[1] * v1 * (g - 3.0) -
+               Ux[2] * v2 * (g - 1.0) + Ux[3] * (g - 1.0) - Uy[0] * v1 * v2 + Uy[1] * v2 +
+               Uy[2] * v1;
+        A[2] = -(Ux[0] * v1 * v2) + Ux[1] * v2 + Ux[2] * v1 +
+               0.5 * Uy[0] * (V_sq * (g - 1.0) - 2.0 * (v2 * v2)) - Uy[1] * v1 * (g - 1.0) -
+               Uy[2] * v2 * (g - 3.0) + Uy[3] * (g - 1.0);
+        A[3] = Ux[0] * v1 * (V_sq * (g - 1.0) - ev * g) -
+               0.5 * Ux[1] * (V_sq * (g - 1.0) - 2.0 * ev * g + 2.0 * (v1 * v1) * (g - 1.0)) -
+               Ux[2] * v1 * v2 * (g - 1.0) + Ux[3] * g * v1 +
+               Uy[0] * v2 * (V_sq * (g - 1.0) - ev * g) - Uy[1] * v1 * v2 * (g - 1.0) -
+               0.5 * Uy[2] * (V_sq * (g - 1.0) - 2.0 * ev * g + 2.0 * (v2 * v2) * (g - 1.0)) +
+               Uy[3] * g * v2;
+        const double* At = A;
+        double B1[4], B2[4];
+        B1[0] = At[1];
+        B1[1] = v1 * (-g + 3.0) * At[1] - v2 * (g - 1.0) * At[2] + (g - 1.0) * At[3] +
+                (0.5 * V_sq * (g - 1.0) - v1 * v1) * At[0];
+        B1[2] = -(v1 * v2 * At[0]) + v1 * At[2] + v2 * At[1];
+        B1[3] = g * v1 * At[3] - v1 * v2 * (g - 1.0) * At[2] +
+                v1 * (V_sq * (g - 1.0) - ev * g) * At[0] +
+                (-(0.5 * V_sq * (g - 1.0)) + ev * g - v1 * v1 * (g - 1.0)) * At[1];
+        B2[0] = At[2];
+        B2[1] = B1[2];
+        B2[2] = -(v1 * (g - 1.0) * At[1]) + v2 * (-g + 3.0) * At[2] + (g - 1.0) * At[3] +
+                (0.5 * V_sq * (g - 1.0) - v2 * v2) * At[0];
+        B2[3] = g * v2 * At[3] - v1 * v2 * (g - 1.0) * At[1] +
+                v2 * (V_sq * (g - 1.0) - ev * g) * At[0] +
+                (-(0.5 * V_sq * (g - 1.0)) + ev * g - v2 * v2 * (g - 1.0)) * At[2];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const double a2 = tau[i] * (Nx[i] * B1[q] + Ny[i] * B2[q]);
+                if (!VISCOUS || q == 0) {
+                    double t = r[i][q];
+                    if (i != k) t = t + 0.5 * A[q];
+                    r[i][q] = t + a2 + a3[i][q];
+                } else {
+                    C(kA2 + 9 * i + 3 * k + (q - 1)) = a2;
+                }
+            }
+        if (VISCOUS) {
+#pragma unroll
+            for (int q = 1; q < 4; ++q) C(kA1 + 3 * k + (q - 1)) = 0.5 * A[q];
+            // the mu-independent factors of K1_k, K2_k (calcRHS.f90:119-137), each formed
+            // exactly as the full expression forms it
+            C(kV + 14 * k + 0) = rho;
+            C(kV + 14 * k + 1) = -(2.0 * Ux[0] * v1) + 2.0 * Ux[1] + Uy[0] * v2 - Uy[2];
+            C(kV + 14 * k + 2) = -(Ux[0] * v2) + Ux[2] - Uy[0] * v1 + Uy[1];
+            C(kV + 14 * k + 3) = -(Uy[0] * v1 * v2) + 3.0 * Uy[1] * v2 - 2.0 * Uy[2] * v1;
+            C(kV + 14 * k + 4) = 3.0 * V_sq + v1 * v1;
+            C(kV + 14 * k + 5) = V_sq - ev;
+            C(kV + 14 * k + 6) = Ux[1] * v1;
+            C(kV + 14 * k + 7) = 3.0 * Ux[2] * v2;
+            C(kV + 14 * k + 8) = Cv * rho;
+            C(kV + 14 * k + 9) = Ux[0] * v1 - Ux[1] - 2.0 * Uy[0] * v2 + 2.0 * Uy[2];
+            C(kV + 14 * k + 10) = -(Ux[0] * v1 * v2) - 2.0 * Ux[1] * v2 + 3.0 * Ux[2] * v1;
+            C(kV + 14 * k + 11) = 3.0 * V_sq + v2 * v2;
+            C(kV + 14 * k + 12) = 3.0 * Uy[1] * v1;
+            C(kV + 14 * k + 13) = Uy[2] * v2;
+        }
+    }
+    if (VISCOUS) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            C(kC0 + i) = r[i][0] * ar * dtl / 3.0;
+#pragma unroll
+            for (int q = 1; q < 4; ++q) C(kA3 + 3 * i + (q - 1)) = a3[i][q];
+        }
+        C(kVG + 0) = Ux[0];
+        C(kVG + 1) = Uy[0];
+        C(kVG + 2) = 3.0 * Ux[3];
+        C(kVG + 3) = 3.0 * Uy[3];
+    } else {
+        double* out = contrib + 12 * (size_t)e;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            double2 a, b;
+            a.x = r[i][0] * ar * dtl / 3.0;
+            a.y = r[i][1] * ar * dtl / 3.0;
+            b.x = r[i][2] * ar * dtl / 3.0;
+            b.y = r[i][3] * ar * dtl / 3.0;
+            reinterpret_cast<double2*>(out + 4 * i)[0] = a;
+            reinterpret_cast<double2*>(out + 4 * i)[1] = b;
+        }
+    }
+    if (contribF) {
+        // FUENTE (subrutinas.f90:1064-1078), as in k_elem_rhs
+        const double AR = ar * dtl / 3.0;
+        const double w0 = WX[p[0]], w1 = WX[p[1]], w2 = WX[p[2]];
+        const double y0 = WY[p[0]], y1 = WY[p[1]], y2 = WY[p[2]];
+        const double wx[3] = {0.5 * w0 + 0.5 * w1, 0.5 * w1 + 0.5 * w2, 0.5 * w0 + 0.5 * w2};
+        const double wy[3] = {0.5 * y0 + 0.5 * y1, 0.5 * y1 + 0.5 * y2, 0.5 * y0 + 0.5 * y2};
+        double* of = contribF + 12 * (size_t)e;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double q0 = Ux[q] * wx[0] + Uy[q] * wy[0];
+            const double q1 = Ux[q] * wx[1] + Uy[q] * wy[1];
+            const double q2 = Ux[q] * wx[2] + Uy[q] * wy[2];
+            of[q] = -(AR * (0.5 * q0 + 0.5 * q2));
+            of[4 + q] = -(AR * (0.5 * q0 + 0.5 * q1));
+            of[8 + q] = -(AR * (0.5 * q1 + 0.5 * q2));
+        }
+    }
+}
+
+// One RK stage of the viscous calcRHS from the cache: mu, lambda from this stage's T, the
+// K fluxes (calcRHS.f90:119-137 with the cached factors) and the sums replayed in the order
+// of k_elem_rhs; writes all 12 contributions (continuity copied from the cache).
+__global__ void __launch_bounds__(128)
+k_elem_replay(int nelem, const int4* __restrict__ elem, const double* __restrict__ T,
+              const double* __restrict__ geo, const double* __restrict__ area,
+              const double* __restrict__ dtl_arr, const double* __restrict__ dtl_scalar,
+              GasConst gc, const double* __restrict__ cache, double* __restrict__ contrib) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    const size_t E = (size_t)nelem;
+    auto C = [&](int plane) -> double { return __ldcs(cache + (size_t)plane * E + e); };
+    const double Cv = gc.cv, lambda_ref = gc.lambda_ref, mu_ref = gc.mu_ref, T_inf = gc.t_inf;
+    const int4 n = elem[e];
+    const double T_avg = (T[n.x] + T[n.y] + T[n.z]) / 3.0;
+    const double mu = mu_ref * pow15(T_avg / T_inf) * (T_inf + 110.0) / (T_avg + 110.0);
+    const double lambda = lambda_ref * pow15(T_avg / T_inf) * (T_inf + 194.0) / (T_avg + 194.0);
+    const double Nx[3] = {geo[e], geo[E + e], geo[2 * E + e]};
+    const double Ny[3] = {geo[3 * E + e], geo[4 * E + e], geo[5 * E + e]};
+    const double dtl = dtl_arr ? dtl_arr[e] : *dtl_scalar;
+    const double ar = area[e];
+    // the mu, lambda subexpressions as calcRHS.f90:119-137 group them
+    const double c23m = 2.0 / 3.0 * mu;
+    const double cm = Cv * mu;
+    const double l3 = 3.0 * lambda;
+    const double c4m_l3 = 4.0 * Cv * mu - 3.0 * lambda;
+    const double cm_l = Cv * mu - lambda;
+    const double Ux0 = C(kVG + 0), Uy0 = C(kVG + 1);
+    const double t5x = C(kVG + 2) * lambda, t5y = C(kVG + 3) * lambda;
+    double r[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) r[i][q] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int b = kV + 14 * k;
+        const double rho = C(b + 0);
+        const double P13c = C(b + 5);
+        double K1[3], K2[3];
+        K1[0] = c23m * C(b + 1) / rho;
+        K1[1] = mu * C(b + 2) / rho;
+        K1[2] = 1.0 / 3.0 *
+                (cm * C(b + 3) - Ux0 * (cm * C(b + 4) - l3 * P13c) + C(b + 6) * c4m_l3 +
+                 C(b + 7) * cm_l + t5x) /
+                C(b + 8);
+        K2[0] = K1[1];
+        K2[1] = c23m * C(b + 9) / rho;
+        K2[2] = 1.0 / 3.0 *
+                (cm * C(b + 10) - Uy0 * (cm * C(b + 11) - l3 * P13c) + C(b + 12) * cm_l +
+                 C(b + 13) * c4m_l3 + t5y) /
+                C(b + 8);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                double t = r[i][q];
+                if (i != k) t = t + C(kA1 + 3 * k + q);
+                t = t + C(kA2 + 9 * i + 3 * k + q) + C(kA3 + 3 * i + q);
+                r[i][q] = t + (Nx[i] * K1[q] + Ny[i] * K2[q]);
+            }
+    }
+    double* out = contrib + 12 * (size_t)e;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double2 a, b;
+        a.x = C(kC0 + i);
+        a.y = r[i][0] * ar * dtl / 3.0;
+        b.x = r[i][1] * ar * dtl / 3.0;
+        b.y = r[i][2] * ar * dtl / 3.0;
+        reinterpret_cast<double2*>(out + 4 * i)[0] = a;
+        reinterpret_cast<double2*>(out + 4 * i)[1] = b;
+    }
+}
+
+cudaError_t launch_elem_inv(bool viscous, cudaStream_t stream, int nelem, const int4* elem,
+                            const double* U, const double* geo, const double* area,
+                            const double* shoc, const double* dtl_arr, const double* dtl_scalar,
+                            const double* ts1, const double* ts2, const double* ts3, GasConst gc,
+                            double* cache, double* contrib, const double* WX, const double* WY,
+                            double* contribF) {
+    const unsigned grid = blocks_for(nelem, 128);
+    if (viscous)
+        k_elem_inv<true><<<grid, 128, 0, stream>>>(nelem, elem, U, geo, area, shoc, dtl_arr,
+                                                   dtl_scalar, ts1, ts2, ts3, gc, cache, contrib,
+                                                   WX, WY, contribF);
+    else
+        k_elem_inv<false><<<grid, 128, 0, stream>>>(nelem, elem, U, geo, area, shoc, dtl_arr,
+                                                    dtl_scalar, ts1, ts2, ts3, gc, cache, contrib,
+                                                    WX, WY, contribF);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_elem_replay(cudaStream_t stream, int nelem, const int4* elem, const double* T,
+                               const double* geo, const double* area, const double* dtl_arr,
+                               const double* dtl_scalar, GasConst gc, const double* cache,
+                               double* contrib) {
+    k_elem_replay<<<blocks_for(nelem, 128), 128, 0, stream>>>(nelem, elem, T, geo, area, dtl_arr,
+                                                               dtl_scalar, gc, cache, contrib);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ RK stage, node side
 // subrutinas.f90:680-825 for one stage: RHS = ordered sum of the calcRHS then the FUENTE
 // contributions of the node's elements; U1 = U - rk_fact/M*RHS; primitives; FIXVEL,

@@ -171,6 +171,13 @@ def test_step_fixed_mesh(gpu_lib):
     run_pair(small_case(1, scale=16, seed=7), 4)
 
 
+def test_step_inviscid(gpu_lib):
+    # FMU = 0: calcRHS has no viscous terms, so the stage-1 element pass is final for all
+    # four stages
+    run_pair(small_case(2, scale=16, seed=5, fmu=0.0, pitch_amp=math.radians(3.0),
+                        motion_freq=2.0), 3)
+
+
 @pytest.mark.parametrize("mass_mode", [0, 1, 2])
 def test_step_heave_pitch(gpu_lib, mass_mode):
     k = small_case(2, scale=16, seed=8, pitch_amp=math.radians(4.0), motion_freq=2.0,
