@@ -327,6 +327,24 @@ int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate) {
     return ctx->impl.set_guess_net(net, gate);
 }
 
+int cfd_ctx_set_guess_refine(cfd_ctx* ctx, int on) {
+    if (!ctx) return arg_error("ctx");
+    return ctx->impl.set_guess_refine(on != 0);
+}
+
+int cfd_ctx_guess_stats_ex(cfd_ctx* ctx, long long* out8) {
+    if (!ctx || !out8) return arg_error("null pointer");
+    Ctx& c = ctx->impl;
+    for (int k = 0; k < 8; ++k) out8[k] = 0;
+    if (!c.d_gstats) return CFD_OK;
+    CFD_CUDA(cudaMemcpyAsync(out8, c.d_gstats, 8 * sizeof(long long), cudaMemcpyDeviceToHost,
+                             c.stream));
+    CFD_CUDA(cudaStreamSynchronize(c.stream));
+    out8[3] = c.guess_steps;
+    out8[7] = 0;
+    return CFD_OK;
+}
+
 int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4) {
     if (!ctx || !out4) return arg_error("null pointer");
     Ctx& c = ctx->impl;

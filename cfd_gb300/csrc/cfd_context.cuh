@@ -20,6 +20,11 @@ int guess_on_stream(cfd_mpnn* net, cfd_mpnn_graph* g, cudaStream_t st, const dou
                     const double* Y, const double* bgx, const double* bgy, double* ux,
                     double* uy, const int* gate);
 void graph_free(cfd_mpnn_graph* g);
+int fields_seed(cfd_mpnn_graph* g, cudaStream_t st);
+int fields_guess(cfd_mpnn_graph* g, cudaStream_t st, const double* X, const double* Y,
+                 const double* bgx, const double* bgy, const double* x0, const double* x1,
+                 double* c0, double* c1);
+int fields_update(cfd_mpnn_graph* g, cudaStream_t st, const double* x0, const double* x1);
 }  // namespace mpnn
 
 // mesh smoothing (smooth.cu)
@@ -135,6 +140,11 @@ struct Ctx {
                                  // above which the network runs
     bool guess_first = false;    // the first solve after attaching runs the network
     long long guess_steps = 0;
+    // refined learned guess (cfd_ctx_set_guess_refine): per-node basis fields seeded by the
+    // network's run and corrected by every solve; each solve between network runs also
+    // tries the fields' guess, and keeps the better of it and the previous step's
+    bool guess_refine = false;
+    bool fields_ready = false;   // the fields were seeded since the network was attached
     int* h_iters = nullptr;      // pinned copy of the last solve's iteration counts
     cudaEvent_t ev_iters = nullptr;  // recorded after that copy
     // mixed form: the clock and the motion increment live on the device
@@ -199,6 +209,7 @@ struct Ctx {
     int widen_mixed(int what);
     int run_pcg(int nsolve, bool learned = false, bool fix_done = false,
                 cudaStream_t sv = nullptr);
+    int set_guess_refine(bool on);
     int enqueue_mixed(bool learned);
     int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);

@@ -346,7 +346,8 @@ __global__ void k_pcg_fp64(PcgArgs a);
 __global__ void k_pcg_mixed(PcgArgs a);
 __global__ void k_selftest_waits(GridBar* gb, int* out, long long limit);
 __global__ void k_bicg_fix_mixed(PcgArgs a);
-__global__ void k_bicg_resid_mixed(PcgArgs a);
+// first pass of a mixed solve (k_bicg_resid_mixed, the variant of a.tol_mode)
+cudaError_t launch_bicg_resid_mixed(unsigned grid, cudaStream_t stream, const PcgArgs& a);
 __global__ void k_bicg_dir_mixed(PcgArgs a);
 // learned-guess judge: r.z of the candidate (cand[s]) per solve when gflag[0] is set
 __global__ void k_guess_judge(PcgArgs a, const double* cand0, const double* cand1, double* rr);

@@ -172,8 +172,11 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         a.bscal = d_bscal;
         a.bcount = d_bcount;
         // learned guess (decided by the caller): k_guess_judge keeps, per solve, the
-        // network's guess or the previous step's, whichever has the smaller r.z
-        a.gflag = learned ? d_gflag : nullptr;
+        // network's guess or the previous step's, whichever has the smaller r.z.  Between
+        // network runs, with the refined guess on, the candidate is the fields' guess.
+        const bool with_net = prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph;
+        const bool fields = with_net && guess_refine && !learned && fields_ready;
+        a.gflag = (learned || fields) ? d_gflag : nullptr;
         a.gate = 0.0;
         a.only_if = nullptr;
         if (nufix > 0 && !fix_done)
@@ -182,7 +185,20 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         const unsigned rgrid = (sv && branch_bpsm > 0)
                                    ? (unsigned)std::min<long>(a.nblk_r, (long)branch_bpsm * nsm)
                                    : (unsigned)a.nblk_r;
-        CFD_LAUNCH(k_bicg_resid_mixed, rgrid, 256, 0, stream, a);
+        CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, a));
+        if (fields) {
+            int st = mpnn::fields_guess(lgraph, stream, d_X, d_Y, d_xfix[0], d_xfix[1], d_pos[0],
+                                        d_pos[1], d_cand[0], d_cand[1]);
+            if (st) return st;
+            const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
+            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                       (const double*)d_cand[1], d_grr);
+            CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                       (const double*)d_cand[1], (const double*)d_grr, d_gstats + 4);
+            PcgArgs b = a;
+            b.only_if = d_gflag + 1;
+            CFD_CUDA(launch_bicg_resid_mixed(gsz, stream, b));
+        }
         if (learned) {
             // the network runs only when the previous-step guess leaves r.z >= gate; its
             // guess replaces it, per solve, when its r.z is the smaller; the first pass is
@@ -198,7 +214,11 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
                        (const double*)d_cand[1], (const double*)d_grr, d_gstats);
             PcgArgs b = a;
             b.only_if = d_gflag + 1;
-            CFD_LAUNCH(k_bicg_resid_mixed, gsz, 256, 0, stream, b);
+            CFD_CUDA(launch_bicg_resid_mixed(gsz, stream, b));
+            if (guess_refine) {
+                if ((st = mpnn::fields_seed(lgraph, stream))) return st;
+                fields_ready = true;
+            }
         }
         CFD_LAUNCH(k_bicg_dir_mixed, rgrid, 256, 0, stream, a);
     }
@@ -207,6 +227,12 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
     CFD_CUDA(cudaLaunchCooperativeKernel(mixed ? (void*)k_pcg_mixed : (void*)k_pcg_fp64, dim3(pcg_grid),
                                          dim3(256), args, 0, stream));
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    // refined learned guess: the solutions correct the basis fields
+    if (mixed && prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph && guess_refine &&
+        fields_ready) {
+        int st = mpnn::fields_update(lgraph, stream, d_pos[0], d_pos[1]);
+        if (st) return st;
+    }
     if (h_iters) {  // the next step's learned-guess decision reads these
         CFD_CUDA(cudaMemcpyAsync(h_iters, d_pcg_iters, 2 * sizeof(int), cudaMemcpyDeviceToHost,
                                  stream));
@@ -233,7 +259,9 @@ int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
     guess_gate = gate;
     guess_first = true;
     guess_steps = 0;
-    if (d_gstats) CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 4 * sizeof(long long), stream));
+    fields_ready = false;
+    drop_graphs();
+    if (d_gstats) CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 8 * sizeof(long long), stream));
     if (!n) return CFD_OK;
     if (!lgraph) {
         const int N = npoin;
@@ -250,15 +278,25 @@ int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
             if ((st = dalloc(&d_cand[s], N))) return st;
         if ((st = dalloc(&d_gflag, 2))) return st;
         if ((st = dalloc(&d_grr, 2))) return st;
-        if ((st = dalloc(&d_gstats, 4))) return st;
+        if ((st = dalloc(&d_gstats, 8))) return st;
         CFD_CUDA(cudaMallocHost((void**)&h_iters, 2 * sizeof(int)));
         h_iters[0] = h_iters[1] = 0;
         // the captured step has no copy of the counts yet: capture it again
         drop_graphs();
         CFD_CUDA(cudaMemsetAsync(d_gflag, 0, 2 * sizeof(int), stream));
-        CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 4 * sizeof(long long), stream));
+        CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 8 * sizeof(long long), stream));
         CFD_CUDA(cudaStreamSynchronize(stream));
     }
+    return CFD_OK;
+}
+
+// Refined learned guess on or off: the network runs again on the next solve (which seeds
+// the fields) and the captured step is captured again with or without the fields' kernels.
+int Ctx::set_guess_refine(bool on) {
+    guess_refine = on;
+    fields_ready = false;
+    guess_first = true;
+    drop_graphs();
     return CFD_OK;
 }
 

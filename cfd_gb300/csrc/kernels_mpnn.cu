@@ -117,6 +117,69 @@ __global__ void k_globals(int nb, const int* __restrict__ bnode, const int* __re
     }
 }
 
+// Basis fields kept per node in FP64 (planes F[0..2] = Phi, Psi_x, Psi_y in length units)
+// for the refined learned guess: seeded from a network run, combined with each solve's
+// affine fit (G) into its guess, and corrected by each solve's solution.
+// Seed: F = (y0, L y1, L y2) at the free nodes, 0 elsewhere.
+__global__ void k_fields_seed(int n, const float* __restrict__ y, const int* __restrict__ kind,
+                              const Globals* __restrict__ G, double* __restrict__ F) {
+    const double L = G->L;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const bool f = kind[i] == KIND_FREE;
+        F[i] = f ? (double)y[OUT * i] : 0.0;
+        F[n + i] = f ? L * (double)y[OUT * i + 1] : 0.0;
+        F[2 * (size_t)n + i] = f ? L * (double)y[OUT * i + 2] : 0.0;
+    }
+}
+
+// Guess: c = t Phi + M (Psi_x, Psi_y) at the free nodes (x: (tx, m11, m12), y: (ty, m21,
+// m22)); the boundary nodes keep x, which already holds this solve's Dirichlet values.
+__global__ void k_fields_guess(int n, const int* __restrict__ kind, const Globals* __restrict__ G,
+                               const double* __restrict__ F, const double* __restrict__ x0,
+                               const double* __restrict__ x1, double* __restrict__ c0,
+                               double* __restrict__ c1) {
+    const Globals g = *G;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double a = x0[i], b = x1[i];
+        if (kind[i] == KIND_FREE) {
+            const double f0 = F[i], f1 = F[n + i], f2 = F[2 * (size_t)n + i];
+            a = g.tx * f0 + g.m11 * f1 + g.m12 * f2;
+            b = g.ty * f0 + g.m21 * f1 + g.m22 * f2;
+        }
+        c0[i] = a;
+        c1[i] = b;
+    }
+}
+
+// Correction after the solves: each solve s with coefficients a_s (its affine fit) and
+// solution x_s gives one equation a_s . F_i = x_s(i) per node; F_i moves to the nearest
+// point that satisfies it (a Kaczmarz step per node: the x solve's, then the y solve's;
+// solves with no prescribed motion are skipped).
+__global__ void k_fields_update(int n, const int* __restrict__ kind, const Globals* __restrict__ G,
+                                const double* __restrict__ x0, const double* __restrict__ x1,
+                                double* __restrict__ F) {
+    const Globals g = *G;
+    const double a[2][3] = {{g.tx, g.m11, g.m12}, {g.ty, g.m21, g.m22}};
+    double q[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) q[s] = a[s][0] * a[s][0] + a[s][1] * a[s][1] + a[s][2] * a[s][2];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (kind[i] != KIND_FREE) continue;
+        double f[3] = {F[i], F[n + i], F[2 * (size_t)n + i]};
+        const double x[2] = {x0[i], x1[i]};
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            if (!(q[s] > 0.0)) continue;
+            const double r = (x[s] - (a[s][0] * f[0] + a[s][1] * f[1] + a[s][2] * f[2])) / q[s];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) f[c] += a[s][c] * r;
+        }
+        F[i] = f[0];
+        F[n + i] = f[1];
+        F[2 * (size_t)n + i] = f[2];
+    }
+}
+
 // per-node prescribed displacement (0 at free nodes) from the boundary list
 __global__ void k_scatter_bc(int nb, const int* __restrict__ bnode, const double* __restrict__ gx,
                              const double* __restrict__ gy, double* __restrict__ gnx,

@@ -65,6 +65,81 @@ __device__ __forceinline__ void spmv_row2_f(const PcgArgs& a, int i, const float
     }
 }
 
+// Row i of A times the FP64 vectors (x0, x1), as accurately as FP64 arithmetic: each x_j is
+// split into FP32 hi + lo (split_bits, exact to 2^-47), a_ij*hi is formed exactly as a
+// float pair (product + fmaf remainder), the products are summed with a compensated (Neumaier)
+// FP32 sum and the remainders and a_ij*lo terms with a plain one, and the three partial
+// sums are added in FP64.  The first residual of a solve, r = b - A.x, takes this product
+// under the relative stopping tests: it is the one SpMV of the solve whose operand is the
+// whole displacement rather than a correction, so an FP32 product's error there (~1e-7 of
+// |A||x|) would be a floor under the starting residual of any good initial guess.  The
+// reference's absolute test, loose against that floor, keeps the FP32 product.  With FIXC
+// also the FP32 sums over the Dirichlet columns (the row of A.x_D).
+struct Acc2 {
+    float s, c, t;  // compensated sum s + c of the exact products' leading parts; tail sum t
+    __device__ __forceinline__ void init() { s = c = t = 0.f; }
+    __device__ __forceinline__ void add(float m, double x) {
+        float hi, lo;
+        split_bits(x, hi, lo);
+        const float p = m * hi;
+        const float e = fmaf(m, hi, -p);
+        const float u = s + p;
+        if (fabsf(s) >= fabsf(p)) c += (s - u) + p;
+        else c += (p - u) + s;
+        s = u;
+        t += e + m * lo;
+    }
+    __device__ __forceinline__ double value() const {
+        return (f2d_bits(s) + f2d_bits(c)) + f2d_bits(t);
+    }
+};
+
+template <int NS, bool FIXC = false, int kRowBatch = 8>
+__device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const double* v0,
+                                            const double* v1, double& d0, double& d1,
+                                            float* f0 = nullptr, float* f1 = nullptr) {
+    Acc2 s0, s1;
+    s0.init();
+    s1.init();
+    float g0 = 0.f, g1 = 0.f;
+    const int j0 = a.rowptr[i], j1 = a.rowptr[i + 1];
+    for (int jb = j0; jb < j1; jb += kRowBatch) {
+        int c[kRowBatch];
+        float m[kRowBatch];
+        double x0[kRowBatch], x1[kRowBatch];
+        bool fx[kRowBatch];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                c[u] = a.col[jb + u];
+                m[u] = a.valf[jb + u];
+            }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                x0[u] = v0[c[u]];
+                if (NS == 2) x1[u] = v1[c[u]];
+                if (FIXC) fx[u] = a.isfix[c[u]] != 0;
+            }
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u)
+            if (jb + u < j1) {
+                s0.add(m[u], x0[u]);
+                if (NS == 2) s1.add(m[u], x1[u]);
+                if (FIXC && fx[u]) {
+                    g0 += m[u] * d2f_trunc(x0[u]);
+                    if (NS == 2) g1 += m[u] * d2f_trunc(x1[u]);
+                }
+            }
+    }
+    d0 = s0.value();
+    d1 = (NS == 2) ? s1.value() : 0.0;
+    if (FIXC) {
+        *f0 = g0;
+        *f1 = g1;
+    }
+}
+
 template <int kRowBatch = 4>
 __device__ __forceinline__ float spmv_row_dir_f(const PcgArgs& a, int i, const float* pf,
                                                 const float* zf, float beta) {
@@ -156,7 +231,7 @@ __device__ bool last_block_fold(unsigned* count, const double* part, long nb, in
 // the reference norm of CFD_BICG_TOL_REL.  y itself is not kept: the next pass overwrites
 // it.  A block visits the 256-row groups blockIdx.x, blockIdx.x + gridDim.x, ... (one
 // group when the grid has a block per group); there is one partial per block.
-template <int NS, bool RELB>
+template <int NS, bool RELB, bool PRECISE>
 __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) {
     const int t = threadIdx.x;
     double rr[2] = {0.0, 0.0}, rp[2] = {0.0, 0.0}, ee[2] = {0.0, 0.0};
@@ -164,10 +239,19 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
     const long i = rb * 256 + t;
     if (i < a.n) {
         const bool fx = a.isfix[i];
-        float d[2] = {0.f, 0.f}, f[2] = {0.f, 0.f};
-        if (!fx) spmv_row2_f<NS, RELB>(a, (int)i, a.xf[0], a.xf[1], d[0], d[1], &f[0], &f[1]);
+        double d[2] = {0.0, 0.0};
+        float f[2] = {0.f, 0.f};
+        if (!fx) {
+            if (PRECISE) {
+                spmv_row2_x<NS, RELB>(a, (int)i, a.x[0], a.x[1], d[0], d[1], &f[0], &f[1]);
+            } else {
+                float d32[2];
+                spmv_row2_f<NS, RELB>(a, (int)i, a.xf[0], a.xf[1], d32[0], d32[1], &f[0], &f[1]);
+                d[0] = f2d_bits(d32[0]);
+                d[1] = f2d_bits(d32[1]);
+            }
+        }
         const double id = a.invdiag[i];
-        const float idf = a.invdiagf[i];
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
             double r, p, e = 0.0;
@@ -176,16 +260,11 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
                 r = 0.0;
                 p = 0.0;
                 pf = 0.f;
-            } else if (a.b[s]) {
-                r = a.b[s][i] - f2d_bits(d[s]);
+            } else {
+                r = a.b[s] ? a.b[s][i] - d[s] : -d[s];
                 p = r * id;
                 pf = d2f_trunc(p);
-                if (RELB) e = a.b[s][i] - f2d_bits(f[s]);
-            } else {
-                r = f2d_bits(-d[s]);
-                p = r * id;
-                pf = -d[s] * idf;
-                if (RELB) e = f2d_bits(-f[s]);
+                if (RELB) e = a.b[s] ? a.b[s][i] - f2d_bits(f[s]) : f2d_bits(-f[s]);
             }
             a.r[s][i] = r;
             a.p[s][0][i] = p;
@@ -215,13 +294,22 @@ __device__ __forceinline__ bool first_done(const PcgArgs& a, int s) {
     return a.tol_mode == CFD_BICG_TOL_ABS ? rr < a.tol : rr <= a.bscal[8 * s + 5];
 }
 
+// REL: the relative tests' variant (accurate product, reference norm of CFD_BICG_TOL_REL
+// when tol_mode asks for it); the absolute test's variant keeps the FP32 product
+template <bool REL>
 __global__ void __launch_bounds__(256) k_bicg_resid_mixed(PcgArgs a) {
     __shared__ double sh[6][256];
     __shared__ double out[6];
     if (a.only_if && !*a.only_if) return;  // the same in every block
     const bool relb = a.tol_mode == CFD_BICG_TOL_REL;
-    if (a.nsolve == 2) relb ? first_rows<2, true>(a, sh) : first_rows<2, false>(a, sh);
-    else relb ? first_rows<1, true>(a, sh) : first_rows<1, false>(a, sh);
+    if (!REL) {
+        if (a.nsolve == 2) first_rows<2, false, false>(a, sh);
+        else first_rows<1, false, false>(a, sh);
+    } else if (a.nsolve == 2) {
+        relb ? first_rows<2, true, true>(a, sh) : first_rows<2, false, true>(a, sh);
+    } else {
+        relb ? first_rows<1, true, true>(a, sh) : first_rows<1, false, true>(a, sh);
+    }
     if (last_block_fold(&a.bcount[0], a.part_r, gridDim.x, relb ? 6 : 4, sh, out) &&
         threadIdx.x == 0) {
         for (int s = 0; s < 2; ++s) {
@@ -240,8 +328,15 @@ __global__ void __launch_bounds__(256) k_bicg_resid_mixed(PcgArgs a) {
     }
 }
 
-// r.z = r.r/diag of the candidate guesses (FP32 SpMV over their d2f_trunc values), per
-// 256-row block, folded by the last block; fixed rows contribute 0 as in the first pass
+cudaError_t launch_bicg_resid_mixed(unsigned grid, cudaStream_t stream, const PcgArgs& a) {
+    if (a.tol_mode == CFD_BICG_TOL_ABS) k_bicg_resid_mixed<false><<<grid, 256, 0, stream>>>(a);
+    else k_bicg_resid_mixed<true><<<grid, 256, 0, stream>>>(a);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+// r.z = r.r/diag of the candidate guesses (with the first pass's SpMV), per 256-row block,
+// folded by the last block; fixed rows contribute 0 as in the first pass
 __global__ void __launch_bounds__(256) k_guess_judge(PcgArgs a, const double* __restrict__ cand0,
                                                      const double* __restrict__ cand1,
                                                      double* __restrict__ rr) {
@@ -253,13 +348,23 @@ __global__ void __launch_bounds__(256) k_guess_judge(PcgArgs a, const double* __
     double q[2] = {0.0, 0.0};
     for (long i = blockIdx.x * (long)blockDim.x + t; i < a.n; i += (long)gridDim.x * blockDim.x) {
         if (a.isfix[i]) continue;
-        const int j0 = a.rowptr[i], j1 = a.rowptr[i + 1];
+        double d[2] = {0.0, 0.0};
+        if (a.tol_mode == CFD_BICG_TOL_ABS) {  // the first pass's FP32 product
+            for (int s = 0; s < a.nsolve; ++s) {
+                float q32 = 0.f;
+                for (int j = a.rowptr[i]; j < a.rowptr[i + 1]; ++j)
+                    q32 += a.valf[j] * d2f_trunc(cand[s][a.col[j]]);
+                d[s] = f2d_bits(q32);
+            }
+        } else if (a.nsolve == 2) {
+            spmv_row2_x<2>(a, (int)i, cand[0], cand[1], d[0], d[1]);
+        } else {
+            spmv_row2_x<1>(a, (int)i, cand[0], cand[1], d[0], d[1]);
+        }
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (s >= a.nsolve) continue;
-            float d = 0.f;
-            for (int j = j0; j < j1; ++j) d += a.valf[j] * d2f_trunc(cand[s][a.col[j]]);
-            const double r = f2d_bits(-d);
+            const double r = -d[s];
             q[s] += r * r * a.invdiag[i];
         }
     }

@@ -53,6 +53,9 @@ struct cfd_mpnn_graph {
     double *X = nullptr, *Y = nullptr, *bgx = nullptr, *bgy = nullptr, *gnx = nullptr,
            *gny = nullptr;
     Globals* G = nullptr;
+    // refined learned guess: per-node basis fields (3 planes of n doubles), allocated on
+    // first use
+    double* F = nullptr;
     float *f = nullptr, *e = nullptr, *target = nullptr;
     // forward cache
     float* a0 = nullptr;                 // n x HID (pre-activation of h0)
@@ -325,6 +328,39 @@ int guess_on_stream(cfd_mpnn* net, cfd_mpnn_graph* g, cudaStream_t st, const dou
     CFD_LAUNCH(k_guess, std::min(blocks_for(g->n, 256), gs), 256, 0, st, g->n,
                (const float*)g->yb, g->kind, (const double*)g->gnx, (const double*)g->gny,
                (const Globals*)g->G, ux, uy, gate);
+    return CFD_OK;
+}
+
+// Refined learned guess (mesh motion in a resident context), three steps on stream st:
+//  fields_seed: the basis fields from the network's last run (its output and the globals of
+//    that run's fit, as guess_on_stream leaves them);
+//  fields_guess: the affine fit of the boundary data (bgx, bgy; bnode order) and the guess
+//    c = t Phi + M Psi from the fields;
+//  fields_update: after the solves, the per-node correction by their solutions (x0, x1),
+//    with the fit the last guess_on_stream or fields_guess formed.
+int fields_seed(cfd_mpnn_graph* g, cudaStream_t st) {
+    if (!g->F) {
+        int rc = dev_alloc(g->owned, &g->F, 3 * (size_t)g->n);
+        if (rc) return rc;
+    }
+    CFD_LAUNCH(k_fields_seed, std::min(blocks_for(g->n, 256), 1216u), 256, 0, st, g->n,
+               (const float*)g->yb, g->kind, (const Globals*)g->G, g->F);
+    return CFD_OK;
+}
+
+int fields_guess(cfd_mpnn_graph* g, cudaStream_t st, const double* X, const double* Y,
+                 const double* bgx, const double* bgy, const double* x0, const double* x1,
+                 double* c0, double* c1) {
+    const int* ng = nullptr;
+    CFD_LAUNCH(k_globals, 1, 256, 0, st, g->nb, g->bnode, g->bkind, bgx, bgy, X, Y, g->G, ng);
+    CFD_LAUNCH(k_fields_guess, std::min(blocks_for(g->n, 256), 1216u), 256, 0, st, g->n, g->kind,
+               (const Globals*)g->G, (const double*)g->F, x0, x1, c0, c1);
+    return CFD_OK;
+}
+
+int fields_update(cfd_mpnn_graph* g, cudaStream_t st, const double* x0, const double* x1) {
+    CFD_LAUNCH(k_fields_update, std::min(blocks_for(g->n, 256), 1216u), 256, 0, st, g->n, g->kind,
+               (const Globals*)g->G, x0, x1, g->F);
     return CFD_OK;
 }
 

@@ -14,6 +14,11 @@ __global__ void k_globals(int nb, const int* bnode, const int* bkind, const doub
                           const int* gate);
 __global__ void k_scatter_bc(int nb, const int* bnode, const double* gx, const double* gy,
                              double* gnx, double* gny, const int* gate);
+__global__ void k_fields_seed(int n, const float* y, const int* kind, const Globals* G, double* F);
+__global__ void k_fields_guess(int n, const int* kind, const Globals* G, const double* F,
+                               const double* x0, const double* x1, double* c0, double* c1);
+__global__ void k_fields_update(int n, const int* kind, const Globals* G, const double* x0,
+                                const double* x1, double* F);
 __global__ void k_features(int n, const double* X, const double* Y, const int* kind,
                            const Globals* G, float* f, const int* gate);
 __global__ void k_edge_features(int m, const int* src, const int* nbr, const double* X,

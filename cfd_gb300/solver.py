@@ -263,6 +263,19 @@ class Solver:
         check(abi.lib().cfd_ctx_guess_stats(self.h, out), "cfd_ctx_guess_stats")
         return tuple(int(v) for v in out)
 
+    def set_guess_refine(self, on=True):
+        """Refined learned guess: basis fields seeded by the network and corrected by every
+        solve (see cfd_ctx_set_guess_refine)."""
+        check(abi.lib().cfd_ctx_set_guess_refine(self.h, int(bool(on))),
+              "cfd_ctx_set_guess_refine")
+
+    def guess_stats_ex(self):
+        """(network guesses formed, x and y taken, steps, fields guesses formed, x and y
+        taken, 0) since the network was attached."""
+        out = (C.c_longlong * 8)()
+        check(abi.lib().cfd_ctx_guess_stats_ex(self.h, out), "cfd_ctx_guess_stats_ex")
+        return tuple(int(v) for v in out)
+
     def smooth(self):
         """The reference's setup smoothing of the resident mesh, then its geometry again.
         -> (iterations, min quality)."""

@@ -391,6 +391,19 @@ int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate);
 /* counters since attach: steps with the network evaluated, solves 1 (x) and 2 (y) that
  * took the network's guess, steps */
 int cfd_ctx_guess_stats(cfd_ctx* ctx, long long* out4);
+/* Refined learned guess (on = 1; default off).  The context keeps the three fields
+ * (Phi, Psi_x, Psi_y) per node in FP64: a network run seeds them with its prediction, and
+ * after every pair of solves each node's fields take the smallest change that makes them
+ * reproduce both solutions (x = t Phi + M Psi with each solve's affine fit).  Between network
+ * runs each solve also tries the fields' guess t Phi + M Psi for its own data, and keeps it
+ * when its r.z is smaller than the previous step's.  The fields then track the moving
+ * mesh's operator, so the guess error is the change of the operator over a step rather
+ * than the change of the motion, which pays under a relative stopping test
+ * (CFD_BICG_TOL_REL).  Switching it makes the network run again on the next solve. */
+int cfd_ctx_set_guess_refine(cfd_ctx* ctx, int on);
+/* out8 = (steps with a network guess formed, x and y taken from it, steps, steps with a
+ * fields guess formed, x and y taken from it, 0) */
+int cfd_ctx_guess_stats_ex(cfd_ctx* ctx, long long* out8);
 
 /* FORCE_VISC (ns2DComp.ALE.f90:819-893): viscous force per force set on its wall edges
  * (F_VX, F_VY: 10 each) and, when skin is not NULL, the SKIN.DAT row of every set edge in
