@@ -115,7 +115,7 @@ struct Ctx {
     float2* d_mulam = nullptr;                  // per element: mu, lambda of the RK stage
     float *d_VXf = nullptr, *d_VYf = nullptr, *d_RHOf = nullptr, *d_Ef = nullptr, *d_Pf = nullptr,
           *d_RMACHf = nullptr;
-    float *d_invMf = nullptr, *d_areaf = nullptr, *d_areaf_old = nullptr;
+    float *d_invMf = nullptr, *d_areaf = nullptr;  // 1/M, element area (FP32 passes)
     float4* d_geo8 = nullptr;  // per element: dNx(1:3), dNy(1:3), area, Laplacian weight
     unsigned long long* d_blockmin = nullptr;  // per-block FP32 DTELEM minima
     double* d_invdiag = nullptr;
@@ -171,7 +171,7 @@ struct Ctx {
     int* d_slot_pos = nullptr;
     float4 *d_recInv = nullptr, *d_recVisc = nullptr;  // slot records, element-around-point order
     float4* d_invSum = nullptr;                         // per node: sum of the recInv slots
-    float2* d_gterms = nullptr;
+    double2* d_gterms = nullptr;  // gcl element terms (FP64)
     double estab_eps = 1.0e-3;  // CFD_ESTAB_REGULARIZED relative gradient scale
     double dir[2] = {1.0, 0.0};  // CFD_ESTAB_REGULARIZED freestream direction
     // mesh motion

@@ -201,13 +201,13 @@ cudaError_t launch_node_mixed(cudaStream_t st, int npoin, const int* esup_ptr, c
 // dynamic shared memory of the bulk-copy node pass for blocks of `block` nodes (0: the
 // variant is not used: its staged slots would not fit)
 int node_bulk_smem(const int* esup_ptr_host, int npoin);
-__global__ void k_elem_geometry(int nelem, const int4* elem, const float2* Xhi, const float2* Xlo,
+__global__ void k_elem_geometry(int nelem, const int4* elem, const double* X, const double* Y,
                                 int gcl, int literal, const float2* W, const float2* Wold,
-                                int put_area, float* area_old, float* areaf, float4* geo,
-                                float2* terms, NormalsArgs nv);
+                                int put_area, double* area_old, double* area64, float* areaf,
+                                float4* geo, double2* terms, NormalsArgs nv);
 constexpr int kGeoNodeBlock = 128;  // block size of k_node_geometry
 __global__ void k_node_geometry(int npoin, const int* esup_ptr, const int* esup_slot,
-                                const uchar4* lap_pos, const float4* geo, const float2* terms,
+                                const uchar4* lap_pos, const float4* geo, const double2* terms,
                                 const double* dtp, int gcl, const int* rowptr, float* valf,
                                 double* invdiag, float* invdiagf, double* M, float* invM,
                                 const float2* W, float2* Wold);

@@ -781,8 +781,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
             if ((st = dalloc(q, N))) return st;
         for (float4** q : {&d_Uhi, &d_Ulo})
             if ((st = dalloc(q, N))) return st;
-        for (float** q : {&d_areaf, &d_areaf_old})
-            if ((st = dalloc(q, E))) return st;
+        if ((st = dalloc(&d_areaf, E))) return st;
         if ((st = dalloc(&d_blockmin, blocks_for(E, 256)))) return st;
         if ((st = dalloc(&d_geo8, 2 * (size_t)E))) return st;
         if ((st = dalloc(&d_mulam, E))) return st;
@@ -867,9 +866,9 @@ int Ctx::widen_mixed(int what) {
     const int nf = (what & 2) ? 7 : ((what & 1) ? 1 : 0);
     for (int i = 0; i < nf; ++i)
         CFD_LAUNCH(k_widen, blocks_for(N, 256), 256, 0, stream, N, src[i], dst[i]);
-    if (what & 4)
+    if (what & 4)  // d_area is the FP64 area the element pass keeps
         CFD_LAUNCH(k_widen_geo, blocks_for(E, 256), 256, 0, stream, (int)E, (const float4*)d_geo8,
-                   d_geo, d_area);
+                   d_geo, (double*)nullptr);
     return CFD_OK;
 }
 
@@ -894,9 +893,9 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
                          d_nrm};
     CFD_LAUNCH(k_elem_geometry,
                nv.nwn > 0 ? blocks_for(E, TB) + blocks_for(nv.nwn, TB) : branch_grid(E, TB, sv), TB,
-               0, stream, E, d_elem, d_Xhi, d_Xlo, gcl ? 1 : 0,
+               0, stream, E, d_elem, d_X, d_Y, gcl ? 1 : 0,
                prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, Wn, Wo,
-               (gcl || put_area) ? 1 : 0, d_areaf_old, d_areaf, geo8, d_gterms, nv);
+               (gcl || put_area) ? 1 : 0, d_area_old, d_area, d_areaf, geo8, d_gterms, nv);
     tstop(TM_DERIV);
     tstart(TM_LAPLACE);
     CFD_LAUNCH(k_node_geometry, branch_grid(N, kGeoNodeBlock, sv), kGeoNodeBlock, 0, stream, N,

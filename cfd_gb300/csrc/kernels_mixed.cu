@@ -680,19 +680,22 @@ k_node_mixed(int npoin, const int* __restrict__ esup_ptr, const int* __restrict_
 // Per element, 8 floats (two float4): geo[2e] = (dNx1, dNx2, dNx3, dNy1),
 // geo[2e+1] = (dNy2, dNy3, area, q) with q the mesh-Laplacian weight of the element.
 //
-// Element pass: deriv (subrutinas.f90:102-115) in FP32 from edge vectors of the hi/lo
-// coordinates (as accurate as FP64 differences rounded to FP32); the Laplacian weight of
-// mLaplace.f90:28-56: with |grad N_i|^2 = l_i^2/(2a)^2 the quality
-// mu = 2*sqrt(3)*(2a)/sum(l_i^2) of mLaplace.f90:96-108 is sqrt(3)/(a*sum|grad N_i|^2), so
-// q = 1/mu^2 = (a*sum|grad N_i|^2)^2/3; with gcl, the element terms of gcl main
-// (gcl.f90:27-45) divW*area/3 and divW_old*area_old/3, then putArea (area_old = area).
+// Element pass: the edge vectors and the signed area 2a = x1*y2 - x2*y1 (deriv,
+// subrutinas.f90:102-115) in FP64 from the FP64 coordinates; the area is kept in FP64 for
+// the gcl (area, putArea's area_old), the gradients and the Laplacian weight in FP32 from
+// the edge vectors truncated to FP32.  The Laplacian weight of mLaplace.f90:28-56: with
+// |grad N_i|^2 = l_i^2/(2a)^2 the quality mu = 2*sqrt(3)*(2a)/sum(l_i^2) of
+// mLaplace.f90:96-108 is sqrt(3)/(a*sum|grad N_i|^2), so q = 1/mu^2 = (a*sum|grad N_i|^2)^2/3;
+// with gcl, the element terms of gcl main (gcl.f90:27-45) divW*area and divW_old*area_old
+// in FP64 (divW itself from the FP32 gradients and W; the node pass applies the 1/3), then
+// putArea.
 __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
-                                const float2* __restrict__ Xhi, const float2* __restrict__ Xlo,
+                                const double* __restrict__ X, const double* __restrict__ Y,
                                 int gcl, int literal, const float2* __restrict__ W,
                                 const float2* __restrict__ Wold, int put_area,
-                                float* __restrict__ area_old, float* __restrict__ areaf,
-                                float4* __restrict__ geo, float2* __restrict__ terms,
-                                NormalsArgs nv) {
+                                double* __restrict__ area_old, double* __restrict__ area64,
+                                float* __restrict__ areaf, float4* __restrict__ geo,
+                                double2* __restrict__ terms, NormalsArgs nv) {
     // the blocks after the elements' do normales (one wall node per thread)
     const int eblocks = (nelem + blockDim.x - 1) / blockDim.x;
     if (nv.nwn > 0 && (int)blockIdx.x >= eblocks) {
@@ -704,11 +707,13 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
     const int estride = (nv.nwn > 0 ? eblocks : (int)gridDim.x) * blockDim.x;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += estride) {
     const int4 n = elem[e];
-    const float2 h0 = Xhi[n.x], h1 = Xhi[n.y], h2 = Xhi[n.z];
-    const float2 l0 = Xlo[n.x], l1 = Xlo[n.y], l2 = Xlo[n.z];
-    const float x1 = (h1.x - h0.x) + (l1.x - l0.x), y1 = (h1.y - h0.y) + (l1.y - l0.y);
-    const float x2 = (h2.x - h0.x) + (l2.x - l0.x), y2 = (h2.y - h0.y) + (l2.y - l0.y);
-    // 2a = x1*y2 - x2*y1 (the reference's signed area from differences to node 1)
+    const double X0 = X[n.x], Y0 = Y[n.x];
+    const double dx1 = X[n.y] - X0, dy1 = Y[n.y] - Y0;
+    const double dx2 = X[n.z] - X0, dy2 = Y[n.z] - Y0;
+    // 2a = x1*y2 - x2*y1 (the reference's signed area from differences to node 1), FP64
+    const double a64 = 0.5 * (dx1 * dy2 - dx2 * dy1);
+    const float x1 = d2f_trunc(dx1), y1 = d2f_trunc(dy1);
+    const float x2 = d2f_trunc(dx2), y2 = d2f_trunc(dy2);
     const float a2f = fmaf(x1, y2, -(x2 * y1));
     const float area = 0.5f * a2f;
     const float ia = fdiv(1.f, a2f);
@@ -721,6 +726,7 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
     geo[2 * (size_t)e] = make_float4(gx[0], gx[1], gx[2], gy[0]);
     geo[2 * (size_t)e + 1] = make_float4(gy[1], gy[2], area, q);
     areaf[e] = area;
+    area64[e] = a64;
     if (gcl) {
         const int nn[3] = {n.x, n.y, n.z};
         float divW = 0.f, divWo = 0.f;
@@ -730,17 +736,17 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
             divW += gx[i] * w.x + gy[i] * (literal ? w.x : w.y);
             divWo += gx[i] * wo.x + gy[i] * (literal ? wo.x : wo.y);
         }
-        terms[e] = make_float2(divW * area * (1.f / 3.f), divWo * area_old[e] * (1.f / 3.f));
+        terms[e] = make_double2(f2d_bits(divW) * a64, f2d_bits(divWo) * area_old[e]);
     }
-    if (put_area) area_old[e] = area;
+    if (put_area) area_old[e] = a64;
     }
 }
 
 // Node pass: the row of the mesh Laplacian (mLaplace.f90:28-56; rows of up to 16 entries
 // are summed in shared memory, longer ones in place), 1/diag, and the lumped mass: MASAS
 // (subrutinas.f90:128-153) as a compensated FP32 sum of area/3, or the gcl update
-// M += dt*(tot1+tot2)/2 in FP64 from compensated FP32 sums of the element terms, followed
-// by putW (W_old = W).
+// M += dt*(tot1+tot2)/2 in FP64 from FP64 sums (slot order) of the FP64 element terms,
+// followed by putW (W_old = W).
 constexpr int kLapRow = 16;
 constexpr int kGeoBatch = 2;  // slots per pass of k_node_geometry
 constexpr int kGeoBlock = kGeoNodeBlock;
@@ -748,7 +754,7 @@ constexpr int kGeoBlock = kGeoNodeBlock;
 __global__ void __launch_bounds__(kGeoBlock)
 k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
                 const uchar4* __restrict__ lap_pos, const float4* __restrict__ geo,
-                const float2* __restrict__ terms, const double* __restrict__ dtp, int gcl,
+                const double2* __restrict__ terms, const double* __restrict__ dtp, int gcl,
                 const int* __restrict__ rowptr, float* __restrict__ valf,
                 double* __restrict__ invdiag, float* __restrict__ invdiagf,
                 double* __restrict__ M, float* __restrict__ invM,
@@ -766,16 +772,16 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     } else {
         for (int k = r0; k < r1; ++k) valf[k] = 0.f;
     }
-    Acc m1, m2;
+    Acc m1;
     m1.init();
-    m2.init();
+    double t1 = 0.0, t2 = 0.0;  // gcl: tot1, tot2 (times 3)
     // kGeoBatch slots per pass: their loads go out together, the sums stay in slot order
     const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
     for (int sb = s0; sb < s1; sb += kGeoBatch) {
         int slot[kGeoBatch];
         uchar4 pos[kGeoBatch];
         float4 ga[kGeoBatch], gb[kGeoBatch];
-        float2 tm[kGeoBatch];
+        double2 tm[kGeoBatch];
 #pragma unroll
         for (int u = 0; u < kGeoBatch; ++u)
             if (sb + u < s1) {
@@ -795,8 +801,8 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
             if (sb + u >= s1) break;
             const int i = slot[u] - 3 * (slot[u] / 3);
             if (gcl) {
-                m1.add(tm[u].x);
-                m2.add(tm[u].y);
+                t1 = t1 + tm[u].x;
+                t2 = t2 + tm[u].y;
             } else {
                 m1.add(gb[u].z);
             }
@@ -825,7 +831,7 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     invdiag[p] = f2d_bits(idf);
     double m;
     if (gcl) {
-        m = M[p] + (*dtp) * (f2d_bits(m1.value()) + f2d_bits(m2.value())) * 0.5;
+        m = M[p] + (*dtp) * ((t1 + t2) * (1.0 / 3.0)) * 0.5;
         if (Wold) Wold[p] = W[p];  // putW (null: the caller swaps W buffers instead)
     } else {
         m = f2d_bits(m1.value()) * (1.0 / 3.0);
@@ -848,7 +854,7 @@ __global__ void k_widen_geo(int nelem, const float4* __restrict__ geo, double* _
     dN[3 * E + e] = ga.w;
     dN[4 * E + e] = gb.x;
     dN[5 * E + e] = gb.y;
-    area[e] = gb.z;
+    if (area) area[e] = gb.z;
 }
 
 // meshMove.f90:99-126: X += XPOS, W = XPOS/DTMIN (as XPOS*(1/DTMIN), the reciprocal formed
