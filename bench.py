@@ -58,6 +58,18 @@ def parse():
                          "side for this many steps and print their state and force errors")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only run warmup + this many steps (for ncu captures)")
+    ap.add_argument("--accuracy-compare-steps", type=int, default=2000,
+                    help="steps of the default run's mixed-vs-FP64 and reference-vs-"
+                         "regularized-ESTAB comparisons (the metric's condition is stated "
+                         "after 2000 steps)")
+    ap.add_argument("--record", choices=["config1", "config2", "config5"], default=None,
+                    help="instead of the benchmark: the long run of a workload as its "
+                         "configuration describes it (histories into --record-out)")
+    ap.add_argument("--record-steps", type=int, default=None)
+    ap.add_argument("--record-out", default=None, help="JSON file of the record's histories")
+    ap.add_argument("--guess-tol-mode", type=int, default=1,
+                    help="BiCG stopping test of the guess report (0: the reference's "
+                         "absolute r.z < 1e-10; 1: ||r|| <= 1e-10 ||b - A x_D||)")
     return ap.parse_args()
 
 
@@ -228,19 +240,6 @@ def algorithmic_bytes(k, iters, precision):
     }
 
 
-def run_cpu_reference(k, threads, steps):
-    """The oracle (CPU restatement of the reference) with `threads` OpenMP threads:
-    seconds per step over `steps` steps after setup."""
-    from oracle import oracle as O
-    O.set_threads(threads)
-    oc = O.OracleCase(k)
-    t = time.perf_counter()
-    rep = oc.step(steps)
-    dt = (time.perf_counter() - t) / steps
-    oc.close()
-    return dt, rep
-
-
 def main_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -372,49 +371,311 @@ def large_mesh_report(W, net, gate, hbm_peak, nr=2048):
                                      "frac_of_hbm_peak": ab / upd / 1e9 / hbm_peak}}
 
 
-def guess_report(args, W, K):
+def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
     """Mesh-motion solve with the previous-step, zero and learned guesses on the workload
-    (mixed form): BiCG iterations on the first (cold) step and per step after warm-up, the
-    mesh-motion time per step (timer of the BiCG group, which holds the network), the step
-    time, and for the learned guess how often it ran and how often its guess was taken."""
+    (mixed form): BiCG iterations (x + y solves) on the first (cold) step and per step after
+    warm-up, the mesh-motion time per step (timer of the BiCG group, which holds the network
+    and the fields), the step time, and for the learned guesses how often a guess was
+    formed and how often it was taken.  tol_mode / tol / maxit: the solve's stopping test
+    (0: the reference's absolute |r.z|; 1: ||r|| <= tol ||b - A x_D||).
+
+    Learned variants: "learned" runs the network on the first solve and after solves above
+    the gate; "learned_every_step" runs it on every solve; "learned_refined" runs it on the
+    first solve and then tries, every step, the guess of the basis fields it seeded and
+    the solves refine (cfd_ctx_set_guess_refine)."""
     from cfd_gb300 import abi, learned, solver
     net = learned.Net.load()
     out = {}
-    modes = (("previous", abi.CFD_GUESS_PREVIOUS, None), ("zero", abi.CFD_GUESS_ZERO, None),
-             ("learned_every_step", abi.CFD_GUESS_LEARNED, 0.0),
-             ("learned", abi.CFD_GUESS_LEARNED, args.guess_gate))
+    all_modes = {"previous": (abi.CFD_GUESS_PREVIOUS, None, False),
+                 "zero": (abi.CFD_GUESS_ZERO, None, False),
+                 "learned_every_step": (abi.CFD_GUESS_LEARNED, 0.0, False),
+                 "learned": (abi.CFD_GUESS_LEARNED, args.guess_gate, False),
+                 "learned_refined": (abi.CFD_GUESS_LEARNED, 1.0e9, True)}
+    modes = modes or ["previous", "zero", "learned_every_step", "learned"]
     os.environ["CFD_TIMERS"] = "1"
     try:
-        for name, mode, gate in modes:
+        for name in modes:
+            mode, gate, refine = all_modes[name]
             k = workload(args)
             k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
             k.params.guess_mode = mode
+            k.params.bicg_tol_mode = tol_mode
+            k.params.bicg_tol = tol
+            k.params.bicg_maxit = maxit
             S = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
             if gate is not None:
                 S.set_guess_net(net, gate)
+                if refine:
+                    S.set_guess_refine(True)
             r1 = S.step(1)
             S.step(max(W - 1, 0))
             t0 = S.timers()
-            its = []
+            its, conv, relres = [], [], []
             S.mark(0)
             for _ in range(K):
-                its.append(sum(S.step(1).bicg_iters))
+                r = S.step(1)
+                its.append(sum(r.bicg_iters))
+                conv.append(min(r.bicg_converged))
+                relres.append(max(r.bicg_relres))
             S.mark(1)
             ms = S.elapsed_ms(0, 1) / K
             t1 = S.timers()
             d = {"first_step_iters": list(r1.bicg_iters), "iters_per_step": float(np.mean(its)),
+                 "iters_per_step_min_max": [int(min(its)), int(max(its))],
+                 "converged_steps": int(sum(conv)), "steps_timed": K,
+                 "max_relres": float(max(relres)) if tol_mode else None,
                  "mesh_motion_ms_per_step": (t1["grad_t"][0] - t0["grad_t"][0]) * 1e3 / K,
                  "ms_per_step": ms}
             if gate is not None:
-                ev, tx, ty, n = S.guess_stats()
+                st = S.guess_stats_ex()
+                ev, tx, ty, n = st[:4]
                 d.update({"gate": gate, "network_steps": ev, "network_taken": tx + ty,
-                          "fallback_rate": (1.0 - (tx + ty) / (2.0 * ev)) if ev else None,
+                          "network_fallback_rate": (1.0 - (tx + ty) / (2.0 * ev)) if ev else None,
                           "steps": n})
+                if refine:
+                    dv, dx, dy = st[4:7]
+                    d.update({"fields_steps": dv, "fields_taken": [dx, dy]})
             S.close()
             out[name] = d
     finally:
         os.environ.pop("CFD_TIMERS", None)
     return out
+
+
+def e2e_loop(S, L, N, KE, dist, ws):
+    """The metric through the C-ABI with host buffers: per step, upload U (the context
+    derives the velocities and keeps T), one step, download U; pinned host memory, copies
+    inside the timed region.  Returns the e2e dict."""
+    import torch
+    from cfd_gb300 import abi
+    hU = torch.empty((N, 4), dtype=torch.float64, pin_memory=True).numpy()
+    hU[:] = S.state()["U"]
+    torch.cuda.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(KE):
+        abi.check(L.cfd_ctx_upload_state(S.h, abi.dptr(hU), None, None, None), "upload")
+        S.step(1)
+        abi.check(L.cfd_ctx_download_state(S.h, abi.dptr(hU), None, None, None), "download")
+    torch.cuda.synchronize()
+    sec = dist.max(time.perf_counter() - t0) / KE
+    return {"value": ws * N / sec, "unit": UNIT, "h2d_bytes_per_step": int(N * 32),
+            "d2h_bytes_per_step": int(N * 32), "ms_per_step": sec * 1e3, "steps": KE}
+
+
+def forces(rep):
+    return float(rep.fx[0]), float(rep.fy[0])
+
+
+def accuracy_compare(args, NS):
+    """Three runs of the workload in lockstep for NS steps: the mixed form (regularized
+    ESTAB, previous-step guess), the FP64 form with the same ESTAB, and the FP64 form with
+    the reference's ESTAB (subrutinas.f90:374-393).  Returns (a) the mixed form's error
+    against the FP64 form of the same method: the whole state and each conserved variable
+    (rel L2, rho*v also against the momentum scale) after NS steps, and the pressure force
+    (drag, lift of body set 1) error over the run against the largest FP64 force; (b) how
+    far the regularized method sits from the reference's: the same measures between the two
+    FP64 runs."""
+    from cfd_gb300 import abi, solver
+    runs = {}
+    for name, prec, estab in (("mixed", abi.CFD_PREC_MIXED, abi.CFD_ESTAB_REGULARIZED),
+                              ("fp64_reg", abi.CFD_PREC_FP64, abi.CFD_ESTAB_REGULARIZED),
+                              ("fp64_ref", abi.CFD_PREC_FP64, abi.CFD_ESTAB_REFERENCE)):
+        k = workload(args)
+        k.params.estab_mode = estab
+        runs[name] = solver.Solver(k, precision=prec)
+    hist = {n: [] for n in runs}
+    t0 = time.perf_counter()
+    for _ in range(NS):
+        for n, S in runs.items():
+            hist[n].append(forces(S.step(1)))
+    wall = time.perf_counter() - t0
+    U = {n: S.state()["U"] for n, S in runs.items()}
+    for S in runs.values():
+        S.close()
+    F = {n: np.array(h) for n, h in hist.items()}
+
+    def compare(a, b):
+        Ua, Ub = U[a], U[b]
+        fmax = float(np.abs(F[b]).max())
+        return {"state_rel_l2": rel_l2(Ua, Ub),
+                "rel_l2": [rel_l2(Ua[:, q], Ub[:, q]) for q in range(4)],
+                "rho_v_rel_l2_momentum_scale": float(np.linalg.norm(Ua[:, 2] - Ub[:, 2]) / max(
+                    np.linalg.norm(Ub[:, 1]), np.linalg.norm(Ub[:, 2]))),
+                "force_err_rel_max": [float(np.abs(F[a][:, c] - F[b][:, c]).max() / fmax)
+                                      for c in range(2)],
+                "force_err_rel_final": [float(abs(F[a][-1, c] - F[b][-1, c]) / fmax)
+                                        for c in range(2)],
+                "finite": bool(np.isfinite(Ua).all() and np.isfinite(Ub).all())}
+    return {"steps": NS, "wall_s": wall,
+            "mixed_vs_fp64": dict(compare("mixed", "fp64_reg"), estab_mode="regularized",
+                                  guess="previous"),
+            "estab_regularized_vs_reference_fp64": compare("fp64_reg", "fp64_ref")}
+
+
+def run_cpu_baselines(k_fn, threads_all):
+    """The oracle on the host cores: all threads (3 steps after 1 warm-up step) and one
+    thread (1 step), each on the full workload."""
+    from oracle import oracle as O
+    out = {}
+    for label, threads, steps, warm in (("all_cores", threads_all, 3, 1), ("one_core", 1, 1, 0)):
+        O.set_threads(threads)
+        k = k_fn()
+        oc = O.OracleCase(k)
+        if warm:
+            oc.step(warm)
+        t = time.perf_counter()
+        oc.step(steps)
+        sec = (time.perf_counter() - t) / steps
+        oc.close()
+        out[label] = {"value": k.npoin / sec, "unit": UNIT, "cores": threads, "kind": "port",
+                      "sample": f"{steps} full step(s) of the {k.npoin}-node workload after "
+                                f"{warm} warm-up step(s) (oracle, OpenMP, {threads} "
+                                f"thread(s), reference ESTAB), setup excluded",
+                      "ms_per_step": sec * 1e3}
+    return out
+
+
+def lift_drag(rep, S):
+    """Drag and lift of body set 1 as the reference's FORCES file takes them: pressure
+    (FX, FY of FORCES, meshMove.f90:153-194) plus viscous (F_VX, F_VY of FORCE_VISC,
+    ns2DComp.ALE.f90:247-248)."""
+    fvx, fvy, _ = S.force_visc()
+    return float(rep.fx[0] + fvx[0]), float(rep.fy[0] + fvy[0])
+
+
+def main_record(args):
+    """Long runs of the workloads as their configurations describe them; the histories go
+    to --record-out (JSON), one summary line to stdout.
+
+    config1: the 8,192-node cylinder (64 x 128, fixed mesh, Mach 0.3, Re 100), FP64 form
+      against the oracle (one thread) for 2000 steps: DTMIN and drag/lift compared every
+      step, the state (U, T, X, Y) every 100th step, bit for bit.
+    config2: the 262,144-node cylinder (512 x 512, heave 0.2 sin(2 pi 0.2 t), Re 200), FP64
+      form, the mesh-motion solve to ||r|| <= 1e-10 ||b - A x_D||, 5000 steps: BiCG
+      iterations and relative residual per step and solve, drag and lift per step.
+    config5: the 4,194,304-node ellipse (2048 x 2048, Mach 0.8, Re 10000, heave 0.05 + pitch
+      3 deg at f = 0.1): the mixed form with the learned guess (refined fields) for 10000
+      steps, node-steps/s, and its pressure forces over the first 500 steps against 500-step
+      FP64 runs of the same case (regularized and reference ESTAB)."""
+    from cfd_gb300 import abi, build, case as C, learned, solver
+    build.build()
+    abi.lib()
+    out = {"record": args.record}
+    hist = []
+    if args.record == "config1":
+        from oracle import oracle as O
+        O.set_threads(1)
+        n = args.record_steps or 2000
+        k = C.config_case(1)
+        S, Oc = solver.Solver(k), O.OracleCase(k)
+        S.set_force_visc(True)
+        Oc.set_force_visc(True)
+        mism, checks = [], 0
+        t0 = time.perf_counter()
+        for s in range(1, n + 1):
+            rg, ro = S.step(1), Oc.step(1)
+            fg, fo = lift_drag(rg, S), lift_drag(ro, Oc)
+            same = rg.dtmin == ro.dtmin and fg == fo
+            if s % 100 == 0 or s == n:
+                sg, so = S.state(), Oc.state()
+                checks += 1
+                same = same and all(np.array_equal(sg[q], so[q]) for q in ("U", "T", "X", "Y"))
+                hist.append({"step": s, "time": rg.time, "dtmin": rg.dtmin, "drag": fg[0],
+                             "lift": fg[1], "bit_exact": bool(same),
+                             "rho_mean": float(sg["U"][:, 0].mean())})
+            if not same:
+                mism.append(s)
+        out.update({"workload": f"cylinder O-grid 64x128 ({k.npoin} nodes, {k.nelem} "
+                                f"triangles), Mach 0.3, Re 100, fixed mesh, FP64",
+                    "steps": n, "state_checks": checks, "mismatched_steps": mism[:20],
+                    "bit_exact_every_step_and_checkpoint": not mism,
+                    "wall_s": time.perf_counter() - t0,
+                    "final_state_finite": bool(np.isfinite(S.state()["U"]).all())})
+        S.close()
+        Oc.close()
+    elif args.record == "config2":
+        n = args.record_steps or 5000
+        k = C.config_case(2)
+        k.params.bicg_tol_mode = abi.CFD_BICG_TOL_REL
+        k.params.bicg_tol = 1.0e-10
+        k.params.bicg_maxit = 20000
+        S = solver.Solver(k)
+        S.set_force_visc(True)
+        t0 = time.perf_counter()
+        S.mark(0)
+        for s in range(1, n + 1):
+            r = S.step(1)
+            d, li = lift_drag(r, S)
+            hist.append({"step": s, "time": r.time, "dtmin": r.dtmin, "drag": d, "lift": li,
+                         "bicg_iters": list(r.bicg_iters), "bicg_relres": list(r.bicg_relres),
+                         "converged": list(r.bicg_converged)})
+        S.mark(1)
+        ms = S.elapsed_ms(0, 1) / n
+        its = np.array([h["bicg_iters"] for h in hist])
+        out.update({"workload": f"cylinder O-grid 512x512 ({k.npoin} nodes, {k.nelem} "
+                                f"triangles), Mach 0.3, Re 200, heave 0.2 sin(2 pi 0.2 t), ALE "
+                                f"+ gcl, FP64, BiCG to ||r|| <= 1e-10 ||b - A x_D||",
+                    "steps": n, "ms_per_step": ms, "node_steps_per_s": k.npoin / (ms / 1e3),
+                    "wall_s": time.perf_counter() - t0,
+                    "bicg_iters_per_solve_mean": its.mean(0).tolist(),
+                    "bicg_iters_per_solve_min": its.min(0).tolist(),
+                    "bicg_iters_per_solve_max": its.max(0).tolist(),
+                    "all_converged": all(min(h["converged"]) == 1 for h in hist),
+                    "max_relres": max(max(h["bicg_relres"]) for h in hist),
+                    "final_time": hist[-1]["time"],
+                    "lift_range": [min(h["lift"] for h in hist), max(h["lift"] for h in hist)],
+                    "drag_range": [min(h["drag"] for h in hist), max(h["drag"] for h in hist)],
+                    "state_finite": bool(np.isfinite(S.state()["U"]).all())})
+        S.close()
+    elif args.record == "config5":
+        n = args.record_steps or 10000
+        nf = min(500, n)
+        net = learned.Net.load()
+        k = C.config_case(5)
+        k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
+        k.params.guess_mode = abi.CFD_GUESS_LEARNED
+        S = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+        S.set_guess_net(net, 1.0e9)
+        S.set_guess_refine(True)
+        fm = []
+        S.mark(0)
+        for s in range(1, nf + 1):
+            fm.append(forces(S.step(1)))
+        S.mark(2)
+        r = S.step(n - nf) if n > nf else S.step(0)
+        S.mark(1)
+        ms = S.elapsed_ms(0, 1) / n
+        ms_tail = S.elapsed_ms(2, 1) / (n - nf) if n > nf else None
+        Um = S.state()["U"]
+        gs = S.guess_stats_ex()
+        S.close()
+        out.update({"workload": f"ellipse O-grid 2048x2048 ({k.npoin} nodes, {k.nelem} "
+                                f"triangles), Mach 0.8, Re 10000, heave 0.05 + pitch 3 deg @ "
+                                f"f=0.1, ALE + gcl, mixed + learned guess (refined fields)",
+                    "steps": n, "ms_per_step": ms, "value": k.npoin / (ms / 1e3),
+                    "ms_per_step_after_force_window": ms_tail,
+                    "bicg_iters_last": list(r.bicg_iters), "guess_stats_ex": list(gs),
+                    "state_finite": bool(np.isfinite(Um).all())})
+        for estab, name in ((abi.CFD_ESTAB_REGULARIZED, "fp64_regularized"),
+                            (abi.CFD_ESTAB_REFERENCE, "fp64_reference")):
+            kd = C.config_case(5)
+            kd.params.estab_mode = estab
+            Sd = solver.Solver(kd)
+            fd = [forces(Sd.step(1)) for _ in range(nf)]
+            Sd.close()
+            Fm, Fd = np.array(fm), np.array(fd)
+            fmax = float(np.abs(Fd).max())
+            out[f"forces_vs_{name}"] = {
+                "steps": nf, "rel_err_max": [float(np.abs(Fm[:, c] - Fd[:, c]).max() / fmax)
+                                             for c in range(2)],
+                "rel_err_final": [float(abs(Fm[-1, c] - Fd[-1, c]) / fmax) for c in range(2)]}
+            hist.append({name: Fd.tolist()})
+        hist.append({"mixed": fm})
+    if args.record_out:
+        with open(args.record_out, "w") as f:
+            json.dump({"summary": out, "history": hist}, f)
+    print(json.dumps(out), flush=True)
 
 
 def main_ours(args):
@@ -461,80 +722,54 @@ def main_ours(args):
     final_U = S.state()["U"]
     # ---- e2e through the C-ABI with pinned host buffers, copies inside the timed region
     N = k.npoin
-    st, f = S.state(), S.fields()
-    hU = torch.empty((N, 4), dtype=torch.float64, pin_memory=True).numpy()
-    hT = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
-    hvx = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
-    hvy = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
-    hU[:], hT[:], hvx[:], hvy[:] = st["U"], st["T"], f["VEL_X"], f["VEL_Y"]
     KE = max(2, min(K, 10))
-    torch.cuda.synchronize()
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(KE):
-        S.set_state(hU, hT, hvx, hvy)
-        S.step(1)
-        abi.check(L.cfd_ctx_download_state(S.h, abi.dptr(hU), abi.dptr(hT), None, None),
-                  "download")
-    torch.cuda.synchronize()
-    e2e_sec = dist.max(time.perf_counter() - t0) / KE
-    e2e = {"value": ws * N / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(N * (32 + 8 * 3)),
-           "d2h_bytes_per_step": int(N * (32 + 8))}
+    e2e = e2e_loop(S, L, N, KE, dist, ws)
     S.close()
-    # ---- the other forms: plain FP64 (reference ESTAB) speed; FP64 with the same ESTAB
-    # as the mixed run for its error
+    # ---- the other forms: plain FP64 (reference ESTAB) speed and e2e; the errors of the
+    # mixed form and of the regularized ESTAB over the comparison run; the mesh-motion solve
+    # with each initial guess under the relative stopping test
     forms = {}
     if mixed and not args.no_compare:
         kp = workload(args)
         Sp, msp, lp, repp = timed_run(solver, kp, abi.CFD_PREC_FP64, W, min(K, 10), L)
         forms["fp64_plain"] = {"value": ws * N / (dist.max(msp) / 1e3), "unit": UNIT,
-                               "ms_per_step": msp, "estab_mode": "reference"}
+                               "ms_per_step": msp, "estab_mode": "reference",
+                               "gpu_launches_per_step": lp / min(K, 10),
+                               "e2e": e2e_loop(Sp, L, N, 3, dist, ws)}
         Sp.close()
-        # the error runs: W + min(K, 52) steps (the FP64 form takes ~29 ms a step)
-        NC = W + min(K, 52)
-        kr = workload(args)
-        kr.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
-        Sr = solver.Solver(kr, precision=abi.CFD_PREC_FP64)
-        repr_ = Sr.step(NC)
-        Ur = Sr.state()["U"]
-        Sr.close()
-        # precision error: the mixed form against the FP64 form, both with the previous-
-        # step guess (the same mesh-motion solves)
-        km = workload(args)
-        km.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
-        Sm = solver.Solver(km, precision=abi.CFD_PREC_MIXED)
-        repm = Sm.step(NC)
-        Um = Sm.state()["U"]
-        Sm.close()
-        forms["mixed_vs_fp64"] = {
-            "steps": NC, "estab_mode": "regularized", "guess": "previous",
-            # the whole conserved state; per variable against its own norm; rho*v (small at
-            # 2 degrees) also against the momentum scale max(|rho*u|, |rho*v|)
-            "state_rel_l2": rel_l2(Um, Ur),
-            "rel_l2": [rel_l2(Um[:, q], Ur[:, q]) for q in range(4)],
-            "rho_v_rel_l2_momentum_scale": float(np.linalg.norm(Um[:, 2] - Ur[:, 2]) / max(
-                np.linalg.norm(Ur[:, 1]), np.linalg.norm(Ur[:, 2]))),
-            "force_rel_err": float(np.hypot(repm.fx[0] - repr_.fx[0], repm.fy[0] - repr_.fy[0])
-                                   / np.hypot(repr_.fx[0], repr_.fy[0]))}
+        forms["speedup_vs_fp64_plain"] = value / forms["fp64_plain"]["value"]
+        forms["e2e_speedup_vs_fp64_plain"] = e2e["value"] / forms["fp64_plain"]["e2e"]["value"]
+        if args.accuracy_compare_steps > 0:
+            forms["accuracy"] = accuracy_compare(args, args.accuracy_compare_steps)
         if net is not None:
-            # the learned guess changes the mesh motion within the solve's absolute tolerance
-            kl = workload(args)
-            kl.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
-            kl.params.guess_mode = abi.CFD_GUESS_LEARNED
-            Sl = solver.Solver(kl, precision=abi.CFD_PREC_MIXED)
-            Sl.set_guess_net(net, gate)
-            Sl.step(NC)
-            Ul = Sl.state()["U"]
-            gs_l = Sl.guess_stats()
-            Sl.close()
+            # under the reference's absolute test the learned guess changes the mesh motion
+            # within the solve's tolerance
+            NC = W + min(K, 52)
+            runs = {}
+            for name, mode in (("previous", abi.CFD_GUESS_PREVIOUS),
+                               ("learned", abi.CFD_GUESS_LEARNED)):
+                kl = workload(args)
+                kl.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
+                kl.params.guess_mode = mode
+                Sl = solver.Solver(kl, precision=abi.CFD_PREC_MIXED)
+                if mode == abi.CFD_GUESS_LEARNED:
+                    Sl.set_guess_net(net, gate)
+                Sl.step(NC)
+                runs[name] = (Sl.state()["U"], Sl.guess_stats() if mode else None)
+                Sl.close()
+            Ul, Um = runs["learned"][0], runs["previous"][0]
             forms["learned_vs_previous_guess"] = {
-                "steps": NC, "rel_l2": [rel_l2(Ul[:, q], Um[:, q]) for q in range(4)],
-                "guess_stats": list(gs_l),
+                "steps": NC, "bicg_tol_mode": "absolute (reference)",
+                "rel_l2": [rel_l2(Ul[:, q], Um[:, q]) for q in range(4)],
+                "guess_stats": list(runs["learned"][1]),
                 # (network evaluated, x and y guesses taken, steps) in the timed run
                 "timed_run_guess_stats": list(guess_stats)}
-        forms["speedup_vs_fp64_plain"] = value / forms["fp64_plain"]["value"]
-        if mixed:
-            forms["guess"] = guess_report(args, W, min(K, 10))
+        tm = args.guess_tol_mode
+        forms["guess"] = guess_report(
+            args, W, min(K, 10), tol_mode=tm, tol=1.0e-10, maxit=20000 if tm else 1000,
+            modes=["previous", "zero", "learned", "learned_every_step", "learned_refined"])
+        forms["guess"]["bicg_test"] = ("||r|| <= 1e-10 ||b - A x_D|| (relative)" if tm else
+                                       "|r.z| < 1e-10 (the reference's absolute test)")
     # ---- per-kernel breakdown and roofline of the dominant kernel (timers on, own ctx)
     os.environ["CFD_TIMERS"] = "1"
     S2 = solver.Solver(k, precision=prec)
@@ -583,21 +818,18 @@ def main_ours(args):
                     "frac_of_hbm_peak": (ab[n_] / per_step[n_] / 1e9 / hbm_peak)
                     if n_ in ab else None}
                for n_ in per_launch}
-    cpu = None
+    cpu, cpu1 = None, None
     if rank == 0 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        kc = workload(args)
-        sec, _ = run_cpu_reference(kc, threads, 1)
-        cpu = {"value": k.npoin / sec, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"1 full step of the {k.npoin}-node workload (oracle, OpenMP, "
-                         f"{threads} threads, reference ESTAB), setup excluded"}
+        cb = run_cpu_baselines(lambda: workload(args), os.cpu_count() or 1)
+        cpu, cpu1 = cb["all_cores"], cb["one_core"]
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": sec_step * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32+f64 (mixed)" if mixed else "f64", "data": "synthetic",
                 "config": config_dict(k, args, ws), "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "forms": forms,
+                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
+                "cpu_baseline_one_core": cpu1, "forms": forms,
                 "kernels": kernels,
                 "breakdown_ms_per_step": {n_: v * 1e3 for n_, v in per_step.items()},
                 "bicg_iters": list(rep.bicg_iters), "bicg_converged": list(rep.bicg_converged),
@@ -610,6 +842,8 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         main_reference(a)
+    elif a.record:
+        main_record(a)
     elif a.accuracy_steps > 0:
         main_accuracy(a)
     else:

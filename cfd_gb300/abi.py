@@ -24,6 +24,7 @@ CFD_MOTION_REFERENCE, CFD_MOTION_HARMONIC, CFD_MOTION_NEWMARK = 0, 1, 2
 CFD_GUESS_PREVIOUS, CFD_GUESS_ZERO, CFD_GUESS_LEARNED = 0, 1, 2
 CFD_ESTAB_REFERENCE, CFD_ESTAB_EXACT, CFD_ESTAB_REGULARIZED = 0, 1, 2
 CFD_BICG_TOL_ABS, CFD_BICG_TOL_REL, CFD_BICG_TOL_REL_R0 = 0, 1, 2
+CFD_SMOOTH_COLOUR, CFD_SMOOTH_NODE_ORDER = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -142,6 +143,8 @@ SIGNATURES = {
     "cfd_ctx_graph_state": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_set_force_visc": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smooth": (C.c_int, [_P, _ip, _dp]),
+    "cfd_ctx_smooth_ex": (C.c_int, [_P, C.c_int, _ip, _dp]),
+    "cfd_smoothing_ex": (C.c_int, [_dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _ip, _dp, C.c_int]),
     "cfd_selftest_waits": (C.c_int, [C.c_longlong, _ip, _ip]),
     "cfd_ctx_set_smoothing": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smoothing_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),

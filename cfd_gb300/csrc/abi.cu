@@ -403,6 +403,12 @@ int cfd_ctx_smooth(cfd_ctx* ctx, int* iters, double* min_quality) {
     return ctx->impl.smooth(iters, min_quality);
 }
 
+int cfd_ctx_smooth_ex(cfd_ctx* ctx, int visit, int* iters, double* min_quality) {
+    if (!ctx) return arg_error("ctx");
+    if (visit != CFD_SMOOTH_COLOUR && visit != CFD_SMOOTH_NODE_ORDER) return arg_error("order");
+    return ctx->impl.smooth(iters, min_quality, visit == CFD_SMOOTH_NODE_ORDER);
+}
+
 int cfd_ctx_graph_state(cfd_ctx* ctx, long long* out3) {
     if (!ctx || !out3) return arg_error("null pointer");
     const Ctx& c = ctx->impl;
@@ -765,7 +771,15 @@ int cfd_force_visc(const int* NELEM, const int* npoin, const int* nsets, const i
 int cfd_smoothing(double* X, double* Y, const int* inpoel, const int* fixed, const int* npoin,
                   const int* nelem, const double* dX, const double* dY, int* iters,
                   double* min_quality) {
-    if (!X || !Y || !inpoel || !fixed || bad_sizes(nelem, npoin) || (!dX != !dY))
+    return cfd_smoothing_ex(X, Y, inpoel, fixed, npoin, nelem, dX, dY, iters, min_quality,
+                            CFD_SMOOTH_COLOUR);
+}
+
+int cfd_smoothing_ex(double* X, double* Y, const int* inpoel, const int* fixed, const int* npoin,
+                     const int* nelem, const double* dX, const double* dY, int* iters,
+                     double* min_quality, int visit) {
+    if (!X || !Y || !inpoel || !fixed || bad_sizes(nelem, npoin) || (!dX != !dY) ||
+        (visit != CFD_SMOOTH_COLOUR && visit != CFD_SMOOTH_NODE_ORDER))
         return arg_error("cfd_smoothing");
     const int E = *nelem, N = *npoin;
     std::vector<int4> el;
@@ -808,7 +822,8 @@ int cfd_smoothing(double* X, double* Y, const int* inpoel, const int* fixed, con
     TRY(s.alloc(&d_scal, 3));
     TRY(s.alloc(&d_flags, 2));
     TRY(smooth_on_device(s.stream, N, E, d_el, d_ep, d_es, d_pp, d_ps, d_fx, d_X, d_Y, d_tol,
-                         offs, d_ord, d_sm, d_scal, d_flags, iters, min_quality, max_star));
+                         offs, d_ord, d_sm, d_scal, d_flags, iters, min_quality, max_star,
+                         visit == CFD_SMOOTH_NODE_ORDER));
     TRY(s.get(X, d_X, N));
     TRY(s.get(Y, d_Y, N));
     return s.sync();

@@ -41,7 +41,8 @@ int smooth_on_device(cudaStream_t st, int npoin, int nelem, const int4* elem,
                      const int* psup, const unsigned char* fixed, double* X, double* Y,
                      const double* tol_move, const std::vector<int>& offs, const int* order,
                      unsigned char* smoothable, unsigned long long* scal, int* flags,
-                     int* iters_out, double* min_quality_out, int max_star);
+                     int* iters_out, double* min_quality_out, int max_star,
+                     bool node_order = false);
 
 enum { TM_DELTAT, TM_ESTAB, TM_CALCRHS, TM_FUENTE, TM_UPDATE, TM_FORCES, TM_TRANSF, TM_GRAD,
        TM_NORMALES, TM_DERIV, TM_MASAS, TM_LAPLACE, TM_N };
@@ -214,7 +215,7 @@ struct Ctx {
     int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);
     int force_visc_now();
-    int smooth(int* iters, double* min_quality);
+    int smooth(int* iters, double* min_quality, bool node_order = false);
     int smooth_setup();
     int set_smoothing(int every);
     int smooth_in_step(cudaStream_t s, double* WX, double* WY, float2* Wf);

@@ -345,7 +345,7 @@ int Ctx::smooth_setup() {
 
 // The setup smoothing of the resident mesh (ns2DComp.ALE.f90:62-72), then the mesh's
 // geometry again (normales, deriv, masses, Laplacian) as at setup
-int Ctx::smooth(int* iters, double* min_quality) {
+int Ctx::smooth(int* iters, double* min_quality, bool node_order) {
     const int N = npoin;
     int st = smooth_setup();
     if (st) return st;
@@ -353,7 +353,7 @@ int Ctx::smooth(int* iters, double* min_quality) {
     for (int p = 0; p < N; ++p) max_star = std::max(max_star, adj.esup_ptr[p + 1] - adj.esup_ptr[p]);
     st = smooth_on_device(stream, N, nelem, d_elem, d_esup_ptr, d_esup_slot, d_psup_ptr, d_psup,
                           d_sm_fixed, d_X, d_Y, nullptr, sm_offs, d_sm_order, d_sm_flag, d_sm_scal,
-                          d_sm_flags, iters, min_quality, max_star);
+                          d_sm_flags, iters, min_quality, max_star, node_order);
     if (st) return st;
     if (prec == CFD_PREC_MIXED) {
         if ((st = narrow_mixed(false, false, false, false, true, false))) return st;

@@ -138,11 +138,8 @@ __global__ void k_sm_check(SmArgs a, unsigned long long* hmin_bits, int* any) {
     if (h1 >= 0.0) atomicMin(hmin_bits, (unsigned long long)__double_as_longlong(h1));
 }
 
-// laplacianSmoothing (:74-114) over one colour
-__global__ void k_sm_laplace(SmArgs a) {
-    const int k = a.begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.end) return;
-    const int p = a.order[k];
+// laplacianSmoothing (:74-114) of node p
+__device__ void sm_laplace_node(const SmArgs& a, int p) {
     if (!a.smoothable[p] || a.fixed[p]) return;
     const double xo = a.X[p], yo = a.Y[p];
     const double mu_old = sm_mu_min(a, p, xo, yo);
@@ -166,12 +163,16 @@ __global__ void k_sm_laplace(SmArgs a) {
     a.Y[p] = yn;
 }
 
-// one worklist sweep (:58-66) over one colour: moveIpoin (:116-188) with getG (:232-255)
-// and getStep (:257-278)
-__global__ void __launch_bounds__(128) k_sm_sweep(SmArgs a) {
+// laplacianSmoothing over one colour
+__global__ void k_sm_laplace(SmArgs a) {
     const int k = a.begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.end) return;
-    const int p = a.order[k];
+    sm_laplace_node(a, a.order[k]);
+}
+
+// one visit of the worklist sweep (:58-66) to node p: moveIpoin (:116-188) with getG
+// (:232-255) and getStep (:257-278)
+__device__ void sm_sweep_node(const SmArgs& a, int p) {
     if (!a.smoothable[p] || a.fixed[p]) return;
     a.smoothable[p] = 0;
     double mu[kMaxStar], gx[kMaxStar], gy[kMaxStar];
@@ -227,6 +228,28 @@ __global__ void __launch_bounds__(128) k_sm_sweep(SmArgs a) {
     atomicMax(a.dmax_bits, (unsigned long long)__double_as_longlong(d_move));
     if (d_move > TINY)
         for (int q = a.psup_ptr[p]; q < a.psup_ptr[p + 1]; ++q) a.smoothable[a.psup[q]] = 1;
+}
+
+// one worklist sweep over one colour
+__global__ void __launch_bounds__(128) k_sm_sweep(SmArgs a) {
+    const int k = a.begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.end) return;
+    sm_sweep_node(a, a.order[k]);
+}
+
+// The reference's own order: one thread visits every node in node order, each visit seeing
+// every move before it (smoothing.f90:55-67 and :80-114 as written).  The chain of
+// dependences runs through the whole mesh (on the O-grids every ring's first node follows
+// the previous ring's last), so this order has no parallel form; it is the setup-time
+// parity variant, the colour kernels above the parallel one.
+__global__ void k_sm_laplace_seq(SmArgs a) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int p = 0; p < a.npoin; ++p) sm_laplace_node(a, p);
+}
+
+__global__ void k_sm_sweep_seq(SmArgs a) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int p = 0; p < a.npoin; ++p) sm_sweep_node(a, p);
 }
 
 // doubles as unsigned integers in the same order (for atomicMin of any sign)
@@ -324,7 +347,7 @@ int smooth_on_device(cudaStream_t st, int npoin, int nelem, const int4* elem,
                      const int* psup, const unsigned char* fixed, double* X, double* Y,
                      const double* tol_move, const std::vector<int>& offs, const int* order,
                      unsigned char* smoothable, unsigned long long* scal, int* flags,
-                     int* iters_out, double* min_quality_out, int max_star) {
+                     int* iters_out, double* min_quality_out, int max_star, bool node_order) {
     if (max_star > kMaxStar) {
         set_last_message("a node has more elements around it than the smoothing handles (32)");
         return CFD_ERR_LIMIT;
@@ -362,12 +385,17 @@ int smooth_on_device(cudaStream_t st, int npoin, int nelem, const int4* elem,
     int iter = 0;
     if (any) {
         const int ncol = (int)offs.size() - 1;
-        for (int it = 0; it < 2; ++it)
+        for (int it = 0; it < 2; ++it) {
+            if (node_order) {
+                CFD_LAUNCH(k_sm_laplace_seq, 1, 1, 0, st, a);
+                continue;
+            }
             for (int c = 0; c < ncol; ++c) {
                 a.begin = offs[c];
                 a.end = offs[c + 1];
                 CFD_LAUNCH(k_sm_laplace, blocks_for(a.end - a.begin, 128), 128, 0, st, a);
             }
+        }
         unsigned long long hb = 0;
         CFD_CUDA(cudaMemcpyAsync(&hb, scal, 8, cudaMemcpyDeviceToHost, st));
         CFD_CUDA(cudaStreamSynchronize(st));
@@ -376,10 +404,14 @@ int smooth_on_device(cudaStream_t st, int npoin, int nelem, const int4* elem,
         const double TOL_DIST = FACTOR_TOL_DIST * hmin;
         for (iter = 1; iter <= NITER; ++iter) {
             CFD_CUDA(cudaMemsetAsync(scal + 1, 0, 8, st));  // d_max = 0
-            for (int c = 0; c < ncol; ++c) {
-                a.begin = offs[c];
-                a.end = offs[c + 1];
-                CFD_LAUNCH(k_sm_sweep, blocks_for(a.end - a.begin, 128), 128, 0, st, a);
+            if (node_order) {
+                CFD_LAUNCH(k_sm_sweep_seq, 1, 1, 0, st, a);
+            } else {
+                for (int c = 0; c < ncol; ++c) {
+                    a.begin = offs[c];
+                    a.end = offs[c + 1];
+                    CFD_LAUNCH(k_sm_sweep, blocks_for(a.end - a.begin, 128), 128, 0, st, a);
+                }
             }
             unsigned long long db = 0;
             CFD_CUDA(cudaMemcpyAsync(&db, scal + 1, 8, cudaMemcpyDeviceToHost, st));

@@ -119,17 +119,18 @@ def FORCE_VISC(NELEM, npoin, nsets, IELEM_SETS, ISET, inpoel, NSET_NUMB, U_inf, 
     return (fvx, fvy, sk[:ne]) if skin else (fvx, fvy)
 
 
-def smoothing(X, Y, inpoel, fixed, dX=None, dY=None):
-    """smoothing.f90:21-72 (GPU colour-by-colour variant) -> (X, Y, iterations, min quality).
-    fixed: per node, True = does not move; dX, dY: the setTol_move path's displacements."""
+def smoothing(X, Y, inpoel, fixed, dX=None, dY=None, order=abi.CFD_SMOOTH_COLOUR):
+    """smoothing.f90:21-72 -> (X, Y, iterations, min quality).  fixed: per node, True = does
+    not move; dX, dY: the setTol_move path's displacements; order: CFD_SMOOTH_COLOUR (the
+    GPU's colour-by-colour variant) or CFD_SMOOTH_NODE_ORDER (the reference's order)."""
     L = abi.lib()
     X, Y = _f64(X).copy(), _f64(Y).copy()
     inp = _i32(inpoel)
     it, q = C.c_int(0), C.c_double(0.0)
-    check(L.cfd_smoothing(dptr(X), dptr(Y), iptr(inp), iptr(_i32(fixed)), _ci(len(X)),
-                          _ci(inp.shape[0]), dptr(None if dX is None else _f64(dX)),
-                          dptr(None if dY is None else _f64(dY)), C.byref(it), C.byref(q)),
-          "cfd_smoothing")
+    check(L.cfd_smoothing_ex(dptr(X), dptr(Y), iptr(inp), iptr(_i32(fixed)), _ci(len(X)),
+                             _ci(inp.shape[0]), dptr(None if dX is None else _f64(dX)),
+                             dptr(None if dY is None else _f64(dY)), C.byref(it), C.byref(q),
+                             int(order)), "cfd_smoothing")
     return X, Y, it.value, q.value
 
 
@@ -276,11 +277,12 @@ class Solver:
         check(abi.lib().cfd_ctx_guess_stats_ex(self.h, out), "cfd_ctx_guess_stats_ex")
         return tuple(int(v) for v in out)
 
-    def smooth(self):
+    def smooth(self, order=abi.CFD_SMOOTH_COLOUR):
         """The reference's setup smoothing of the resident mesh, then its geometry again.
-        -> (iterations, min quality)."""
+        order: CFD_SMOOTH_COLOUR or CFD_SMOOTH_NODE_ORDER.  -> (iterations, min quality)."""
         it, q = C.c_int(0), C.c_double(0.0)
-        check(abi.lib().cfd_ctx_smooth(self.h, C.byref(it), C.byref(q)), "cfd_ctx_smooth")
+        check(abi.lib().cfd_ctx_smooth_ex(self.h, int(order), C.byref(it), C.byref(q)),
+              "cfd_ctx_smooth")
         return it.value, q.value
 
     def set_force_visc(self, each_step):

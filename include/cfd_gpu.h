@@ -191,6 +191,19 @@ int cfd_deltat(const double* T, const double* VEL_X, const double* VEL_Y,
 int cfd_smoothing(double* X, double* Y, const int* inpoel, const int* fixed, const int* npoin,
                   const int* nelem, const double* dX, const double* dY, int* iters,
                   double* min_quality);
+/* The node visiting order of the smoothing: */
+enum {
+    CFD_SMOOTH_COLOUR = 0,    /* nodes coloured so that no two of a colour share an element,
+                                 one colour at a time (parallel; a nearby smoothed mesh)    */
+    CFD_SMOOTH_NODE_ORDER = 1 /* one node at a time in node order, as smoothing.f90:55-67
+                                 and :80-114 visit them (the reference's mesh, bit for bit
+                                 with its FP64 arithmetic; sequential by construction: one
+                                 GPU thread, a setup-time step)                            */
+};
+/* smoothing (smoothing.f90:21-72) with the visiting order chosen (cfd_smoothing: colour). */
+int cfd_smoothing_ex(double* X, double* Y, const int* inpoel, const int* fixed, const int* npoin,
+                     const int* nelem, const double* dX, const double* dY, int* iters,
+                     double* min_quality, int order);
 
 /* FORCE_VISC (ns2DComp.ALE.f90:819-893), drop-in: the reference's argument list (RMU and
  * RHO are unused by its body), F_VX/F_VY 10 each; skin: NULL, or 3 doubles per set edge
@@ -431,6 +444,9 @@ int cfd_ctx_graph_state(cfd_ctx* ctx, long long* out3);
  * element is below the quality threshold 0.85); min_quality: the worst element's mu
  * afterwards.  Either may be NULL. */
 int cfd_ctx_smooth(cfd_ctx* ctx, int* iters, double* min_quality);
+/* cfd_ctx_smooth with the visiting order chosen: CFD_SMOOTH_NODE_ORDER gives the mesh the
+ * reference's setup call (ns2DComp.ALE.f90:76) gives. */
+int cfd_ctx_smooth_ex(cfd_ctx* ctx, int order, int* iters, double* min_quality);
 
 /* Smooth the moved mesh inside the time loop every `every` steps (0: never, the default):
  * after the step's mesh update, the smoothing moves each node at most |XPOS| + |YPOS| (the

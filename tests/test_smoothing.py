@@ -1,10 +1,10 @@
-"""The mesh smoothing (smoothing.f90), GPU colour-by-colour variant: the oracle restates the
-reference's node-by-node order; the GPU moves one colour of mutually non-adjacent nodes at
-a time.  A colour-by-colour pass is the sequential pass visiting the nodes colour by
-colour, so the oracle run in the GPU's colour order must give the GPU's mesh bit for bit;
-against the node-order oracle the checks are the properties the algorithm guarantees —
-fixed nodes stay, no node makes its worst element worse, the worst element of the mesh
-improves about as far as the oracle's."""
+"""The mesh smoothing (smoothing.f90) on the GPU in its two visiting orders.  The colour-by-
+colour variant moves one colour of mutually non-adjacent nodes at a time: it is the
+sequential pass visiting the nodes colour by colour, so the oracle run in the GPU's colour
+order must give the GPU's mesh bit for bit, and against the node-order oracle the checks are
+the properties the algorithm guarantees (fixed nodes stay, no node makes its worst element
+worse, the worst element improves about as far as the oracle's).  The node-order variant
+visits the nodes as the reference does and must give the node-order oracle's mesh."""
 import numpy as np
 import pytest
 
@@ -260,5 +260,51 @@ def test_gpu_fp64_smoothing_in_the_loop_bit_exact(gpu_lib, oracle):
         for key in ("U", "T", "X", "Y"):
             assert np.array_equal(sg[key], so[key]), (s, key, np.abs(sg[key] - so[key]).max())
     assert g.smoothing_stats()[0] == 3
+    g.close()
+    o.close()
+
+
+@pytest.mark.gpu
+def test_gpu_node_order_smoothing_is_the_reference(gpu_lib, oracle):
+    """CFD_SMOOTH_NODE_ORDER visits the nodes one at a time in node order, as the reference
+    does (smoothing.f90:55-67, :80-114): the mesh, the sweep count and the quality are the
+    node-order oracle's, bit for bit, on the setup path and on the setTol_move path."""
+    from cfd_gb300 import abi, solver
+    k, x, y, fixed = jittered()
+    xs, ys, it, q = solver.smoothing(x, y, k.inpoel, fixed, order=abi.CFD_SMOOTH_NODE_ORDER)
+    xo, yo, ito, qo = oracle.smoothing(x, y, k.inpoel, fixed)
+    assert (it, q) == (ito, qo) and it >= 1
+    assert np.array_equal(xs, xo) and np.array_equal(ys, yo)
+    rng = np.random.default_rng(4)
+    h = 1e-3
+    dX, dY = h * rng.uniform(-1, 1, k.npoin), h * rng.uniform(-1, 1, k.npoin)
+    xs, ys, it, q = solver.smoothing(x, y, k.inpoel, fixed, dX=dX, dY=dY,
+                                     order=abi.CFD_SMOOTH_NODE_ORDER)
+    xo, yo, ito, qo = oracle.smoothing(x, y, k.inpoel, fixed, dX=dX, dY=dY)
+    assert (it, q) == (ito, qo)
+    assert np.array_equal(xs, xo) and np.array_equal(ys, yo)
+
+
+@pytest.mark.gpu
+def test_gpu_setup_smoothing_in_node_order_then_steps_are_the_references(gpu_lib):
+    """A host that smooths at setup (ns2DComp.ALE.f90:76) through cfd_ctx_smooth_ex with the
+    node order gets the reference's mesh, and the steps after it match the oracle's run of
+    the same setup bit for bit."""
+    from cfd_gb300 import abi, solver
+    from oracle import oracle as O
+    from test_gpu_parity import eq
+    k = small_case(2, scale=16, seed=3)
+    g = solver.Solver(k)
+    g.smooth(order=abi.CFD_SMOOTH_NODE_ORDER)
+    o = O.OracleCase(k, smoothing=True)
+    sg, so = g.state(), o.state()
+    eq(sg["X"], so["X"], "X after setup smoothing")
+    eq(sg["Y"], so["Y"], "Y after setup smoothing")
+    for s in range(2):
+        rg, ro = g.step(1), o.step(1)
+        assert rg.dtmin == ro.dtmin and tuple(rg.bicg_iters) == tuple(ro.bicg_iters)
+        sg, so = g.state(), o.state()
+        for key in ("U", "T", "X", "Y"):
+            eq(sg[key], so[key], f"step {s + 1}: {key}")
     g.close()
     o.close()
