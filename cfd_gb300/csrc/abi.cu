@@ -247,22 +247,11 @@ int cfd_ctx_upload_state(cfd_ctx* ctx, const double* U, const double* T, const d
     const size_t N = c.npoin;
     if (U) CFD_CUDA(cudaMemcpyAsync(c.d_U, U, 32 * N, cudaMemcpyHostToDevice, c.stream));
     if (T) CFD_CUDA(cudaMemcpyAsync(c.d_T, T, 8 * N, cudaMemcpyHostToDevice, c.stream));
-    std::vector<double> v;
-    if (VEL_X) {
-        CFD_CUDA(cudaMemcpyAsync(c.d_VX, VEL_X, 8 * N, cudaMemcpyHostToDevice, c.stream));
-    } else if (U) {
-        v.resize(N);
-        for (size_t i = 0; i < N; ++i) v[i] = U[4 * i + 1] / U[4 * i];
-        CFD_CUDA(cudaMemcpyAsync(c.d_VX, v.data(), 8 * N, cudaMemcpyHostToDevice, c.stream));
-        CFD_CUDA(cudaStreamSynchronize(c.stream));
-    }
-    if (VEL_Y) {
-        CFD_CUDA(cudaMemcpyAsync(c.d_VY, VEL_Y, 8 * N, cudaMemcpyHostToDevice, c.stream));
-    } else if (U) {
-        v.resize(N);
-        for (size_t i = 0; i < N; ++i) v[i] = U[4 * i + 2] / U[4 * i];
-        CFD_CUDA(cudaMemcpyAsync(c.d_VY, v.data(), 8 * N, cudaMemcpyHostToDevice, c.stream));
-    }
+    if (VEL_X) CFD_CUDA(cudaMemcpyAsync(c.d_VX, VEL_X, 8 * N, cudaMemcpyHostToDevice, c.stream));
+    if (VEL_Y) CFD_CUDA(cudaMemcpyAsync(c.d_VY, VEL_Y, 8 * N, cudaMemcpyHostToDevice, c.stream));
+    if (U && (!VEL_X || !VEL_Y))  // the velocities the caller left out, from U on the device
+        CFD_LAUNCH(k_vel_from_U, blocks_for((long)N, 256), 256, 0, c.stream, (int)N, c.d_U,
+                   VEL_X ? nullptr : c.d_VX, VEL_Y ? nullptr : c.d_VY);
     if (c.prec == CFD_PREC_MIXED)
         TRY(c.narrow_mixed(U != nullptr, T != nullptr, VEL_X || U, VEL_Y || U, false, false));
     CFD_CUDA(cudaStreamSynchronize(c.stream));

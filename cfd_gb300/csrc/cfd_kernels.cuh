@@ -245,6 +245,7 @@ __global__ void k_estab(int nelem, const int4* elem, const double* U, const doub
                         double RHOINF, double TINF, int estab_mode, double eps_dir,
                         double dirx, double diry, double* SHOC, double* TS1, double* TS2,
                         double* TS3);
+__global__ void k_vel_from_U(int npoin, const double* U, double* VX, double* VY);
 // calcRHS split into its stage-invariant part (once per step: the cached addends and
 // factors, FUENTE into contribF; with !viscous the final contributions into contrib) and
 // the per-stage viscous replay from the cache (kernels_fp64.cu); cache: kInvPlanes x nelem

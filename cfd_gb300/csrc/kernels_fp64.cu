@@ -448,6 +448,17 @@ cudaError_t launch_elem_rhs(bool viscous, bool with_theta, cudaStream_t stream, 
     return cudaGetLastError();
 }
 
+// VEL_X = rho u / rho, VEL_Y = rho v / rho from U(4,npoin) (either output may be null)
+__global__ void k_vel_from_U(int npoin, const double* __restrict__ U, double* __restrict__ VX,
+                             double* __restrict__ VY) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npoin) return;
+    const double2 a = reinterpret_cast<const double2*>(U + 4 * (size_t)i)[0];
+    const double b = U[4 * (size_t)i + 2];
+    if (VX) VX[i] = a.y / a.x;
+    if (VY) VY[i] = b / a.x;
+}
+
 // ------------------------------------------------------------------ calcRHS, stage-invariant split
 // All four RK stages evaluate calcRHS at the step-start U (subrutinas.f90:685); between the
 // stages only T changes, and T enters only mu and lambda (calcRHS.f90:49-51), i.e. only

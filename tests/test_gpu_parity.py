@@ -203,6 +203,19 @@ def test_step_from_shared_perturbed_state(gpu_lib):
     run_pair(k, 2, setup=setup)
 
 
+def test_step_after_upload_of_U_only(gpu_lib):
+    """cfd_ctx_upload_state with U and T only: the velocities come from U (rho u / rho,
+    rho v / rho) as the oracle forms them; the steps after it are bit-exact."""
+    k = small_case(3, scale=16, seed=5)
+    U, T, _, _ = perturbed_state(k, seed=4, amp=0.05)
+
+    def setup(g, o):
+        for side in (g, o):
+            side.set_state(U, T)
+
+    run_pair(k, 2, setup=setup)
+
+
 def test_bad_inputs_return_status(gpu_lib):
     from cfd_gb300 import abi, solver
     k = small_case(1, scale=8)
