@@ -67,6 +67,9 @@ def parse():
                          "configuration describes it (histories into --record-out)")
     ap.add_argument("--record-steps", type=int, default=None)
     ap.add_argument("--record-out", default=None, help="JSON file of the record's histories")
+    ap.add_argument("--bicg-tol-mode", type=int, default=0,
+                    help="BiCG stopping test of the headline run and of --profile-steps "
+                         "(0: the reference's absolute test; 1: relative 1e-10, cap 20000)")
     ap.add_argument("--guess-tol-mode", type=int, default=1,
                     help="BiCG stopping test of the guess report (0: the reference's "
                          "absolute r.z < 1e-10; 1: ||r|| <= 1e-10 ||b - A x_D||)")
@@ -700,6 +703,9 @@ def main_ours(args):
         net, gate = learned.Net.load(), args.guess_gate
     elif args.guess == "zero":
         k.params.guess_mode = abi.CFD_GUESS_ZERO
+    if args.bicg_tol_mode:
+        k.params.bicg_tol_mode = args.bicg_tol_mode
+        k.params.bicg_maxit = 20000
     if args.profile_steps:
         S = solver.Solver(k, precision=prec)
         if net is not None:
