@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
             }
 }
 
-__global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
+__global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
     __shared__ double red[9];
     __shared__ double s_thr[2], s_ref2[2];  // relative modes: threshold on r.r, ref.ref
     const int t = threadIdx.x;
@@ -508,22 +508,45 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
                      k < a.maxit;
         if (!act[0] && !act[1]) break;
         k = k + 1;
-        // phase 1: x += alfa p; r -= alfa y; z = r/diag; r.z (and r.r, relative modes)
+        // phase 1: x += alfa p; r -= alfa y; z = r/diag; r.z (and r.r, relative modes).
+        // A thread's four rows of a chunk are loaded together, then updated, so that their
+        // loads are in flight at once.
         for (long c = blockIdx.x; c < nc; c += gridDim.x) {
             double acc[2] = {0.0, 0.0}, accr[2] = {0.0, 0.0};
-            for (int kk = 0; kk < 4; ++kk) {
-                const long i = c * kChunk + t + 256L * kk;
-                if (i >= n) break;
-                const double id = a.invdiag[i];
+            const long i0 = c * kChunk + t;
+            double id[4];
 #pragma unroll
-                for (int s = 0; s < 2; ++s) {
-                    if (pend[s]) a.x[s][i] += alfa[s] * a.p[s][cur[s]][i];
+            for (int kk = 0; kk < 4; ++kk) id[kk] = (i0 + 256L * kk < n) ? a.invdiag[i0 + 256L * kk] : 0.0;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                if (!pend[s] && !act[s]) continue;
+                double* __restrict__ xs = a.x[s];
+                const double* __restrict__ ps = a.p[s][cur[s]];
+                double* __restrict__ rs = a.r[s];
+                const double* __restrict__ ys = a.y[s];
+                double* __restrict__ zs = a.z[s];
+                float* __restrict__ zfs = a.zf[s];
+                double xv[4], pv[4], rv[4], yv[4];
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const long i = i0 + 256L * kk;
+                    const bool in = i < n;
+                    xv[kk] = (in && pend[s]) ? xs[i] : 0.0;
+                    pv[kk] = (in && pend[s]) ? ps[i] : 0.0;
+                    rv[kk] = (in && act[s]) ? rs[i] : 0.0;
+                    yv[kk] = (in && act[s]) ? ys[i] : 0.0;
+                }
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const long i = i0 + 256L * kk;
+                    if (i >= n) break;
+                    if (pend[s]) xs[i] = xv[kk] + alfa[s] * pv[kk];
                     if (!act[s]) continue;
-                    const double ri = a.r[s][i] - alfa[s] * a.y[s][i];
-                    const double zi = ri * id;
-                    a.r[s][i] = ri;
-                    a.z[s][i] = zi;
-                    a.zf[s][i] = d2f_trunc(zi);
+                    const double ri = rv[kk] - alfa[s] * yv[kk];
+                    const double zi = ri * id[kk];
+                    rs[i] = ri;
+                    zs[i] = zi;
+                    zfs[i] = d2f_trunc(zi);
                     acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
                     if (rel) accr[s] = (kk == 0) ? ri * ri : accr[s] + ri * ri;
                 }
@@ -553,24 +576,77 @@ __global__ void __launch_bounds__(256, 3) k_pcg_mixed(PcgArgs a) {
             beta[s] = err_new[s] / err_old[s];
             betaf[s] = d2f_trunc(beta[s]);
         }
-        // phase 2: p_new = beta p + z (FP64 for the row, FP32 shadow for the SpMV); y = A p_new
+        // phase 2: p_new = beta p + z (FP64 for the row, FP32 shadow for the SpMV); y = A p_new.
+        // Per solve, a thread's rows go in pairs: the two rows' pointers, p and z, then their
+        // column batches and gathers are issued together.
         for (long c = blockIdx.x; c < nc; c += gridDim.x) {
             double acc[2] = {0.0, 0.0};
-            for (int kk = 0; kk < 4; ++kk) {
-                const long i = c * kChunk + t + 256L * kk;
-                if (i >= n) break;
-                const bool fx = a.isfix[i];
+            const long i0 = c * kChunk + t;
 #pragma unroll
-                for (int s = 0; s < 2; ++s) {
-                    if (!act[s]) continue;
-                    const double pn = beta[s] * a.p[s][cur[s]][i] + a.z[s][i];
-                    const double yi =
-                        fx ? 1.0e30 * pn
-                           : f2d_bits(spmv_row_dir_f(a, (int)i, a.pf[s][cur[s]], a.zf[s], betaf[s]));
-                    a.p[s][cur[s] ^ 1][i] = pn;
-                    a.pf[s][cur[s] ^ 1][i] = d2f_trunc(pn);
-                    a.y[s][i] = yi;
-                    acc[s] = (kk == 0) ? pn * yi : acc[s] + pn * yi;
+            for (int s = 0; s < 2; ++s) {
+                if (!act[s]) continue;
+                const double* __restrict__ ps = a.p[s][cur[s]];
+                const double* __restrict__ zs = a.z[s];
+                const float* __restrict__ pfs = a.pf[s][cur[s]];
+                const float* __restrict__ zfs = a.zf[s];
+                double* __restrict__ pn_out = a.p[s][cur[s] ^ 1];
+                float* __restrict__ pfn_out = a.pf[s][cur[s] ^ 1];
+                double* __restrict__ ys = a.y[s];
+#pragma unroll
+                for (int kp = 0; kp < 4; kp += 2) {
+                    long ii[2];
+                    bool in[2], fx[2];
+                    int j0[2], j1[2];
+                    double pv[2], zv[2];
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        ii[q] = i0 + 256L * (kp + q);
+                        in[q] = ii[q] < n;
+                        fx[q] = in[q] ? a.isfix[ii[q]] != 0 : true;
+                        j0[q] = (in[q] && !fx[q]) ? a.rowptr[ii[q]] : 0;
+                        j1[q] = (in[q] && !fx[q]) ? a.rowptr[ii[q] + 1] : 0;
+                        pv[q] = in[q] ? ps[ii[q]] : 0.0;
+                        zv[q] = in[q] ? zs[ii[q]] : 0.0;
+                    }
+                    float dot[2] = {0.f, 0.f};
+                    const int len = max(j1[0] - j0[0], j1[1] - j0[1]);
+                    constexpr int B = 3;
+                    for (int u0 = 0; u0 < len; u0 += B) {
+                        int cc[2][B];
+                        float mm[2][B], pp[2][B], zz[2][B];
+#pragma unroll
+                        for (int q = 0; q < 2; ++q)
+#pragma unroll
+                            for (int u = 0; u < B; ++u)
+                                if (j0[q] + u0 + u < j1[q]) {
+                                    cc[q][u] = a.col[j0[q] + u0 + u];
+                                    mm[q][u] = a.valf[j0[q] + u0 + u];
+                                }
+#pragma unroll
+                        for (int q = 0; q < 2; ++q)
+#pragma unroll
+                            for (int u = 0; u < B; ++u)
+                                if (j0[q] + u0 + u < j1[q]) {
+                                    pp[q][u] = pfs[cc[q][u]];
+                                    zz[q][u] = zfs[cc[q][u]];
+                                }
+#pragma unroll
+                        for (int q = 0; q < 2; ++q)
+#pragma unroll
+                            for (int u = 0; u < B; ++u)
+                                if (j0[q] + u0 + u < j1[q])
+                                    dot[q] += mm[q][u] * (betaf[s] * pp[q][u] + zz[q][u]);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        if (!in[q]) continue;
+                        const double pn = beta[s] * pv[q] + zv[q];
+                        const double yi = fx[q] ? 1.0e30 * pn : f2d_bits(dot[q]);
+                        pn_out[ii[q]] = pn;
+                        pfn_out[ii[q]] = d2f_trunc(pn);
+                        ys[ii[q]] = yi;
+                        acc[s] = (kp + q == 0) ? pn * yi : acc[s] + pn * yi;
+                    }
                 }
             }
 #pragma unroll
