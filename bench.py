@@ -62,7 +62,7 @@ def parse():
                     help="steps of the default run's mixed-vs-FP64 and reference-vs-"
                          "regularized-ESTAB comparisons (the metric's condition is stated "
                          "after 2000 steps)")
-    ap.add_argument("--record", choices=["config1", "config2", "config5"], default=None,
+    ap.add_argument("--record", choices=["config2", "config5"], default=None,
                     help="instead of the benchmark: the long run of a workload as its "
                          "configuration describes it (histories into --record-out)")
     ap.add_argument("--record-steps", type=int, default=None)
@@ -549,11 +549,10 @@ def lift_drag(rep, S):
 
 def main_record(args):
     """Long runs of the workloads as their configurations describe them; the histories go
-    to --record-out (JSON), one summary line to stdout.
+    to --record-out (JSON), one summary line to stdout.  (The runs that compare against the
+    oracle step by step, the 8,192-node cylinder over 2000 steps among them, are
+    tests/test_records.py.)
 
-    config1: the 8,192-node cylinder (64 x 128, fixed mesh, Mach 0.3, Re 100), FP64 form
-      against the oracle (one thread) for 2000 steps: DTMIN and drag/lift compared every
-      step, the state (U, T, X, Y) every 100th step, bit for bit.
     config2: the 262,144-node cylinder (512 x 512, heave 0.2 sin(2 pi 0.2 t), Re 200), FP64
       form, the mesh-motion solve to ||r|| <= 1e-10 ||b - A x_D||, 5000 steps: BiCG
       iterations and relative residual per step and solve, drag and lift per step.
@@ -566,38 +565,7 @@ def main_record(args):
     abi.lib()
     out = {"record": args.record}
     hist = []
-    if args.record == "config1":
-        from oracle import oracle as O
-        O.set_threads(1)
-        n = args.record_steps or 2000
-        k = C.config_case(1)
-        S, Oc = solver.Solver(k), O.OracleCase(k)
-        S.set_force_visc(True)
-        Oc.set_force_visc(True)
-        mism, checks = [], 0
-        t0 = time.perf_counter()
-        for s in range(1, n + 1):
-            rg, ro = S.step(1), Oc.step(1)
-            fg, fo = lift_drag(rg, S), lift_drag(ro, Oc)
-            same = rg.dtmin == ro.dtmin and fg == fo
-            if s % 100 == 0 or s == n:
-                sg, so = S.state(), Oc.state()
-                checks += 1
-                same = same and all(np.array_equal(sg[q], so[q]) for q in ("U", "T", "X", "Y"))
-                hist.append({"step": s, "time": rg.time, "dtmin": rg.dtmin, "drag": fg[0],
-                             "lift": fg[1], "bit_exact": bool(same),
-                             "rho_mean": float(sg["U"][:, 0].mean())})
-            if not same:
-                mism.append(s)
-        out.update({"workload": f"cylinder O-grid 64x128 ({k.npoin} nodes, {k.nelem} "
-                                f"triangles), Mach 0.3, Re 100, fixed mesh, FP64",
-                    "steps": n, "state_checks": checks, "mismatched_steps": mism[:20],
-                    "bit_exact_every_step_and_checkpoint": not mism,
-                    "wall_s": time.perf_counter() - t0,
-                    "final_state_finite": bool(np.isfinite(S.state()["U"]).all())})
-        S.close()
-        Oc.close()
-    elif args.record == "config2":
+    if args.record == "config2":
         n = args.record_steps or 5000
         k = C.config_case(2)
         k.params.bicg_tol_mode = abi.CFD_BICG_TOL_REL
@@ -668,11 +636,18 @@ def main_record(args):
             fd = [forces(Sd.step(1)) for _ in range(nf)]
             Sd.close()
             Fm, Fd = np.array(fm), np.array(fd)
-            fmax = float(np.abs(Fd).max())
+            # the reference's ESTAB breaks down on this case (its state stops being finite,
+            # bit for bit with the oracle): compare over the steps before that
+            bad = np.flatnonzero(~np.isfinite(Fd).all(axis=1))
+            m = int(bad[0]) if bad.size else nf
+            fmax = float(np.abs(Fd[:m]).max())
             out[f"forces_vs_{name}"] = {
-                "steps": nf, "rel_err_max": [float(np.abs(Fm[:, c] - Fd[:, c]).max() / fmax)
-                                             for c in range(2)],
-                "rel_err_final": [float(abs(Fm[-1, c] - Fd[-1, c]) / fmax) for c in range(2)]}
+                "steps": nf, "steps_compared": m,
+                "first_nonfinite_step": int(bad[0]) + 1 if bad.size else None,
+                "rel_err_max": [float(np.abs(Fm[:m, c] - Fd[:m, c]).max() / fmax)
+                                for c in range(2)],
+                "rel_err_final": [float(abs(Fm[m - 1, c] - Fd[m - 1, c]) / fmax)
+                                  for c in range(2)]}
             hist.append({name: Fd.tolist()})
         hist.append({"mixed": fm})
     if args.record_out:

@@ -27,6 +27,12 @@ inline double pow15(double x) { return g_pow_mode ? std::pow(x, 1.5) : x * std::
 inline double powm05(double x) { return g_pow_mode ? std::pow(x, -0.5) : 1.0 / std::sqrt(x); }
 inline double pow05(double x) { return g_pow_mode ? std::pow(x, 0.5) : std::sqrt(x); }
 
+// calcRHS and FUENTE scatter their element contributions with OpenMP atomics, as the
+// reference does: with more than one thread the adds into a node arrive in thread order.
+// With or_set_ordered_scatter(1) the elements are still formed in parallel but the adds
+// run in element order afterwards, so any thread count gives the one-thread result.
+int g_ordered_scatter = 0;
+
 // ESTAB's DUX/DUY evaluation (CFD_ESTAB_*), set by or_set_estab_mode / the case params
 int g_estab_mode = CFD_ESTAB_REFERENCE;
 double g_estab_eps = 1.0e-3;  // CFD_ESTAB_REGULARIZED: relative gradient scale
@@ -51,6 +57,7 @@ void or_set_threads(int n) {
 #endif
 }
 
+void or_set_ordered_scatter(int on) { g_ordered_scatter = on; }
 void or_set_estab_mode(int mode) { g_estab_mode = mode; }
 void or_set_pow_mode(int mode) { g_pow_mode = mode; }
 int or_get_pow_mode(void) { return g_pow_mode; }
@@ -263,6 +270,17 @@ void or_estab(int npoin, int nelem, const double* U, const double* T, const doub
     }
 }
 
+// The adds of the held element rows r[e][i][q] into rhs, element by element: the order in
+// which the one-thread loop makes them (the twelve adds of one element go to distinct
+// entries, so only the element order matters).
+static void scatter_in_order(double* rhs, const double* held, const int* inpoel, int nelem) {
+    for (int e = 0; e < nelem; ++e)
+        for (int i = 0; i < 3; ++i) {
+            const int p = inpoel[3 * e + i] - 1;
+            for (int q = 0; q < 4; ++q) rhs[4 * p + q] += held[12 * (size_t)e + 4 * i + q];
+        }
+}
+
 // calcRHS: calcRHS.f90:4-154.  OpenMP atomics like the reference; 1 thread = element order.
 void or_calcrhs(double* rhs, const double* U, const double* theta, const double* dNx,
                 const double* dNy, const double* area, const double* shoc,
@@ -275,6 +293,8 @@ void or_calcrhs(double* rhs, const double* U, const double* theta, const double*
     // N(3,3) of calcRHS.f90:18-23, N[i][k] = N(i+1,k+1)
     static const double N[3][3] = {{0.0, 0.5, 0.5}, {0.5, 0.0, 0.5}, {0.5, 0.5, 0.0}};
     const bool viscous = mu_ref > 2.2250738585072014e-308;  // tiny(0d0), :119
+    const bool ordered = g_ordered_scatter && or_get_threads() > 1;
+    std::vector<double> held(ordered ? 12 * (size_t)nelem : 0);
 #pragma omp parallel for schedule(static)
     for (int e = 0; e < nelem; ++e) {
         double r[3][4] = {{0}};
@@ -359,12 +379,17 @@ void or_calcrhs(double* rhs, const double* U, const double* theta, const double*
         }
         for (int i = 0; i < 3; ++i)  // :141
             for (int q = 0; q < 4; ++q) r[i][q] = r[i][q] * area[e] * dtl[e] / 3.0;
+        if (ordered) {
+            std::memcpy(&held[12 * (size_t)e], r, sizeof(r));
+            continue;
+        }
         for (int q = 0; q < 4; ++q)  // :143-150
             for (int i = 0; i < 3; ++i) {
 #pragma omp atomic
                 rhs[4 * p[i] + q] += r[i][q];
             }
     }
+    if (ordered) scatter_in_order(rhs, held.data(), inpoel, nelem);
 }
 
 // FUENTE: subrutinas.f90:1036-1094
@@ -374,6 +399,8 @@ void or_fuente(double* rhs, const double* U, const double* W_X, const double* W_
     (void)npoin;
     // sp(:,k) of :1052-1054, sp[i][k] = sp(i+1,k+1)
     static const double sp[3][3] = {{0.5, 0.0, 0.5}, {0.5, 0.5, 0.0}, {0.0, 0.5, 0.5}};
+    const bool ordered = g_ordered_scatter && or_get_threads() > 1;
+    std::vector<double> held(ordered ? 12 * (size_t)nelem : 0);
 #pragma omp parallel for schedule(static)
     for (int e = 0; e < nelem; ++e) {
         const int p[3] = {inpoel[3 * e] - 1, inpoel[3 * e + 1] - 1, inpoel[3 * e + 2] - 1};
@@ -394,12 +421,17 @@ void or_fuente(double* rhs, const double* U, const double* W_X, const double* W_
                 r[i][q] = -(AR * (sp[i][0] * (Ux[q] * wx[0] + Uy[q] * wy[0]) +
                                   sp[i][1] * (Ux[q] * wx[1] + Uy[q] * wy[1]) +
                                   sp[i][2] * (Ux[q] * wx[2] + Uy[q] * wy[2])));
+        if (ordered) {
+            std::memcpy(&held[12 * (size_t)e], r, sizeof(r));
+            continue;
+        }
         for (int i = 0; i < 3; ++i)
             for (int q = 0; q < 4; ++q) {
 #pragma omp atomic
                 rhs[4 * p[i] + q] += r[i][q];
             }
     }
+    if (ordered) scatter_in_order(rhs, held.data(), inpoel, nelem);
 }
 
 // gcl_mod::main: gcl.f90:8-46 (mode 1 literal divW, mode 2 dNy.W_y)

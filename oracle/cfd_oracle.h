@@ -30,6 +30,10 @@ extern "C" {
 #endif
 
 void or_set_threads(int n);
+/* 0 (default): calcRHS and FUENTE scatter with OpenMP atomics, as the reference does (with
+ * more than one thread the adds into a node come in thread order); 1: the element rows are
+ * formed in parallel and added in element order, the one-thread result at any thread count */
+void or_set_ordered_scatter(int on);
 void or_set_estab_mode(int mode);  /* CFD_ESTAB_* for the per-routine or_estab */
 /* 0 (default): the compositions above; 1: x**1.5d0, x**.5d0 and x**(-.5d0) through the C
  * library's pow, as a Fortran compiler without unsafe-math options evaluates them */

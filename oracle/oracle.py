@@ -23,6 +23,7 @@ _d, _i = C.c_double, C.c_int
 
 _SIG = {
     "or_set_threads": (None, [_i]),
+    "or_set_ordered_scatter": (None, [_i]),
     "or_set_estab_mode": (None, [_i]),
     "or_set_estab_eps": (None, [_d]),
     "or_get_threads": (_i, []),
@@ -102,6 +103,12 @@ def i32(a):
 
 def set_threads(n):
     lib().or_set_threads(int(n))
+
+
+def set_ordered_scatter(on):
+    """True: calcRHS/FUENTE add their element rows in element order at any thread count
+    (the one-thread result); False (default): OpenMP atomics, as the reference."""
+    lib().or_set_ordered_scatter(1 if on else 0)
 
 
 def set_pow_mode(mode):
