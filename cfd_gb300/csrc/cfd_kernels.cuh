@@ -256,6 +256,7 @@ cudaError_t launch_elem_inv(bool viscous, cudaStream_t stream, int nelem, const 
                             const double* ts1, const double* ts2, const double* ts3, GasConst gc,
                             double* cache, double* contrib, const double* WX, const double* WY,
                             double* contribF);
+cudaError_t launch_selftest_div3(long long n, unsigned long long seed, unsigned long long* bad);
 cudaError_t launch_elem_replay(cudaStream_t stream, int nelem, const int4* elem, const double* T,
                                const double* geo, const double* area, const double* dtl_arr,
                                const double* dtl_scalar, GasConst gc, const double* cache,

@@ -49,7 +49,7 @@ __global__ void k_mass(int npoin, const int* __restrict__ esup_ptr, const int* _
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npoin) return;
     double acc = 0.0;
-    for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) acc = acc + area[esup_slot[s] / 3] / 3.0;
+    for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) acc = acc + div3(area[esup_slot[s] / 3]);
     M[p] = acc;
 }
 
@@ -81,8 +81,8 @@ __global__ void k_gcl(int npoin, int nelem, const int4* __restrict__ elem,
         double f0 = geo[3 * E + e], f1 = geo[4 * E + e], f2 = geo[5 * E + e];
         double divW = d0 * wx[0] + d1 * wx[1] + d2 * wx[2] + f0 * wy[0] + f1 * wy[1] + f2 * wy[2];
         double divWo = d0 * wxo[0] + d1 * wxo[1] + d2 * wxo[2] + f0 * wyo[0] + f1 * wyo[1] + f2 * wyo[2];
-        t1 = t1 + divW * area[e] / 3.0;
-        t2 = t2 + divWo * area_old[e] / 3.0;
+        t1 = t1 + div3(divW * area[e]);
+        t2 = t2 + div3(divWo * area_old[e]);
     }
     M[p] = M[p] + (*dtp) * (t1 + t2) / 2.0;
 }
@@ -101,7 +101,7 @@ __global__ void k_deltat(int nelem, const int4* __restrict__ elem, const double*
         int4 n = elem[e];
         int nn[3] = {n.x, n.y, n.z};
         double vumax = 0.0, vvmax = 0.0;
-        double T_iel = (T[nn[0]] + T[nn[1]] + T[nn[2]]) / 3.0;
+        double T_iel = div3(T[nn[0]] + T[nn[1]] + T[nn[2]]);
         for (int i = 0; i < 3; ++i) {
             double vu = fabs(VX[nn[i]] - WX[nn[i]]);
             double vv = fabs(VY[nn[i]] - WY[nn[i]]);
@@ -114,7 +114,7 @@ __global__ void k_deltat(int nelem, const int4* __restrict__ elem, const double*
         double fmu = 0.017 * pow15(T_iel / t_inf) * (t_inf + smu) / (T_iel + smu);
         double et = fmu;
         double pe = (vel * hh) / (2.0 * et);
-        double alpha = fmin(pe / 3.0, 1.0);
+        double alpha = fmin(div3(pe), 1.0);
         double deltatu = 1.0 / (4.0 * et / (hh * hh) + alpha * vel / hh);
         double deltatc = 1.0 / (4.0 * et / (hh * hh));
         double dtelem = fsafe / (1.0 / deltatc + 1.0 / deltatu);
@@ -175,14 +175,14 @@ __global__ void k_estab(int nelem, const int4* __restrict__ elem, const double* 
     const int n1 = n.x, n2 = n.y, n3 = n.z;
     const double DX[3] = {geo[e], geo[E + e], geo[2 * E + e]};
     const double DY[3] = {geo[3 * E + e], geo[4 * E + e], geo[5 * E + e]};
-    double gm = GAMM ? (GAMM[n1] + GAMM[n2] + GAMM[n3]) / 3.0 : (gamm + gamm + gamm) / 3.0;
+    double gm = GAMM ? div3(GAMM[n1] + GAMM[n2] + GAMM[n3]) : div3(gamm + gamm + gamm);
     double tau = 0.0, h_rgne = 0.0, h_rgn = 0.0, h_jgn = 0.0;
     const double r1 = U[4 * (size_t)n1], r2 = U[4 * (size_t)n2], r3 = U[4 * (size_t)n3];
-    double rho_elem = (r1 + r2 + r3) / 3.0;
-    double vx = (VX[n1] + VX[n2] + VX[n3]) / 3.0;
-    double vy = (VY[n1] + VY[n2] + VY[n3]) / 3.0;
-    double wx = (WX[n1] + WX[n2] + WX[n3]) / 3.0;
-    double wy = (WY[n1] + WY[n2] + WY[n3]) / 3.0;
+    double rho_elem = div3(r1 + r2 + r3);
+    double vx = div3(VX[n1] + VX[n2] + VX[n3]);
+    double vy = div3(VY[n1] + VY[n2] + VY[n3]);
+    double wx = div3(WX[n1] + WX[n2] + WX[n3]);
+    double wy = div3(WY[n1] + WY[n2] + WY[n3]);
     vx = vx - wx;
     vy = vy - wy;
     double vel2 = sqrt(vx * vx + vy * vy);
@@ -209,7 +209,7 @@ __global__ void k_estab(int nelem, const int4* __restrict__ elem, const double* 
         double ge = 0.0;
         for (int i = 0; i < 3; ++i) ge += sqrt(DX[i] * DX[i] + DY[i] * DY[i]);
         const double sr = eps_dir * rho_elem * ge;
-        const double st = eps_dir * ((t1 + t2 + t3) / 3.0) * ge;
+        const double st = eps_dir * (div3(t1 + t2 + t3)) * ge;
         const double gx = drx + sr * dirx, gy = dry + sr * diry;
         const double hx = dtx + st * dirx, hy = dty + st * diry;
         const double gn = sqrt(gx * gx + gy * gy), hn = sqrt(hx * hx + hy * hy);
@@ -220,7 +220,7 @@ __global__ void k_estab(int nelem, const int4* __restrict__ elem, const double* 
         rux = dirx;
         ruy = diry;
     }
-    double temp = (t1 + t2 + t3) / 3.0;
+    double temp = div3(t1 + t2 + t3);
     double c = sqrt(gm * FR * temp);
     const double smu = 110.0;
     double fmu = 0.017 * pow15(temp / TINF) * (TINF + smu) / (temp + smu);
@@ -303,7 +303,7 @@ k_elem_rhs(int nelem, const int4* __restrict__ elem, const double* __restrict__ 
     const double nu = shoc[e] * cte;
     double mu = 0.0, lambda = 0.0;
     if (VISCOUS) {
-        const double T_avg = (T[p[0]] + T[p[1]] + T[p[2]]) / 3.0;
+        const double T_avg = div3(T[p[0]] + T[p[1]] + T[p[2]]);
         mu = mu_ref * pow15(T_avg / T_inf) * (T_inf + 110.0) / (T_avg + 110.0);
         lambda = lambda_ref * pow15(T_avg / T_inf) * (T_inf + 194.0) / (T_avg + 194.0);
     }
@@ -400,17 +400,17 @@ k_elem_rhs(int nelem, const int4* __restrict__ elem, const double* __restrict__ 
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         double2 a, b;
-        a.x = r[i][0] * ar * dtl / 3.0;
-        a.y = r[i][1] * ar * dtl / 3.0;
-        b.x = r[i][2] * ar * dtl / 3.0;
-        b.y = r[i][3] * ar * dtl / 3.0;
+        a.x = div3(r[i][0] * ar * dtl);
+        a.y = div3(r[i][1] * ar * dtl);
+        b.x = div3(r[i][2] * ar * dtl);
+        b.y = div3(r[i][3] * ar * dtl);
         reinterpret_cast<double2*>(out + 4 * i)[0] = a;
         reinterpret_cast<double2*>(out + 4 * i)[1] = b;
     }
     }  // contrib
     if (contribF) {
         // FUENTE (subrutinas.f90:1064-1078); its Ux/Uy expression equals calcRHS's.
-        const double AR = ar * dtl / 3.0;
+        const double AR = div3(ar * dtl);
         const double w0 = WX[p[0]], w1 = WX[p[1]], w2 = WX[p[2]];
         const double y0 = WY[p[0]], y1 = WY[p[1]], y2 = WY[p[2]];
         // sp(:,1)=(.5,.5,0), sp(:,2)=(0,.5,.5), sp(:,3)=(.5,0,.5); zero terms dropped
@@ -607,7 +607,7 @@ k_elem_inv(int nelem, const int4* __restrict__ elem, const double* __restrict__ 
     if (VISCOUS) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            C(kC0 + i) = r[i][0] * ar * dtl / 3.0;
+            C(kC0 + i) = div3(r[i][0] * ar * dtl);
 #pragma unroll
             for (int q = 1; q < 4; ++q) C(kA3 + 3 * i + (q - 1)) = a3[i][q];
         }
@@ -620,17 +620,17 @@ k_elem_inv(int nelem, const int4* __restrict__ elem, const double* __restrict__ 
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             double2 a, b;
-            a.x = r[i][0] * ar * dtl / 3.0;
-            a.y = r[i][1] * ar * dtl / 3.0;
-            b.x = r[i][2] * ar * dtl / 3.0;
-            b.y = r[i][3] * ar * dtl / 3.0;
+            a.x = div3(r[i][0] * ar * dtl);
+            a.y = div3(r[i][1] * ar * dtl);
+            b.x = div3(r[i][2] * ar * dtl);
+            b.y = div3(r[i][3] * ar * dtl);
             reinterpret_cast<double2*>(out + 4 * i)[0] = a;
             reinterpret_cast<double2*>(out + 4 * i)[1] = b;
         }
     }
     if (contribF) {
         // FUENTE (subrutinas.f90:1064-1078), as in k_elem_rhs
-        const double AR = ar * dtl / 3.0;
+        const double AR = div3(ar * dtl);
         const double w0 = WX[p[0]], w1 = WX[p[1]], w2 = WX[p[2]];
         const double y0 = WY[p[0]], y1 = WY[p[1]], y2 = WY[p[2]];
         const double wx[3] = {0.5 * w0 + 0.5 * w1, 0.5 * w1 + 0.5 * w2, 0.5 * w0 + 0.5 * w2};
@@ -662,7 +662,7 @@ k_elem_replay(int nelem, const int4* __restrict__ elem, const double* __restrict
     auto C = [&](int plane) -> double { return __ldcs(cache + (size_t)plane * E + e); };
     const double Cv = gc.cv, lambda_ref = gc.lambda_ref, mu_ref = gc.mu_ref, T_inf = gc.t_inf;
     const int4 n = elem[e];
-    const double T_avg = (T[n.x] + T[n.y] + T[n.z]) / 3.0;
+    const double T_avg = div3(T[n.x] + T[n.y] + T[n.z]);
     const double mu = mu_ref * pow15(T_avg / T_inf) * (T_inf + 110.0) / (T_avg + 110.0);
     const double lambda = lambda_ref * pow15(T_avg / T_inf) * (T_inf + 194.0) / (T_avg + 194.0);
     const double Nx[3] = {geo[e], geo[E + e], geo[2 * E + e]};
@@ -715,9 +715,9 @@ k_elem_replay(int nelem, const int4* __restrict__ elem, const double* __restrict
     for (int i = 0; i < 3; ++i) {
         double2 a, b;
         a.x = C(kC0 + i);
-        a.y = r[i][0] * ar * dtl / 3.0;
-        b.x = r[i][1] * ar * dtl / 3.0;
-        b.y = r[i][2] * ar * dtl / 3.0;
+        a.y = div3(r[i][0] * ar * dtl);
+        b.x = div3(r[i][1] * ar * dtl);
+        b.y = div3(r[i][2] * ar * dtl);
         reinterpret_cast<double2*>(out + 4 * i)[0] = a;
         reinterpret_cast<double2*>(out + 4 * i)[1] = b;
     }
@@ -1059,7 +1059,7 @@ __global__ void k_force_visc_terms(int nedges, const int2* __restrict__ edges,
         dvy = dvy + ny[jj] * vy;
         press = press + (double)P[nn[jj]];
     }
-    press = press / 3.0;
+    press = div3(press);
     const double txx = -press - fmu * (2.0 / 3.0 * (dux + dvy) - 2.0 * dux);
     const double txy = fmu * (duy + dvx);
     const double tyx = txy;
@@ -1135,6 +1135,45 @@ __global__ void k_pack_report(const StepScal* __restrict__ sc, const MotionScal*
         out->relres[s] = rz[2 + s];
     }
     out->bar_err = bar->err | (wait_err ? *wait_err : 0);
+}
+
+// ------------------------------------------------------------------ div3 self-test
+// div3 against the division x / 3.0 over n inputs: a third raw 64-bit patterns (splitmix64
+// of seed + i: every exponent and sign, zeros, subnormals, infinities, NaNs), a third
+// values of magnitude 2^-40 .. 2^40, a third multiples of 3 times a power of two moved by
+// up to +-2^12 ulps (quotients next to binade edges and halfway cases).  Counts the inputs
+// whose results differ in any bit (two NaNs count as equal).
+__global__ void k_selftest_div3(long long n, unsigned long long seed,
+                                unsigned long long* __restrict__ bad) {
+    unsigned long long local = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        unsigned long long z = seed + (unsigned long long)i * 0x9e3779b97f4a7c15ull;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        z ^= z >> 31;
+        unsigned long long bits = z;
+        const int kind = (int)(i % 3);
+        if (kind == 1) {  // sign | exponent 1023-40 .. 1023+40 | random significand
+            const unsigned long long ex = 983ull + (z >> 52) % 81ull;
+            bits = (z & 0x800fffffffffffffull) | (ex << 52);
+        } else if (kind == 2) {  // 3 * 2^k, then +-(up to 4096) ulps
+            const int k = (int)((z >> 40) % 121ull) - 60;
+            const long long d = (long long)(z & 0x1fffull) - 4096;
+            const long long b3 = __double_as_longlong(ldexp(3.0, k)) + d;
+            bits = (unsigned long long)b3 | (z & 0x8000000000000000ull);
+        }
+        const double x = __longlong_as_double((long long)bits);
+        const double a = div3(x), b = x / 3.0;
+        if (__double_as_longlong(a) != __double_as_longlong(b) && !(a != a && b != b)) ++local;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
+cudaError_t launch_selftest_div3(long long n, unsigned long long seed, unsigned long long* bad) {
+    k_selftest_div3<<<152 * 8, 256>>>(n, seed, bad);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
 }
 
 }  // namespace cfd

@@ -471,6 +471,13 @@ long long cfd_kernel_launches(void);
  * come back as CFD_ERR_BARRIER and the device stays usable. */
 int cfd_selftest_waits(long long polls, int* barrier_status, int* mbarrier_status);
 
+/* Arithmetic self-test (no counterpart in the reference): the FP64 kernels divide by 3 with
+ * a multiply and two FMAs (Markstein's correction of the quotient by the rounded reciprocal);
+ * this compares it with the IEEE division x / 3.0 over n inputs (1 .. 2^36: raw 64-bit
+ * patterns from `seed`, values in 2^-40 .. 2^40, and values next to 3 * 2^k) and returns
+ * the number whose bits differ. */
+int cfd_selftest_div3(long long n, unsigned long long seed, unsigned long long* mismatches);
+
 const char* cfd_strerror(int status);
 /* 1 if a CUDA device is usable by this library. */
 int cfd_device_available(void);

@@ -117,3 +117,16 @@ def test_bounded_waits_give_up_and_the_device_stays_usable(gpu_lib):
     rep = s.step(2)
     assert rep.iter == 2 and np.isfinite(s.state()["U"]).all()
     s.close()
+
+
+@pytest.mark.gpu
+def test_div3_equals_the_division(gpu_lib):
+    """The FP64 kernels' division by 3 (a multiply and two FMAs) gives the IEEE quotient
+    x / 3.0 bit for bit over 2^32 inputs: raw bit patterns (every exponent, zeros,
+    subnormals, infinities, NaNs), values in 2^-40 .. 2^40, and values next to 3 * 2^k."""
+    import ctypes as C
+    from cfd_gb300 import abi
+    bad = C.c_ulonglong(12345)
+    abi.check(abi.lib().cfd_selftest_div3(1 << 32, 0x5eed, C.byref(bad)), "div3 self-test")
+    assert bad.value == 0
+    assert abi.lib().cfd_selftest_div3(0, 1, C.byref(bad)) == abi.CFD_ERR_ARG
