@@ -451,8 +451,61 @@ __global__ void __launch_bounds__(256) k_bicg_dir_mixed(PcgArgs a) {
             }
 }
 
+// The iteration kernel's block sums and folds (FP64, in an order of the mixed solve's own;
+// the FP64 solve keeps the oracle's tree).  Up to four sums ("slots") at once, one warp
+// each: a block sum puts the threads' values in shared memory and warp j adds slot j's 256
+// entries (warp_sum256: 7 adds, then the shuffle tree); a fold of nc chunk partials gives
+// each slot 256/m threads (m = the slot count rounded up to 1, 2 or 4) that add the
+// partials with that stride before warp j finishes.  A sum costs 12 FP64 warp instructions
+// instead of the 43 of block_tree256, and the slots' sums run side by side.
+__device__ __forceinline__ void block_sums_m(double (&v)[4], int m, double (*sh)[256],
+                                             double* res) {
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (j < m) sh[j][t] = v[j];
+    __syncthreads();
+    if ((t >> 5) < m) {
+        const double r = warp_sum256(sh[t >> 5]);
+        if ((t & 31) == 0) res[t >> 5] = r;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (j < m) v[j] = res[j];
+}
+
+__device__ __forceinline__ void fold_m(const double* const (&src)[4], int m, long nc,
+                                       double (*sh)[256], double* res, double (&out)[4]) {
+    const int t = threadIdx.x;
+    const int lg = m > 2 ? 2 : (m > 1 ? 1 : 0);  // m rounded up to 2^lg
+    const int g = 256 >> lg;                     // threads per slot
+    const int j = t >> (8 - lg), u = t & (g - 1);
+    double acc = 0.0;
+    if (j < m) {
+        const double* pj = j == 0 ? src[0] : (j == 1 ? src[1] : (j == 2 ? src[2] : src[3]));
+        for (long c = u; c < nc; c += g) acc = acc + __ldcg(pj + c);
+    }
+    double* flat = &sh[0][0];
+    flat[t] = acc;
+    __syncthreads();
+    if ((t >> 5) < m) {
+        const double* v = flat + (t >> 5) * g;
+        const int l = t & 31;
+        double s = v[l];
+        for (int q = 1; q < (g >> 5); ++q) s = s + v[l + 32 * q];
+        s = warp_tree32(s);
+        if (l == 0) res[t >> 5] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k < m) out[k] = res[k];
+}
+
 __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
-    __shared__ double red[9];
+    __shared__ double sh[4][256];
+    __shared__ double res[4];
     __shared__ double s_thr[2], s_ref2[2];  // relative modes: threshold on r.r, ref.ref
     const int t = threadIdx.x;
     const int n = a.n;
@@ -551,14 +604,22 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                     if (rel) accr[s] = (kk == 0) ? ri * ri : accr[s] + ri * ri;
                 }
             }
+            double v[4] = {0.0, 0.0, 0.0, 0.0};
+            int m = 0;
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
                 if (!act[s]) continue;
-                double v = block_tree256(acc[s], red);
-                if (t == 0) part(1, s)[c] = v;
-                if (rel) {
-                    v = block_tree256(accr[s], red);
-                    if (t == 0) part(2, s)[c] = v;
+                v[m++] = acc[s];
+                if (rel) v[m++] = accr[s];
+            }
+            block_sums_m(v, m, sh, res);
+            if (t == 0) {
+                int j = 0;
+#pragma unroll
+                for (int s = 0; s < 2; ++s) {
+                    if (!act[s]) continue;
+                    part(1, s)[c] = v[j++];
+                    if (rel) part(2, s)[c] = v[j++];
                 }
             }
         }
@@ -568,11 +629,28 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
         if (bar_failed_m(a.bar)) return;
         double beta[2] = {0.0, 0.0};
         float betaf[2] = {0.f, 0.f};
+        {
+            const double* src[4] = {nullptr, nullptr, nullptr, nullptr};
+            double out[4] = {0.0, 0.0, 0.0, 0.0};
+            int m = 0;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                if (!act[s]) continue;
+                src[m++] = part(1, s);
+                if (rel) src[m++] = part(2, s);
+            }
+            fold_m(src, m, nc, sh, res, out);
+            int j = 0;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                if (!act[s]) continue;
+                err_new[s] = out[j++];
+                if (rel) rrc[s] = out[j++];
+            }
+        }
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (!act[s]) continue;
-            err_new[s] = fold_partials(part(1, s), nc, red);
-            if (rel) rrc[s] = fold_partials(part(2, s), nc, red);
             beta[s] = err_new[s] / err_old[s];
             betaf[s] = d2f_trunc(beta[s]);
         }
@@ -649,19 +727,35 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                     }
                 }
             }
+            double v[4] = {0.0, 0.0, 0.0, 0.0};
+            int m = 0;
 #pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                if (!act[s]) continue;
-                const double v = block_tree256(acc[s], red);
-                if (t == 0) part(0, s)[c] = v;
+            for (int s = 0; s < 2; ++s)
+                if (act[s]) v[m++] = acc[s];
+            block_sums_m(v, m, sh, res);
+            if (t == 0) {
+                int j = 0;
+#pragma unroll
+                for (int s = 0; s < 2; ++s)
+                    if (act[s]) part(0, s)[c] = v[j++];
             }
         }
         grid_barrier(a.bar, nb);
         if (bar_failed_m(a.bar)) return;
+        double pyv[4] = {0.0, 0.0, 0.0, 0.0};
+        {
+            const double* src[4] = {nullptr, nullptr, nullptr, nullptr};
+            int m = 0;
+#pragma unroll
+            for (int s = 0; s < 2; ++s)
+                if (act[s]) src[m++] = part(0, s);
+            fold_m(src, m, nc, sh, res, pyv);
+        }
+        int jpy = 0;
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (!act[s]) continue;
-            const double py = fold_partials(part(0, s), nc, red);
+            const double py = pyv[jpy++];
             alfa[s] = err_new[s] / py;
             err_old[s] = err_new[s];
             cur[s] ^= 1;
