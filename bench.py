@@ -385,7 +385,8 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
     Learned variants: "learned" runs the network on the first solve and after solves above
     the gate; "learned_every_step" runs it on every solve; "learned_refined" runs it on the
     first solve and then tries, every step, the guess of the basis fields it seeded and
-    the solves refine (cfd_ctx_set_guess_refine)."""
+    the solves refine (cfd_ctx_set_guess_refine).  "*_extrapolated": the same with the
+    second-order guess in time as a further candidate (cfd_ctx_set_guess_extrapolate)."""
     from cfd_gb300 import abi, learned, solver
     net = learned.Net.load()
     out = {}
@@ -394,6 +395,8 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
                  "learned_every_step": (abi.CFD_GUESS_LEARNED, 0.0, False),
                  "learned": (abi.CFD_GUESS_LEARNED, args.guess_gate, False),
                  "learned_refined": (abi.CFD_GUESS_LEARNED, 1.0e9, True)}
+    for base in ("previous", "learned_refined"):
+        all_modes[base + "_extrapolated"] = all_modes[base]
     modes = modes or ["previous", "zero", "learned_every_step", "learned"]
     os.environ["CFD_TIMERS"] = "1"
     try:
@@ -410,6 +413,9 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
                 S.set_guess_net(net, gate)
                 if refine:
                     S.set_guess_refine(True)
+            extrap = name.endswith("_extrapolated")
+            if extrap:
+                S.set_guess_extrapolate(True)
             r1 = S.step(1)
             S.step(max(W - 1, 0))
             t0 = S.timers()
@@ -438,6 +444,9 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
                 if refine:
                     dv, dx, dy = st[4:7]
                     d.update({"fields_steps": dv, "fields_taken": [dx, dy]})
+            if extrap:
+                ev, tx, ty = S.guess_stats_extrapolate()
+                d.update({"extrapolated_formed": ev, "extrapolated_taken": [tx, ty]})
             S.close()
             out[name] = d
     finally:
@@ -748,7 +757,8 @@ def main_ours(args):
         tm = args.guess_tol_mode
         forms["guess"] = guess_report(
             args, W, min(K, 10), tol_mode=tm, tol=1.0e-10, maxit=20000 if tm else 1000,
-            modes=["previous", "zero", "learned", "learned_every_step", "learned_refined"])
+            modes=["previous", "zero", "learned", "learned_every_step", "learned_refined",
+                   "previous_extrapolated", "learned_refined_extrapolated"])
         forms["guess"]["bicg_test"] = ("||r|| <= 1e-10 ||b - A x_D|| (relative)" if tm else
                                        "|r.z| < 1e-10 (the reference's absolute test)")
     # ---- per-kernel breakdown and roofline of the dominant kernel (timers on, own ctx)

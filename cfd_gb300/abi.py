@@ -140,6 +140,8 @@ SIGNATURES = {
     "cfd_ctx_guess_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_set_guess_refine": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_guess_stats_ex": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "cfd_ctx_set_guess_extrapolate": (C.c_int, [_P, C.c_int]),
+    "cfd_ctx_guess_stats_extrapolate": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_graph_state": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_set_force_visc": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smooth": (C.c_int, [_P, _ip, _dp]),

@@ -336,6 +336,22 @@ int cfd_ctx_set_guess_refine(cfd_ctx* ctx, int on) {
     return ctx->impl.set_guess_refine(on != 0);
 }
 
+int cfd_ctx_set_guess_extrapolate(cfd_ctx* ctx, int on) {
+    if (!ctx) return arg_error("ctx");
+    return ctx->impl.set_guess_extrapolate(on != 0);
+}
+
+int cfd_ctx_guess_stats_extrapolate(cfd_ctx* ctx, long long* out3) {
+    if (!ctx || !out3) return arg_error("null pointer");
+    Ctx& c = ctx->impl;
+    for (int k = 0; k < 3; ++k) out3[k] = 0;
+    if (!c.d_xstats) return CFD_OK;
+    CFD_CUDA(cudaMemcpyAsync(out3, c.d_xstats, 3 * sizeof(long long), cudaMemcpyDeviceToHost,
+                             c.stream));
+    CFD_CUDA(cudaStreamSynchronize(c.stream));
+    return CFD_OK;
+}
+
 int cfd_ctx_guess_stats_ex(cfd_ctx* ctx, long long* out8) {
     if (!ctx || !out8) return arg_error("null pointer");
     Ctx& c = ctx->impl;

@@ -176,7 +176,8 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         // network runs, with the refined guess on, the candidate is the fields' guess.
         const bool with_net = prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph;
         const bool fields = with_net && guess_refine && !learned && fields_ready;
-        a.gflag = (learned || fields) ? d_gflag : nullptr;
+        const bool extrap = guess_extrap && prm.guess_mode != CFD_GUESS_ZERO;
+        a.gflag = (learned || fields || extrap) ? d_gflag : nullptr;
         a.gate = 0.0;
         a.only_if = nullptr;
         if (nufix > 0 && !fix_done)
@@ -186,6 +187,21 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
                                    ? (unsigned)std::min<long>(a.nblk_r, (long)branch_bpsm * nsm)
                                    : (unsigned)a.nblk_r;
         CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, a));
+        if (extrap) {
+            // the previous solutions extrapolated to this step, against the previous one
+            const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
+            const double* dtn = &d_scal->dtmin;
+            CFD_LAUNCH(k_guess_extrap, gsz, 256, 0, stream, a, dtn, (const double*)d_xhist,
+                       d_xprev[0], d_xprev[1], d_cand[0], d_cand[1]);
+            CFD_LAUNCH(k_guess_extrap_hist, 1, 32, 0, stream, dtn, d_xhist);
+            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                       (const double*)d_cand[1], d_grr);
+            CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                       (const double*)d_cand[1], (const double*)d_grr, d_xstats);
+            PcgArgs b = a;
+            b.only_if = d_gflag + 1;
+            CFD_CUDA(launch_bicg_resid_mixed(gsz, stream, b));
+        }
         if (fields) {
             int st = mpnn::fields_guess(lgraph, stream, d_X, d_Y, d_xfix[0], d_xfix[1], d_pos[0],
                                         d_pos[1], d_cand[0], d_cand[1]);
@@ -274,11 +290,7 @@ int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
         int st = mpnn::graph_build(&lgraph, N, adj.rowptr, adj.col, x.data(), y.data(), nnmove,
                                    bc.fix_node.data(), bkind.data(), false, stream);
         if (st) return st;
-        for (int s = 0; s < 2; ++s)
-            if ((st = dalloc(&d_cand[s], N))) return st;
-        if ((st = dalloc(&d_gflag, 2))) return st;
-        if ((st = dalloc(&d_grr, 2))) return st;
-        if ((st = dalloc(&d_gstats, 8))) return st;
+        if ((st = guess_buffers())) return st;
         CFD_CUDA(cudaMallocHost((void**)&h_iters, 2 * sizeof(int)));
         h_iters[0] = h_iters[1] = 0;
         // the captured step has no copy of the counts yet: capture it again
@@ -287,6 +299,44 @@ int Ctx::set_guess_net(cfd_mpnn* n, double gate) {
         CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 8 * sizeof(long long), stream));
         CFD_CUDA(cudaStreamSynchronize(stream));
     }
+    return CFD_OK;
+}
+
+// The candidate buffers, gate flags, judge sums and counters of the guess selection
+// (allocated once, by the first of set_guess_net and set_guess_extrapolate)
+int Ctx::guess_buffers() {
+    if (d_gstats) return CFD_OK;
+    int st;
+    for (int s = 0; s < 2; ++s)
+        if ((st = dalloc(&d_cand[s], npoin))) return st;
+    if ((st = dalloc(&d_gflag, 2))) return st;
+    if ((st = dalloc(&d_grr, 2))) return st;
+    if ((st = dalloc(&d_gstats, 8))) return st;
+    CFD_CUDA(cudaMemsetAsync(d_gflag, 0, 2 * sizeof(int), stream));
+    CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 8 * sizeof(long long), stream));
+    return CFD_OK;
+}
+
+// Second-order guess in time on or off (mixed form).  The history starts again: the first
+// two solves after switching it on only record their solutions.
+int Ctx::set_guess_extrapolate(bool on) {
+    if (prec != CFD_PREC_MIXED) {
+        set_last_message("the extrapolated guess runs in the mixed-precision form");
+        return CFD_ERR_ARG;
+    }
+    int st;
+    if (on) {
+        if ((st = guess_buffers())) return st;
+        for (int s = 0; s < 2; ++s)
+            if (!d_xprev[s] && (st = dalloc(&d_xprev[s], npoin))) return st;
+        if (!d_xhist && (st = dalloc(&d_xhist, 3))) return st;
+        if (!d_xstats && (st = dalloc(&d_xstats, 3))) return st;
+        CFD_CUDA(cudaMemsetAsync(d_xhist, 0, 3 * sizeof(double), stream));
+        CFD_CUDA(cudaMemsetAsync(d_xstats, 0, 3 * sizeof(long long), stream));
+        CFD_CUDA(cudaStreamSynchronize(stream));
+    }
+    guess_extrap = on;
+    drop_graphs();
     return CFD_OK;
 }
 

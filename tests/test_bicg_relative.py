@@ -181,3 +181,35 @@ def test_gpu_mixed_relative_mode(gpu_lib, oracle):
             assert d <= 1e-3, (s, q, d)
     gm.close()
     gd.close()
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_extrapolated_guess(gpu_lib):
+    """The second-order guess in time (cfd_ctx_set_guess_extrapolate): once two solutions
+    are kept it is formed on every solve, taken when better, and the solves still reach the
+    relative tolerance, in fewer iterations than from the previous step's increment; the
+    mesh increments stay within the solve's accuracy of the previous-guess run's."""
+    from cfd_gb300 import abi, solver
+    k = small_case(2, scale=32, seed=8, pitch_amp=math.radians(4.0), motion_freq=2.0,
+                   mass_mode=abi.CFD_MASS_GCL_CORRECTED, bicg_tol_mode=abi.CFD_BICG_TOL_REL,
+                   bicg_maxit=3000, estab_mode=abi.CFD_ESTAB_REGULARIZED)
+    gp = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    ge = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    ge.set_guess_extrapolate(True)
+    its_p, its_e = [], []
+    for s in range(8):
+        rp, re = gp.step(1), ge.step(1)
+        assert all(re.bicg_converged) and max(re.bicg_relres) <= 1e-10
+        if s >= 3:
+            its_p.append(sum(rp.bicg_iters))
+            its_e.append(sum(re.bicg_iters))
+        for q, (a, b) in enumerate(zip(ge.motion(), gp.motion())):
+            d = np.abs(a - b).max() / np.abs(b).max()
+            assert d <= 1e-3, (s, q, d)
+    formed, tx, ty = ge.guess_stats_extrapolate()
+    assert formed == 8 and tx + ty > 0
+    assert sum(its_e) < sum(its_p), (its_e, its_p)
+    gp.close()
+    ge.close()
+    with pytest.raises(abi.CfdError):
+        solver.Solver(k).set_guess_extrapolate(True)
