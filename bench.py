@@ -200,10 +200,9 @@ def config_dict(k, args, ws):
 # profiles/step_mixed_1M_launches.md (the full-size workload fits the capture rules: ~2.5 GB
 # on the device, kernels of 13-130 us).
 NCU_TRAFFIC_PER_STEP = {
-    "update_t": 1059.5e6,   # 4 node passes (946.4 MB) + 3 mu/lambda passes (113.1 MB)
-    "calcrhs_t": 350.1e6,   # k_elem_stage1_mixed (ESTAB's DTMIN-free part included)
-    "deltat_t": 63.3e6,     # k_deltat_mixed (the FP64 refinement reads a few chunks)
-    "laplace_t": 181.8e6,
+    "update_t": 1047.2e6,   # 4 node passes (934.0 MB) + 3 mu/lambda passes (113.2 MB)
+    "calcrhs_t": 347.9e6,   # k_elem_stage1_mixed (ESTAB's DTMIN-free part included)
+    "deltat_t": 62.9e6,     # k_deltat_mixed (the FP64 refinement reads a few chunks)
 }
 
 
@@ -374,7 +373,8 @@ def large_mesh_report(W, net, gate, hbm_peak, nr=2048):
                                      "frac_of_hbm_peak": ab / upd / 1e9 / hbm_peak}}
 
 
-def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
+def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None,
+                 precision=None):
     """Mesh-motion solve with the previous-step, zero and learned guesses on the workload
     (mixed form): BiCG iterations (x + y solves) on the first (cold) step and per step after
     warm-up, the mesh-motion time per step (timer of the BiCG group, which holds the network
@@ -385,8 +385,9 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
     Learned variants: "learned" runs the network on the first solve and after solves above
     the gate; "learned_every_step" runs it on every solve; "learned_refined" runs it on the
     first solve and then tries, every step, the guess of the basis fields it seeded and
-    the solves refine (cfd_ctx_set_guess_refine).  "*_extrapolated": the same with the
-    second-order guess in time as a further candidate (cfd_ctx_set_guess_extrapolate)."""
+    the solves refine (cfd_ctx_set_guess_refine).  "extrapolated": CFD_GUESS_EXTRAPOLATED,
+    the last two increments extrapolated to the step's DTMIN.  precision: the form that
+    solves (the learned variants run in the mixed form only)."""
     from cfd_gb300 import abi, learned, solver
     net = learned.Net.load()
     out = {}
@@ -395,8 +396,7 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
                  "learned_every_step": (abi.CFD_GUESS_LEARNED, 0.0, False),
                  "learned": (abi.CFD_GUESS_LEARNED, args.guess_gate, False),
                  "learned_refined": (abi.CFD_GUESS_LEARNED, 1.0e9, True)}
-    for base in ("previous", "learned_refined"):
-        all_modes[base + "_extrapolated"] = all_modes[base]
+    all_modes["extrapolated"] = (abi.CFD_GUESS_EXTRAPOLATED, None, False)
     modes = modes or ["previous", "zero", "learned_every_step", "learned"]
     os.environ["CFD_TIMERS"] = "1"
     try:
@@ -408,14 +408,11 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
             k.params.bicg_tol_mode = tol_mode
             k.params.bicg_tol = tol
             k.params.bicg_maxit = maxit
-            S = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+            S = solver.Solver(k, precision=abi.CFD_PREC_MIXED if precision is None else precision)
             if gate is not None:
                 S.set_guess_net(net, gate)
                 if refine:
                     S.set_guess_refine(True)
-            extrap = name.endswith("_extrapolated")
-            if extrap:
-                S.set_guess_extrapolate(True)
             r1 = S.step(1)
             S.step(max(W - 1, 0))
             t0 = S.timers()
@@ -444,9 +441,6 @@ def guess_report(args, W, K, tol_mode=0, tol=1.0e-10, maxit=1000, modes=None):
                 if refine:
                     dv, dx, dy = st[4:7]
                     d.update({"fields_steps": dv, "fields_taken": [dx, dy]})
-            if extrap:
-                ev, tx, ty = S.guess_stats_extrapolate()
-                d.update({"extrapolated_formed": ev, "extrapolated_taken": [tx, ty]})
             S.close()
             out[name] = d
     finally:
@@ -758,9 +752,15 @@ def main_ours(args):
         forms["guess"] = guess_report(
             args, W, min(K, 10), tol_mode=tm, tol=1.0e-10, maxit=20000 if tm else 1000,
             modes=["previous", "zero", "learned", "learned_every_step", "learned_refined",
-                   "previous_extrapolated", "learned_refined_extrapolated"])
+                   "extrapolated"])
         forms["guess"]["bicg_test"] = ("||r|| <= 1e-10 ||b - A x_D|| (relative)" if tm else
                                        "|r.z| < 1e-10 (the reference's absolute test)")
+        # the same solves in the plain FP64 form (its operator is assembled in FP64, so the
+        # previous solutions carry no FP32 rounding of the operator into the next solve)
+        forms["guess_fp64"] = guess_report(
+            args, W, min(K, 10), tol_mode=tm, tol=1.0e-10, maxit=20000 if tm else 1000,
+            modes=["previous", "extrapolated"], precision=abi.CFD_PREC_FP64)
+        forms["guess_fp64"]["bicg_test"] = forms["guess"]["bicg_test"]
     # ---- per-kernel breakdown and roofline of the dominant kernel (timers on, own ctx)
     os.environ["CFD_TIMERS"] = "1"
     S2 = solver.Solver(k, precision=prec)

@@ -21,7 +21,7 @@ STATUS_NAMES = {0: "CFD_OK", 1: "CFD_ERR_ARG", 2: "CFD_ERR_MESH", 3: "CFD_ERR_CU
 CFD_PREC_FP64, CFD_PREC_MIXED = 0, 1
 CFD_MASS_MASAS, CFD_MASS_GCL_LITERAL, CFD_MASS_GCL_CORRECTED = 0, 1, 2
 CFD_MOTION_REFERENCE, CFD_MOTION_HARMONIC, CFD_MOTION_NEWMARK = 0, 1, 2
-CFD_GUESS_PREVIOUS, CFD_GUESS_ZERO, CFD_GUESS_LEARNED = 0, 1, 2
+CFD_GUESS_PREVIOUS, CFD_GUESS_ZERO, CFD_GUESS_LEARNED, CFD_GUESS_EXTRAPOLATED = 0, 1, 2, 3
 CFD_ESTAB_REFERENCE, CFD_ESTAB_EXACT, CFD_ESTAB_REGULARIZED = 0, 1, 2
 CFD_BICG_TOL_ABS, CFD_BICG_TOL_REL, CFD_BICG_TOL_REL_R0 = 0, 1, 2
 CFD_SMOOTH_COLOUR, CFD_SMOOTH_NODE_ORDER = 0, 1
@@ -140,8 +140,6 @@ SIGNATURES = {
     "cfd_ctx_guess_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_set_guess_refine": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_guess_stats_ex": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
-    "cfd_ctx_set_guess_extrapolate": (C.c_int, [_P, C.c_int]),
-    "cfd_ctx_guess_stats_extrapolate": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_graph_state": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_ctx_set_force_visc": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smooth": (C.c_int, [_P, _ip, _dp]),

@@ -238,6 +238,8 @@ int cfd_ctx_create(cfd_ctx** out, const cfd_mesh* mesh, const cfd_params* p, int
         return arg_error("estab_mode");
     if (p->bicg_tol_mode < CFD_BICG_TOL_ABS || p->bicg_tol_mode > CFD_BICG_TOL_REL_R0)
         return arg_error("bicg_tol_mode");
+    if (p->guess_mode < CFD_GUESS_PREVIOUS || p->guess_mode > CFD_GUESS_EXTRAPOLATED)
+        return arg_error("guess_mode");
     if (p->ngas != 0) {
         set_last_message("only the perfect-gas path (NGAS = 0) is implemented");
         return CFD_ERR_ARG;
@@ -334,22 +336,6 @@ int cfd_ctx_set_guess_net(cfd_ctx* ctx, cfd_mpnn* net, double gate) {
 int cfd_ctx_set_guess_refine(cfd_ctx* ctx, int on) {
     if (!ctx) return arg_error("ctx");
     return ctx->impl.set_guess_refine(on != 0);
-}
-
-int cfd_ctx_set_guess_extrapolate(cfd_ctx* ctx, int on) {
-    if (!ctx) return arg_error("ctx");
-    return ctx->impl.set_guess_extrapolate(on != 0);
-}
-
-int cfd_ctx_guess_stats_extrapolate(cfd_ctx* ctx, long long* out3) {
-    if (!ctx || !out3) return arg_error("null pointer");
-    Ctx& c = ctx->impl;
-    for (int k = 0; k < 3; ++k) out3[k] = 0;
-    if (!c.d_xstats) return CFD_OK;
-    CFD_CUDA(cudaMemcpyAsync(out3, c.d_xstats, 3 * sizeof(long long), cudaMemcpyDeviceToHost,
-                             c.stream));
-    CFD_CUDA(cudaStreamSynchronize(c.stream));
-    return CFD_OK;
 }
 
 int cfd_ctx_guess_stats_ex(cfd_ctx* ctx, long long* out8) {

@@ -146,12 +146,9 @@ struct Ctx {
     // tries the fields' guess, and keeps the better of it and the previous step's
     bool guess_refine = false;
     bool fields_ready = false;   // the fields were seeded since the network was attached
-    // second-order guess in time (cfd_ctx_set_guess_extrapolate, mixed form): the last two
-    // solutions' increments extrapolated to this step, judged against the current guess
-    bool guess_extrap = false;
+    // CFD_GUESS_EXTRAPOLATED: the previous step's solutions and the history of DTMIN
     double* d_xprev[2] = {};
-    double* d_xhist = nullptr;        // (dt1, dt2, solves kept)
-    long long* d_xstats = nullptr;    // (formed, x taken, y taken)
+    double* d_xhist = nullptr;        // (dt1, dt2, solutions kept)
     int* h_iters = nullptr;      // pinned copy of the last solve's iteration counts
     cudaEvent_t ev_iters = nullptr;  // recorded after that copy
     // mixed form: the clock and the motion increment live on the device
@@ -217,8 +214,8 @@ struct Ctx {
     int run_pcg(int nsolve, bool learned = false, bool fix_done = false,
                 cudaStream_t sv = nullptr);
     int set_guess_refine(bool on);
-    int set_guess_extrapolate(bool on);
     int guess_buffers();
+    int guess_extrapolate(const PcgArgs& a, cudaStream_t s, unsigned grid);
     int enqueue_mixed(bool learned);
     int launch_step_graph(bool* launched);
     int set_guess_net(cfd_mpnn* n, double gate);

@@ -353,9 +353,9 @@ cudaError_t launch_bicg_resid_mixed(unsigned grid, cudaStream_t stream, const Pc
 __global__ void k_bicg_dir_mixed(PcgArgs a);
 // learned-guess judge: r.z of the candidate (cand[s]) per solve when gflag[0] is set
 __global__ void k_guess_judge(PcgArgs a, const double* cand0, const double* cand1, double* rr);
-__global__ void k_guess_extrap(PcgArgs a, const double* dtn_p, const double* hist, double* xprev0,
-                               double* xprev1, double* cand0, double* cand1);
-__global__ void k_guess_extrap_hist(const double* dtn_p, double* hist);
+__global__ void k_guess_extrapolate(PcgArgs a, const double* dtn_p, double* hist,
+                                    double* xprev0, double* xprev1);
+__global__ void k_guess_extrapolate_hist(const double* dtn_p, double* hist);
 // per solve, the candidate replaces x (and its shadow) when its r.z is the smaller; sets
 // gflag[1]; stats[0..3) += (gate open, solve 0 took it, solve 1 took it)
 __global__ void k_guess_select(PcgArgs a, const double* cand0, const double* cand1,

@@ -124,6 +124,16 @@ int Ctx::geometry(bool masas, bool with_laplace) {
 }
 
 // ------------------------------------------------------------------ PCG launch
+// CFD_GUESS_EXTRAPOLATED: x becomes the last two increments extrapolated to this step's
+// DTMIN (k_guess_extrapolate), then the history moves on
+int Ctx::guess_extrapolate(const PcgArgs& a, cudaStream_t s, unsigned grid) {
+    const double* dtn = &d_scal->dtmin;
+    CFD_LAUNCH(k_guess_extrapolate, std::min(grid, (unsigned)(4 * nsm)), 256, 0, s, a, dtn, d_xhist,
+               d_xprev[0], d_xprev[1]);
+    CFD_LAUNCH(k_guess_extrapolate_hist, 1, 32, 0, s, dtn, d_xhist);
+    return CFD_OK;
+}
+
 int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
     const cudaStream_t stream = sv ? sv : this->stream;  // the solve's stream
     PcgArgs a{};
@@ -176,8 +186,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         // network runs, with the refined guess on, the candidate is the fields' guess.
         const bool with_net = prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph;
         const bool fields = with_net && guess_refine && !learned && fields_ready;
-        const bool extrap = guess_extrap && prm.guess_mode != CFD_GUESS_ZERO;
-        a.gflag = (learned || fields || extrap) ? d_gflag : nullptr;
+        a.gflag = (learned || fields) ? d_gflag : nullptr;
         a.gate = 0.0;
         a.only_if = nullptr;
         if (nufix > 0 && !fix_done)
@@ -186,22 +195,11 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         const unsigned rgrid = (sv && branch_bpsm > 0)
                                    ? (unsigned)std::min<long>(a.nblk_r, (long)branch_bpsm * nsm)
                                    : (unsigned)a.nblk_r;
-        CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, a));
-        if (extrap) {
-            // the previous solutions extrapolated to this step, against the previous one
-            const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
-            const double* dtn = &d_scal->dtmin;
-            CFD_LAUNCH(k_guess_extrap, gsz, 256, 0, stream, a, dtn, (const double*)d_xhist,
-                       d_xprev[0], d_xprev[1], d_cand[0], d_cand[1]);
-            CFD_LAUNCH(k_guess_extrap_hist, 1, 32, 0, stream, dtn, d_xhist);
-            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
-                       (const double*)d_cand[1], d_grr);
-            CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
-                       (const double*)d_cand[1], (const double*)d_grr, d_xstats);
-            PcgArgs b = a;
-            b.only_if = d_gflag + 1;
-            CFD_CUDA(launch_bicg_resid_mixed(gsz, stream, b));
+        if (prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+            int st = guess_extrapolate(a, stream, rgrid);
+            if (st) return st;
         }
+        CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, a));
         if (fields) {
             int st = mpnn::fields_guess(lgraph, stream, d_X, d_Y, d_xfix[0], d_xfix[1], d_pos[0],
                                         d_pos[1], d_cand[0], d_cand[1]);
@@ -237,6 +235,10 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
             }
         }
         CFD_LAUNCH(k_bicg_dir_mixed, rgrid, 256, 0, stream, a);
+    }
+    if (!mixed && prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+        int st = guess_extrapolate(a, stream, blocks_for(npoin, 256));
+        if (st) return st;
     }
     CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
     void* args[] = {&a};
@@ -314,29 +316,6 @@ int Ctx::guess_buffers() {
     if ((st = dalloc(&d_gstats, 8))) return st;
     CFD_CUDA(cudaMemsetAsync(d_gflag, 0, 2 * sizeof(int), stream));
     CFD_CUDA(cudaMemsetAsync(d_gstats, 0, 8 * sizeof(long long), stream));
-    return CFD_OK;
-}
-
-// Second-order guess in time on or off (mixed form).  The history starts again: the first
-// two solves after switching it on only record their solutions.
-int Ctx::set_guess_extrapolate(bool on) {
-    if (prec != CFD_PREC_MIXED) {
-        set_last_message("the extrapolated guess runs in the mixed-precision form");
-        return CFD_ERR_ARG;
-    }
-    int st;
-    if (on) {
-        if ((st = guess_buffers())) return st;
-        for (int s = 0; s < 2; ++s)
-            if (!d_xprev[s] && (st = dalloc(&d_xprev[s], npoin))) return st;
-        if (!d_xhist && (st = dalloc(&d_xhist, 3))) return st;
-        if (!d_xstats && (st = dalloc(&d_xstats, 3))) return st;
-        CFD_CUDA(cudaMemsetAsync(d_xhist, 0, 3 * sizeof(double), stream));
-        CFD_CUDA(cudaMemsetAsync(d_xstats, 0, 3 * sizeof(long long), stream));
-        CFD_CUDA(cudaStreamSynchronize(stream));
-    }
-    guess_extrap = on;
-    drop_graphs();
     return CFD_OK;
 }
 
@@ -773,6 +752,14 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_xfix[s], nnmove))) return st;
         CFD_CUDA(cudaMemsetAsync(d_pos[s], 0, sizeof(double) * N, stream));
         CFD_CUDA(cudaMemsetAsync(d_xfix[s], 0, sizeof(double) * (nnmove ? nnmove : 1), stream));
+        if (prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+            if ((st = dalloc(&d_xprev[s], N))) return st;
+            CFD_CUDA(cudaMemsetAsync(d_xprev[s], 0, sizeof(double) * N, stream));
+        }
+    }
+    if (prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+        if ((st = dalloc(&d_xhist, 3))) return st;
+        CFD_CUDA(cudaMemsetAsync(d_xhist, 0, 3 * sizeof(double), stream));
     }
     const long nc = ((long)N + kChunk - 1) / kChunk;
     if ((st = dalloc(&d_part, 6 * (size_t)(nc > 0 ? nc : 1)))) return st;

@@ -305,6 +305,53 @@ __global__ void __launch_bounds__(256, 3) k_pcg_fp64(PcgArgs a) {
 // expects a second block that never comes, and an mbarrier nothing arrives on.  Both give
 // up after `limit` polls; out[0] = the barrier's error word, out[1] = CFD_ERR_BARRIER when
 // the mbarrier wait gave up (0 if it completed).
+// CFD_GUESS_EXTRAPOLATED: the solves start from the last two increments extrapolated to
+// this step.  A solve's unknown is the step's mesh increment, the mean mesh velocity over the
+// step times DTMIN; with that velocity linear in time through the last two steps' midpoints,
+//     x = c1 x_{n-1} + c2 x_{n-2},  h = (dt_n + dt1) / (dt1 + dt2),
+//     c1 = dt_n / dt1 (1 + h),  c2 = -(dt_n / dt2) h
+// on the free rows (x_{n-1} is the previous solution, still in x), in the oracle's operation
+// order (--fmad=false: the same bits); x_{n-1} is kept as the next step's x_{n-2}.  hist =
+// (dt1, dt2, solutions kept); with fewer than two kept the guess stays x_{n-1}.  The fixed
+// rows are left to the Dirichlet values (set before, or by the solve).  The float shadow
+// (mixed form) follows x.
+__global__ void k_guess_extrapolate(PcgArgs a, const double* __restrict__ dtn_p,
+                                    double* __restrict__ hist, double* __restrict__ xprev0,
+                                    double* __restrict__ xprev1) {
+    const double dtn = *dtn_p, dt1 = hist[0], dt2 = hist[1];
+    const bool two = hist[2] >= 2.0;
+    double c1 = 1.0, c2 = 0.0;
+    if (two) {
+        const double h = (dtn + dt1) / (dt1 + dt2);
+        c1 = dtn / dt1 * (1.0 + h);
+        c2 = -(dtn / dt2) * h;
+    }
+    double* xprev[2] = {xprev0, xprev1};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < a.n;
+         i += (long)gridDim.x * blockDim.x) {
+        if (a.isfix[i]) continue;
+        for (int s = 0; s < a.nsolve; ++s) {
+            const double x1 = a.x[s][i];
+            const double xn = two ? c1 * x1 + c2 * xprev[s][i] : x1;
+            xprev[s][i] = x1;
+            if (two) {
+                a.x[s][i] = xn;
+                if (a.xf[s]) a.xf[s][i] = d2f_trunc(xn);
+            }
+        }
+    }
+}
+
+// after k_guess_extrapolate: hist = (dt_n, dt1, solutions kept + 1)
+__global__ void k_guess_extrapolate_hist(const double* __restrict__ dtn_p,
+                                         double* __restrict__ hist) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        hist[1] = hist[0];
+        hist[0] = *dtn_p;
+        hist[2] = hist[2] + 1.0;
+    }
+}
+
 __global__ void k_selftest_waits(GridBar* gb, int* out, long long limit) {
     __shared__ __align__(8) unsigned long long bar;
     grid_barrier(gb, 2u, limit);

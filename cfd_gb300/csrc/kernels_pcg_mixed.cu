@@ -409,53 +409,6 @@ __global__ void k_guess_select(PcgArgs a, const double* __restrict__ cand0,
     }
 }
 
-// Second-order guess in time (mixed form, cfd_ctx_set_guess_extrapolate).  A solve's
-// unknown is the step's mesh increment, i.e. the mean mesh velocity over the step times
-// DTMIN; with that velocity linear in time through the last two steps' midpoints,
-//     cand = dt_n (v1 + (v1 - v2) (dt_n + dt1) / (dt1 + dt2)),  v_k = x_{n-k} / dt_k,
-// on the free rows (x_{n-1}, the previous solution, is still in x: the reference's guess),
-// and the step's Dirichlet values on the fixed rows.  x_{n-1} is then kept as the next
-// step's x_{n-2}.  hist = (dt1, dt2, solves kept); before two are kept the candidate is
-// x itself (which the judge does not take: it keeps a candidate only if strictly better).
-__global__ void k_guess_extrap(PcgArgs a, const double* __restrict__ dtn_p,
-                               const double* __restrict__ hist, double* __restrict__ xprev0,
-                               double* __restrict__ xprev1, double* __restrict__ cand0,
-                               double* __restrict__ cand1) {
-    const double dtn = *dtn_p, dt1 = hist[0], dt2 = hist[1];
-    double c1 = 1.0, c2 = 0.0;  // cand = c1 x_{n-1} + c2 x_{n-2}
-    if (hist[2] >= 2.0 && dt1 > 0.0 && dt2 > 0.0) {
-        const double h = (dtn + dt1) / (dt1 + dt2);
-        c1 = dtn / dt1 * (1.0 + h);
-        c2 = -(dtn / dt2) * h;
-    }
-    double* xprev[2] = {xprev0, xprev1};
-    double* cand[2] = {cand0, cand1};
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < a.n;
-         i += (long)gridDim.x * blockDim.x) {
-        const bool fx = a.isfix[i];
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            if (s >= a.nsolve) continue;
-            const double x1 = a.x[s][i];
-            if (fx) {
-                cand[s][i] = x1;
-            } else {
-                cand[s][i] = c1 * x1 + c2 * xprev[s][i];
-                xprev[s][i] = x1;
-            }
-        }
-    }
-}
-
-// after k_guess_extrap: hist = (dt_n, dt1, solves kept + 1)
-__global__ void k_guess_extrap_hist(const double* __restrict__ dtn_p, double* __restrict__ hist) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        hist[1] = hist[0];
-        hist[0] = *dtn_p;
-        hist[2] = hist[2] + 1.0;
-    }
-}
-
 // Second pass, for the solves with r.r >= tol: y = A.p (FP32 over the shadow), y(fix) =
 // 1e30 p(fix); per-block partials of p.y; the last block forms alfa = r.p / p.y
 // (biconjGrad.f90:39-43)

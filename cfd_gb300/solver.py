@@ -270,19 +270,6 @@ class Solver:
         check(abi.lib().cfd_ctx_set_guess_refine(self.h, int(bool(on))),
               "cfd_ctx_set_guess_refine")
 
-    def set_guess_extrapolate(self, on=True):
-        """Second-order guess in time for the mesh-motion solves (mixed form; see
-        cfd_ctx_set_guess_extrapolate)."""
-        check(abi.lib().cfd_ctx_set_guess_extrapolate(self.h, int(bool(on))),
-              "cfd_ctx_set_guess_extrapolate")
-
-    def guess_stats_extrapolate(self):
-        """(solves with an extrapolated guess formed, x taken, y taken)"""
-        out = (C.c_longlong * 3)()
-        check(abi.lib().cfd_ctx_guess_stats_extrapolate(self.h, out),
-              "cfd_ctx_guess_stats_extrapolate")
-        return tuple(int(v) for v in out)
-
     def guess_stats_ex(self):
         """(network guesses formed, x and y taken, steps, fields guesses formed, x and y
         taken, 0) since the network was attached."""

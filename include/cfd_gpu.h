@@ -65,7 +65,15 @@ enum {
 enum {
     CFD_GUESS_PREVIOUS = 0,   /* previous step's increment (reference, meshMove.f90:97) */
     CFD_GUESS_ZERO = 1,
-    CFD_GUESS_LEARNED = 2     /* edge message-passing network (falls back to PREVIOUS)  */
+    CFD_GUESS_LEARNED = 2,    /* edge message-passing network (falls back to PREVIOUS)  */
+    /* the last two increments extrapolated to this step (no counterpart in the reference):
+     * a solve's unknown is the step's mesh increment, the mean mesh velocity over the step
+     * times DTMIN; with that velocity linear in time through the last two steps' midpoints
+     * the guess on the free rows is x = c1 x_{n-1} + c2 x_{n-2}, h = (dt_n + dt_1)/(dt_1 +
+     * dt_2), c1 = dt_n/dt_1 (1 + h), c2 = -(dt_n/dt_2) h (2 x_{n-1} - x_{n-2} at a constant
+     * DTMIN); PREVIOUS until two solutions are kept.  The solves reach the same tolerance;
+     * FP64 form and oracle stay bit-identical. */
+    CFD_GUESS_EXTRAPOLATED = 3
 };
 
 /* estab_mode: the "velocity gradient" of ESTAB (subrutinas.f90:380-383) is
@@ -417,17 +425,6 @@ int cfd_ctx_set_guess_refine(cfd_ctx* ctx, int on);
 /* out8 = (steps with a network guess formed, x and y taken from it, steps, steps with a
  * fields guess formed, x and y taken from it, 0) */
 int cfd_ctx_guess_stats_ex(cfd_ctx* ctx, long long* out8);
-/* Second-order guess in time (mixed form; on = 1, default off; no counterpart in the
- * reference, whose guess is the previous step's increment, meshMove.f90:97).  A solve's
- * unknown is the step's mesh increment, the mean mesh velocity over the step times DTMIN;
- * each solve also tries the increment that the last two solutions give with that velocity
- * linear in time, cand = dt_n (v1 + (v1 - v2)(dt_n + dt1)/(dt1 + dt2)), v_k = x_{n-k}/dt_k
- * (2 x_{n-1} - x_{n-2} at a constant DTMIN), and keeps it when its r.z is smaller than the
- * current guess's (previous step's, or the learned guess's when that runs too).  Every
- * solve still reaches the same tolerance.  Switching it on starts the history again. */
-int cfd_ctx_set_guess_extrapolate(cfd_ctx* ctx, int on);
-/* out3 = (solves with an extrapolated guess formed, x and y taken from it) */
-int cfd_ctx_guess_stats_extrapolate(cfd_ctx* ctx, long long* out3);
 
 /* FORCE_VISC (ns2DComp.ALE.f90:819-893): viscous force per force set on its wall edges
  * (F_VX, F_VY: 10 each) and, when skin is not NULL, the SKIN.DAT row of every set edge in

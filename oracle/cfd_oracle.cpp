@@ -1085,6 +1085,9 @@ struct or_case {
     std::vector<double> W_x_old, W_y_old, area_old;
     std::vector<int> esup1, esup2, lap_rowptr, lap_idx;
     std::vector<double> lap_sparse, lap_diag, xpos, ypos;
+    std::vector<double> xprev[2];          // CFD_GUESS_EXTRAPOLATED: x_{n-2} of both solves
+    double xhist_dt[2] = {0.0, 0.0};       // DTMIN of the last two steps
+    int xhist_n = 0;                       // solutions kept
     int m = 0; std::vector<int> n_ipoin; std::vector<double> n_x, n_y;
     int iter = 0, bandera = 1;
     double time = 0.0, dtmin = 0.0, dtmin1 = 0.0, disn[2] = {0.0, 0.0};
@@ -1286,6 +1289,35 @@ void smooth_moved_mesh(or_case* c, double dtmin) {
     }
 }
 
+// CFD_GUESS_EXTRAPOLATED (no counterpart in the reference, whose guess is the previous
+// increment, meshMove.f90:97): the two solves start from the last two increments
+// extrapolated with the mesh velocity linear in time through the last two steps' midpoints,
+// x = c1 x_{n-1} + c2 x_{n-2}, h = (dt_n + dt1)/(dt1 + dt2), c1 = dt_n/dt1 (1 + h),
+// c2 = -(dt_n/dt2) h; the previous increment until two are kept.  The rows biCG fixes are
+// overwritten by their Dirichlet values in the solve.
+void extrapolate_guess(or_case* c, double dtn) {
+    const int N = c->npoin;
+    const bool two = c->xhist_n >= 2;
+    double c1 = 1.0, c2 = 0.0;
+    if (two) {
+        const double h = (dtn + c->xhist_dt[0]) / (c->xhist_dt[0] + c->xhist_dt[1]);
+        c1 = dtn / c->xhist_dt[0] * (1.0 + h);
+        c2 = -(dtn / c->xhist_dt[1]) * h;
+    }
+    double* x[2] = {c->xpos.data(), c->ypos.data()};
+    for (int s = 0; s < 2; ++s) {
+        double* xp = c->xprev[s].data();
+        for (int i = 0; i < N; ++i) {
+            const double x1 = x[s][i];
+            if (two) x[s][i] = c1 * x1 + c2 * xp[i];
+            xp[i] = x1;
+        }
+    }
+    c->xhist_dt[1] = c->xhist_dt[0];
+    c->xhist_dt[0] = dtn;
+    c->xhist_n += 1;
+}
+
 void fluid_structure(or_case* c, double dtmin, double time) {
     const int N = c->npoin;
     std::vector<double> dxpos(N, 0.0), dypos(N, 0.0);
@@ -1325,6 +1357,7 @@ void fluid_structure(or_case* c, double dtmin, double time) {
     c->timers[TM_TRANSF] += tt.sec();
     const int nn = c->nmove + c->nfix_move;
     std::vector<double> pos_aux(nn, 0.0), b(N, 0.0);
+    if (c->p.guess_mode == CFD_GUESS_EXTRAPOLATED) extrapolate_guess(c, dtmin);
     for (int i = 0; i < c->nmove; ++i) pos_aux[i] = dxpos[c->ilaux[i] - 1];
     Clock tg;
     or_bicg_mode(c->lap_sparse.data(), c->lap_idx.data(), c->lap_rowptr.data(), c->lap_diag.data(),
@@ -1403,7 +1436,7 @@ or_case* or_case_create(const cfd_mesh* mesh, const cfd_params* prm, int do_smoo
     z4(c->U); z4(c->U1); z4(c->RHS); z4(c->UN);
     for (auto* v : {&c->T, &c->RHO, &c->E, &c->P, &c->RMACH, &c->VEL_X, &c->VEL_Y, &c->W_X,
                     &c->W_Y, &c->GAMM, &c->M, &c->lap_diag, &c->xpos, &c->ypos, &c->n_x, &c->n_y,
-                    &c->W_x_old, &c->W_y_old})
+                    &c->W_x_old, &c->W_y_old, &c->xprev[0], &c->xprev[1]})
         v->assign(N, 0.0);
     c->n_ipoin.assign(N, 0);
     for (auto* v : {&c->area, &c->DT, &c->DTL, &c->SHOC, &c->TS1, &c->TS2, &c->TS3, &c->area_old})
