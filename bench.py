@@ -66,6 +66,9 @@ def parse():
                     help="instead of the benchmark: the long run of a workload as its "
                          "configuration describes it (histories into --record-out)")
     ap.add_argument("--record-steps", type=int, default=None)
+    ap.add_argument("--record-guess", choices=["previous", "extrapolated"], default="previous",
+                    help="config2: the mesh-motion solves' initial guess (previous: the "
+                         "reference's; extrapolated: CFD_GUESS_EXTRAPOLATED)")
     ap.add_argument("--record-out", default=None, help="JSON file of the record's histories")
     ap.add_argument("--bicg-tol-mode", type=int, default=0,
                     help="BiCG stopping test of the headline run and of --profile-steps "
@@ -574,6 +577,8 @@ def main_record(args):
         k.params.bicg_tol_mode = abi.CFD_BICG_TOL_REL
         k.params.bicg_tol = 1.0e-10
         k.params.bicg_maxit = 20000
+        if args.record_guess == "extrapolated":
+            k.params.guess_mode = abi.CFD_GUESS_EXTRAPOLATED
         S = solver.Solver(k)
         S.set_force_visc(True)
         t0 = time.perf_counter()
@@ -589,7 +594,8 @@ def main_record(args):
         its = np.array([h["bicg_iters"] for h in hist])
         out.update({"workload": f"cylinder O-grid 512x512 ({k.npoin} nodes, {k.nelem} "
                                 f"triangles), Mach 0.3, Re 200, heave 0.2 sin(2 pi 0.2 t), ALE "
-                                f"+ gcl, FP64, BiCG to ||r|| <= 1e-10 ||b - A x_D||",
+                                f"+ gcl, FP64, BiCG to ||r|| <= 1e-10 ||b - A x_D|| from "
+                                f"the {args.record_guess} guess",
                     "steps": n, "ms_per_step": ms, "node_steps_per_s": k.npoin / (ms / 1e3),
                     "wall_s": time.perf_counter() - t0,
                     "bicg_iters_per_solve_mean": its.mean(0).tolist(),
