@@ -545,6 +545,37 @@ def run_cpu_baselines(k_fn, threads_all):
     return out
 
 
+def config1_report(threads_all, steps=2000):
+    """The reference's CPU-runnable case run fully (the 8,192-node cylinder, fixed mesh,
+    2000 steps): the FP64 form on the GPU (device time over one cfd_step call) and the
+    oracle on all host cores and on one core, node-steps/s each."""
+    from cfd_gb300 import abi, case as C, solver
+    from oracle import oracle as O
+    out = {"workload": "cylinder O-grid 64x128 (8192 nodes, 16128 triangles), Mach 0.3, "
+                       "Re 100, fixed mesh, FP64, reference ESTAB", "steps": steps}
+    k = C.config_case(1)
+    S = solver.Solver(k)
+    S.step(3)
+    S.mark(0)
+    S.step(steps)
+    S.mark(1)
+    ms = S.elapsed_ms(0, 1) / steps
+    S.close()
+    out["gpu_fp64"] = {"value": k.npoin / (ms / 1e3), "unit": UNIT, "ms_per_step": ms}
+    for label, threads in (("oracle_all_cores", threads_all), ("oracle_one_core", 1)):
+        O.set_threads(threads)
+        oc = O.OracleCase(C.config_case(1))
+        oc.step(3)
+        t = time.perf_counter()
+        oc.step(steps)
+        sec = (time.perf_counter() - t) / steps
+        oc.close()
+        out[label] = {"value": k.npoin / sec, "unit": UNIT, "cores": threads, "kind": "port",
+                      "ms_per_step": sec * 1e3}
+    O.set_threads(1)
+    return out
+
+
 def lift_drag(rep, S):
     """Drag and lift of body set 1 as the reference's FORCES file takes them: pressure
     (FX, FY of FORCES, meshMove.f90:153-194) plus viscous (F_VX, F_VY of FORCE_VISC,
@@ -819,6 +850,8 @@ def main_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         cb = run_cpu_baselines(lambda: workload(args), os.cpu_count() or 1)
         cpu, cpu1 = cb["all_cores"], cb["one_core"]
+        if mixed and args.scale is None and not args.no_compare:
+            forms["config1_gpu_vs_cpu"] = config1_report(os.cpu_count() or 1)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": sec_step * 1e3, "higher_is_better": True,
