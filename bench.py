@@ -646,13 +646,18 @@ def main_record(args):
         k = C.config_case(5)
         k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED
         k.params.guess_mode = abi.CFD_GUESS_LEARNED
+        if args.bicg_tol_mode:  # the configs' relative test instead of the reference's
+            k.params.bicg_tol_mode = args.bicg_tol_mode
+            k.params.bicg_maxit = 20000
         S = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
         S.set_guess_net(net, 1.0e9)
         S.set_guess_refine(True)
-        fm = []
+        fm, its = [], []
         S.mark(0)
         for s in range(1, nf + 1):
-            fm.append(forces(S.step(1)))
+            rs = S.step(1)
+            fm.append(forces(rs))
+            its.append(list(rs.bicg_iters))
         S.mark(2)
         r = S.step(n - nf) if n > nf else S.step(0)
         S.mark(1)
@@ -667,9 +672,15 @@ def main_record(args):
                     "steps": n, "ms_per_step": ms, "value": k.npoin / (ms / 1e3),
                     "ms_per_step_after_force_window": ms_tail,
                     "bicg_iters_last": list(r.bicg_iters), "guess_stats_ex": list(gs),
+                    "bicg_test": "relative" if args.bicg_tol_mode else "absolute (reference)",
+                    "bicg_iters_per_step_force_window": {
+                        "first": its[0], "mean_after_first": (np.array(its[1:]).sum(1).mean()
+                                                              if len(its) > 1 else None)},
                     "state_finite": bool(np.isfinite(Um).all())})
-        for estab, name in ((abi.CFD_ESTAB_REGULARIZED, "fp64_regularized"),
-                            (abi.CFD_ESTAB_REFERENCE, "fp64_reference")):
+        # the FP64 comparison runs belong to the absolute-test record
+        for estab, name in (() if args.bicg_tol_mode else
+                            ((abi.CFD_ESTAB_REGULARIZED, "fp64_regularized"),
+                             (abi.CFD_ESTAB_REFERENCE, "fp64_reference"))):
             kd = C.config_case(5)
             kd.params.estab_mode = estab
             Sd = solver.Solver(kd)
@@ -689,7 +700,7 @@ def main_record(args):
                 "rel_err_final": [float(abs(Fm[m - 1, c] - Fd[m - 1, c]) / fmax)
                                   for c in range(2)]}
             hist.append({name: Fd.tolist()})
-        hist.append({"mixed": fm})
+        hist.append({"mixed": fm, "bicg_iters": its})
     if args.record_out:
         with open(args.record_out, "w") as f:
             json.dump({"summary": out, "history": hist}, f)
