@@ -206,6 +206,11 @@ __global__ void k_elem_geometry(int nelem, const int4* elem, const double* X, co
                                 int put_area, double* area_old, double* area64, float* areaf,
                                 float4* geo, double2* terms, NormalsArgs nv);
 constexpr int kGeoNodeBlock = 128;  // block size of k_node_geometry
+__global__ void k_elem_grad64(int nelem, const int4* elem, const double* X, const double* Y,
+                              double4* g64);
+__global__ void k_lap64(int npoin, const int* esup_ptr, const int* esup_slot,
+                        const uchar4* lap_pos, const double4* g64, const int* rowptr,
+                        float* valf, float* val_lo, double* invdiag, float* invdiagf);
 __global__ void k_node_geometry(int npoin, const int* esup_ptr, const int* esup_slot,
                                 const uchar4* lap_pos, const float4* geo, const double2* terms,
                                 const double* dtp, int gcl, const int* rowptr, float* valf,
@@ -318,6 +323,8 @@ struct PcgArgs {
     double* part;                // [2 phases][2 solves][nchunks] chunk partial sums
     // mixed form only: FP32 matrix values, 1/diag, FP32 shadows of p (ping-pong) and z
     const float* valf;
+    const float* val_lo;         // relative tests: valf + val_lo = the FP64-assembled matrix
+                                 // to 2^-47 (null: valf alone)
     const double* invdiag;
     float* pf[2][2];
     float* zf[2];

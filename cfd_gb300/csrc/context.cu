@@ -169,6 +169,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
     const bool mixed = (prec == CFD_PREC_MIXED);
     if (mixed) {
         a.valf = d_valf;
+        a.val_lo = d_val_lo;
         a.invdiag = d_invdiag;
         for (int s = 0; s < 2; ++s) {
             a.pf[s][0] = d_pf[s][0];
@@ -837,6 +838,10 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         CFD_CUDA(cudaMemsetAsync(d_bscal, 0, 16 * sizeof(double), stream));
         CFD_CUDA(cudaMemsetAsync(d_bcount, 0, 3 * sizeof(unsigned), stream));
         if ((st = dalloc(&d_valf, adj.col.size()))) return st;
+        if (prm.bicg_tol_mode != CFD_BICG_TOL_ABS) {  // the FP64-assembled operator
+            if ((st = dalloc(&d_val_lo, adj.col.size()))) return st;
+            if ((st = dalloc(&d_g64, 2 * (size_t)E))) return st;
+        }
         if ((st = dalloc(&d_gterms, E))) return st;
         // slot (e, i) -> its position in element-around-point order
         std::vector<int> pos(3 * (size_t)E);
@@ -939,6 +944,13 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
                d_esup_ptr, d_esup_slot, d_lap_pos, geo8, d_gterms, &d_scal->dtmin, gcl ? 1 : 0,
                d_rowptr, d_valf, d_invdiag, d_invdiagf, d_M, invMf, Wn,
                to_next ? (float2*)nullptr : d_Wof);
+    if (d_val_lo) {  // relative tests: the mesh-motion operator again, in FP64 (k_lap64)
+        CFD_LAUNCH(k_elem_grad64, branch_grid(E, TB, sv), TB, 0, stream, E, d_elem, d_X, d_Y,
+                   d_g64);
+        CFD_LAUNCH(k_lap64, branch_grid(N, 128, sv), 128, 0, stream, N, d_esup_ptr, d_esup_slot,
+                   d_lap_pos, (const double4*)d_g64, d_rowptr, d_valf, d_val_lo, d_invdiag,
+                   d_invdiagf);
+    }
     tstop(TM_LAPLACE);
     return CFD_OK;
 }

@@ -841,6 +841,91 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     }
 }
 
+// The mesh-motion matrix assembled in FP64 (the mixed form under the relative stopping
+// tests).  The FP32 assembly above rounds every entry afresh each step; the entries move by
+// far more than an ulp per step, so that rounding is new noise in every step's operator,
+// and the previous steps' solutions carry it into this step's residual (~1e-7 of it): a
+// floor under every guess built from them.  Assembled in FP64 and held as valf + val_lo
+// (split_bits, 2^-47), the operator moves as smoothly as the mesh, the first residual (the
+// precise product) sees only that, and the FP32 iterations keep valf.
+// Per element: the FP64 gradients and Laplacian weight q of mLaplace.f90:28-56, as the FP32
+// element pass forms them (edge vectors from the first node, q = (a sum|grad N_i|^2)^2/3).
+__global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
+                              const double* __restrict__ X, const double* __restrict__ Y,
+                              double4* __restrict__ g64) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += gridDim.x * blockDim.x) {
+        const int4 n = elem[e];
+        const double X0 = X[n.x], Y0 = Y[n.x];
+        const double x1 = X[n.y] - X0, y1 = Y[n.y] - Y0;
+        const double x2 = X[n.z] - X0, y2 = Y[n.z] - Y0;
+        const double a2 = x1 * y2 - x2 * y1;
+        const double ia = 1.0 / a2;
+        const double gx0 = (y1 - y2) * ia, gx1 = y2 * ia, gx2 = -y1 * ia;
+        const double gy0 = (x2 - x1) * ia, gy1 = -x2 * ia, gy2 = x1 * ia;
+        const double s2 = gx0 * gx0 + gy0 * gy0 + gx1 * gx1 + gy1 * gy1 + gx2 * gx2 + gy2 * gy2;
+        const double am = 0.5 * a2 * s2;
+        g64[2 * (size_t)e] = make_double4(gx0, gx1, gx2, gy0);
+        g64[2 * (size_t)e + 1] = make_double4(gy1, gy2, am * am * (1.0 / 3.0), 0.0);
+    }
+}
+
+// Per node: the FP64 row (in shared memory; rows longer than kLapRow summed per entry),
+// written as valf + val_lo, and 1/diag from the FP64 diagonal
+constexpr int kLap64Block = 128;
+__global__ void __launch_bounds__(kLap64Block)
+k_lap64(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
+        const uchar4* __restrict__ lap_pos, const double4* __restrict__ g64,
+        const int* __restrict__ rowptr, float* __restrict__ valf, float* __restrict__ val_lo,
+        double* __restrict__ invdiag, float* __restrict__ invdiagf) {
+    __shared__ double row[kLap64Block][kLapRow + 1];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npoin; p += gridDim.x * blockDim.x) {
+        double* acc = row[threadIdx.x];
+        const int r0 = rowptr[p], len = rowptr[p + 1] - r0;
+        const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
+        const int nk = len <= kLapRow ? 1 : len;  // passes: one, or one per entry
+        double diag = 0.0;
+        for (int kk = 0; kk < nk; ++kk) {
+#pragma unroll
+            for (int k = 0; k < kLapRow; ++k) acc[k] = 0.0;
+            double one = 0.0;  // the entry kk of a long row
+            for (int sl = s0; sl < s1; ++sl) {
+                const int slot = esup_slot[sl];
+                const int e = slot / 3, i = slot - 3 * e;
+                const double4 ga = g64[2 * (size_t)e], gb = g64[2 * (size_t)e + 1];
+                const double gx[3] = {ga.x, ga.y, ga.z}, gy[3] = {ga.w, gb.x, gb.y};
+                const double q = gb.z;
+                const double dxi = gx[i], dyi = gy[i];
+                const uchar4 pos = lap_pos[sl];
+                const unsigned char pj[3] = {pos.x, pos.y, pos.z};
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const double v = (dxi * gx[j] + dyi * gy[j]) * q;
+                    if (nk == 1) acc[pj[j]] += v;
+                    else if (pj[j] == kk) one += v;
+                }
+            }
+            if (nk == 1) {
+                for (int k = 0; k < len; ++k) {
+                    float hi, lo;
+                    split_bits(acc[k], hi, lo);
+                    valf[r0 + k] = hi;
+                    val_lo[r0 + k] = lo;
+                }
+                diag = acc[0];
+            } else {
+                float hi, lo;
+                split_bits(one, hi, lo);
+                valf[r0 + kk] = hi;
+                val_lo[r0 + kk] = lo;
+                if (kk == 0) diag = one;
+            }
+        }
+        const float idf = d2f_trunc(1.0 / diag);
+        invdiagf[p] = idf;
+        invdiag[p] = f2d_bits(idf);
+    }
+}
+
 // geo -> the FP64 dNx/dNy (column-major [6][nelem]) and area the download entries read
 __global__ void k_widen_geo(int nelem, const float4* __restrict__ geo, double* __restrict__ dN,
                             double* __restrict__ area) {

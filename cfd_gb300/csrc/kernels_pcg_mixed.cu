@@ -69,7 +69,9 @@ __device__ __forceinline__ void spmv_row2_f(const PcgArgs& a, int i, const float
 // split into FP32 hi + lo (split_bits, exact to 2^-47), a_ij*hi is formed exactly as a
 // float pair (product + fmaf remainder), the products are summed with a compensated (Neumaier)
 // FP32 sum and the remainders and a_ij*lo terms with a plain one, and the three partial
-// sums are added in FP64.  The first residual of a solve, r = b - A.x, takes this product
+// sums are added in FP64; with val_lo (the relative tests: the matrix assembled in FP64 and
+// held as valf + val_lo) the a_lo*hi terms join the plain sum.  The first residual of a
+// solve, r = b - A.x, takes this product
 // under the relative stopping tests: it is the one SpMV of the solve whose operand is the
 // whole displacement rather than a correction, so an FP32 product's error there (~1e-7 of
 // |A||x|) would be a floor under the starting residual of any good initial guess.  The
@@ -78,7 +80,7 @@ __device__ __forceinline__ void spmv_row2_f(const PcgArgs& a, int i, const float
 struct Acc2 {
     float s, c, t;  // compensated sum s + c of the exact products' leading parts; tail sum t
     __device__ __forceinline__ void init() { s = c = t = 0.f; }
-    __device__ __forceinline__ void add(float m, double x) {
+    __device__ __forceinline__ void add(float m, double x, float mlo = 0.f) {
         float hi, lo;
         split_bits(x, hi, lo);
         const float p = m * hi;
@@ -87,7 +89,7 @@ struct Acc2 {
         if (fabsf(s) >= fabsf(p)) c += (s - u) + p;
         else c += (p - u) + s;
         s = u;
-        t += e + m * lo;
+        t += e + m * lo + mlo * hi;
     }
     __device__ __forceinline__ double value() const {
         return (f2d_bits(s) + f2d_bits(c)) + f2d_bits(t);
@@ -105,7 +107,7 @@ __device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const doubl
     const int j0 = a.rowptr[i], j1 = a.rowptr[i + 1];
     for (int jb = j0; jb < j1; jb += kRowBatch) {
         int c[kRowBatch];
-        float m[kRowBatch];
+        float m[kRowBatch], ml[kRowBatch];
         double x0[kRowBatch], x1[kRowBatch];
         bool fx[kRowBatch];
 #pragma unroll
@@ -113,6 +115,7 @@ __device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const doubl
             if (jb + u < j1) {
                 c[u] = a.col[jb + u];
                 m[u] = a.valf[jb + u];
+                ml[u] = a.val_lo ? a.val_lo[jb + u] : 0.f;
             }
 #pragma unroll
         for (int u = 0; u < kRowBatch; ++u)
@@ -124,8 +127,8 @@ __device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const doubl
 #pragma unroll
         for (int u = 0; u < kRowBatch; ++u)
             if (jb + u < j1) {
-                s0.add(m[u], x0[u]);
-                if (NS == 2) s1.add(m[u], x1[u]);
+                s0.add(m[u], x0[u], ml[u]);
+                if (NS == 2) s1.add(m[u], x1[u], ml[u]);
                 if (FIXC && fx[u]) {
                     g0 += m[u] * d2f_trunc(x0[u]);
                     if (NS == 2) g1 += m[u] * d2f_trunc(x1[u]);
@@ -513,6 +516,10 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
     const long nc = ((long)n + kChunk - 1) / kChunk;
     const unsigned nb = gridDim.x;
     auto part = [&](int buf, int s) { return a.part + ((long)buf * 2 + s) * nc; };
+    // each block owns one contiguous range of rows (a multiple of 256, so the ranges differ
+    // by at most 256 rows between blocks) and leaves one partial per sum
+    const long R = (((long)n + nb - 1) / nb + 255) / 256 * 256;
+    const long rb = blockIdx.x * R, re = min((long)n, rb + R);
 
     // x(fix), r, p, err = r.p, y = A.p and alfa come from k_bicg_fix_mixed,
     // k_bicg_resid_mixed and k_bicg_dir_mixed
@@ -564,12 +571,12 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
         // phase 1: x += alfa p; r -= alfa y; z = r/diag; r.z (and r.r, relative modes).
         // A thread's four rows of a chunk are loaded together, then updated, so that their
         // loads are in flight at once.
-        for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-            double acc[2] = {0.0, 0.0}, accr[2] = {0.0, 0.0};
-            const long i0 = c * kChunk + t;
+        {
+        double acc[2] = {0.0, 0.0}, accr[2] = {0.0, 0.0};
+        for (long i0 = rb + t; i0 < re; i0 += kChunk) {
             double id[4];
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) id[kk] = (i0 + 256L * kk < n) ? a.invdiag[i0 + 256L * kk] : 0.0;
+            for (int kk = 0; kk < 4; ++kk) id[kk] = (i0 + 256L * kk < re) ? a.invdiag[i0 + 256L * kk] : 0.0;
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
                 if (!pend[s] && !act[s]) continue;
@@ -583,7 +590,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk) {
                     const long i = i0 + 256L * kk;
-                    const bool in = i < n;
+                    const bool in = i < re;
                     xv[kk] = (in && pend[s]) ? xs[i] : 0.0;
                     pv[kk] = (in && pend[s]) ? ps[i] : 0.0;
                     rv[kk] = (in && act[s]) ? rs[i] : 0.0;
@@ -592,7 +599,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk) {
                     const long i = i0 + 256L * kk;
-                    if (i >= n) break;
+                    if (i >= re) break;
                     if (pend[s]) xs[i] = xv[kk] + alfa[s] * pv[kk];
                     if (!act[s]) continue;
                     const double ri = rv[kk] - alfa[s] * yv[kk];
@@ -600,10 +607,11 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                     rs[i] = ri;
                     zs[i] = zi;
                     zfs[i] = d2f_trunc(zi);
-                    acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
-                    if (rel) accr[s] = (kk == 0) ? ri * ri : accr[s] + ri * ri;
+                    acc[s] = acc[s] + ri * zi;
+                    if (rel) accr[s] = accr[s] + ri * ri;
                 }
             }
+        }
             double v[4] = {0.0, 0.0, 0.0, 0.0};
             int m = 0;
 #pragma unroll
@@ -618,8 +626,8 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
 #pragma unroll
                 for (int s = 0; s < 2; ++s) {
                     if (!act[s]) continue;
-                    part(1, s)[c] = v[j++];
-                    if (rel) part(2, s)[c] = v[j++];
+                    part(1, s)[blockIdx.x] = v[j++];
+                    if (rel) part(2, s)[blockIdx.x] = v[j++];
                 }
             }
         }
@@ -639,7 +647,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                 src[m++] = part(1, s);
                 if (rel) src[m++] = part(2, s);
             }
-            fold_m(src, m, nc, sh, res, out);
+            fold_m(src, m, (long)nb, sh, res, out);
             int j = 0;
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
@@ -657,9 +665,9 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
         // phase 2: p_new = beta p + z (FP64 for the row, FP32 shadow for the SpMV); y = A p_new.
         // Per solve, a thread's rows go in pairs: the two rows' pointers, p and z, then their
         // column batches and gathers are issued together.
-        for (long c = blockIdx.x; c < nc; c += gridDim.x) {
-            double acc[2] = {0.0, 0.0};
-            const long i0 = c * kChunk + t;
+        {
+        double acc[2] = {0.0, 0.0};
+        for (long i0 = rb + t; i0 < re; i0 += kChunk) {
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
                 if (!act[s]) continue;
@@ -679,7 +687,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
 #pragma unroll
                     for (int q = 0; q < 2; ++q) {
                         ii[q] = i0 + 256L * (kp + q);
-                        in[q] = ii[q] < n;
+                        in[q] = ii[q] < re;
                         fx[q] = in[q] ? a.isfix[ii[q]] != 0 : true;
                         j0[q] = (in[q] && !fx[q]) ? a.rowptr[ii[q]] : 0;
                         j1[q] = (in[q] && !fx[q]) ? a.rowptr[ii[q] + 1] : 0;
@@ -723,10 +731,11 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                         pn_out[ii[q]] = pn;
                         pfn_out[ii[q]] = d2f_trunc(pn);
                         ys[ii[q]] = yi;
-                        acc[s] = (kp + q == 0) ? pn * yi : acc[s] + pn * yi;
+                        acc[s] = acc[s] + pn * yi;
                     }
                 }
             }
+        }
             double v[4] = {0.0, 0.0, 0.0, 0.0};
             int m = 0;
 #pragma unroll
@@ -737,7 +746,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                 int j = 0;
 #pragma unroll
                 for (int s = 0; s < 2; ++s)
-                    if (act[s]) part(0, s)[c] = v[j++];
+                    if (act[s]) part(0, s)[blockIdx.x] = v[j++];
             }
         }
         grid_barrier(a.bar, nb);
@@ -749,7 +758,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
 #pragma unroll
             for (int s = 0; s < 2; ++s)
                 if (act[s]) src[m++] = part(0, s);
-            fold_m(src, m, nc, sh, res, pyv);
+            fold_m(src, m, (long)nb, sh, res, pyv);
         }
         int jpy = 0;
 #pragma unroll
