@@ -22,6 +22,7 @@ CFD_PREC_FP64, CFD_PREC_MIXED = 0, 1
 CFD_MASS_MASAS, CFD_MASS_GCL_LITERAL, CFD_MASS_GCL_CORRECTED = 0, 1, 2
 CFD_MOTION_REFERENCE, CFD_MOTION_HARMONIC, CFD_MOTION_NEWMARK = 0, 1, 2
 CFD_GUESS_PREVIOUS, CFD_GUESS_ZERO, CFD_GUESS_LEARNED, CFD_GUESS_EXTRAPOLATED = 0, 1, 2, 3
+CFD_GUESS_LEARNED_EXTRAPOLATED = 4
 CFD_ESTAB_REFERENCE, CFD_ESTAB_EXACT, CFD_ESTAB_REGULARIZED = 0, 1, 2
 CFD_BICG_TOL_ABS, CFD_BICG_TOL_REL, CFD_BICG_TOL_REL_R0 = 0, 1, 2
 CFD_SMOOTH_COLOUR, CFD_SMOOTH_NODE_ORDER = 0, 1

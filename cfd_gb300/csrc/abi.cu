@@ -238,7 +238,7 @@ int cfd_ctx_create(cfd_ctx** out, const cfd_mesh* mesh, const cfd_params* p, int
         return arg_error("estab_mode");
     if (p->bicg_tol_mode < CFD_BICG_TOL_ABS || p->bicg_tol_mode > CFD_BICG_TOL_REL_R0)
         return arg_error("bicg_tol_mode");
-    if (p->guess_mode < CFD_GUESS_PREVIOUS || p->guess_mode > CFD_GUESS_EXTRAPOLATED)
+    if (p->guess_mode < CFD_GUESS_PREVIOUS || p->guess_mode > CFD_GUESS_LEARNED_EXTRAPOLATED)
         return arg_error("guess_mode");
     if (p->ngas != 0) {
         set_last_message("only the perfect-gas path (NGAS = 0) is implemented");

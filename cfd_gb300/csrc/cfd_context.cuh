@@ -217,6 +217,13 @@ struct Ctx {
                 cudaStream_t sv = nullptr);
     int set_guess_refine(bool on);
     int guess_buffers();
+    bool learned_mode() const {
+        return prm.guess_mode == CFD_GUESS_LEARNED || prm.guess_mode == CFD_GUESS_LEARNED_EXTRAPOLATED;
+    }
+    bool extrap_mode() const {
+        return prm.guess_mode == CFD_GUESS_EXTRAPOLATED ||
+               prm.guess_mode == CFD_GUESS_LEARNED_EXTRAPOLATED;
+    }
     int guess_extrapolate(const PcgArgs& a, cudaStream_t s, unsigned grid);
     int enqueue_mixed(bool learned);
     int launch_step_graph(bool* launched);

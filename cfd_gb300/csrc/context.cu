@@ -185,7 +185,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         // learned guess (decided by the caller): k_guess_judge keeps, per solve, the
         // network's guess or the previous step's, whichever has the smaller r.z.  Between
         // network runs, with the refined guess on, the candidate is the fields' guess.
-        const bool with_net = prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph;
+        const bool with_net = learned_mode() && net && lgraph;
         const bool fields = with_net && guess_refine && !learned && fields_ready;
         a.gflag = (learned || fields) ? d_gflag : nullptr;
         a.gate = 0.0;
@@ -196,7 +196,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         const unsigned rgrid = (sv && branch_bpsm > 0)
                                    ? (unsigned)std::min<long>(a.nblk_r, (long)branch_bpsm * nsm)
                                    : (unsigned)a.nblk_r;
-        if (prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+        if (extrap_mode()) {
             int st = guess_extrapolate(a, stream, rgrid);
             if (st) return st;
         }
@@ -237,7 +237,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         }
         CFD_LAUNCH(k_bicg_dir_mixed, rgrid, 256, 0, stream, a);
     }
-    if (!mixed && prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+    if (!mixed && extrap_mode()) {
         int st = guess_extrapolate(a, stream, blocks_for(npoin, 256));
         if (st) return st;
     }
@@ -247,7 +247,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
                                          dim3(256), args, 0, stream));
     g_launches.fetch_add(1, std::memory_order_relaxed);
     // refined learned guess: the solutions correct the basis fields
-    if (mixed && prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph && guess_refine &&
+    if (mixed && learned_mode() && net && lgraph && guess_refine &&
         fields_ready) {
         int st = mpnn::fields_update(lgraph, stream, d_pos[0], d_pos[1]);
         if (st) return st;
@@ -753,12 +753,12 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_xfix[s], nnmove))) return st;
         CFD_CUDA(cudaMemsetAsync(d_pos[s], 0, sizeof(double) * N, stream));
         CFD_CUDA(cudaMemsetAsync(d_xfix[s], 0, sizeof(double) * (nnmove ? nnmove : 1), stream));
-        if (prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+        if (extrap_mode()) {
             if ((st = dalloc(&d_xprev[s], N))) return st;
             CFD_CUDA(cudaMemsetAsync(d_xprev[s], 0, sizeof(double) * N, stream));
         }
     }
-    if (prm.guess_mode == CFD_GUESS_EXTRAPOLATED) {
+    if (extrap_mode()) {
         if ((st = dalloc(&d_xhist, 3))) return st;
         CFD_CUDA(cudaMemsetAsync(d_xhist, 0, 3 * sizeof(double), stream));
     }
@@ -1179,7 +1179,7 @@ int Ctx::launch_step_graph(bool* launched) {
 int Ctx::step_once_mixed() {
     iter += 1;
     bool learned = false;
-    if (prm.guess_mode == CFD_GUESS_LEARNED && net && lgraph) {
+    if (learned_mode() && net && lgraph) {
         guess_steps += 1;
         if (!guess_first && guess_gate > 0.0) CFD_CUDA(cudaEventSynchronize(ev_iters));
         learned = guess_first || guess_gate <= 0.0 ||

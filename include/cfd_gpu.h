@@ -73,7 +73,11 @@ enum {
      * dt_2), c1 = dt_n/dt_1 (1 + h), c2 = -(dt_n/dt_2) h (2 x_{n-1} - x_{n-2} at a constant
      * DTMIN); PREVIOUS until two solutions are kept.  The solves reach the same tolerance;
      * FP64 form and oracle stay bit-identical. */
-    CFD_GUESS_EXTRAPOLATED = 3
+    CFD_GUESS_EXTRAPOLATED = 3,
+    /* LEARNED with EXTRAPOLATED as the guess the network's and the fields' guesses are
+     * judged against (per solve: the x and y solves of a pitching body can prefer
+     * different guesses) */
+    CFD_GUESS_LEARNED_EXTRAPOLATED = 4
 };
 
 /* estab_mode: the "velocity gradient" of ESTAB (subrutinas.f90:380-383) is

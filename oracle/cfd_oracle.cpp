@@ -1357,7 +1357,9 @@ void fluid_structure(or_case* c, double dtmin, double time) {
     c->timers[TM_TRANSF] += tt.sec();
     const int nn = c->nmove + c->nfix_move;
     std::vector<double> pos_aux(nn, 0.0), b(N, 0.0);
-    if (c->p.guess_mode == CFD_GUESS_EXTRAPOLATED) extrapolate_guess(c, dtmin);
+    if (c->p.guess_mode == CFD_GUESS_EXTRAPOLATED ||
+        c->p.guess_mode == CFD_GUESS_LEARNED_EXTRAPOLATED)  // no network here: its fallback
+        extrapolate_guess(c, dtmin);
     for (int i = 0; i < c->nmove; ++i) pos_aux[i] = dxpos[c->ilaux[i] - 1];
     Clock tg;
     or_bicg_mode(c->lap_sparse.data(), c->lap_idx.data(), c->lap_rowptr.data(), c->lap_diag.data(),

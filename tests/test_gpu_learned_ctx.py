@@ -68,3 +68,32 @@ def test_gate_runs_the_network_on_the_cold_solve_only(gpu_lib):
     # after the cold solve, steps whose solve took >= 1 iteration trigger the next one
     expect = 1 + sum(1 for r in reps2[:-1] if max(r.bicg_iters) > 0.5)
     assert stats2[0] == expect and stats2[3] == 6
+
+
+def test_refined_guess_under_the_relative_test(gpu_lib):
+    """Under the 1e-10 relative test the mixed form assembles the mesh-motion operator in
+    FP64 as well (the first residual's precise product): the refined learned guess then
+    meets the test in far fewer iterations than the previous step's increment, and every
+    solve still reaches the test."""
+    from cfd_gb300 import abi, learned, solver
+    if not os.path.exists(learned.DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights in the package")
+    net = learned.Net.load()
+    its = {}
+    for refined in (False, True):
+        k = small_case(3, scale=96, seed=13, estab_mode=abi.CFD_ESTAB_REGULARIZED, fsafe=0.25,
+                       bicg_tol_mode=abi.CFD_BICG_TOL_REL, bicg_maxit=20000)
+        if refined:
+            k.params.guess_mode = abi.CFD_GUESS_LEARNED
+        S = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+        if refined:
+            S.set_guess_net(net, 1.0e9)
+            S.set_guess_refine(True)
+        per_step = []
+        for _ in range(8):
+            r = S.step(1)
+            assert all(r.bicg_converged) and max(r.bicg_relres) <= 1e-10
+            per_step.append(sum(r.bicg_iters))
+        its[refined] = per_step
+        S.close()
+    assert sum(its[True][3:]) * 4 < sum(its[False][3:]), its
