@@ -346,6 +346,8 @@ struct PcgArgs {
     int tol_mode;                // CFD_BICG_TOL_*: the relative modes also sum r.r per
                                  // iteration, in part[2][s] (part then holds 6 x nchunks)
     int* iters_out;              // [2]
+    int accumulate;              // mixed form: a second pass of the same solves (iterations
+                                 // add to iters_out, the cap counts both passes)
     double* rz_out;              // [2]
     double* relres_out;          // [2] ||r||/||ref|| (relative modes), may be null
     int* conv_out;               // [2]

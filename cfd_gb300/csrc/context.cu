@@ -246,6 +246,25 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
     CFD_CUDA(cudaLaunchCooperativeKernel(mixed ? (void*)k_pcg_mixed : (void*)k_pcg_fp64, dim3(pcg_grid),
                                          dim3(256), args, 0, stream));
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (mixed && prm.bicg_tol_mode == CFD_BICG_TOL_REL) {
+        // refinement: the FP32 iterations meet the test on their recursive residual; the
+        // precise residual of the solution (against the FP64-assembled matrix) is formed
+        // again, and the solves that it leaves above the test iterate once more
+        PcgArgs b = a;
+        b.gflag = nullptr;
+        b.only_if = nullptr;
+        b.accumulate = 1;
+        const unsigned rgrid = (sv && branch_bpsm > 0)
+                                   ? (unsigned)std::min<long>(b.nblk_r, (long)branch_bpsm * nsm)
+                                   : (unsigned)b.nblk_r;
+        CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, b));
+        CFD_LAUNCH(k_bicg_dir_mixed, rgrid, 256, 0, stream, b);
+        CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
+        void* bargs[] = {&b};
+        CFD_CUDA(cudaLaunchCooperativeKernel((void*)k_pcg_mixed, dim3(pcg_grid), dim3(256), bargs, 0,
+                                             stream));
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    }
     // refined learned guess: the solutions correct the basis fields
     if (mixed && learned_mode() && net && lgraph && guess_refine &&
         fields_ready) {

@@ -535,15 +535,17 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
         s_thr[t] = a.bscal[8 * t + 5];
     }
     __syncthreads();
+    int prev[2] = {0, 0};  // a second pass: the first pass's iterations
 #pragma unroll
     for (int s = 0; s < 2; ++s)
         if (s < ns) {
             const double rr = a.bscal[8 * s];
             done[s] = first_done(a, s);
+            if (a.accumulate) prev[s] = *((volatile const int*)&a.iters_out[s]);
             if (rel) rrc[s] = rr;
             if (done[s]) {
                 if (blockIdx.x == 0 && t == 0) {
-                    a.iters_out[s] = 0;
+                    if (!a.accumulate) a.iters_out[s] = 0;
                     a.rz_out[s] = rr;
                     a.conv_out[s] = 1;
                     if (a.relres_out)
@@ -565,7 +567,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             act[s] = !done[s] && (rel ? rrc[s] > s_thr[s] : fabs(err_old[s]) > a.tol) &&
-                     k < a.maxit;
+                     k + prev[s] < a.maxit;
         if (!act[0] && !act[1]) break;
         k = k + 1;
         // phase 1: x += alfa p; r -= alfa y; z = r/diag; r.z (and r.r, relative modes).
@@ -792,7 +794,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (done[s]) continue;
-            a.iters_out[s] = last_iter[s];
+            a.iters_out[s] = prev[s] + last_iter[s];
             a.rz_out[s] = fabs(err_old[s]);
             a.conv_out[s] = (rel ? rrc[s] > s_thr[s] : fabs(err_old[s]) > a.tol) ? 0 : 1;
             if (a.relres_out)

@@ -159,11 +159,13 @@ def test_gpu_step_relative_mode_bit_exact(gpu_lib):
 
 @pytest.mark.gpu
 def test_gpu_mixed_relative_mode(gpu_lib, oracle):
-    """The mixed form's solve under CFD_BICG_TOL_REL: it converges on its own test (FP32
-    SpMV, FP64 vectors) in about the FP64 form's iterations, and the mesh increments it
-    solves for stay within the FP32 operator's accuracy of the FP64 form's: the mixed form
-    assembles the Laplacian in FP32 (entries within ~1e-7), and the solve amplifies that by
-    the operator's conditioning (~1e3 here), so the increments agree to ~1e-4."""
+    """The mixed form's solve under CFD_BICG_TOL_REL: FP32 iterations against the precise
+    residual of the FP64-assembled matrix, with a refinement pass when the first pass's
+    recursive residual met the test before the precise one did; it takes at most about
+    twice the FP64 form's iterations (the first pass and the refinement), and the mesh
+    increments it solves for stay within the FP32 iterations' accuracy of the FP64 form's
+    (the solve amplifies the FP32 matrix's ~1e-7 by the operator's conditioning, ~1e3 here,
+    so the increments agree to ~1e-4)."""
     from cfd_gb300 import abi, solver
     k = small_case(2, scale=24, seed=8, pitch_amp=math.radians(4.0), motion_freq=2.0,
                    mass_mode=abi.CFD_MASS_GCL_CORRECTED, bicg_tol_mode=abi.CFD_BICG_TOL_REL,
@@ -174,7 +176,7 @@ def test_gpu_mixed_relative_mode(gpu_lib, oracle):
         rm, rd = gm.step(1), gd.step(1)
         assert all(rm.bicg_converged) and max(rm.bicg_relres) <= 1e-10
         for q in range(2):
-            assert abs(rm.bicg_iters[q] - rd.bicg_iters[q]) <= 0.2 * rd.bicg_iters[q] + 3, (
+            assert 0.8 * rd.bicg_iters[q] - 3 <= rm.bicg_iters[q] <= 2 * rd.bicg_iters[q] + 10, (
                 s, tuple(rm.bicg_iters), tuple(rd.bicg_iters))
         for q, (a, b) in enumerate(zip(gm.motion(), gd.motion())):
             d = np.abs(a - b).max() / np.abs(b).max()
