@@ -148,6 +148,7 @@ SIGNATURES = {
     "cfd_smoothing_ex": (C.c_int, [_dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _ip, _dp, C.c_int]),
     "cfd_selftest_waits": (C.c_int, [C.c_longlong, _ip, _ip]),
     "cfd_selftest_div3": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]),
+    "cfd_selftest_div_rcp": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]),
     "cfd_ctx_set_smoothing": (C.c_int, [_P, C.c_int]),
     "cfd_ctx_smoothing_stats": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "cfd_smoothing": (C.c_int, [_dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _ip, _dp]),

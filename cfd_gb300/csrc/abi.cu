@@ -160,6 +160,21 @@ int cfd_selftest_div3(long long n, unsigned long long seed, unsigned long long* 
     return CFD_OK;
 }
 
+int cfd_selftest_div_rcp(long long n, unsigned long long seed, unsigned long long* mismatches) {
+    if (n < 1 || n > (1LL << 36) || !mismatches)
+        return arg_error("n in [1, 2^36] and a mismatch counter");
+    unsigned long long* bad = nullptr;
+    CFD_CUDA(cudaMalloc(&bad, sizeof(unsigned long long)));
+    unsigned long long h = ~0ull;
+    cudaError_t e = cudaMemset(bad, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = launch_selftest_divrcp(n, seed, bad);
+    if (e == cudaSuccess) e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    CFD_CUDA(e);
+    *mismatches = h;
+    return CFD_OK;
+}
+
 int cfd_selftest_waits(long long polls, int* barrier_status, int* mbarrier_status) {
     if (polls < 1 || polls > (1LL << 24) || !barrier_status || !mbarrier_status)
         return arg_error("polls in [1, 2^24] and two status pointers");

@@ -55,6 +55,25 @@ __device__ __forceinline__ double div3(double x) {
     return fma(r, R3, q0);
 }
 
+// x / d correctly rounded from y = RN(1/d) (formed once per d, by the division) in a
+// multiply and four FMAs: q0 = RN(x*y) is within 1.5 ulp of x/d; one correction
+// q1 = RN(q0 + RN(x - d*q0)*y) brings it within an ulp (the remainder's rounding and the
+// product error move it by far less than an ulp); with q1 within an ulp the remainder
+// x - d*q1 is exact in one FMA and RN(q1 + (x - d*q1)*y) is the correctly rounded x/d
+// (Markstein's theorem: y within half an ulp of 1/d, q1 within an ulp of x/d).  The range
+// check (both exponents and the quotient's) keeps every intermediate normal and finite;
+// other operands (zeros included) take the division.  Bit-identical to x / d (checked on the GPU against the division).
+__device__ __forceinline__ double div_rcp(double x, double d, double y) {
+    const int ex = (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
+    const int ed = (int)((unsigned long long)__double_as_longlong(d) >> 52) & 0x7ff;
+    // both exponents in [200, 1800] and the quotient's within 2^+-800
+    if ((unsigned)(ex - 200) > 1600u || (unsigned)(ed - 200) > 1600u || abs(ex - ed) > 800)
+        return x / d;
+    const double q0 = x * y;
+    const double q1 = fma(fma(-d, q0, x), y, q0);
+    return fma(fma(-d, q1, x), y, q1);
+}
+
 // ------------------------------------------------------------------ FP32 <-> FP64 by bits
 // GB300's FP64 pipe (1/64 of the FP32 rate) also executes the F2F conversions, so the
 // mixed-precision kernels move values between the two formats with integer operations.

@@ -121,7 +121,8 @@ struct Ctx {
     unsigned long long* d_blockmin = nullptr;  // per-block FP32 DTELEM minima
     double* d_invdiag = nullptr;
     float* d_valf = nullptr;
-    float* d_val_lo = nullptr;   // relative tests: valf + val_lo = the FP64-assembled matrix
+    float* d_val_lo = nullptr;
+    double* d_rdiag = nullptr;   // FP64 form: RN(1/diag) of the BiCG (formed by each solve)   // relative tests: valf + val_lo = the FP64-assembled matrix
     double4* d_g64 = nullptr;    // relative tests: FP64 element gradients and weight
     float* d_dtef = nullptr;  // mixed form, ITLOCAL != 0: FP32 DT per element
     float* d_pf[2][2] = {};

@@ -262,6 +262,7 @@ cudaError_t launch_elem_inv(bool viscous, cudaStream_t stream, int nelem, const 
                             double* cache, double* contrib, const double* WX, const double* WY,
                             double* contribF);
 cudaError_t launch_selftest_div3(long long n, unsigned long long seed, unsigned long long* bad);
+cudaError_t launch_selftest_divrcp(long long n, unsigned long long seed, unsigned long long* bad);
 cudaError_t launch_elem_replay(cudaStream_t stream, int nelem, const int4* elem, const double* T,
                                const double* geo, const double* area, const double* dtl_arr,
                                const double* dtl_scalar, GasConst gc, const double* cache,
@@ -309,6 +310,8 @@ struct PcgArgs {
     const int* col;
     const double* val;
     const double* diag;
+    double* rdiag;               // FP64 form: RN(1/diag), formed by the first pass and used
+                                 // for the iterations' quotients (null: the division)
     const unsigned char* isfix;  // per node: Dirichlet row
     int nfix;                    // unique fixed nodes (last entry of the reference list)
     const int* fix_node;

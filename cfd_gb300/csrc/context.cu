@@ -143,6 +143,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
     a.col = d_col;
     a.val = d_val;
     a.diag = d_diag;
+    a.rdiag = d_rdiag;  // null in the mixed form
     a.isfix = d_isfix;
     a.nfix = nufix;
     a.fix_node = d_ufix_node;
@@ -723,6 +724,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if ((st = upload(&d_col, adj.col.data(), adj.col.size()))) return st;
     if ((st = dalloc(&d_val, adj.col.size()))) return st;
     if ((st = dalloc(&d_diag, N))) return st;
+    if (prec == CFD_PREC_FP64 && (st = dalloc(&d_rdiag, N))) return st;
     // BC tables
     std::vector<uint8_t> fl = bc.flag;
     for (auto& f : fl) {  // host bits -> device bits (same values, normals set on device)

@@ -3,12 +3,14 @@
 // The reference's solver is Jacobi-preconditioned CG with Dirichlet rows handled by
 // overwrite and a 1e30 penalty; every vector operation is a separate OpenMP loop and the
 // dots are OpenMP reductions.  Here the whole solve (both mesh-motion right-hand sides at
-// once, sharing the matrix reads) is one launch: each iteration is two grid-wide phases
-// separated by a bounded grid barrier.
+// once, sharing the matrix reads) is one launch: each iteration is three grid-wide passes
+// separated by bounded grid barriers.
 //   phase 1: x += alfa*p (deferred from the previous iteration), r -= alfa*y, z = r/diag,
 //            partial sums of r.z (and of r.r under a relative stopping test)
-//   phase 2: p_new = beta*p + z computed on the fly inside the SpMV row loop
-//            (y_i = sum_j A_ij*(beta*p_j + z_j)), y(fix) = 1e30*p_new(fix), partial p.y
+//   phase 2: p_new = beta*p + z per row (biconjGrad.f90's vector update), a grid barrier,
+//            then y = A.p_new, y(fix) = 1e30*p_new(fix), partial p.y
+//   (the quotients z = r/diag use a reciprocal formed once per solve and two FMA
+//   corrections, which give the division's bits: div_rcp)
 // Every block folds the chunk partials itself in the fixed order of cfd_common.cuh, so
 // all blocks hold bit-identical scalars and take the same branch.  With --fmad=false the
 // iterates equal the CPU restatement's bit for bit.
@@ -20,17 +22,6 @@ __device__ __forceinline__ double spmv_row(const PcgArgs& a, int i, const double
     double dot = 0.0;
     const int j1 = a.rowptr[i + 1];
     for (int j = a.rowptr[i]; j < j1; ++j) dot = dot + a.val[j] * v[a.col[j]];
-    return dot;
-}
-
-__device__ __forceinline__ double spmv_row_dir(const PcgArgs& a, int i, const double* p,
-                                               const double* z, double beta) {
-    double dot = 0.0;
-    const int j1 = a.rowptr[i + 1];
-    for (int j = a.rowptr[i]; j < j1; ++j) {
-        const int c = a.col[j];
-        dot = dot + a.val[j] * (beta * p[c] + z[c]);
-    }
     return dot;
 }
 
@@ -146,6 +137,7 @@ __global__ void __launch_bounds__(256, 3) k_pcg_fp64(PcgArgs a) {
             const long i = c * kChunk + t + 256L * k;
             if (i >= n) break;
             const double d = a.diag[i];
+            if (a.rdiag) a.rdiag[i] = 1.0 / d;
             for (int s = 0; s < ns; ++s) {
                 if (done[s]) continue;
                 double ri = a.r[s][i];
@@ -215,11 +207,12 @@ __global__ void __launch_bounds__(256, 3) k_pcg_fp64(PcgArgs a) {
                 const long i = c * kChunk + t + 256L * kk;
                 if (i >= n) break;
                 const double d = a.diag[i];
+                const double rd = a.rdiag ? a.rdiag[i] : 0.0;
                 for (int s = 0; s < ns; ++s) {
                     if (pend[s]) a.x[s][i] = alfa[s] * a.p[s][cur[s]][i] + a.x[s][i];
                     if (!act[s]) continue;
                     double ri = (-alfa[s]) * a.y[s][i] + a.r[s][i];
-                    double zi = ri / d;
+                    double zi = a.rdiag ? div_rcp(ri, d, rd) : ri / d;
                     a.r[s][i] = ri;
                     a.z[s][i] = zi;
                     acc[s] = (kk == 0) ? ri * zi : acc[s] + ri * zi;
@@ -246,7 +239,18 @@ __global__ void __launch_bounds__(256, 3) k_pcg_fp64(PcgArgs a) {
             if (rel) rrc[s] = fold_partials(part(2, s), nc, red);
             beta[s] = err_new[s] / err_old[s];
         }
-        // phase 2
+        // phase 2a: p_new = beta p + z, once per row (the SpMV below reads it; forming it
+        // inside every row's column loop would cost two FP64 operations per entry)
+        for (long c = blockIdx.x; c < nc; c += gridDim.x)
+            for (int kk = 0; kk < 4; ++kk) {
+                const long i = c * kChunk + t + 256L * kk;
+                if (i >= n) break;
+                for (int s = 0; s < ns; ++s)
+                    if (act[s]) a.p[s][cur[s] ^ 1][i] = beta[s] * a.p[s][cur[s]][i] + a.z[s][i];
+            }
+        grid_barrier(a.bar, nb);
+        if (bar_failed(a.bar)) return;
+        // phase 2b: y = A p_new, y(fix) = 1e30 p_new(fix), partial p.y
         for (long c = blockIdx.x; c < nc; c += gridDim.x) {
             double acc[2] = {0.0, 0.0};
             for (int kk = 0; kk < 4; ++kk) {
@@ -255,11 +259,9 @@ __global__ void __launch_bounds__(256, 3) k_pcg_fp64(PcgArgs a) {
                 const bool fx = a.isfix[i];
                 for (int s = 0; s < ns; ++s) {
                     if (!act[s]) continue;
-                    const double* p = a.p[s][cur[s]];
-                    const double* z = a.z[s];
-                    double pn = beta[s] * p[i] + z[i];
-                    double yi = fx ? 1.0e30 * pn : spmv_row_dir(a, (int)i, p, z, beta[s]);
-                    a.p[s][cur[s] ^ 1][i] = pn;
+                    const double* pn_v = a.p[s][cur[s] ^ 1];
+                    const double pn = pn_v[i];
+                    double yi = fx ? 1.0e30 * pn : spmv_row(a, (int)i, pn_v);
                     a.y[s][i] = yi;
                     acc[s] = (kk == 0) ? pn * yi : acc[s] + pn * yi;
                 }
@@ -350,6 +352,49 @@ __global__ void k_guess_extrapolate_hist(const double* __restrict__ dtn_p,
         hist[0] = *dtn_p;
         hist[2] = hist[2] + 1.0;
     }
+}
+
+// div_rcp against the division x / d over n input pairs: a third raw 64-bit patterns for
+// both (splitmix64: every exponent and sign, zeros, subnormals, infinities, NaNs), a third
+// with both of magnitude 2^-60 .. 2^60, a third with x = d * m for a random significand m
+// moved by up to +-2^12 ulps (quotients next to binade edges and to halfway cases).  Counts
+// the pairs whose results differ in any bit (two NaNs count as equal).
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__global__ void k_selftest_divrcp(long long n, unsigned long long seed,
+                                  unsigned long long* __restrict__ bad) {
+    unsigned long long local = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long z1 = splitmix(seed + (unsigned long long)i * 0x9e3779b97f4a7c15ull);
+        const unsigned long long z2 = splitmix(z1 + 0x632be59bd9b4e019ull);
+        unsigned long long bx = z1, bd = z2;
+        const int kind = (int)(i % 3);
+        if (kind == 1) {
+            bx = (z1 & 0x800fffffffffffffull) | ((963ull + (z1 >> 52) % 121ull) << 52);
+            bd = (z2 & 0x800fffffffffffffull) | ((963ull + (z2 >> 52) % 121ull) << 52);
+        } else if (kind == 2) {
+            bd = (z2 & 0x800fffffffffffffull) | ((993ull + (z2 >> 52) % 61ull) << 52);
+            const double m = __longlong_as_double((long long)((z1 & 0x000fffffffffffffull) |
+                                                              (1023ull << 52)));
+            const long long b = __double_as_longlong(__longlong_as_double((long long)bd) * m);
+            bx = (unsigned long long)(b + ((long long)(z1 >> 52 & 0x1fffull) - 4096));
+        }
+        const double x = __longlong_as_double((long long)bx), d = __longlong_as_double((long long)bd);
+        const double y = 1.0 / d;
+        const double a = div_rcp(x, d, y), b = x / d;
+        if (__double_as_longlong(a) != __double_as_longlong(b) && !(a != a && b != b)) ++local;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
+cudaError_t launch_selftest_divrcp(long long n, unsigned long long seed, unsigned long long* bad) {
+    k_selftest_divrcp<<<152 * 8, 256>>>(n, seed, bad);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
 }
 
 __global__ void k_selftest_waits(GridBar* gb, int* out, long long limit) {

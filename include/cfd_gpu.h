@@ -489,6 +489,10 @@ int cfd_selftest_waits(long long polls, int* barrier_status, int* mbarrier_statu
  * patterns from `seed`, values in 2^-40 .. 2^40, and values next to 3 * 2^k) and returns
  * the number whose bits differ. */
 int cfd_selftest_div3(long long n, unsigned long long seed, unsigned long long* mismatches);
+/* The same for the FP64 BiCG's quotients r/diag: a multiply by RN(1/diag) and four FMAs
+ * (two Markstein corrections) against the division, over n pairs from `seed` (raw bit
+ * patterns, magnitudes 2^-60 .. 2^60, quotients next to binade edges and halfway cases). */
+int cfd_selftest_div_rcp(long long n, unsigned long long seed, unsigned long long* mismatches);
 
 const char* cfd_strerror(int status);
 /* 1 if a CUDA device is usable by this library. */

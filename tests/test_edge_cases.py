@@ -130,3 +130,15 @@ def test_div3_equals_the_division(gpu_lib):
     abi.check(abi.lib().cfd_selftest_div3(1 << 32, 0x5eed, C.byref(bad)), "div3 self-test")
     assert bad.value == 0
     assert abi.lib().cfd_selftest_div3(0, 1, C.byref(bad)) == abi.CFD_ERR_ARG
+
+
+@pytest.mark.gpu
+def test_div_rcp_equals_the_division(gpu_lib):
+    """The FP64 BiCG's quotients r/diag from the reciprocal and two FMA corrections give the
+    IEEE quotient bit for bit over 2^31 pairs (raw bit patterns, 2^-60 .. 2^60, quotients
+    next to binade edges and halfway cases)."""
+    import ctypes as C
+    from cfd_gb300 import abi
+    bad = C.c_ulonglong(12345)
+    abi.check(abi.lib().cfd_selftest_div_rcp(1 << 31, 0xd1f, C.byref(bad)), "div_rcp self-test")
+    assert bad.value == 0
