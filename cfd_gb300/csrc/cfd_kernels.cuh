@@ -254,7 +254,7 @@ __global__ void k_vel_from_U(int npoin, const double* U, double* VX, double* VY)
 // calcRHS split into its stage-invariant part (once per step: the cached addends and
 // factors, FUENTE into contribF; with !viscous the final contributions into contrib) and
 // the per-stage viscous replay from the cache (kernels_fp64.cu); cache: kInvPlanes x nelem
-constexpr int kElemInvPlanes = 94;
+constexpr int kElemInvPlanes = 100;
 cudaError_t launch_elem_inv(bool viscous, cudaStream_t stream, int nelem, const int4* elem,
                             const double* U, const double* geo, const double* area,
                             const double* shoc, const double* dtl_arr, const double* dtl_scalar,

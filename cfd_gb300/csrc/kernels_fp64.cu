@@ -480,7 +480,10 @@ constexpr int kA2 = 12;   // [i][k][q-1] tau_i*(Nx_i*B1_k(q) + Ny_i*B2_k(q))
 constexpr int kA3 = 39;   // [i][q-1]   nu*(Nx_i*Ux(q) + Ny_i*Uy(q))
 constexpr int kV = 48;    // [k][14]    mu-independent factors of K1_k, K2_k (below)
 constexpr int kVG = 90;   // [4]        Ux(1), Uy(1), 3*Ux(4), 3*Uy(4)
-constexpr int kInvPlanes = 94;
+constexpr int kRc = 94;   // [k][2]     RN(1/rho_k), RN(1/(Cv*rho_k)): the replay's quotients
+                          //            by them take div_rcp (bit-identical, fewer FP64 ops)
+constexpr int kInvPlanes = 100;
+static_assert(kInvPlanes == kElemInvPlanes, "cache planes");
 // kV + 14*k + m: 0 rho, 1 P11, 2 P12, 3 P13a, 4 P13b, 5 P13c, 6 Ux(2)*v1, 7 3*Ux(3)*v2,
 // 8 Cv*rho, 9 P22, 10 P23a, 11 P23b, 12 3*Uy(2)*v1, 13 Uy(3)*v2
 
@@ -597,6 +600,8 @@ k_elem_inv(int nelem, const int4* __restrict__ elem, const double* __restrict__ 
             C(kV + 14 * k + 6) = Ux[1] * v1;
             C(kV + 14 * k + 7) = 3.0 * Ux[2] * v2;
             C(kV + 14 * k + 8) = Cv * rho;
+            C(kRc + 2 * k) = 1.0 / rho;
+            C(kRc + 2 * k + 1) = 1.0 / (Cv * rho);
             C(kV + 14 * k + 9) = Ux[0] * v1 - Ux[1] - 2.0 * Uy[0] * v2 + 2.0 * Uy[2];
             C(kV + 14 * k + 10) = -(Ux[0] * v1 * v2) - 2.0 * Ux[1] * v2 + 3.0 * Ux[2] * v1;
             C(kV + 14 * k + 11) = 3.0 * V_sq + v2 * v2;
@@ -687,19 +692,21 @@ k_elem_replay(int nelem, const int4* __restrict__ elem, const double* __restrict
         const int b = kV + 14 * k;
         const double rho = C(b + 0);
         const double P13c = C(b + 5);
+        const double crho = C(b + 8);
+        const double rr = C(kRc + 2 * k), rc = C(kRc + 2 * k + 1);
         double K1[3], K2[3];
-        K1[0] = c23m * C(b + 1) / rho;
-        K1[1] = mu * C(b + 2) / rho;
-        K1[2] = 1.0 / 3.0 *
-                (cm * C(b + 3) - Ux0 * (cm * C(b + 4) - l3 * P13c) + C(b + 6) * c4m_l3 +
-                 C(b + 7) * cm_l + t5x) /
-                C(b + 8);
+        K1[0] = div_rcp(c23m * C(b + 1), rho, rr);
+        K1[1] = div_rcp(mu * C(b + 2), rho, rr);
+        K1[2] = div_rcp(1.0 / 3.0 *
+                            (cm * C(b + 3) - Ux0 * (cm * C(b + 4) - l3 * P13c) +
+                             C(b + 6) * c4m_l3 + C(b + 7) * cm_l + t5x),
+                        crho, rc);
         K2[0] = K1[1];
-        K2[1] = c23m * C(b + 9) / rho;
-        K2[2] = 1.0 / 3.0 *
-                (cm * C(b + 10) - Uy0 * (cm * C(b + 11) - l3 * P13c) + C(b + 12) * cm_l +
-                 C(b + 13) * c4m_l3 + t5y) /
-                C(b + 8);
+        K2[1] = div_rcp(c23m * C(b + 9), rho, rr);
+        K2[2] = div_rcp(1.0 / 3.0 *
+                            (cm * C(b + 10) - Uy0 * (cm * C(b + 11) - l3 * P13c) +
+                             C(b + 12) * cm_l + C(b + 13) * c4m_l3 + t5y),
+                        crho, rc);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
