@@ -947,8 +947,10 @@ int cfd_gcl(double* M, const double* W_x, const double* W_y, const double* W_x_o
     TRY(s.put(&d_a, area, E));
     TRY(s.put(&d_ao, area_old, E));
     TRY(s.put(&d_dt, dt, 1));
-    CFD_LAUNCH(k_gcl, blocks_for(N, 256), 256, 0, s.stream, N, E, d_el, d_ptr, d_slot, d_geo, d_a, d_ao,
-               d_wx, d_wy, d_wxo, d_wyo, d_dt, mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_M);
+    double2* d_terms;
+    TRY(s.alloc(&d_terms, E));
+    CFD_CUDA(launch_gcl(s.stream, N, E, d_el, d_ptr, d_slot, d_geo, d_a, d_ao, d_wx, d_wy, d_wxo,
+                        d_wyo, d_dt, mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_terms, d_M));
     TRY(s.get(M, d_M, N));
     return s.sync();
 }
@@ -1004,8 +1006,10 @@ int cfd_laplace(const int* inpoel, const double* area, const double* dNx, const 
     TRY(s.put(&d_Y, Y, N));
     TRY(s.alloc(&d_v, nnz));
     TRY(s.alloc(&d_d, N));
-    CFD_LAUNCH(k_laplace, blocks_for(N, 128), 128, 0, s.stream, N, E, d_el, d_ptr, d_slot, d_pos, d_geo,
-               d_X, d_Y, d_rp, d_v, d_d);
+    double* d_q;
+    TRY(s.alloc(&d_q, E));
+    CFD_CUDA(launch_laplace(s.stream, N, E, d_el, d_ptr, d_slot, d_pos, d_geo, d_X, d_Y, d_rp, d_q,
+                            d_v, d_d));
     TRY(s.get(lap_sparse, d_v, nnz));
     TRY(s.get(lap_diag, d_d, N));
     return s.sync();

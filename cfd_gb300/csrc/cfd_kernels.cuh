@@ -233,11 +233,13 @@ __global__ void k_deriv(int nelem, const int4* elem, const double* X, const doub
                         double* area, double* geo, double* hh, double* hhx, double* hhy);
 __global__ void k_mass(int npoin, const int* esup_ptr, const int* esup_slot, const double* area,
                        double* M);
-__global__ void k_gcl(int npoin, int nelem, const int4* elem, const int* esup_ptr,
-                      const int* esup_slot, const double* geo, const double* area,
-                      const double* area_old, const double* Wx, const double* Wy,
-                      const double* Wxo, const double* Wyo, const double* dtp, int literal,
-                      double* M);
+// gcl main (gcl.f90:8-46): the element terms once per element (scratch: nelem double2),
+// then per node M += dt (tot1 + tot2)/2 over them in element order
+cudaError_t launch_gcl(cudaStream_t st, int npoin, int nelem, const int4* elem,
+                       const int* esup_ptr, const int* esup_slot, const double* geo,
+                       const double* area, const double* area_old, const double* Wx,
+                       const double* Wy, const double* Wxo, const double* Wyo, const double* dtp,
+                       int literal, double2* scratch, double* M);
 __global__ void k_deltat(int nelem, const int4* elem, const double* T, const double* VX,
                          const double* VY, const double* WX, const double* WY,
                          const double* area, double fsafe, double t_inf, double* DT,
@@ -288,10 +290,12 @@ __global__ void k_min_positive(long n, const double* x, unsigned long long* bits
 __global__ void k_normales(int nwn, const int* wnode, const int* wptr, const int2* wedge_of,
                            const int2* walls, const double* X, const double* Y,
                            unsigned char* bcflag, double2* nrm);
-__global__ void k_laplace(int npoin, int nelem, const int4* elem, const int* esup_ptr,
-                          const int* esup_slot, const uchar4* lap_pos, const double* geo,
-                          const double* X, const double* Y, const int* rowptr, double* vals,
-                          double* diag);
+// laplace (mLaplace.f90:7-58): each element's weight 1/mu^2 once (scratch: nelem
+// doubles), then the rows
+cudaError_t launch_laplace(cudaStream_t st, int npoin, int nelem, const int4* elem,
+                           const int* esup_ptr, const int* esup_slot, const uchar4* lap_pos,
+                           const double* geo, const double* X, const double* Y, const int* rowptr,
+                           double* scratch, double* vals, double* diag);
 __global__ void k_forces(int nset_numb, const int* set_ptr, const int2* set_edges,
                          const double* P, const double* X, const double* Y, const double* xref,
                          const double* yref, StepScal* sc);

@@ -116,8 +116,8 @@ int Ctx::geometry(bool masas, bool with_laplace) {
     }
     if (with_laplace) {
         tstart(TM_LAPLACE);
-        CFD_LAUNCH(k_laplace, blocks_for(N, 128), 128, 0, stream, N, E, d_elem, d_esup_ptr,
-                   d_esup_slot, d_lap_pos, d_geo, d_X, d_Y, d_rowptr, d_val, d_diag);
+        CFD_CUDA(launch_laplace(stream, N, E, d_elem, d_esup_ptr, d_esup_slot, d_lap_pos, d_geo,
+                                d_X, d_Y, d_rowptr, d_lapq, d_val, d_diag));
         tstop(TM_LAPLACE);
     }
     return CFD_OK;
@@ -588,17 +588,17 @@ int Ctx::step_once() {
         if (st) return st;
         if (prm.mass_mode != CFD_MASS_MASAS) {  // gcl main, then putW/putArea
             tstart(TM_MASAS);
-            CFD_LAUNCH(k_gcl, blocks_for(N, TB), TB, 0, stream, N, E, d_elem, d_esup_ptr,
-                       d_esup_slot, d_geo, d_area, d_area_old, d_WX, d_WY, d_Wxo, d_Wyo,
-                       &d_scal->dtmin, prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_M);
+            CFD_CUDA(launch_gcl(stream, N, E, d_elem, d_esup_ptr, d_esup_slot, d_geo, d_area,
+                                d_area_old, d_WX, d_WY, d_Wxo, d_Wyo, &d_scal->dtmin,
+                                prm.mass_mode == CFD_MASS_GCL_LITERAL ? 1 : 0, d_gcl64, d_M));
             CFD_CUDA(cudaMemcpyAsync(d_Wxo, d_WX, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
             CFD_CUDA(cudaMemcpyAsync(d_Wyo, d_WY, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream));
             CFD_CUDA(cudaMemcpyAsync(d_area_old, d_area, sizeof(double) * E, cudaMemcpyDeviceToDevice, stream));
             tstop(TM_MASAS);
         }
         tstart(TM_LAPLACE);
-        CFD_LAUNCH(k_laplace, blocks_for(N, 128), 128, 0, stream, N, E, d_elem, d_esup_ptr,
-                   d_esup_slot, d_lap_pos, d_geo, d_X, d_Y, d_rowptr, d_val, d_diag);
+        CFD_CUDA(launch_laplace(stream, N, E, d_elem, d_esup_ptr, d_esup_slot, d_lap_pos, d_geo,
+                                d_X, d_Y, d_rowptr, d_lapq, d_val, d_diag));
         tstop(TM_LAPLACE);
     }
     std::swap(d_U, d_U1);  // U = U1 (:277-281)
@@ -725,6 +725,8 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if ((st = dalloc(&d_val, adj.col.size()))) return st;
     if ((st = dalloc(&d_diag, N))) return st;
     if (prec == CFD_PREC_FP64 && (st = dalloc(&d_rdiag, N))) return st;
+    if (prec == CFD_PREC_FP64 && (st = dalloc(&d_lapq, E))) return st;
+    if (prec == CFD_PREC_FP64 && (st = dalloc(&d_gcl64, E))) return st;
     // BC tables
     std::vector<uint8_t> fl = bc.flag;
     for (auto& f : fl) {  // host bits -> device bits (same values, normals set on device)

@@ -55,36 +55,60 @@ __global__ void k_mass(int npoin, const int* __restrict__ esup_ptr, const int* _
 
 // ------------------------------------------------------------------ gcl main (gather)
 // gcl.f90:29-45 with putW/putArea's saved arrays; literal divW (:38-41) or dNy.W_y.
-__global__ void k_gcl(int npoin, int nelem, const int4* __restrict__ elem,
-                      const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
-                      const double* __restrict__ geo, const double* __restrict__ area,
-                      const double* __restrict__ area_old, const double* __restrict__ Wx,
-                      const double* __restrict__ Wy, const double* __restrict__ Wxo,
-                      const double* __restrict__ Wyo, const double* __restrict__ dtp,
-                      int literal, double* __restrict__ M) {
+// The element terms divW*area/3 and divW_old*area_old/3 (gcl.f90:27-45; divW as written,
+// dNy.W_x, when literal), formed once per element: every node around the element adds the
+// same two values, in the same expressions as the reference's per-node loop.
+__global__ void k_gcl_terms(int nelem, const int4* __restrict__ elem,
+                            const double* __restrict__ geo, const double* __restrict__ area,
+                            const double* __restrict__ area_old, const double* __restrict__ Wx,
+                            const double* __restrict__ Wy, const double* __restrict__ Wxo,
+                            const double* __restrict__ Wyo, int literal,
+                            double2* __restrict__ terms) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    const size_t E = (size_t)nelem;
+    const int4 n = elem[e];
+    const int nn[3] = {n.x, n.y, n.z};
+    double wx[3], wy[3], wxo[3], wyo[3];
+    for (int i = 0; i < 3; ++i) {
+        wx[i] = Wx[nn[i]];
+        wy[i] = literal ? Wx[nn[i]] : Wy[nn[i]];
+        wxo[i] = Wxo[nn[i]];
+        wyo[i] = literal ? Wxo[nn[i]] : Wyo[nn[i]];
+    }
+    const double d0 = geo[e], d1 = geo[E + e], d2 = geo[2 * E + e];
+    const double f0 = geo[3 * E + e], f1 = geo[4 * E + e], f2 = geo[5 * E + e];
+    const double divW = d0 * wx[0] + d1 * wx[1] + d2 * wx[2] + f0 * wy[0] + f1 * wy[1] + f2 * wy[2];
+    const double divWo =
+        d0 * wxo[0] + d1 * wxo[1] + d2 * wxo[2] + f0 * wyo[0] + f1 * wyo[1] + f2 * wyo[2];
+    terms[e] = make_double2(div3(divW * area[e]), div3(divWo * area_old[e]));
+}
+
+// Per node: tot1, tot2 as the ordered sums over the elements around it, M += dt(t1 + t2)/2
+__global__ void k_gcl(int npoin, const int* __restrict__ esup_ptr,
+                      const int* __restrict__ esup_slot, const double2* __restrict__ terms,
+                      const double* __restrict__ dtp, double* __restrict__ M) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npoin) return;
-    const size_t E = (size_t)nelem;
     double t1 = 0.0, t2 = 0.0;
     for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) {
-        int e = esup_slot[s] / 3;
-        int4 n = elem[e];
-        int nn[3] = {n.x, n.y, n.z};
-        double wx[3], wy[3], wxo[3], wyo[3];
-        for (int i = 0; i < 3; ++i) {
-            wx[i] = Wx[nn[i]];
-            wy[i] = literal ? Wx[nn[i]] : Wy[nn[i]];
-            wxo[i] = Wxo[nn[i]];
-            wyo[i] = literal ? Wxo[nn[i]] : Wyo[nn[i]];
-        }
-        double d0 = geo[e], d1 = geo[E + e], d2 = geo[2 * E + e];
-        double f0 = geo[3 * E + e], f1 = geo[4 * E + e], f2 = geo[5 * E + e];
-        double divW = d0 * wx[0] + d1 * wx[1] + d2 * wx[2] + f0 * wy[0] + f1 * wy[1] + f2 * wy[2];
-        double divWo = d0 * wxo[0] + d1 * wxo[1] + d2 * wxo[2] + f0 * wyo[0] + f1 * wyo[1] + f2 * wyo[2];
-        t1 = t1 + div3(divW * area[e]);
-        t2 = t2 + div3(divWo * area_old[e]);
+        const double2 tm = terms[esup_slot[s] / 3];
+        t1 = t1 + tm.x;
+        t2 = t2 + tm.y;
     }
     M[p] = M[p] + (*dtp) * (t1 + t2) / 2.0;
+}
+
+cudaError_t launch_gcl(cudaStream_t st, int npoin, int nelem, const int4* elem,
+                       const int* esup_ptr, const int* esup_slot, const double* geo,
+                       const double* area, const double* area_old, const double* Wx,
+                       const double* Wy, const double* Wxo, const double* Wyo, const double* dtp,
+                       int literal, double2* scratch, double* M) {
+    k_gcl_terms<<<blocks_for(nelem, 256), 256, 0, st>>>(nelem, elem, geo, area, area_old, Wx, Wy,
+                                                        Wxo, Wyo, literal, scratch);
+    k_gcl<<<blocks_for(npoin, 256), 256, 0, st>>>(npoin, esup_ptr, esup_slot, scratch, dtp, M);
+    g_launches.fetch_add(2, std::memory_order_relaxed);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ deltat
@@ -867,10 +891,22 @@ __device__ __forceinline__ double mesh_mu(const double* X3, const double* Y3) {
     return TWOSQRT3 * a / l;
 }
 
-__global__ void k_laplace(int npoin, int nelem, const int4* __restrict__ elem,
-                          const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
-                          const uchar4* __restrict__ lap_pos, const double* __restrict__ geo,
-                          const double* __restrict__ X, const double* __restrict__ Y,
+// Each element's weight q = 1/mu^2 (mLaplace.f90:40), formed once: the reference forms it
+// for every (node, element) pair of its loop, with the same value each time
+__global__ void k_lap_q(int nelem, const int4* __restrict__ elem, const double* __restrict__ X,
+                        const double* __restrict__ Y, double* __restrict__ q) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    const int4 n = elem[e];
+    const double X3[3] = {X[n.x], X[n.y], X[n.z]};
+    const double Y3[3] = {Y[n.x], Y[n.y], Y[n.z]};
+    const double m = mesh_mu(X3, Y3);
+    q[e] = 1.0 / (m * m);
+}
+
+__global__ void k_laplace(int npoin, int nelem, const int* __restrict__ esup_ptr,
+                          const int* __restrict__ esup_slot, const uchar4* __restrict__ lap_pos,
+                          const double* __restrict__ geo, const double* __restrict__ qe,
                           const int* __restrict__ rowptr, double* __restrict__ vals,
                           double* __restrict__ diag) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -881,11 +917,7 @@ __global__ void k_laplace(int npoin, int nelem, const int4* __restrict__ elem,
     for (int s = esup_ptr[p]; s < esup_ptr[p + 1]; ++s) {
         const int slot = esup_slot[s];
         const int e = slot / 3, i = slot - 3 * e;
-        int4 n = elem[e];
-        double X3[3] = {X[n.x], X[n.y], X[n.z]};
-        double Y3[3] = {Y[n.x], Y[n.y], Y[n.z]};
-        double m = mesh_mu(X3, Y3);
-        double q = 1.0 / (m * m);
+        const double q = qe[e];
         const double dxi = geo[i * E + e], dyi = geo[(3 + i) * E + e];
         uchar4 pos = lap_pos[s];
         const unsigned char pj[3] = {pos.x, pos.y, pos.z};
@@ -896,6 +928,17 @@ __global__ void k_laplace(int npoin, int nelem, const int4* __restrict__ elem,
         }
     }
     diag[p] = vals[r0];
+}
+
+cudaError_t launch_laplace(cudaStream_t st, int npoin, int nelem, const int4* elem,
+                           const int* esup_ptr, const int* esup_slot, const uchar4* lap_pos,
+                           const double* geo, const double* X, const double* Y, const int* rowptr,
+                           double* scratch, double* vals, double* diag) {
+    k_lap_q<<<blocks_for(nelem, 256), 256, 0, st>>>(nelem, elem, X, Y, scratch);
+    k_laplace<<<blocks_for(npoin, 128), 128, 0, st>>>(npoin, nelem, esup_ptr, esup_slot, lap_pos,
+                                                      geo, scratch, rowptr, vals, diag);
+    g_launches.fetch_add(2, std::memory_order_relaxed);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ FORCES
