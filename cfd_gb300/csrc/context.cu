@@ -896,10 +896,11 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         CFD_CUDA(cudaMemsetAsync(d_tcount, 0, 4 * sizeof(unsigned), stream));
         CFD_CUDA(cudaMemsetAsync(d_motion, 0, sizeof(MotionScal), stream));
         graphs_on = !timers_on && !(getenv("CFD_GRAPHS") && atoi(getenv("CFD_GRAPHS")) == 0);
-        // 6 blocks per SM measured best at 1M nodes with the current passes (0.535 ms; 3, 4,
-        // 5, 7, 8, 10, 12: 0.606, 0.568, 0.539, 0.538, 0.550, 0.561, 0.563); 0 = full grids
+        // 5 blocks per SM measured best at 1M nodes with the current passes (the FP64 gcl
+        // areas on the branch; 1000-step runs: 5: 0.557-0.559 ms, 6: 0.561-0.562; 600-step
+        // runs, 4, 8, 12: 0.579, 0.568, 0.586); 0 = full grids
         branch_bpsm = getenv("CFD_BRANCH_BLOCKS_PER_SM") ? atoi(getenv("CFD_BRANCH_BLOCKS_PER_SM"))
-                                                         : 6;
+                                                         : 5;
         if ((st = narrow_mixed(true, true, true, true, true, true))) return st;
     }
     // setup geometry: NORMALES, DERIV, MASAS, laplace (ns2DComp.ALE.f90:88-100)
