@@ -48,8 +48,11 @@ def parse():
                     help="nodes per direction of the large heave + pitch O-grid report "
                          "(default 2048, the 4,194,304-node workload; given, it also runs "
                          "under --no-compare)")
-    ap.add_argument("--guess", choices=["learned", "previous", "zero"], default="learned",
-                    help="initial guess of the mesh-motion solve in the mixed form")
+    ap.add_argument("--guess", choices=["learned", "learned_refined", "previous", "zero"],
+                    default="learned",
+                    help="initial guess of the mesh-motion solve in the mixed form "
+                         "(learned_refined: the network once, then its refined fields judged "
+                         "against the extrapolated increments)")
     ap.add_argument("--guess-gate", type=float, default=20.0,
                     help="learned guess: iterations of the previous solve above which the "
                          "network runs (it also runs on the first solve)")
@@ -277,13 +280,15 @@ def main_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def timed_run(solver_mod, k, prec, W, K, L, net=None, gate=0.0):
-    """Create a context (with the learned-guess network attached when given), W warm-up
-    steps, then K steps between CUDA events on the context's stream.  Returns (solver, ms
-    per step, kernel launches, report)."""
+def timed_run(solver_mod, k, prec, W, K, L, net=None, gate=0.0, refine=False):
+    """Create a context (with the learned-guess network attached when given, and its
+    refined fields when refine), W warm-up steps, then K steps between CUDA events on the
+    context's stream.  Returns (solver, ms per step, kernel launches, report)."""
     S = solver_mod.Solver(k, precision=prec)
     if net is not None:
         S.set_guess_net(net, gate)
+        if refine:
+            S.set_guess_refine(True)
     S.step(W)
     import torch
     torch.cuda.synchronize()
@@ -767,10 +772,12 @@ def main_ours(args):
     k.params.estab_mode = abi.CFD_ESTAB_REGULARIZED if mixed else abi.CFD_ESTAB_REFERENCE
     W, K = max(3, args.warmup), args.steps
     net, gate = None, 0.0
-    if mixed and args.guess == "learned":
+    refine = mixed and args.guess == "learned_refined"
+    if mixed and args.guess in ("learned", "learned_refined"):
         from cfd_gb300 import learned
-        k.params.guess_mode = abi.CFD_GUESS_LEARNED
-        net, gate = learned.Net.load(), args.guess_gate
+        k.params.guess_mode = (abi.CFD_GUESS_LEARNED_EXTRAPOLATED if refine
+                               else abi.CFD_GUESS_LEARNED)
+        net, gate = learned.Net.load(), (1.0e9 if refine else args.guess_gate)
     elif args.guess == "zero":
         k.params.guess_mode = abi.CFD_GUESS_ZERO
     if args.bicg_tol_mode:
@@ -780,6 +787,8 @@ def main_ours(args):
         S = solver.Solver(k, precision=prec)
         if net is not None:
             S.set_guess_net(net, gate)
+            if refine:
+                S.set_guess_refine(True)
         S.step(W)
         S.step(args.profile_steps)
         return
@@ -788,7 +797,7 @@ def main_ours(args):
     dist.barrier()
     clocks = Clocks(local)
     clocks.start()
-    S, ms_step, launches, rep = timed_run(solver, k, prec, W, K, L, net, gate)
+    S, ms_step, launches, rep = timed_run(solver, k, prec, W, K, L, net, gate, refine)
     guess_stats = S.guess_stats() if net is not None else None
     torch.cuda.synchronize()
     dist.barrier()

@@ -355,6 +355,8 @@ struct PcgArgs {
     int* iters_out;              // [2]
     int accumulate;              // mixed form: a second pass of the same solves (iterations
                                  // add to iters_out, the cap counts both passes)
+    int* iterated;               // mixed form (nullable): set to 1 when a solve iterated (x
+                                 // moved from the guess whose precise residual was formed)
     double* rz_out;              // [2]
     double* relres_out;          // [2] ||r||/||ref|| (relative modes), may be null
     int* conv_out;               // [2]

@@ -243,6 +243,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         if (st) return st;
     }
     CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
+    if (mixed && prm.bicg_tol_mode == CFD_BICG_TOL_REL) a.iterated = d_iterated;
     void* args[] = {&a};
     CFD_CUDA(cudaLaunchCooperativeKernel(mixed ? (void*)k_pcg_mixed : (void*)k_pcg_fp64, dim3(pcg_grid),
                                          dim3(256), args, 0, stream));
@@ -253,7 +254,8 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         // again, and the solves that it leaves above the test iterate once more
         PcgArgs b = a;
         b.gflag = nullptr;
-        b.only_if = nullptr;
+        b.only_if = d_iterated;  // nothing to refine where no solve moved from its guess
+        b.iterated = nullptr;
         b.accumulate = 1;
         const unsigned rgrid = (sv && branch_bpsm > 0)
                                    ? (unsigned)std::min<long>(b.nblk_r, (long)branch_bpsm * nsm)
@@ -864,6 +866,8 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if (prm.bicg_tol_mode != CFD_BICG_TOL_ABS) {  // the FP64-assembled operator
             if ((st = dalloc(&d_val_lo, adj.col.size()))) return st;
             if ((st = dalloc(&d_g64, 2 * (size_t)E))) return st;
+            if ((st = dalloc(&d_iterated, 1))) return st;
+            CFD_CUDA(cudaMemsetAsync(d_iterated, 0, sizeof(int), stream));
         }
         if ((st = dalloc(&d_gterms, E))) return st;
         // slot (e, i) -> its position in element-around-point order

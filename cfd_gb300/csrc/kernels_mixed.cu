@@ -848,8 +848,9 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
 // floor under every guess built from them.  Assembled in FP64 and held as valf + val_lo
 // (split_bits, 2^-47), the operator moves as smoothly as the mesh, the first residual (the
 // precise product) sees only that, and the FP32 iterations keep valf.
-// Per element: the FP64 gradients and Laplacian weight q of mLaplace.f90:28-56, as the FP32
-// element pass forms them (edge vectors from the first node, q = (a sum|grad N_i|^2)^2/3).
+// Per element: the 3x3 element matrix q (grad N_i . grad N_j) of mLaplace.f90:28-56 in FP64,
+// with the gradients and weight as the FP32 element pass forms them (edge vectors from the
+// first node, q = (a sum|grad N_i|^2)^2/3); stored symmetric: K00, K01, K02, K11, K12, K22.
 __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
                               const double* __restrict__ X, const double* __restrict__ Y,
                               double4* __restrict__ g64) {
@@ -862,15 +863,18 @@ __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
         const double ia = 1.0 / a2;
         const double gx0 = (y1 - y2) * ia, gx1 = y2 * ia, gx2 = -y1 * ia;
         const double gy0 = (x2 - x1) * ia, gy1 = -x2 * ia, gy2 = x1 * ia;
-        const double s2 = gx0 * gx0 + gy0 * gy0 + gx1 * gx1 + gy1 * gy1 + gx2 * gx2 + gy2 * gy2;
-        const double am = 0.5 * a2 * s2;
-        g64[2 * (size_t)e] = make_double4(gx0, gx1, gx2, gy0);
-        g64[2 * (size_t)e + 1] = make_double4(gy1, gy2, am * am * (1.0 / 3.0), 0.0);
+        const double k00 = gx0 * gx0 + gy0 * gy0, k11 = gx1 * gx1 + gy1 * gy1;
+        const double k22 = gx2 * gx2 + gy2 * gy2;
+        const double am = 0.5 * a2 * ((k00 + k11) + k22);
+        const double q = am * am * (1.0 / 3.0);
+        g64[2 * (size_t)e] = make_double4(k00 * q, (gx0 * gx1 + gy0 * gy1) * q,
+                                          (gx0 * gx2 + gy0 * gy2) * q, k11 * q);
+        g64[2 * (size_t)e + 1] = make_double4((gx1 * gx2 + gy1 * gy2) * q, k22 * q, 0.0, 0.0);
     }
 }
 
-// Per node: the FP64 row (in shared memory; rows longer than kLapRow summed per entry),
-// written as valf + val_lo, and 1/diag from the FP64 diagonal
+// Per node: the FP64 row (in shared memory; rows longer than kLapRow summed per entry) from
+// row i of each element's matrix, written as valf + val_lo, and 1/diag from the FP64 diagonal
 constexpr int kLap64Block = 128;
 __global__ void __launch_bounds__(kLap64Block)
 k_lap64(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
@@ -892,16 +896,16 @@ k_lap64(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esu
                 const int slot = esup_slot[sl];
                 const int e = slot / 3, i = slot - 3 * e;
                 const double4 ga = g64[2 * (size_t)e], gb = g64[2 * (size_t)e + 1];
-                const double gx[3] = {ga.x, ga.y, ga.z}, gy[3] = {ga.w, gb.x, gb.y};
-                const double q = gb.z;
-                const double dxi = gx[i], dyi = gy[i];
+                // row i of the symmetric element matrix (K00 K01 K02 / K11 K12 / K22)
+                const double r[3] = {i == 0 ? ga.x : (i == 1 ? ga.y : ga.z),
+                                     i == 0 ? ga.y : (i == 1 ? ga.w : gb.x),
+                                     i == 0 ? ga.z : (i == 1 ? gb.x : gb.y)};
                 const uchar4 pos = lap_pos[sl];
                 const unsigned char pj[3] = {pos.x, pos.y, pos.z};
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
-                    const double v = (dxi * gx[j] + dyi * gy[j]) * q;
-                    if (nk == 1) acc[pj[j]] += v;
-                    else if (pj[j] == kk) one += v;
+                    if (nk == 1) acc[pj[j]] += r[j];
+                    else if (pj[j] == kk) one += r[j];
                 }
             }
             if (nk == 1) {

@@ -558,7 +558,10 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                 pend[s] = true;
             }
         }
-    if (done[0] && done[1]) return;
+    if (done[0] && done[1]) {
+        if (a.iterated && blockIdx.x == 0 && t == 0) *a.iterated = 0;
+        return;
+    }
 
     int k = 0;
     int last_iter[2] = {0, 0};
@@ -790,6 +793,7 @@ __global__ void __launch_bounds__(256, 2) k_pcg_mixed(PcgArgs a) {
                 a.xf[s][i] = d2f_trunc(xi);
             }
         }
+    if (blockIdx.x == 0 && t == 0 && a.iterated) *a.iterated = (last_iter[0] + last_iter[1]) > 0;
     if (blockIdx.x == 0 && t == 0)
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
