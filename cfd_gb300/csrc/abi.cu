@@ -69,6 +69,19 @@ int arg_error(const char* what) {
     return CFD_ERR_ARG;
 }
 
+// The device's view of a pointer into pinned (page-locked, mapped) host memory, 16-B
+// aligned; nullptr for pageable or device memory, which then take cudaMemcpyAsync.
+const double* pinned_device_view(const double* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+    if (reinterpret_cast<uintptr_t>(a.devicePointer) & 15) return nullptr;
+    return static_cast<const double*>(a.devicePointer);
+}
+
 // inpoel(3,nelem) 1-based -> int4 0-based, with range checks
 int make_elems(const int* inpoel, int nelem, int npoin, std::vector<int4>& el) {
     el.resize(nelem);
@@ -277,6 +290,21 @@ int cfd_ctx_upload_state(cfd_ctx* ctx, const double* U, const double* T, const d
     if (!ctx) return arg_error("ctx");
     Ctx& c = ctx->impl;
     const size_t N = c.npoin;
+    // U in pinned host memory with the velocities left out: one kernel reads it over the
+    // host link and writes U, the velocities and the mixed form's shadows (k_upload_U)
+    const double* hU = (U && !VEL_X && !VEL_Y) ? pinned_device_view(U) : nullptr;
+    if (hU) {
+        const bool mx = c.prec == CFD_PREC_MIXED;
+        CFD_LAUNCH(k_upload_U, blocks_for((long)N, 256), 256, 0, c.stream, (int)N, hU, c.d_U,
+                   c.d_VX, c.d_VY, mx ? c.d_Uhi : nullptr, mx ? c.d_Ulo : nullptr,
+                   mx ? c.d_VXf : nullptr, mx ? c.d_VYf : nullptr);
+        if (T) {
+            CFD_CUDA(cudaMemcpyAsync(c.d_T, T, 8 * N, cudaMemcpyHostToDevice, c.stream));
+            if (mx) TRY(c.narrow_mixed(false, true, false, false, false, false));
+        }
+        CFD_CUDA(cudaStreamSynchronize(c.stream));
+        return CFD_OK;
+    }
     if (U) CFD_CUDA(cudaMemcpyAsync(c.d_U, U, 32 * N, cudaMemcpyHostToDevice, c.stream));
     if (T) CFD_CUDA(cudaMemcpyAsync(c.d_T, T, 8 * N, cudaMemcpyHostToDevice, c.stream));
     if (VEL_X) CFD_CUDA(cudaMemcpyAsync(c.d_VX, VEL_X, 8 * N, cudaMemcpyHostToDevice, c.stream));

@@ -77,6 +77,37 @@ __global__ void k_narrow_state(int npoin, const double* __restrict__ U, const do
     if (WX) Wf[p] = make_float2((float)WX[p], (float)WY[p]);
 }
 
+// Upload of U straight from pinned host memory (read by the kernel over the host link): the
+// FP64 copy, the velocities ρu/ρ, ρv/ρ (k_vel_from_U's quotients) and, when Uhi is given,
+// the mixed form's hi/lo split and float velocities (k_narrow_state's) in one pass, so
+// the HBM writes ride under the link's transfer instead of following it.  hU is 16-B
+// aligned (the caller checks).
+__global__ void k_upload_U(int npoin, const double* __restrict__ hU, double* __restrict__ U,
+                           double* __restrict__ VX, double* __restrict__ VY,
+                           float4* __restrict__ Uhi, float4* __restrict__ Ulo,
+                           float* __restrict__ VXf, float* __restrict__ VYf) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npoin) return;
+    const double2 a = reinterpret_cast<const double2*>(hU)[2 * (size_t)p];
+    const double2 b = reinterpret_cast<const double2*>(hU)[2 * (size_t)p + 1];
+    reinterpret_cast<double2*>(U)[2 * (size_t)p] = a;
+    reinterpret_cast<double2*>(U)[2 * (size_t)p + 1] = b;
+    const double vx = a.y / a.x, vy = b.x / a.x;
+    VX[p] = vx;
+    VY[p] = vy;
+    if (Uhi) {
+        float h[4], l[4];
+        split(a.x, h[0], l[0]);
+        split(a.y, h[1], l[1]);
+        split(b.x, h[2], l[2]);
+        split(b.y, h[3], l[3]);
+        Uhi[p] = make_float4(h[0], h[1], h[2], h[3]);
+        Ulo[p] = make_float4(l[0], l[1], l[2], l[3]);
+        VXf[p] = (float)vx;
+        VYf[p] = (float)vy;
+    }
+}
+
 // double -> float
 __global__ void k_narrow(long n, const double* __restrict__ a, float* __restrict__ b) {
     const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;

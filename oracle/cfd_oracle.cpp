@@ -33,6 +33,11 @@ inline double pow05(double x) { return g_pow_mode ? std::pow(x, 0.5) : std::sqrt
 // run in element order afterwards, so any thread count gives the one-thread result.
 int g_ordered_scatter = 0;
 
+// The thread count of every parallel loop, given on each loop (num_threads) rather than
+// through the OpenMP runtime's per-thread default, which another library in the same
+// process (one that shares the runtime) may change.
+int g_threads = 1;
+
 // ESTAB's DUX/DUY evaluation (CFD_ESTAB_*), set by or_set_estab_mode / the case params
 int g_estab_mode = CFD_ESTAB_REFERENCE;
 double g_estab_eps = 1.0e-3;  // CFD_ESTAB_REGULARIZED: relative gradient scale
@@ -49,13 +54,7 @@ struct Clock {
 
 extern "C" {
 
-void or_set_threads(int n) {
-#ifdef _OPENMP
-    omp_set_num_threads(n > 0 ? n : 1);
-#else
-    (void)n;
-#endif
-}
+void or_set_threads(int n) { g_threads = n > 0 ? n : 1; }
 
 void or_set_ordered_scatter(int on) { g_ordered_scatter = on; }
 void or_set_estab_mode(int mode) { g_estab_mode = mode; }
@@ -85,7 +84,7 @@ void or_set_estab_dir(double ux, double uy) {
 
 int or_get_threads(void) {
 #ifdef _OPENMP
-    return omp_get_max_threads();
+    return g_threads;
 #else
     return 1;
 #endif
@@ -96,7 +95,7 @@ void or_deriv(int npoin, int nelem, const double* X, const double* Y, const int*
               double* area, double* dNx, double* dNy, double* HH, double* HHX,
               double* HHY, double* hmin) {
     (void)npoin;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int e = 0; e < nelem; ++e) {
         double xl[3], yl[3];
         for (int i = 0; i < 3; ++i) {
@@ -295,7 +294,7 @@ void or_calcrhs(double* rhs, const double* U, const double* theta, const double*
     const bool viscous = mu_ref > 2.2250738585072014e-308;  // tiny(0d0), :119
     const bool ordered = g_ordered_scatter && or_get_threads() > 1;
     std::vector<double> held(ordered ? 12 * (size_t)nelem : 0);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int e = 0; e < nelem; ++e) {
         double r[3][4] = {{0}};
         const int p[3] = {inpoel[3 * e] - 1, inpoel[3 * e + 1] - 1, inpoel[3 * e + 2] - 1};
@@ -401,7 +400,7 @@ void or_fuente(double* rhs, const double* U, const double* W_X, const double* W_
     static const double sp[3][3] = {{0.5, 0.0, 0.5}, {0.5, 0.5, 0.0}, {0.0, 0.5, 0.5}};
     const bool ordered = g_ordered_scatter && or_get_threads() > 1;
     std::vector<double> held(ordered ? 12 * (size_t)nelem : 0);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int e = 0; e < nelem; ++e) {
         const int p[3] = {inpoel[3 * e] - 1, inpoel[3 * e + 1] - 1, inpoel[3 * e + 2] - 1};
         double Ux[4], Uy[4];
@@ -552,7 +551,7 @@ void or_laplace(const int* inpoel, const double* dNx, const double* dNy, int nel
                 const int* lap_rowptr, double* lap_diag) {
     (void)nelem;
     for (int k = 0; k < lap_rowptr[npoin]; ++k) lap_sparse[k] = 0.0;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int ip = 1; ip <= npoin; ++ip) {
         for (int s = esup2[ip - 1]; s < esup2[ip]; ++s) {
             int e = esup1[s] - 1;
@@ -598,7 +597,7 @@ static double tree256(double* s) {
 double or_vecdot(int n, const double* x, const double* y) {
     const long nc = (n + 1023) / 1024;
     std::vector<double> part(nc > 0 ? nc : 1);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (long c = 0; c < nc; ++c) {
         double s[256];
         long base = c * 1024;
@@ -633,7 +632,7 @@ void or_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
                   cfd_solve_info* info) {
     std::vector<double> y(npoin), p(npoin), r(npoin), z(npoin);
     auto spmv = [&](const double* v, double* out) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < npoin; ++i) {
             double dot = 0.0;
             for (int j = spRowptr[i]; j < spRowptr[i + 1]; ++j) dot = dot + spMtx[j] * v[spIdx[j] - 1];
@@ -657,7 +656,7 @@ void or_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
     }
     spmv(x, y.data());
     copy2(x, y.data());
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int i = 0; i < npoin; ++i) r[i] = -1.0 * y[i] + b[i];  // vecsum(-1, y, b, r)
     for (int i = 0; i < nfix; ++i) r[x_fixIdx[i] - 1] = 0.0;  // assign2
     double rr = or_vecdot(npoin, r.data(), r.data());
@@ -668,20 +667,20 @@ void or_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
         if (info) { info->iters = 0; info->converged = 1; info->rz = rr; info->relres = relres(rr); }
         return;
     }
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int i = 0; i < npoin; ++i) p[i] = r[i] / diagMtx[i];
     double err_new = or_vecdot(npoin, r.data(), p.data());
     spmv(p.data(), y.data());
     copy2(p.data(), y.data());
     double py = or_vecdot(npoin, p.data(), y.data());
     double alfa = err_new / py;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int i = 0; i < npoin; ++i) x[i] = alfa * p[i] + x[i];
     double err_old = err_new;
     while ((rel ? rr > thr : std::fabs(err_old) > tol) && k < maxit) {
         k = k + 1;
         const double malfa = -alfa;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < npoin; ++i) {
             r[i] = malfa * y[i] + r[i];
             z[i] = r[i] / diagMtx[i];
@@ -689,13 +688,13 @@ void or_bicg_mode(const double* spMtx, const int* spIdx, const int* spRowptr,
         err_new = or_vecdot(npoin, r.data(), z.data());
         if (rel) rr = or_vecdot(npoin, r.data(), r.data());
         double beta = err_new / err_old;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < npoin; ++i) p[i] = beta * p[i] + z[i];
         spmv(p.data(), y.data());
         copy2(p.data(), y.data());
         py = or_vecdot(npoin, p.data(), y.data());
         alfa = err_new / py;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < npoin; ++i) x[i] = alfa * p[i] + x[i];
         err_old = err_new;
     }
@@ -1155,7 +1154,7 @@ void rk(or_case* c, double dtmin) {
         double* U = c->U.data();
         double* U1 = c->U1.data();
         const double* R = c->RHS.data();
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {  // :696-698 and :708-717
             for (int q = 0; q < 4; ++q) U1[4 * i + q] = U[4 * i + q] - rk_fact / c->M[i] * R[4 * i + q];
             double rho = U1[4 * i];
@@ -1187,7 +1186,7 @@ void rk(or_case* c, double dtmin) {
             c->T[j] = c->rfixt[i];
             c->E[j] = c->T[j] * p.fr / gm + 0.5 * (c->VEL_X[j] * c->VEL_X[j] + c->VEL_Y[j] * c->VEL_Y[j]);
         }
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {  // :820-825
             U1[4 * i] = c->RHO[i];
             U1[4 * i + 1] = c->VEL_X[i] * c->RHO[i];

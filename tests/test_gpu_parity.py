@@ -216,6 +216,40 @@ def test_step_after_upload_of_U_only(gpu_lib):
     run_pair(k, 2, setup=setup)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_upload_from_pinned_memory(gpu_lib, prec):
+    """cfd_ctx_upload_state with U in pinned host memory reads it with one kernel
+    (k_upload_U: U, the velocities and the mixed form's shadows); the state, the fields and
+    the steps after it equal those of the copy-engine path (pageable U) bit for bit."""
+    import torch
+    from cfd_gb300 import abi, solver
+    k = small_case(3, scale=16, seed=5)
+    U, T, _, _ = perturbed_state(k, seed=4, amp=0.05)
+    p = abi.CFD_PREC_FP64 if prec == "fp64" else abi.CFD_PREC_MIXED
+    hU = torch.empty(U.shape, dtype=torch.float64, pin_memory=True).numpy()
+    hU[:] = U
+    L = abi.lib()
+    for withT in (True, False):
+        a, b = solver.Solver(k, precision=p), solver.Solver(k, precision=p)
+        a.set_state(U, T if withT else None)
+        l0 = L.cfd_kernel_launches()
+        b.set_state(hU, T if withT else None)
+        if prec == "mixed" and not withT:  # one kernel instead of k_vel_from_U + k_narrow_state
+            assert L.cfd_kernel_launches() - l0 == 1
+        for key in ("U", "T"):
+            eq(a.state()[key], b.state()[key], f"{prec} upload {key}")
+        fa, fb = a.fields(), b.fields()
+        for key in ("VEL_X", "VEL_Y"):
+            eq(fa[key], fb[key], f"{prec} upload {key}")
+        a.step(2)
+        b.step(2)
+        sa, sb = a.state(), b.state()
+        for key in ("U", "T", "X", "Y"):
+            eq(sa[key], sb[key], f"{prec} 2 steps after the upload {key}")
+        a.close()
+        b.close()
+
+
 def test_bad_inputs_return_status(gpu_lib):
     from cfd_gb300 import abi, solver
     k = small_case(1, scale=8)
