@@ -209,10 +209,10 @@ __global__ void k_elem_geometry(int nelem, const int4* elem, const double* X, co
                                 float4* geo, double2* terms, NormalsArgs nv);
 constexpr int kGeoNodeBlock = 128;  // block size of k_node_geometry
 __global__ void k_elem_grad64(int nelem, const int4* elem, const double* X, const double* Y,
-                              double4* g64);
-__global__ void k_lap64(int npoin, const int* esup_ptr, const int* esup_slot,
-                        const uchar4* lap_pos, const double4* g64, const int* rowptr,
-                        float* valf, float* val_lo, double* invdiag, float* invdiagf);
+                              const int* slot_pos, double* k64);
+__global__ void k_lap64(int npoin, const int* esup_ptr, const uchar4* lap_pos, const double* k64,
+                        const int* rowptr, float* valf, float* val_lo, double* invdiag,
+                        float* invdiagf);
 __global__ void k_node_geometry(int npoin, const int* esup_ptr, const int* esup_slot,
                                 const uchar4* lap_pos, const float4* geo, const double2* terms,
                                 const double* dtp, int gcl, const int* rowptr, float* valf,
@@ -338,6 +338,8 @@ struct PcgArgs {
     float* pf[2][2];
     float* zf[2];
     float* xf[2];                // (float)x, kept equal to it on entry and exit
+    float2* xs[2];               // relative tests: (hi, lo) = split_bits of the vector the
+                                 // precise product reads (k_split_x before each such pass)
     const float* invdiagf;       // (float)(1/diag), with invdiag = (double)invdiagf
     double* part_r;              // [4][nblk_r] per-block partials of the row kernels
     long nblk_r;                 // 256-row blocks of the row kernels
@@ -370,6 +372,9 @@ __global__ void k_selftest_waits(GridBar* gb, int* out, long long limit);
 __global__ void k_bicg_fix_mixed(PcgArgs a);
 // first pass of a mixed solve (k_bicg_resid_mixed, the variant of a.tol_mode)
 cudaError_t launch_bicg_resid_mixed(unsigned grid, cudaStream_t stream, const PcgArgs& a);
+// relative tests: a.xs[s] = split_bits(v_s) for the precise product of the next pass; runs
+// only when gate is null or *gate != 0
+__global__ void k_split_x(PcgArgs a, const double* v0, const double* v1, const int* gate);
 __global__ void k_bicg_dir_mixed(PcgArgs a);
 // learned-guess judge: r.z of the candidate (cand[s]) per solve when gflag[0] is set
 __global__ void k_guess_judge(PcgArgs a, const double* cand0, const double* cand1, double* rr);

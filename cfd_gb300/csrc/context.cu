@@ -177,6 +177,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
             a.pf[s][1] = d_pf[s][1];
             a.zf[s] = d_zf[s];
             a.xf[s] = d_posf[s];
+            a.xs[s] = d_xs[s];
         }
         a.invdiagf = d_invdiagf;
         a.part_r = d_part_r;
@@ -201,18 +202,29 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
             int st = guess_extrapolate(a, stream, rgrid);
             if (st) return st;
         }
+        // the relative tests' precise products read x (and the candidates) split in hi + lo
+        const bool split = prm.bicg_tol_mode != CFD_BICG_TOL_ABS;
+        if (split)
+            CFD_LAUNCH(k_split_x, rgrid, 256, 0, stream, a, (const double*)d_pos[0],
+                       (const double*)d_pos[1], (const int*)nullptr);
         CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, a));
         if (fields) {
             int st = mpnn::fields_guess(lgraph, stream, d_X, d_Y, d_xfix[0], d_xfix[1], d_pos[0],
                                         d_pos[1], d_cand[0], d_cand[1]);
             if (st) return st;
             const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
+            if (split)
+                CFD_LAUNCH(k_split_x, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                           (const double*)d_cand[1], (const int*)d_gflag);
             CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
                        (const double*)d_cand[1], d_grr);
             CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
                        (const double*)d_cand[1], (const double*)d_grr, d_gstats + 4);
             PcgArgs b = a;
             b.only_if = d_gflag + 1;
+            if (split)
+                CFD_LAUNCH(k_split_x, gsz, 256, 0, stream, b, (const double*)d_pos[0],
+                           (const double*)d_pos[1], b.only_if);
             CFD_CUDA(launch_bicg_resid_mixed(gsz, stream, b));
         }
         if (learned) {
@@ -224,12 +236,18 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
             if (st) return st;
             // grid-stride grids of a few waves: a closed gate costs little
             const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
+            if (split)
+                CFD_LAUNCH(k_split_x, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                           (const double*)d_cand[1], (const int*)d_gflag);
             CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
                        (const double*)d_cand[1], d_grr);
             CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
                        (const double*)d_cand[1], (const double*)d_grr, d_gstats);
             PcgArgs b = a;
             b.only_if = d_gflag + 1;
+            if (split)
+                CFD_LAUNCH(k_split_x, gsz, 256, 0, stream, b, (const double*)d_pos[0],
+                           (const double*)d_pos[1], b.only_if);
             CFD_CUDA(launch_bicg_resid_mixed(gsz, stream, b));
             if (guess_refine) {
                 if ((st = mpnn::fields_seed(lgraph, stream))) return st;
@@ -260,6 +278,8 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         const unsigned rgrid = (sv && branch_bpsm > 0)
                                    ? (unsigned)std::min<long>(b.nblk_r, (long)branch_bpsm * nsm)
                                    : (unsigned)b.nblk_r;
+        CFD_LAUNCH(k_split_x, rgrid, 256, 0, stream, b, (const double*)d_pos[0],
+                   (const double*)d_pos[1], b.only_if);
         CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, b));
         CFD_LAUNCH(k_bicg_dir_mixed, rgrid, 256, 0, stream, b);
         CFD_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), stream));
@@ -865,8 +885,10 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
         if ((st = dalloc(&d_valf, adj.col.size()))) return st;
         if (prm.bicg_tol_mode != CFD_BICG_TOL_ABS) {  // the FP64-assembled operator
             if ((st = dalloc(&d_val_lo, adj.col.size()))) return st;
-            if ((st = dalloc(&d_g64, 2 * (size_t)E))) return st;
+            if ((st = dalloc(&d_k64, 9 * (size_t)E))) return st;
             if ((st = dalloc(&d_iterated, 1))) return st;
+            for (int k = 0; k < 2; ++k)
+                if ((st = dalloc(&d_xs[k], (size_t)N))) return st;
             CFD_CUDA(cudaMemsetAsync(d_iterated, 0, sizeof(int), stream));
         }
         if ((st = dalloc(&d_gterms, E))) return st;
@@ -974,9 +996,9 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
                to_next ? (float2*)nullptr : d_Wof);
     if (d_val_lo) {  // relative tests: the mesh-motion operator again, in FP64 (k_lap64)
         CFD_LAUNCH(k_elem_grad64, branch_grid(E, TB, sv), TB, 0, stream, E, d_elem, d_X, d_Y,
-                   d_g64);
-        CFD_LAUNCH(k_lap64, branch_grid(N, 128, sv), 128, 0, stream, N, d_esup_ptr, d_esup_slot,
-                   d_lap_pos, (const double4*)d_g64, d_rowptr, d_valf, d_val_lo, d_invdiag,
+                   (const int*)d_slot_pos, d_k64);
+        CFD_LAUNCH(k_lap64, branch_grid(N, 128, sv), 128, 0, stream, N, d_esup_ptr, d_lap_pos,
+                   (const double*)d_k64, d_rowptr, d_valf, d_val_lo, d_invdiag,
                    d_invdiagf);
     }
     tstop(TM_LAPLACE);

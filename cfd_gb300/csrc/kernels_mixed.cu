@@ -880,36 +880,49 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
 // (split_bits, 2^-47), the operator moves as smoothly as the mesh, the first residual (the
 // precise product) sees only that, and the FP32 iterations keep valf.
 // Per element: the 3x3 element matrix q (grad N_i . grad N_j) of mLaplace.f90:28-56 in FP64,
-// with the gradients and weight as the FP32 element pass forms them (edge vectors from the
-// first node, q = (a sum|grad N_i|^2)^2/3); stored symmetric: K00, K01, K02, K11, K12, K22.
+// q = (a sum |grad N_i|^2)^2 / 3 with a the area.  With e_i = a2 grad N_i (the edge vectors
+// from the first node, rotated; a2 = twice the signed area) the entries are
+// (e_i . e_j) S^2 / (12 a2^4), S = sum |e_i|^2: one division per element (GB300's FP64 pipe
+// bounds this pass).  Row i goes to the element's slot (e, i) in element-around-point order
+// (slot_pos), so that k_lap64 reads each node's rows contiguously.
 __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
                               const double* __restrict__ X, const double* __restrict__ Y,
-                              double4* __restrict__ g64) {
+                              const int* __restrict__ slot_pos, double* __restrict__ k64) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += gridDim.x * blockDim.x) {
         const int4 n = elem[e];
         const double X0 = X[n.x], Y0 = Y[n.x];
         const double x1 = X[n.y] - X0, y1 = Y[n.y] - Y0;
         const double x2 = X[n.z] - X0, y2 = Y[n.z] - Y0;
+        const double ex0 = y1 - y2, ey0 = x2 - x1;  // e_0; e_1 = (y2, -x2), e_2 = (-y1, x1)
+        const double d00 = ex0 * ex0 + ey0 * ey0;
+        const double d11 = y2 * y2 + x2 * x2;
+        const double d22 = y1 * y1 + x1 * x1;
+        const double d01 = ex0 * y2 - ey0 * x2;
+        const double d02 = ey0 * x1 - ex0 * y1;
+        const double d12 = -(y2 * y1 + x2 * x1);
+        const double S = (d00 + d11) + d22;
         const double a2 = x1 * y2 - x2 * y1;
-        const double ia = 1.0 / a2;
-        const double gx0 = (y1 - y2) * ia, gx1 = y2 * ia, gx2 = -y1 * ia;
-        const double gy0 = (x2 - x1) * ia, gy1 = -x2 * ia, gy2 = x1 * ia;
-        const double k00 = gx0 * gx0 + gy0 * gy0, k11 = gx1 * gx1 + gy1 * gy1;
-        const double k22 = gx2 * gx2 + gy2 * gy2;
-        const double am = 0.5 * a2 * ((k00 + k11) + k22);
-        const double q = am * am * (1.0 / 3.0);
-        g64[2 * (size_t)e] = make_double4(k00 * q, (gx0 * gx1 + gy0 * gy1) * q,
-                                          (gx0 * gx2 + gy0 * gy2) * q, k11 * q);
-        g64[2 * (size_t)e + 1] = make_double4((gx1 * gx2 + gy1 * gy2) * q, k22 * q, 0.0, 0.0);
+        const double t = S / (a2 * a2);
+        const double c = t * t * (1.0 / 12.0);
+        const double K[3][3] = {{d00 * c, d01 * c, d02 * c},
+                                {d01 * c, d11 * c, d12 * c},
+                                {d02 * c, d12 * c, d22 * c}};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            double* r = k64 + 3 * (size_t)slot_pos[3 * (size_t)e + i];
+            r[0] = K[i][0];
+            r[1] = K[i][1];
+            r[2] = K[i][2];
+        }
     }
 }
 
 // Per node: the FP64 row (in shared memory; rows longer than kLapRow summed per entry) from
-// row i of each element's matrix, written as valf + val_lo, and 1/diag from the FP64 diagonal
+// its slots' element-matrix rows (contiguous in k64), written as valf + val_lo, and 1/diag from the FP64 diagonal
 constexpr int kLap64Block = 128;
 __global__ void __launch_bounds__(kLap64Block)
-k_lap64(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
-        const uchar4* __restrict__ lap_pos, const double4* __restrict__ g64,
+k_lap64(int npoin, const int* __restrict__ esup_ptr, const uchar4* __restrict__ lap_pos,
+        const double* __restrict__ k64,
         const int* __restrict__ rowptr, float* __restrict__ valf, float* __restrict__ val_lo,
         double* __restrict__ invdiag, float* __restrict__ invdiagf) {
     __shared__ double row[kLap64Block][kLapRow + 1];
@@ -924,13 +937,9 @@ k_lap64(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esu
             for (int k = 0; k < kLapRow; ++k) acc[k] = 0.0;
             double one = 0.0;  // the entry kk of a long row
             for (int sl = s0; sl < s1; ++sl) {
-                const int slot = esup_slot[sl];
-                const int e = slot / 3, i = slot - 3 * e;
-                const double4 ga = g64[2 * (size_t)e], gb = g64[2 * (size_t)e + 1];
-                // row i of the symmetric element matrix (K00 K01 K02 / K11 K12 / K22)
-                const double r[3] = {i == 0 ? ga.x : (i == 1 ? ga.y : ga.z),
-                                     i == 0 ? ga.y : (i == 1 ? ga.w : gb.x),
-                                     i == 0 ? ga.z : (i == 1 ? gb.x : gb.y)};
+                // the row of this slot's element matrix (k_elem_grad64)
+                const double* k = k64 + 3 * (size_t)sl;
+                const double r[3] = {k[0], k[1], k[2]};
                 const uchar4 pos = lap_pos[sl];
                 const unsigned char pj[3] = {pos.x, pos.y, pos.z};
 #pragma unroll
@@ -955,7 +964,9 @@ k_lap64(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esu
                 if (kk == 0) diag = one;
             }
         }
-        const float idf = d2f_trunc(1.0 / diag);
+        // the Jacobi scaling is FP32 in every pass (invdiag = (double)invdiagf): its quotient
+        // is formed in FP32, as k_node_geometry forms it
+        const float idf = 1.f / d2f_trunc(diag);
         invdiagf[p] = idf;
         invdiag[p] = f2d_bits(idf);
     }

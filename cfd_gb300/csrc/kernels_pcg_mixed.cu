@@ -16,8 +16,9 @@
 
 namespace cfd {
 
-// The SpMV rows gather in batches of B entries (8 in the residual kernel, 4 in the
-// register-limited persistent kernel): the column indices and values of a batch are loaded
+// The SpMV rows gather in batches of B entries (8 in the FP32 residual kernel, 4 in the
+// register-limited persistent kernel and in the precise residual, whose 4-entry batches
+// measured 1.29 -> 1.25 ms per 1M-node step against 8): the column indices and values of a batch are loaded
 // together, then the gathered vector entries, so each batch costs two dependent memory
 // latencies instead of two per entry.  The products are still summed in column order.
 
@@ -65,31 +66,30 @@ __device__ __forceinline__ void spmv_row2_f(const PcgArgs& a, int i, const float
     }
 }
 
-// Row i of A times the FP64 vectors (x0, x1), as accurately as FP64 arithmetic: each x_j is
-// split into FP32 hi + lo (split_bits, exact to 2^-47), a_ij*hi is formed exactly as a
-// float pair (product + fmaf remainder), the products are summed with a compensated (Neumaier)
-// FP32 sum and the remainders and a_ij*lo terms with a plain one, and the three partial
-// sums are added in FP64; with val_lo (the relative tests: the matrix assembled in FP64 and
-// held as valf + val_lo) the a_lo*hi terms join the plain sum.  The first residual of a
-// solve, r = b - A.x, takes this product
-// under the relative stopping tests: it is the one SpMV of the solve whose operand is the
-// whole displacement rather than a correction, so an FP32 product's error there (~1e-7 of
-// |A||x|) would be a floor under the starting residual of any good initial guess.  The
-// reference's absolute test, loose against that floor, keeps the FP32 product.  With FIXC
-// also the FP32 sums over the Dirichlet columns (the row of A.x_D).
+// Row i of A times the FP64 vectors (x0, x1), as accurately as FP64 arithmetic: each x_j
+// comes split into FP32 hi + lo (split_bits, exact to 2^-47; k_split_x forms the split once
+// per node, so a row gathers 8 B per entry as the FP64 vector would), a_ij*hi is formed
+// exactly as a float pair (product + fmaf remainder), the products are summed with a
+// compensated FP32 sum (TwoSum: the exact error of every add, without a branch) and the
+// remainders and a_ij*lo terms with a plain one, and the three partial sums are added in
+// FP64; with val_lo (the relative tests: the matrix assembled in FP64 and held as valf +
+// val_lo) the a_lo*hi terms join the plain sum.  The first residual of a solve, r = b - A.x,
+// takes this product under the relative stopping tests: it is the one SpMV of the solve
+// whose operand is the whole displacement rather than a correction, so an FP32 product's
+// error there (~1e-7 of |A||x|) would be a floor under the starting residual of any good
+// initial guess.  The reference's absolute test, loose against that floor, keeps the FP32
+// product.  With FIXC also the FP32 sums over the Dirichlet columns (the row of A.x_D).
 struct Acc2 {
     float s, c, t;  // compensated sum s + c of the exact products' leading parts; tail sum t
     __device__ __forceinline__ void init() { s = c = t = 0.f; }
-    __device__ __forceinline__ void add(float m, double x, float mlo = 0.f) {
-        float hi, lo;
-        split_bits(x, hi, lo);
-        const float p = m * hi;
-        const float e = fmaf(m, hi, -p);
+    __device__ __forceinline__ void add(float m, float2 x, float mlo = 0.f) {
+        const float p = m * x.x;
+        const float e = fmaf(m, x.x, -p);
         const float u = s + p;
-        if (fabsf(s) >= fabsf(p)) c += (s - u) + p;
-        else c += (p - u) + s;
+        const float bp = u - s;
+        c += (s - (u - bp)) + (p - bp);
         s = u;
-        t += e + m * lo + mlo * hi;
+        t += e + m * x.y + mlo * x.x;
     }
     __device__ __forceinline__ double value() const {
         return (f2d_bits(s) + f2d_bits(c)) + f2d_bits(t);
@@ -97,8 +97,8 @@ struct Acc2 {
 };
 
 template <int NS, bool FIXC = false, int kRowBatch = 8>
-__device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const double* v0,
-                                            const double* v1, double& d0, double& d1,
+__device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const float2* v0,
+                                            const float2* v1, double& d0, double& d1,
                                             float* f0 = nullptr, float* f1 = nullptr) {
     Acc2 s0, s1;
     s0.init();
@@ -108,7 +108,7 @@ __device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const doubl
     for (int jb = j0; jb < j1; jb += kRowBatch) {
         int c[kRowBatch];
         float m[kRowBatch], ml[kRowBatch];
-        double x0[kRowBatch], x1[kRowBatch];
+        float2 x0[kRowBatch], x1[kRowBatch];
         bool fx[kRowBatch];
 #pragma unroll
         for (int u = 0; u < kRowBatch; ++u)
@@ -129,9 +129,9 @@ __device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const doubl
             if (jb + u < j1) {
                 s0.add(m[u], x0[u], ml[u]);
                 if (NS == 2) s1.add(m[u], x1[u], ml[u]);
-                if (FIXC && fx[u]) {
-                    g0 += m[u] * d2f_trunc(x0[u]);
-                    if (NS == 2) g1 += m[u] * d2f_trunc(x1[u]);
+                if (FIXC && fx[u]) {  // hi = d2f_trunc(x), the FP32 shadow's value
+                    g0 += m[u] * x0[u].x;
+                    if (NS == 2) g1 += m[u] * x1[u].x;
                 }
             }
     }
@@ -141,6 +141,22 @@ __device__ __forceinline__ void spmv_row2_x(const PcgArgs& a, int i, const doubl
         *f0 = g0;
         *f1 = g1;
     }
+}
+
+// a.xs[s] = split_bits(v_s) (the precise product's operand; relative tests)
+__global__ void k_split_x(PcgArgs a, const double* __restrict__ v0, const double* __restrict__ v1,
+                          const int* __restrict__ gate) {
+    if (gate && !*gate) return;  // the same in every block
+    const double* v[2] = {v0, v1};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < a.n;
+         i += (long)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+            if (s < a.nsolve) {
+                float hi, lo;
+                split_bits(v[s][i], hi, lo);
+                a.xs[s][i] = make_float2(hi, lo);
+            }
 }
 
 template <int kRowBatch = 4>
@@ -246,7 +262,7 @@ __device__ __forceinline__ void first_rows(const PcgArgs& a, double (*sh)[256]) 
         float f[2] = {0.f, 0.f};
         if (!fx) {
             if (PRECISE) {
-                spmv_row2_x<NS, RELB>(a, (int)i, a.x[0], a.x[1], d[0], d[1], &f[0], &f[1]);
+                spmv_row2_x<NS, RELB, 4>(a, (int)i, a.xs[0], a.xs[1], d[0], d[1], &f[0], &f[1]);
             } else {
                 float d32[2];
                 spmv_row2_f<NS, RELB>(a, (int)i, a.xf[0], a.xf[1], d32[0], d32[1], &f[0], &f[1]);
@@ -359,10 +375,10 @@ __global__ void __launch_bounds__(256) k_guess_judge(PcgArgs a, const double* __
                     q32 += a.valf[j] * d2f_trunc(cand[s][a.col[j]]);
                 d[s] = f2d_bits(q32);
             }
-        } else if (a.nsolve == 2) {
-            spmv_row2_x<2>(a, (int)i, cand[0], cand[1], d[0], d[1]);
+        } else if (a.nsolve == 2) {  // the candidates' split (k_split_x)
+            spmv_row2_x<2, false, 4>(a, (int)i, a.xs[0], a.xs[1], d[0], d[1]);
         } else {
-            spmv_row2_x<1>(a, (int)i, cand[0], cand[1], d[0], d[1]);
+            spmv_row2_x<1, false, 4>(a, (int)i, a.xs[0], a.xs[1], d[0], d[1]);
         }
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
