@@ -318,7 +318,10 @@ int cfd_ctx_create(cfd_ctx** ctx, const cfd_mesh* mesh, const cfd_params* p,
 void cfd_ctx_destroy(cfd_ctx* ctx);
 
 /* Overwrite the flow state.  U(4,npoin), T, VEL_X, VEL_Y may be NULL to keep the
- * current ones; when VEL_* are NULL they are derived from U. */
+ * current ones; when VEL_* are NULL they are derived from U.  With VEL_* NULL and U in
+ * pinned host memory (cudaHostAlloc / cudaHostRegister, 16-byte aligned) one kernel reads
+ * U over the host link and forms the device copies as it arrives; otherwise the arrays are
+ * copied.  Returns when U, T, VEL_* may be reused by the caller. */
 int cfd_ctx_upload_state(cfd_ctx* ctx, const double* U, const double* T,
                          const double* VEL_X, const double* VEL_Y);
 /* Overwrite the mesh-motion state: X, Y, W_X, W_Y, xpos, ypos (any may be NULL), and
