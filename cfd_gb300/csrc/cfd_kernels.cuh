@@ -210,14 +210,15 @@ __global__ void k_elem_geometry(int nelem, const int4* elem, const double* X, co
 constexpr int kGeoNodeBlock = 128;  // block size of k_node_geometry
 __global__ void k_elem_grad64(int nelem, const int4* elem, const double* X, const double* Y,
                               const int* slot_pos, double* k64);
-__global__ void k_lap64(int npoin, const int* esup_ptr, const uchar4* lap_pos, const double* k64,
-                        const int* rowptr, float* valf, float* val_lo, double* invdiag,
-                        float* invdiagf);
-__global__ void k_node_geometry(int npoin, const int* esup_ptr, const int* esup_slot,
-                                const uchar4* lap_pos, const float4* geo, const double2* terms,
-                                const double* dtp, int gcl, const int* rowptr, float* valf,
-                                double* invdiag, float* invdiagf, double* M, float* invM,
-                                const float2* W, float2* Wold);
+// k_node_geometry (block kGeoNodeBlock); row64 (relative tests): the Laplacian rows from
+// k64 (FP64, written as valf + val_lo), not from geo
+cudaError_t launch_node_geometry(bool row64, unsigned grid, cudaStream_t stream, int npoin,
+                                 const int* esup_ptr, const int* esup_slot,
+                                 const uchar4* lap_pos, const float4* geo, const double2* terms,
+                                 const double* dtp, int gcl, const int* rowptr, float* valf,
+                                 double* invdiag, float* invdiagf, double* M, float* invM,
+                                 const float2* W, float2* Wold, const double* k64,
+                                 float* val_lo);
 __global__ void k_widen_geo(int nelem, const float4* geo, double* dN, double* area);
 __global__ void k_motion_update_mixed(int npoin, const double* xpos, const double* ypos,
                                       const StepScal* sc, double* X, double* Y, double* WX,

@@ -990,17 +990,14 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
                (gcl || put_area) ? 1 : 0, d_area_old, d_area, d_areaf, geo8, d_gterms, nv);
     tstop(TM_DERIV);
     tstart(TM_LAPLACE);
-    CFD_LAUNCH(k_node_geometry, branch_grid(N, kGeoNodeBlock, sv), kGeoNodeBlock, 0, stream, N,
-               d_esup_ptr, d_esup_slot, d_lap_pos, geo8, d_gterms, &d_scal->dtmin, gcl ? 1 : 0,
-               d_rowptr, d_valf, d_invdiag, d_invdiagf, d_M, invMf, Wn,
-               to_next ? (float2*)nullptr : d_Wof);
-    if (d_val_lo) {  // relative tests: the mesh-motion operator again, in FP64 (k_lap64)
+    if (d_val_lo)  // relative tests: the mesh-motion operator in FP64 (element matrices)
         CFD_LAUNCH(k_elem_grad64, branch_grid(E, TB, sv), TB, 0, stream, E, d_elem, d_X, d_Y,
                    (const int*)d_slot_pos, d_k64);
-        CFD_LAUNCH(k_lap64, branch_grid(N, 128, sv), 128, 0, stream, N, d_esup_ptr, d_lap_pos,
-                   (const double*)d_k64, d_rowptr, d_valf, d_val_lo, d_invdiag,
-                   d_invdiagf);
-    }
+    CFD_CUDA(launch_node_geometry(d_val_lo != nullptr, branch_grid(N, kGeoNodeBlock, sv), stream,
+                                  N, d_esup_ptr, d_esup_slot, d_lap_pos, geo8, d_gterms,
+                                  &d_scal->dtmin, gcl ? 1 : 0, d_rowptr, d_valf, d_invdiag,
+                                  d_invdiagf, d_M, invMf, Wn, to_next ? (float2*)nullptr : d_Wof,
+                                  (const double*)d_k64, d_val_lo));
     tstop(TM_LAPLACE);
     return CFD_OK;
 }

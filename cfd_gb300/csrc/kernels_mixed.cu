@@ -777,11 +777,21 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
 // are summed in shared memory, longer ones in place), 1/diag, and the lumped mass: MASAS
 // (subrutinas.f90:128-153) as a compensated FP32 sum of area/3, or the gcl update
 // M += dt*(tot1+tot2)/2 in FP64 from FP64 sums (slot order) of the FP64 element terms,
-// followed by putW (W_old = W).
+// followed by putW (W_old = W).  ROW64 (the relative stopping tests): the row is the sum, in
+// FP64 and slot order, of the slots' rows of the FP64 element matrices (k_elem_grad64),
+// written as valf + val_lo; the FP32 geometry is then read only for MASAS.
 constexpr int kLapRow = 16;
 constexpr int kGeoBatch = 2;  // slots per pass of k_node_geometry
 constexpr int kGeoBlock = kGeoNodeBlock;
 
+__device__ __forceinline__ void row64_put(float* valf, float* val_lo, int at, double v) {
+    float hi, lo;
+    split_bits(v, hi, lo);
+    valf[at] = hi;
+    val_lo[at] = lo;
+}
+
+template <bool ROW64>
 __global__ void __launch_bounds__(kGeoBlock)
 k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restrict__ esup_slot,
                 const uchar4* __restrict__ lap_pos, const float4* __restrict__ geo,
@@ -789,15 +799,22 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
                 const int* __restrict__ rowptr, float* __restrict__ valf,
                 double* __restrict__ invdiag, float* __restrict__ invdiagf,
                 double* __restrict__ M, float* __restrict__ invM,
-                const float2* __restrict__ W, float2* __restrict__ Wold) {
-    __shared__ float row[kGeoBlock][kLapRow + 1];
+                const float2* __restrict__ W, float2* __restrict__ Wold,
+                const double* __restrict__ k64, float* __restrict__ val_lo) {
+    __shared__ float row[ROW64 ? 1 : kGeoBlock][kLapRow + 1];
+    __shared__ double row64[ROW64 ? kGeoBlock : 1][kLapRow + 1];
+    const bool need_geo = !ROW64 || !gcl;
     // grid-stride (a smaller grid leaves room for kernels running beside it)
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npoin; p += gridDim.x * blockDim.x) {
-    float* acc = row[threadIdx.x];
+    float* acc = row[ROW64 ? 0 : threadIdx.x];
+    double* acc64 = row64[ROW64 ? threadIdx.x : 0];
     const int r0 = rowptr[p], r1 = rowptr[p + 1];
     const int len = r1 - r0;
     const bool in_smem = len <= kLapRow;
-    if (in_smem) {
+    if (ROW64) {
+        if (in_smem)
+            for (int k = 0; k < len; ++k) acc64[k] = 0.0;
+    } else if (in_smem) {
 #pragma unroll
         for (int k = 0; k < kLapRow; ++k) acc[k] = 0.f;
     } else {
@@ -813,30 +830,47 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
         uchar4 pos[kGeoBatch];
         float4 ga[kGeoBatch], gb[kGeoBatch];
         double2 tm[kGeoBatch];
+        double kr[kGeoBatch][3];
 #pragma unroll
         for (int u = 0; u < kGeoBatch; ++u)
             if (sb + u < s1) {
                 slot[u] = esup_slot[sb + u];
                 pos[u] = lap_pos[sb + u];
+                if (ROW64) {
+                    const double* k = k64 + 3 * (size_t)(sb + u);
+                    kr[u][0] = k[0];
+                    kr[u][1] = k[1];
+                    kr[u][2] = k[2];
+                }
             }
 #pragma unroll
         for (int u = 0; u < kGeoBatch; ++u)
             if (sb + u < s1) {
                 const int e = slot[u] / 3;
-                ga[u] = geo[2 * (size_t)e];
-                gb[u] = geo[2 * (size_t)e + 1];
+                if (need_geo) {
+                    ga[u] = geo[2 * (size_t)e];
+                    gb[u] = geo[2 * (size_t)e + 1];
+                }
                 if (gcl) tm[u] = terms[e];
             }
 #pragma unroll
         for (int u = 0; u < kGeoBatch; ++u) {
             if (sb + u >= s1) break;
-            const int i = slot[u] - 3 * (slot[u] / 3);
             if (gcl) {
                 t1 = t1 + tm[u].x;
                 t2 = t2 + tm[u].y;
             } else {
                 m1.add(gb[u].z);
             }
+            if (ROW64) {
+                if (in_smem) {
+                    acc64[pos[u].x] += kr[u][0];
+                    acc64[pos[u].y] += kr[u][1];
+                    acc64[pos[u].z] += kr[u][2];
+                }
+                continue;
+            }
+            const int i = slot[u] - 3 * (slot[u] / 3);
             const float gx[3] = {ga[u].x, ga[u].y, ga[u].z}, gy[3] = {ga[u].w, gb[u].x, gb[u].y};
             const float q = gb[u].w;
             const float dxi = (i == 0) ? gx[0] : (i == 1 ? gx[1] : gx[2]);
@@ -850,14 +884,38 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
             }
         }
     }
-    float diag;
-    if (in_smem) {
-        for (int k = 0; k < len; ++k) valf[r0 + k] = acc[k];
-        diag = acc[0];
+    float idf;
+    if (ROW64) {
+        double diag;
+        if (in_smem) {
+            for (int k = 0; k < len; ++k) row64_put(valf, val_lo, r0 + k, acc64[k]);
+            diag = acc64[0];
+        } else {  // long rows (rare): one pass over the slots per entry
+            diag = 0.0;
+            for (int kk = 0; kk < len; ++kk) {
+                double one = 0.0;
+                for (int sl = s0; sl < s1; ++sl) {
+                    const double* k = k64 + 3 * (size_t)sl;
+                    const uchar4 ps = lap_pos[sl];
+                    if (ps.x == kk) one += k[0];
+                    if (ps.y == kk) one += k[1];
+                    if (ps.z == kk) one += k[2];
+                }
+                row64_put(valf, val_lo, r0 + kk, one);
+                if (kk == 0) diag = one;
+            }
+        }
+        idf = 1.f / d2f_trunc(diag);  // the Jacobi scaling is FP32 in every pass
     } else {
-        diag = valf[r0];
+        float diag;
+        if (in_smem) {
+            for (int k = 0; k < len; ++k) valf[r0 + k] = acc[k];
+            diag = acc[0];
+        } else {
+            diag = valf[r0];
+        }
+        idf = 1.f / diag;
     }
-    const float idf = 1.f / diag;
     invdiagf[p] = idf;
     invdiag[p] = f2d_bits(idf);
     double m;
@@ -871,6 +929,24 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     invM[p] = 1.f / d2f_trunc(m);
     }
 }
+cudaError_t launch_node_geometry(bool row64, unsigned grid, cudaStream_t stream, int npoin,
+                                 const int* esup_ptr, const int* esup_slot,
+                                 const uchar4* lap_pos, const float4* geo, const double2* terms,
+                                 const double* dtp, int gcl, const int* rowptr, float* valf,
+                                 double* invdiag, float* invdiagf, double* M, float* invM,
+                                 const float2* W, float2* Wold, const double* k64,
+                                 float* val_lo) {
+    if (row64)
+        k_node_geometry<true><<<grid, kGeoBlock, 0, stream>>>(
+            npoin, esup_ptr, esup_slot, lap_pos, geo, terms, dtp, gcl, rowptr, valf, invdiag,
+            invdiagf, M, invM, W, Wold, k64, val_lo);
+    else
+        k_node_geometry<false><<<grid, kGeoBlock, 0, stream>>>(
+            npoin, esup_ptr, esup_slot, lap_pos, geo, terms, dtp, gcl, rowptr, valf, invdiag,
+            invdiagf, M, invM, W, Wold, k64, val_lo);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
 
 // The mesh-motion matrix assembled in FP64 (the mixed form under the relative stopping
 // tests).  The FP32 assembly above rounds every entry afresh each step; the entries move by
@@ -878,13 +954,15 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
 // and the previous steps' solutions carry it into this step's residual (~1e-7 of it): a
 // floor under every guess built from them.  Assembled in FP64 and held as valf + val_lo
 // (split_bits, 2^-47), the operator moves as smoothly as the mesh, the first residual (the
-// precise product) sees only that, and the FP32 iterations keep valf.
+// precise product) sees only that, and the FP32 iterations keep valf.  k_node_geometry<true>
+// sums the rows.
+//
 // Per element: the 3x3 element matrix q (grad N_i . grad N_j) of mLaplace.f90:28-56 in FP64,
 // q = (a sum |grad N_i|^2)^2 / 3 with a the area.  With e_i = a2 grad N_i (the edge vectors
 // from the first node, rotated; a2 = twice the signed area) the entries are
 // (e_i . e_j) S^2 / (12 a2^4), S = sum |e_i|^2: one division per element (GB300's FP64 pipe
 // bounds this pass).  Row i goes to the element's slot (e, i) in element-around-point order
-// (slot_pos), so that k_lap64 reads each node's rows contiguously.
+// (slot_pos), so that the node pass reads each node's rows contiguously.
 __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
                               const double* __restrict__ X, const double* __restrict__ Y,
                               const int* __restrict__ slot_pos, double* __restrict__ k64) {
@@ -914,61 +992,6 @@ __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
             r[1] = K[i][1];
             r[2] = K[i][2];
         }
-    }
-}
-
-// Per node: the FP64 row (in shared memory; rows longer than kLapRow summed per entry) from
-// its slots' element-matrix rows (contiguous in k64), written as valf + val_lo, and 1/diag from the FP64 diagonal
-constexpr int kLap64Block = 128;
-__global__ void __launch_bounds__(kLap64Block)
-k_lap64(int npoin, const int* __restrict__ esup_ptr, const uchar4* __restrict__ lap_pos,
-        const double* __restrict__ k64,
-        const int* __restrict__ rowptr, float* __restrict__ valf, float* __restrict__ val_lo,
-        double* __restrict__ invdiag, float* __restrict__ invdiagf) {
-    __shared__ double row[kLap64Block][kLapRow + 1];
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npoin; p += gridDim.x * blockDim.x) {
-        double* acc = row[threadIdx.x];
-        const int r0 = rowptr[p], len = rowptr[p + 1] - r0;
-        const int s0 = esup_ptr[p], s1 = esup_ptr[p + 1];
-        const int nk = len <= kLapRow ? 1 : len;  // passes: one, or one per entry
-        double diag = 0.0;
-        for (int kk = 0; kk < nk; ++kk) {
-#pragma unroll
-            for (int k = 0; k < kLapRow; ++k) acc[k] = 0.0;
-            double one = 0.0;  // the entry kk of a long row
-            for (int sl = s0; sl < s1; ++sl) {
-                // the row of this slot's element matrix (k_elem_grad64)
-                const double* k = k64 + 3 * (size_t)sl;
-                const double r[3] = {k[0], k[1], k[2]};
-                const uchar4 pos = lap_pos[sl];
-                const unsigned char pj[3] = {pos.x, pos.y, pos.z};
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    if (nk == 1) acc[pj[j]] += r[j];
-                    else if (pj[j] == kk) one += r[j];
-                }
-            }
-            if (nk == 1) {
-                for (int k = 0; k < len; ++k) {
-                    float hi, lo;
-                    split_bits(acc[k], hi, lo);
-                    valf[r0 + k] = hi;
-                    val_lo[r0 + k] = lo;
-                }
-                diag = acc[0];
-            } else {
-                float hi, lo;
-                split_bits(one, hi, lo);
-                valf[r0 + kk] = hi;
-                val_lo[r0 + kk] = lo;
-                if (kk == 0) diag = one;
-            }
-        }
-        // the Jacobi scaling is FP32 in every pass (invdiag = (double)invdiagf): its quotient
-        // is formed in FP32, as k_node_geometry forms it
-        const float idf = 1.f / d2f_trunc(diag);
-        invdiagf[p] = idf;
-        invdiag[p] = f2d_bits(idf);
     }
 }
 
