@@ -166,6 +166,7 @@ SIGNATURES = {
     "cfd_ctx_download_fields": (C.c_int, [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "cfd_ctx_download_motion": (C.c_int, [_P, _dp, _dp]),
     "cfd_ctx_download_geometry": (C.c_int, [_P, _dp, _dp, _dp, _dp]),
+    "cfd_ctx_download_laplace": (C.c_int, [_P, _dp]),
     "cfd_ctx_timers": (C.c_int, [_P, _dp, C.c_int, _ip]),
     "cfd_ctx_timer_calls": (C.c_int, [_P, C.POINTER(C.c_longlong), C.c_int, _ip]),
     "cfd_timer_name": (C.c_char_p, [C.c_int]),

@@ -530,6 +530,28 @@ int cfd_ctx_download_geometry(cfd_ctx* ctx, double* area, double* dNx, double* d
     return CFD_OK;
 }
 
+int cfd_ctx_download_laplace(cfd_ctx* ctx, double* val) {
+    if (!ctx || !val) return arg_error("ctx/val");
+    Ctx& c = ctx->impl;
+    const size_t n = (size_t)c.nnz;
+    if (c.prec != CFD_PREC_MIXED) {
+        CFD_CUDA(cudaMemcpyAsync(val, c.d_val, 8 * n, cudaMemcpyDeviceToHost, c.stream));
+        CFD_CUDA(cudaStreamSynchronize(c.stream));
+        return CFD_OK;
+    }
+    double* tmp = nullptr;  // an inspection call: its own scratch
+    CFD_CUDA(cudaMalloc(&tmp, 8 * n));
+    k_widen_pair<<<blocks_for((long)n, 256), 256, 0, c.stream>>>(
+        (long)n, (const float*)c.d_valf, (const float*)c.d_val_lo, tmp);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(val, tmp, 8 * n, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    cudaFree(tmp);
+    CFD_CUDA(e);
+    return CFD_OK;
+}
+
 int cfd_ctx_timers(cfd_ctx* ctx, double* seconds, int max, int* n) {
     if (!ctx || !seconds) return arg_error("ctx/seconds");
     int k = max < TM_N ? max : TM_N;

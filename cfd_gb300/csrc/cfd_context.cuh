@@ -52,6 +52,7 @@ std::string last_message();
 
 struct Ctx {
     int npoin = 0, nelem = 0, prec = 0;
+    long nnz = 0;  // entries of the mesh-motion matrix (CSR, diagonal first in each row)
     cfd_params prm{};
     Adjacency adj;
     BcTables bc;

@@ -167,6 +167,7 @@ __global__ void k_narrow_state(int npoin, const double* U, const double* T, cons
 __global__ void k_upload_U(int npoin, const double* hU, double* U, double* VX, double* VY,
                            float4* Uhi, float4* Ulo, float* VXf, float* VYf);
 __global__ void k_widen(long n, const float* a, double* b);
+__global__ void k_widen_pair(long n, const float* hi, const float* lo, double* out);
 __global__ void k_narrow(long n, const double* a, float* b);
 __global__ void k_deltat_mixed(int nelem, const int4* elem, const float* T, const float* VX,
                                const float* VY, const float2* W, const float* areaf, float TINF,

@@ -745,6 +745,7 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     if ((st = upload(&d_rowptr, adj.rowptr.data(), N + 1))) return st;
     if ((st = upload(&d_col, adj.col.data(), adj.col.size()))) return st;
     if ((st = dalloc(&d_val, adj.col.size()))) return st;
+    nnz = (long)adj.col.size();
     if ((st = dalloc(&d_diag, N))) return st;
     if (prec == CFD_PREC_FP64 && (st = dalloc(&d_rdiag, N))) return st;
     if (prec == CFD_PREC_FP64 && (st = dalloc(&d_lapq, E))) return st;

@@ -114,6 +114,13 @@ __global__ void k_narrow(long n, const double* __restrict__ a, float* __restrict
     if (i < n) b[i] = (float)a[i];
 }
 
+// hi + lo -> double (exact: lo starts below hi's last bit); lo may be null
+__global__ void k_widen_pair(long n, const float* __restrict__ hi, const float* __restrict__ lo,
+                             double* __restrict__ out) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = lo ? f2d_bits(hi[i]) + f2d_bits(lo[i]) : f2d_bits(hi[i]);
+}
+
 // float -> double (downloads of the mixed form's float fields)
 __global__ void k_widen(long n, const float* __restrict__ a, double* __restrict__ b) {
     const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;

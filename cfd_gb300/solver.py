@@ -349,6 +349,13 @@ class Solver:
               "cfd_ctx_download_geometry")
         return dict(area=a, dNx=dnx, dNy=dny, M=M)
 
+    def laplace_values(self):
+        """The mesh-motion matrix of the last assembly, in the order of laplace_pattern."""
+        rp, _ = laplace_pattern(self.case.inpoel, self.n)
+        v = np.zeros(int(rp[-1]))
+        check(abi.lib().cfd_ctx_download_laplace(self.h, dptr(v)), "cfd_ctx_download_laplace")
+        return v
+
     def set_state(self, U=None, T=None, VEL_X=None, VEL_Y=None):
         conv = [None if a is None else _f64(a) for a in (U, T, VEL_X, VEL_Y)]
         check(abi.lib().cfd_ctx_upload_state(self.h, *[dptr(a) for a in conv]),

@@ -346,6 +346,13 @@ int cfd_ctx_download_motion(cfd_ctx* ctx, double* xpos, double* ypos);
 /* Geometry of the current mesh: area(nelem), dNx(3,nelem), dNy(3,nelem), M(npoin). */
 int cfd_ctx_download_geometry(cfd_ctx* ctx, double* area, double* dNx, double* dNy,
                               double* M);
+/* The mesh-motion matrix of the last assembly (laplace, mLaplace.f90:7-58): its nnz values in
+ * the CSR order of cfd_laplace_pattern (the diagonal first in each row).  The FP64 form
+ * assembles it for each step's solve from the mesh before the step moves it, the mixed form
+ * for the next step from the moved mesh.  FP64 form: the FP64 values; mixed form: the FP32
+ * values, or under the relative BiCG tests the FP64-assembled ones (held as FP32 hi + lo,
+ * to 2^-47). */
+int cfd_ctx_download_laplace(cfd_ctx* ctx, double* val);
 
 /* Per-kernel timers (CUDA events) accumulated since create, in seconds; names follow
  * the reference TIMERS module (commonModules.f90:31-35).  n = slots written. */

@@ -271,3 +271,44 @@ def test_gpu_mixed_extrapolated_guess(gpu_lib):
     assert sum(ie[2:]) < sum(ip[2:]), (ie, ip)
     for a, b in zip(runs[abi.CFD_GUESS_EXTRAPOLATED][1], runs[abi.CFD_GUESS_PREVIOUS][1]):
         assert np.abs(a - b).max() <= 1e-3 * np.abs(b).max()
+
+
+@pytest.mark.gpu
+def test_gpu_mesh_motion_matrix_assemblies(gpu_lib, oracle):
+    """The mesh-motion matrix each form assembles (cfd_ctx_download_laplace) against the
+    oracle's laplace (mLaplace.f90:7-58) of the context's own mesh: the FP64 form bit for
+    bit at set-up; the mixed form's FP64 assembly (relative tests: element matrices formed
+    once per element, rows summed per node, held as FP32 hi + lo) within FP64 rounding at
+    set-up and after steps that moved the mesh (it assembles for the next step from the
+    moved mesh); its FP32 assembly (absolute test) within FP32 rounding."""
+    from cfd_gb300 import abi, solver
+    kw = dict(pitch_amp=math.radians(4.0), motion_freq=2.0, heave_amp=0.1,
+              mass_mode=abi.CFD_MASS_GCL_CORRECTED, bicg_maxit=3000,
+              estab_mode=abi.CFD_ESTAB_REGULARIZED)
+    krel = small_case(2, scale=24, seed=8, bicg_tol_mode=abi.CFD_BICG_TOL_REL, **kw)
+    kabs = small_case(2, scale=24, seed=8, **kw)
+    rp, idx = oracle.laplace_pattern(krel.inpoel, krel.npoin)
+    rows = np.repeat(np.arange(krel.npoin), np.diff(rp))
+
+    def ref(X, Y):
+        g = oracle.deriv(X, Y, krel.inpoel)
+        vals, _ = oracle.laplace(krel.inpoel, g["dNx"], g["dNy"], X, Y, rp, idx)
+        return vals
+
+    def rel_err(v, r):  # per entry, against the largest entry of its row
+        scale = np.maximum.reduceat(np.abs(r), rp[:-1])[rows]
+        return float((np.abs(v - r) / scale).max())
+
+    gd = solver.Solver(krel)
+    np.testing.assert_array_equal(gd.laplace_values(), ref(krel.x, krel.y))
+    gd.close()
+    for k, bound in ((krel, 1e-13), (kabs, 1e-6)):
+        gm = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+        for s in range(3):
+            st = gm.state()
+            e = rel_err(gm.laplace_values(), ref(st["X"], st["Y"]))
+            assert e <= bound, (k.params.bicg_tol_mode, s, e)
+            gm.step(2)
+        moved = np.abs(gm.state()["Y"] - k.y).max()
+        assert moved > 1e-4, moved
+        gm.close()
