@@ -964,34 +964,80 @@ cudaError_t launch_node_geometry(bool row64, unsigned grid, cudaStream_t stream,
 // precise product) sees only that, and the FP32 iterations keep valf.  k_node_geometry<true>
 // sums the rows.
 //
-// Per element: the 3x3 element matrix q (grad N_i . grad N_j) of mLaplace.f90:28-56 in FP64,
+// Double-float arithmetic (a value as an unevaluated FP32 pair h + l, |l| <= ulp(h)): the
+// element matrices below in ~2^-46 relative accuracy on the FP32 pipe, which runs 64 times
+// the FP64 pipe's operations on this GPU.  TwoSum, Fast2Sum (|a| >= |b|) and the exact
+// product by fmaf are the error-free transformations; the quotient takes two remainder
+// corrections.
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF df_fast2(float a, float b) {
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_two(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return DF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+    const DF s = df_two(x.h, y.h);
+    return df_fast2(s.h, s.l + (x.l + y.l));
+}
+__device__ __forceinline__ DF df_sub(DF x, DF y) { return df_add(x, DF{-y.h, -y.l}); }
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+    const float p = x.h * y.h;
+    float e = fmaf(x.h, y.h, -p);
+    e = fmaf(x.h, y.l, e);
+    e = fmaf(x.l, y.h, e);
+    return df_fast2(p, e);
+}
+__device__ __forceinline__ DF df_div(DF x, DF y) {
+    const float q1 = x.h / y.h;
+    const DF r1 = df_sub(x, df_mul(y, DF{q1, 0.f}));
+    const DF s = df_fast2(q1, r1.h / y.h);
+    const DF r2 = df_sub(x, df_mul(y, s));
+    return df_add(s, DF{r2.h / y.h, 0.f});
+}
+__device__ __forceinline__ DF df_of(double v) {
+    DF r;
+    split_bits(v, r.h, r.l);
+    return r;
+}
+__device__ __forceinline__ double df_value(DF x) { return f2d_bits(x.h) + f2d_bits(x.l); }
+
+// Per element: the 3x3 element matrix q (grad N_i . grad N_j) of mLaplace.f90:28-56,
 // q = (a sum |grad N_i|^2)^2 / 3 with a the area.  With e_i = a2 grad N_i (the edge vectors
 // from the first node, rotated; a2 = twice the signed area) the entries are
-// (e_i . e_j) S^2 / (12 a2^4), S = sum |e_i|^2: one division per element (GB300's FP64 pipe
-// bounds this pass).  Row i goes to the element's slot (e, i) in element-around-point order
-// (slot_pos), so that the node pass reads each node's rows contiguously.
+// (e_i . e_j) S^2 / (12 a2^4), S = sum |e_i|^2.  The edge vectors are FP64 differences of
+// the FP64 coordinates (exact for the close nodes of an element); the rest runs in
+// double-float (~2^-46, within the 2^-47 of the valf + val_lo the rows are stored as), so
+// that 10 FP64 operations remain per element instead of ~40 and a division.  Row i goes to
+// the element's slot (e, i) in element-around-point order (slot_pos), so that the node
+// pass reads each node's rows contiguously.
 __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
                               const double* __restrict__ X, const double* __restrict__ Y,
                               const int* __restrict__ slot_pos, double* __restrict__ k64) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += gridDim.x * blockDim.x) {
         const int4 n = elem[e];
         const double X0 = X[n.x], Y0 = Y[n.x];
-        const double x1 = X[n.y] - X0, y1 = Y[n.y] - Y0;
-        const double x2 = X[n.z] - X0, y2 = Y[n.z] - Y0;
-        const double ex0 = y1 - y2, ey0 = x2 - x1;  // e_0; e_1 = (y2, -x2), e_2 = (-y1, x1)
-        const double d00 = ex0 * ex0 + ey0 * ey0;
-        const double d11 = y2 * y2 + x2 * x2;
-        const double d22 = y1 * y1 + x1 * x1;
-        const double d01 = ex0 * y2 - ey0 * x2;
-        const double d02 = ey0 * x1 - ex0 * y1;
-        const double d12 = -(y2 * y1 + x2 * x1);
-        const double S = (d00 + d11) + d22;
-        const double a2 = x1 * y2 - x2 * y1;
-        const double t = S / (a2 * a2);
-        const double c = t * t * (1.0 / 12.0);
-        const double K[3][3] = {{d00 * c, d01 * c, d02 * c},
-                                {d01 * c, d11 * c, d12 * c},
-                                {d02 * c, d12 * c, d22 * c}};
+        const DF x1 = df_of(X[n.y] - X0), y1 = df_of(Y[n.y] - Y0);
+        const DF x2 = df_of(X[n.z] - X0), y2 = df_of(Y[n.z] - Y0);
+        const DF ex0 = df_sub(y1, y2), ey0 = df_sub(x2, x1);  // e_0; e_1 = (y2, -x2), e_2 = (-y1, x1)
+        const DF d00 = df_add(df_mul(ex0, ex0), df_mul(ey0, ey0));
+        const DF d11 = df_add(df_mul(y2, y2), df_mul(x2, x2));
+        const DF d22 = df_add(df_mul(y1, y1), df_mul(x1, x1));
+        const DF d01 = df_sub(df_mul(ex0, y2), df_mul(ey0, x2));
+        const DF d02 = df_sub(df_mul(ey0, x1), df_mul(ex0, y1));
+        const DF d12 = df_add(df_mul(y2, y1), df_mul(x2, x1));  // -d12
+        const DF S = df_add(df_add(d00, d11), d22);
+        const DF a2 = df_sub(df_mul(x1, y2), df_mul(x2, y1));
+        const DF t = df_div(S, df_mul(a2, a2));
+        const DF c = df_mul(df_mul(t, t), df_of(1.0 / 12.0));
+        const double k00 = df_value(df_mul(d00, c)), k11 = df_value(df_mul(d11, c));
+        const double k22 = df_value(df_mul(d22, c)), k01 = df_value(df_mul(d01, c));
+        const double k02 = df_value(df_mul(d02, c)), k12 = -df_value(df_mul(d12, c));
+        const double K[3][3] = {{k00, k01, k02}, {k01, k11, k12}, {k02, k12, k22}};
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             double* r = k64 + 3 * (size_t)slot_pos[3 * (size_t)e + i];
