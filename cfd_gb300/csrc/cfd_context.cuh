@@ -126,7 +126,7 @@ struct Ctx {
     double* d_rdiag = nullptr;   // FP64 form: RN(1/diag) of the BiCG (formed by each solve)
     double* d_lapq = nullptr;    // FP64 form: the Laplacian weight per element
     double2* d_gcl64 = nullptr;  // FP64 form: the gcl element terms   // relative tests: valf + val_lo = the FP64-assembled matrix
-    double* d_k64 = nullptr;     // relative tests: FP64 element-matrix rows, per slot (3 each)
+    float2* d_k64 = nullptr;     // relative tests: element-matrix rows (hi, lo), per slot (3 each)
     int* d_iterated = nullptr;   // relative tests: a solve iterated (the refinement runs)
     float2* d_xs[2] = {};        // relative tests: split_bits of the precise product's operand
     float* d_dtef = nullptr;  // mixed form, ITLOCAL != 0: FP32 DT per element

@@ -210,15 +210,15 @@ __global__ void k_elem_geometry(int nelem, const int4* elem, const double* X, co
                                 float4* geo, double2* terms, NormalsArgs nv);
 constexpr int kGeoNodeBlock = 128;  // block size of k_node_geometry
 __global__ void k_elem_grad64(int nelem, const int4* elem, const double* X, const double* Y,
-                              const int* slot_pos, double* k64);
-// k_node_geometry (block kGeoNodeBlock); row64 (relative tests): the Laplacian rows from
-// k64 (FP64, written as valf + val_lo), not from geo
+                              const int* slot_pos, float2* k64);
+// k_node_geometry (block kGeoNodeBlock); row64 (relative tests): the Laplacian rows summed
+// from k64 (element-matrix rows as double-float pairs, written as valf + val_lo), not from geo
 cudaError_t launch_node_geometry(bool row64, unsigned grid, cudaStream_t stream, int npoin,
                                  const int* esup_ptr, const int* esup_slot,
                                  const uchar4* lap_pos, const float4* geo, const double2* terms,
                                  const double* dtp, int gcl, const int* rowptr, float* valf,
                                  double* invdiag, float* invdiagf, double* M, float* invM,
-                                 const float2* W, float2* Wold, const double* k64,
+                                 const float2* W, float2* Wold, const float2* k64,
                                  float* val_lo);
 __global__ void k_widen_geo(int nelem, const float4* geo, double* dN, double* area);
 __global__ void k_motion_update_mixed(int npoin, const double* xpos, const double* ypos,

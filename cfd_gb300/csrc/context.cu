@@ -998,7 +998,7 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
                                   N, d_esup_ptr, d_esup_slot, d_lap_pos, geo8, d_gterms,
                                   &d_scal->dtmin, gcl ? 1 : 0, d_rowptr, d_valf, d_invdiag,
                                   d_invdiagf, d_M, invMf, Wn, to_next ? (float2*)nullptr : d_Wof,
-                                  (const double*)d_k64, d_val_lo));
+                                  (const float2*)d_k64, d_val_lo));
     tstop(TM_LAPLACE);
     return CFD_OK;
 }

@@ -780,23 +780,64 @@ __global__ void k_elem_geometry(int nelem, const int4* __restrict__ elem,
     }
 }
 
+// Double-float arithmetic (a value as an unevaluated FP32 pair h + l, |l| <= ulp(h)): the
+// relative tests' element matrices and their row sums in ~2^-46 relative accuracy on the
+// FP32 pipe, which runs 64 times the FP64 pipe's operations on this GPU.  TwoSum, Fast2Sum (|a| >= |b|) and the exact
+// product by fmaf are the error-free transformations; the quotient takes two remainder
+// corrections.
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF df_fast2(float a, float b) {
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_two(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return DF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+    const DF s = df_two(x.h, y.h);
+    return df_fast2(s.h, s.l + (x.l + y.l));
+}
+__device__ __forceinline__ DF df_sub(DF x, DF y) { return df_add(x, DF{-y.h, -y.l}); }
+// a += b for pairs held as float2 (x = h, y = l)
+__device__ __forceinline__ void df_acc(float2& a, float2 b) {
+    const DF s = df_add(DF{a.x, a.y}, DF{b.x, b.y});
+    a = make_float2(s.h, s.l);
+}
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+    const float p = x.h * y.h;
+    float e = fmaf(x.h, y.h, -p);
+    e = fmaf(x.h, y.l, e);
+    e = fmaf(x.l, y.h, e);
+    return df_fast2(p, e);
+}
+__device__ __forceinline__ DF df_div(DF x, DF y) {
+    const float q1 = x.h / y.h;
+    const DF r1 = df_sub(x, df_mul(y, DF{q1, 0.f}));
+    const DF s = df_fast2(q1, r1.h / y.h);
+    const DF r2 = df_sub(x, df_mul(y, s));
+    return df_add(s, DF{r2.h / y.h, 0.f});
+}
+__device__ __forceinline__ DF df_of(double v) {
+    DF r;
+    split_bits(v, r.h, r.l);
+    return r;
+}
+
 // Node pass: the row of the mesh Laplacian (mLaplace.f90:28-56; rows of up to 16 entries
 // are summed in shared memory, longer ones in place), 1/diag, and the lumped mass: MASAS
 // (subrutinas.f90:128-153) as a compensated FP32 sum of area/3, or the gcl update
 // M += dt*(tot1+tot2)/2 in FP64 from FP64 sums (slot order) of the FP64 element terms,
 // followed by putW (W_old = W).  ROW64 (the relative stopping tests): the row is the sum, in
-// FP64 and slot order, of the slots' rows of the FP64 element matrices (k_elem_grad64),
-// written as valf + val_lo; the FP32 geometry is then read only for MASAS.
+// double-float and slot order, of the slots' rows of the element matrices (k_elem_grad64),
+// written as valf + val_lo (the pair's h and l); the FP32 geometry is then read only for
+// MASAS.
 constexpr int kLapRow = 16;
 constexpr int kGeoBatch = 2;  // slots per pass of k_node_geometry
 constexpr int kGeoBlock = kGeoNodeBlock;
 
-__device__ __forceinline__ void row64_put(float* valf, float* val_lo, int at, double v) {
-    float hi, lo;
-    split_bits(v, hi, lo);
-    valf[at] = hi;
-    val_lo[at] = lo;
-}
 
 template <bool ROW64>
 __global__ void __launch_bounds__(kGeoBlock)
@@ -807,20 +848,20 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
                 double* __restrict__ invdiag, float* __restrict__ invdiagf,
                 double* __restrict__ M, float* __restrict__ invM,
                 const float2* __restrict__ W, float2* __restrict__ Wold,
-                const double* __restrict__ k64, float* __restrict__ val_lo) {
+                const float2* __restrict__ k64, float* __restrict__ val_lo) {
     __shared__ float row[ROW64 ? 1 : kGeoBlock][kLapRow + 1];
-    __shared__ double row64[ROW64 ? kGeoBlock : 1][kLapRow + 1];
+    __shared__ float2 row64[ROW64 ? kGeoBlock : 1][kLapRow + 1];
     const bool need_geo = !ROW64 || !gcl;
     // grid-stride (a smaller grid leaves room for kernels running beside it)
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npoin; p += gridDim.x * blockDim.x) {
     float* acc = row[ROW64 ? 0 : threadIdx.x];
-    double* acc64 = row64[ROW64 ? threadIdx.x : 0];
+    float2* acc64 = row64[ROW64 ? threadIdx.x : 0];
     const int r0 = rowptr[p], r1 = rowptr[p + 1];
     const int len = r1 - r0;
     const bool in_smem = len <= kLapRow;
     if (ROW64) {
         if (in_smem)
-            for (int k = 0; k < len; ++k) acc64[k] = 0.0;
+            for (int k = 0; k < len; ++k) acc64[k] = make_float2(0.f, 0.f);
     } else if (in_smem) {
 #pragma unroll
         for (int k = 0; k < kLapRow; ++k) acc[k] = 0.f;
@@ -837,14 +878,14 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
         uchar4 pos[kGeoBatch];
         float4 ga[kGeoBatch], gb[kGeoBatch];
         double2 tm[kGeoBatch];
-        double kr[kGeoBatch][3];
+        float2 kr[kGeoBatch][3];
 #pragma unroll
         for (int u = 0; u < kGeoBatch; ++u)
             if (sb + u < s1) {
                 slot[u] = esup_slot[sb + u];
                 pos[u] = lap_pos[sb + u];
                 if (ROW64) {
-                    const double* k = k64 + 3 * (size_t)(sb + u);
+                    const float2* k = k64 + 3 * (size_t)(sb + u);
                     kr[u][0] = k[0];
                     kr[u][1] = k[1];
                     kr[u][2] = k[2];
@@ -871,9 +912,9 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
             }
             if (ROW64) {
                 if (in_smem) {
-                    acc64[pos[u].x] += kr[u][0];
-                    acc64[pos[u].y] += kr[u][1];
-                    acc64[pos[u].z] += kr[u][2];
+                    df_acc(acc64[pos[u].x], kr[u][0]);
+                    df_acc(acc64[pos[u].y], kr[u][1]);
+                    df_acc(acc64[pos[u].z], kr[u][2]);
                 }
                 continue;
             }
@@ -893,26 +934,30 @@ k_node_geometry(int npoin, const int* __restrict__ esup_ptr, const int* __restri
     }
     float idf;
     if (ROW64) {
-        double diag;
+        float diag;
         if (in_smem) {
-            for (int k = 0; k < len; ++k) row64_put(valf, val_lo, r0 + k, acc64[k]);
-            diag = acc64[0];
+            for (int k = 0; k < len; ++k) {
+                valf[r0 + k] = acc64[k].x;
+                val_lo[r0 + k] = acc64[k].y;
+            }
+            diag = acc64[0].x;
         } else {  // long rows (rare): one pass over the slots per entry
-            diag = 0.0;
+            diag = 0.f;
             for (int kk = 0; kk < len; ++kk) {
-                double one = 0.0;
+                float2 one = make_float2(0.f, 0.f);
                 for (int sl = s0; sl < s1; ++sl) {
-                    const double* k = k64 + 3 * (size_t)sl;
+                    const float2* k = k64 + 3 * (size_t)sl;
                     const uchar4 ps = lap_pos[sl];
-                    if (ps.x == kk) one += k[0];
-                    if (ps.y == kk) one += k[1];
-                    if (ps.z == kk) one += k[2];
+                    if (ps.x == kk) df_acc(one, k[0]);
+                    if (ps.y == kk) df_acc(one, k[1]);
+                    if (ps.z == kk) df_acc(one, k[2]);
                 }
-                row64_put(valf, val_lo, r0 + kk, one);
-                if (kk == 0) diag = one;
+                valf[r0 + kk] = one.x;
+                val_lo[r0 + kk] = one.y;
+                if (kk == 0) diag = one.x;
             }
         }
-        idf = 1.f / d2f_trunc(diag);  // the Jacobi scaling is FP32 in every pass
+        idf = 1.f / diag;  // the Jacobi scaling is FP32 in every pass
     } else {
         float diag;
         if (in_smem) {
@@ -941,7 +986,7 @@ cudaError_t launch_node_geometry(bool row64, unsigned grid, cudaStream_t stream,
                                  const uchar4* lap_pos, const float4* geo, const double2* terms,
                                  const double* dtp, int gcl, const int* rowptr, float* valf,
                                  double* invdiag, float* invdiagf, double* M, float* invM,
-                                 const float2* W, float2* Wold, const double* k64,
+                                 const float2* W, float2* Wold, const float2* k64,
                                  float* val_lo) {
     if (row64)
         k_node_geometry<true><<<grid, kGeoBlock, 0, stream>>>(
@@ -964,60 +1009,18 @@ cudaError_t launch_node_geometry(bool row64, unsigned grid, cudaStream_t stream,
 // precise product) sees only that, and the FP32 iterations keep valf.  k_node_geometry<true>
 // sums the rows.
 //
-// Double-float arithmetic (a value as an unevaluated FP32 pair h + l, |l| <= ulp(h)): the
-// element matrices below in ~2^-46 relative accuracy on the FP32 pipe, which runs 64 times
-// the FP64 pipe's operations on this GPU.  TwoSum, Fast2Sum (|a| >= |b|) and the exact
-// product by fmaf are the error-free transformations; the quotient takes two remainder
-// corrections.
-struct DF {
-    float h, l;
-};
-__device__ __forceinline__ DF df_fast2(float a, float b) {
-    const float s = a + b;
-    return DF{s, b - (s - a)};
-}
-__device__ __forceinline__ DF df_two(float a, float b) {
-    const float s = a + b, bb = s - a;
-    return DF{s, (a - (s - bb)) + (b - bb)};
-}
-__device__ __forceinline__ DF df_add(DF x, DF y) {
-    const DF s = df_two(x.h, y.h);
-    return df_fast2(s.h, s.l + (x.l + y.l));
-}
-__device__ __forceinline__ DF df_sub(DF x, DF y) { return df_add(x, DF{-y.h, -y.l}); }
-__device__ __forceinline__ DF df_mul(DF x, DF y) {
-    const float p = x.h * y.h;
-    float e = fmaf(x.h, y.h, -p);
-    e = fmaf(x.h, y.l, e);
-    e = fmaf(x.l, y.h, e);
-    return df_fast2(p, e);
-}
-__device__ __forceinline__ DF df_div(DF x, DF y) {
-    const float q1 = x.h / y.h;
-    const DF r1 = df_sub(x, df_mul(y, DF{q1, 0.f}));
-    const DF s = df_fast2(q1, r1.h / y.h);
-    const DF r2 = df_sub(x, df_mul(y, s));
-    return df_add(s, DF{r2.h / y.h, 0.f});
-}
-__device__ __forceinline__ DF df_of(double v) {
-    DF r;
-    split_bits(v, r.h, r.l);
-    return r;
-}
-__device__ __forceinline__ double df_value(DF x) { return f2d_bits(x.h) + f2d_bits(x.l); }
-
 // Per element: the 3x3 element matrix q (grad N_i . grad N_j) of mLaplace.f90:28-56,
 // q = (a sum |grad N_i|^2)^2 / 3 with a the area.  With e_i = a2 grad N_i (the edge vectors
 // from the first node, rotated; a2 = twice the signed area) the entries are
 // (e_i . e_j) S^2 / (12 a2^4), S = sum |e_i|^2.  The edge vectors are FP64 differences of
 // the FP64 coordinates (exact for the close nodes of an element); the rest runs in
-// double-float (~2^-46, within the 2^-47 of the valf + val_lo the rows are stored as), so
-// that 10 FP64 operations remain per element instead of ~40 and a division.  Row i goes to
-// the element's slot (e, i) in element-around-point order (slot_pos), so that the node
-// pass reads each node's rows contiguously.
+// double-float (~2^-46, the accuracy of the valf + val_lo pair the rows end up in), so that
+// 4 FP64 operations remain per element instead of ~40 and a division.  Row i goes, as
+// (h, l) pairs, to the element's slot (e, i) in element-around-point order (slot_pos), so
+// that the node pass reads each node's rows contiguously.
 __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
                               const double* __restrict__ X, const double* __restrict__ Y,
-                              const int* __restrict__ slot_pos, double* __restrict__ k64) {
+                              const int* __restrict__ slot_pos, float2* __restrict__ k64) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += gridDim.x * blockDim.x) {
         const int4 n = elem[e];
         const double X0 = X[n.x], Y0 = Y[n.x];
@@ -1034,13 +1037,14 @@ __global__ void k_elem_grad64(int nelem, const int4* __restrict__ elem,
         const DF a2 = df_sub(df_mul(x1, y2), df_mul(x2, y1));
         const DF t = df_div(S, df_mul(a2, a2));
         const DF c = df_mul(df_mul(t, t), df_of(1.0 / 12.0));
-        const double k00 = df_value(df_mul(d00, c)), k11 = df_value(df_mul(d11, c));
-        const double k22 = df_value(df_mul(d22, c)), k01 = df_value(df_mul(d01, c));
-        const double k02 = df_value(df_mul(d02, c)), k12 = -df_value(df_mul(d12, c));
-        const double K[3][3] = {{k00, k01, k02}, {k01, k11, k12}, {k02, k12, k22}};
+        const DF k00 = df_mul(d00, c), k11 = df_mul(d11, c), k22 = df_mul(d22, c);
+        const DF k01 = df_mul(d01, c), k02 = df_mul(d02, c), m12 = df_mul(d12, c);
+        const float2 K[3][3] = {{make_float2(k00.h, k00.l), make_float2(k01.h, k01.l), make_float2(k02.h, k02.l)},
+                                {make_float2(k01.h, k01.l), make_float2(k11.h, k11.l), make_float2(-m12.h, -m12.l)},
+                                {make_float2(k02.h, k02.l), make_float2(-m12.h, -m12.l), make_float2(k22.h, k22.l)}};
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            double* r = k64 + 3 * (size_t)slot_pos[3 * (size_t)e + i];
+            float2* r = k64 + 3 * (size_t)slot_pos[3 * (size_t)e + i];
             r[0] = K[i][0];
             r[1] = K[i][1];
             r[2] = K[i][2];
