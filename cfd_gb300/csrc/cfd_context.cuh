@@ -60,6 +60,11 @@ struct Ctx {
     // mixed form: the mesh-motion solve's stream, forked from and joined to `stream`
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the refined learned guess's own kernels beside the mesh-motion branch (stream3): the
+    // fields' guess beside the first residual pass, their update beside the mesh update
+    cudaStream_t stream3 = nullptr;
+    cudaEvent_t ev_side[4] = {};
+    bool side_join = false;  // the branch still has to wait for ev_side[3]
     cudaEvent_t ev_scal = nullptr;
     StepScal* h_scal = nullptr;  // pinned
     StepOut* h_out = nullptr;    // pinned step report
@@ -129,6 +134,7 @@ struct Ctx {
     float2* d_k64 = nullptr;     // relative tests: element-matrix rows (hi, lo), per slot (3 each)
     int* d_iterated = nullptr;   // relative tests: a solve iterated (the refinement runs)
     float2* d_xs[2] = {};        // relative tests: split_bits of the precise product's operand
+    float2* d_xs_c[2] = {};      // the same for the learned guess's candidates (k_guess_judge)
     float* d_dtef = nullptr;  // mixed form, ITLOCAL != 0: FP32 DT per element
     float* d_pf[2][2] = {};
     float* d_zf[2] = {};

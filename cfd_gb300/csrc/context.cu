@@ -92,6 +92,9 @@ Ctx::~Ctx() {
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (auto& m : mark)
         if (m) cudaEventDestroy(m);
+    for (cudaEvent_t e : ev_side)
+        if (e) cudaEventDestroy(e);
+    if (stream3) cudaStreamDestroy(stream3);
     if (stream2) cudaStreamDestroy(stream2);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -204,19 +207,41 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         }
         // the relative tests' precise products read x (and the candidates) split in hi + lo
         const bool split = prm.bicg_tol_mode != CFD_BICG_TOL_ABS;
+        // on the mesh-motion branch the fields' guess (boundary fit, guess, its split) runs on
+        // stream3 beside the first pass: it reads the mesh, the Dirichlet values and the
+        // fields, and writes only the candidates and their split
+        const bool side = fields && sv != nullptr;
+        const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
+        PcgArgs ac = a;  // the judge's arguments: the candidates' split
+        for (int s = 0; s < 2; ++s) ac.xs[s] = d_xs_c[s];
+        auto cand_guess = [&](cudaStream_t cs) -> int {
+            int st = mpnn::fields_guess(lgraph, cs, d_X, d_Y, d_xfix[0], d_xfix[1], d_pos[0],
+                                        d_pos[1], d_cand[0], d_cand[1]);
+            if (st) return st;
+            if (split)  // the gate is open on this path (gate 0)
+                CFD_LAUNCH(k_split_x, gsz, 256, 0, cs, ac, (const double*)d_cand[0],
+                           (const double*)d_cand[1], (const int*)nullptr);
+            return CFD_OK;
+        };
+        if (side) {
+            CFD_CUDA(cudaEventRecord(ev_side[0], stream));
+            CFD_CUDA(cudaStreamWaitEvent(stream3, ev_side[0], 0));
+            int st = cand_guess(stream3);
+            if (st) return st;
+            CFD_CUDA(cudaEventRecord(ev_side[1], stream3));
+        }
         if (split)
             CFD_LAUNCH(k_split_x, rgrid, 256, 0, stream, a, (const double*)d_pos[0],
                        (const double*)d_pos[1], (const int*)nullptr);
         CFD_CUDA(launch_bicg_resid_mixed(rgrid, stream, a));
         if (fields) {
-            int st = mpnn::fields_guess(lgraph, stream, d_X, d_Y, d_xfix[0], d_xfix[1], d_pos[0],
-                                        d_pos[1], d_cand[0], d_cand[1]);
-            if (st) return st;
-            const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
-            if (split)
-                CFD_LAUNCH(k_split_x, gsz, 256, 0, stream, a, (const double*)d_cand[0],
-                           (const double*)d_cand[1], (const int*)d_gflag);
-            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+            if (side) {
+                CFD_CUDA(cudaStreamWaitEvent(stream, ev_side[1], 0));
+            } else {
+                int st = cand_guess(stream);
+                if (st) return st;
+            }
+            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, ac, (const double*)d_cand[0],
                        (const double*)d_cand[1], d_grr);
             CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
                        (const double*)d_cand[1], (const double*)d_grr, d_gstats + 4);
@@ -235,11 +260,10 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
                                            d_cand[0], d_cand[1], d_gflag);
             if (st) return st;
             // grid-stride grids of a few waves: a closed gate costs little
-            const unsigned gsz = std::min((unsigned)a.nblk_r, (unsigned)(4 * nsm));
             if (split)
-                CFD_LAUNCH(k_split_x, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+                CFD_LAUNCH(k_split_x, gsz, 256, 0, stream, ac, (const double*)d_cand[0],
                            (const double*)d_cand[1], (const int*)d_gflag);
-            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, a, (const double*)d_cand[0],
+            CFD_LAUNCH(k_guess_judge, gsz, 256, 0, stream, ac, (const double*)d_cand[0],
                        (const double*)d_cand[1], d_grr);
             CFD_LAUNCH(k_guess_select, gsz, 256, 0, stream, a, (const double*)d_cand[0],
                        (const double*)d_cand[1], (const double*)d_grr, d_gstats);
@@ -288,11 +312,22 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
                                              stream));
         g_launches.fetch_add(1, std::memory_order_relaxed);
     }
-    // refined learned guess: the solutions correct the basis fields
+    // refined learned guess: the solutions correct the basis fields (on the branch: on
+    // stream3 beside the mesh update, which reads the solutions too; the branch waits for it
+    // at its end, side_join)
     if (mixed && learned_mode() && net && lgraph && guess_refine &&
         fields_ready) {
-        int st = mpnn::fields_update(lgraph, stream, d_pos[0], d_pos[1]);
-        if (st) return st;
+        if (sv != nullptr) {
+            CFD_CUDA(cudaEventRecord(ev_side[2], stream));
+            CFD_CUDA(cudaStreamWaitEvent(stream3, ev_side[2], 0));
+            int st = mpnn::fields_update(lgraph, stream3, d_pos[0], d_pos[1]);
+            if (st) return st;
+            CFD_CUDA(cudaEventRecord(ev_side[3], stream3));
+            side_join = true;
+        } else {
+            int st = mpnn::fields_update(lgraph, stream, d_pos[0], d_pos[1]);
+            if (st) return st;
+        }
     }
     if (h_iters) {  // the next step's learned-guess decision reads these
         CFD_CUDA(cudaMemcpyAsync(h_iters, d_pcg_iters, 2 * sizeof(int), cudaMemcpyDeviceToHost,
@@ -726,6 +761,8 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
     CFD_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     CFD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     CFD_CUDA(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    CFD_CUDA(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
+    for (auto& e : ev_side) CFD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CFD_CUDA(cudaMallocHost((void**)&h_scal, sizeof(StepScal)));
     CFD_CUDA(cudaMallocHost((void**)&h_out, sizeof(StepOut)));
     // mesh
@@ -888,8 +925,10 @@ int Ctx::create(const cfd_mesh* m, const cfd_params* p, int precision_mode) {
             if ((st = dalloc(&d_val_lo, adj.col.size()))) return st;
             if ((st = dalloc(&d_k64, 9 * (size_t)E))) return st;
             if ((st = dalloc(&d_iterated, 1))) return st;
-            for (int k = 0; k < 2; ++k)
+            for (int k = 0; k < 2; ++k) {
                 if ((st = dalloc(&d_xs[k], (size_t)N))) return st;
+                if ((st = dalloc(&d_xs_c[k], (size_t)N))) return st;
+            }
             CFD_CUDA(cudaMemsetAsync(d_iterated, 0, sizeof(int), stream));
         }
         if ((st = dalloc(&d_gterms, E))) return st;
@@ -1081,6 +1120,10 @@ int Ctx::enqueue_mixed(bool learned) {
                    d_scal, d_X, d_Y, d_WX_n, d_WY_n, d_Xhi, d_Xlo, d_Wf_n);
         if (smoothing_now && (st = smooth_in_step(s, d_WX_n, d_WY_n, d_Wf_n))) return st;
         if (prm.moving == 1 && (st = geometry_mixed(false, false, true, s))) return st;
+        if (side_join) {  // the fields' update on stream3 (it reads this step's solutions)
+            CFD_CUDA(cudaStreamWaitEvent(s, ev_side[3], 0));
+            side_join = false;
+        }
         return CFD_OK;
     };
     if (fork) {

@@ -160,17 +160,20 @@ __global__ void k_fields_update(int n, const int* __restrict__ kind, const Globa
                                 double* __restrict__ F) {
     const Globals g = *G;
     const double a[2][3] = {{g.tx, g.m11, g.m12}, {g.ty, g.m21, g.m22}};
-    double q[2];
+    double iq[2];  // 1/|a_s|^2 (0: the solve has no prescribed motion), once per launch
 #pragma unroll
-    for (int s = 0; s < 2; ++s) q[s] = a[s][0] * a[s][0] + a[s][1] * a[s][1] + a[s][2] * a[s][2];
+    for (int s = 0; s < 2; ++s) {
+        const double q = a[s][0] * a[s][0] + a[s][1] * a[s][1] + a[s][2] * a[s][2];
+        iq[s] = q > 0.0 ? 1.0 / q : 0.0;
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (kind[i] != KIND_FREE) continue;
         double f[3] = {F[i], F[n + i], F[2 * (size_t)n + i]};
         const double x[2] = {x0[i], x1[i]};
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
-            if (!(q[s] > 0.0)) continue;
-            const double r = (x[s] - (a[s][0] * f[0] + a[s][1] * f[1] + a[s][2] * f[2])) / q[s];
+            if (iq[s] == 0.0) continue;
+            const double r = (x[s] - (a[s][0] * f[0] + a[s][1] * f[1] + a[s][2] * f[2])) * iq[s];
 #pragma unroll
             for (int c = 0; c < 3; ++c) f[c] += a[s][c] * r;
         }
