@@ -352,6 +352,8 @@ struct PcgArgs {
     // and clears gflag[1]; a pass with only_if != null runs only when *only_if != 0
     int* gflag;
     double gate;
+    int gate_undone;             // 1: the gate opens when a solve's guess fails the stopping
+                                 // test (the refined guess's candidate is judged only then)
     const int* only_if;
     GridBar* bar;
     double tol;

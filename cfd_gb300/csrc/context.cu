@@ -194,6 +194,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
         const bool fields = with_net && guess_refine && !learned && fields_ready;
         a.gflag = (learned || fields) ? d_gflag : nullptr;
         a.gate = 0.0;
+        a.gate_undone = fields ? 1 : 0;  // the fields' guess is judged when the first one fails
         a.only_if = nullptr;
         if (nufix > 0 && !fix_done)
             CFD_LAUNCH(k_bicg_fix_mixed, blocks_for(nufix, 256), 256, 0, stream, a);

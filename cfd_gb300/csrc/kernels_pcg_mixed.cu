@@ -340,8 +340,13 @@ __global__ void __launch_bounds__(256) k_bicg_resid_mixed(PcgArgs a) {
                 a.bscal[8 * s + 5] = (a.tol * a.tol) * ref2;
             }
         }
-        if (a.gflag && !a.only_if) {  // gate on r.z, the convergence measure of the solve
-            a.gflag[0] = (out[2] + out[3] >= a.gate) ? 1 : 0;
+        if (a.gflag && !a.only_if) {  // gate on r.z, the convergence measure of the solve,
+            bool open = out[2] + out[3] >= a.gate;  // or on the stopping test itself
+            if (a.gate_undone) {
+                open = false;
+                for (int s = 0; s < a.nsolve; ++s) open = open || !first_done(a, s);
+            }
+            a.gflag[0] = open ? 1 : 0;
             a.gflag[1] = 0;
         }
     }
