@@ -97,3 +97,39 @@ def test_refined_guess_under_the_relative_test(gpu_lib):
         its[refined] = per_step
         S.close()
     assert sum(its[True][3:]) * 4 < sum(its[False][3:]), its
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["learned", "learned_extrapolated"])
+def test_refined_guess_graph_replay_matches_launches(gpu_lib, monkeypatch, mode):
+    """The refined learned guess's kernels run on a side stream beside the mesh-motion
+    branch (the fields' guess beside the first residual pass, their update beside the mesh
+    update), joined by events.  Steps replayed from the captured graph give the iterations,
+    the guess statistics and the state of the same steps enqueued launch by launch
+    (CFD_GRAPHS=0), bit for bit."""
+    from cfd_gb300 import abi, learned, solver
+    if not os.path.exists(learned.DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights in the package")
+    net = learned.Net.load()
+    gm = abi.CFD_GUESS_LEARNED if mode == "learned" else abi.CFD_GUESS_LEARNED_EXTRAPOLATED
+    k = small_case(3, scale=48, seed=13, estab_mode=abi.CFD_ESTAB_REGULARIZED, fsafe=0.25,
+                   bicg_tol_mode=abi.CFD_BICG_TOL_REL, bicg_maxit=20000, guess_mode=gm)
+    monkeypatch.setenv("CFD_GRAPHS", "0")
+    a = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    monkeypatch.delenv("CFD_GRAPHS")
+    b = solver.Solver(k, precision=abi.CFD_PREC_MIXED)
+    for s in (a, b):
+        s.set_guess_net(net, 1.0e9)
+        s.set_guess_refine(True)
+    for n in (1, 1, 3, 4):
+        ra, rb = a.step(n), b.step(n)
+        assert list(ra.bicg_iters) == list(rb.bicg_iters)
+        assert list(ra.bicg_relres) == list(rb.bicg_relres)
+        assert all(rb.bicg_converged) and max(rb.bicg_relres) <= 1e-10
+        sa, sb = a.state(), b.state()
+        for key in ("U", "X", "Y"):
+            assert np.array_equal(sa[key], sb[key]), key
+    assert list(a.guess_stats_ex()) == list(b.guess_stats_ex())
+    assert a.graph_state()[0] == 0 and b.graph_state()[0] == 1 and b.graph_state()[1] > 0
+    a.close()
+    b.close()
