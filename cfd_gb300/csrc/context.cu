@@ -219,7 +219,7 @@ int Ctx::run_pcg(int nsolve, bool learned, bool fix_done, cudaStream_t sv) {
             int st = mpnn::fields_guess(lgraph, cs, d_X, d_Y, d_xfix[0], d_xfix[1], d_pos[0],
                                         d_pos[1], d_cand[0], d_cand[1]);
             if (st) return st;
-            if (split)  // the gate is open on this path (gate 0)
+            if (split)  // ungated: beside the first pass, which sets the gate, on the branch
                 CFD_LAUNCH(k_split_x, gsz, 256, 0, cs, ac, (const double*)d_cand[0],
                            (const double*)d_cand[1], (const int*)nullptr);
             return CFD_OK;
@@ -1031,7 +1031,7 @@ int Ctx::geometry_mixed(bool setup, bool put_area, bool to_next, cudaStream_t sv
                (gcl || put_area) ? 1 : 0, d_area_old, d_area, d_areaf, geo8, d_gterms, nv);
     tstop(TM_DERIV);
     tstart(TM_LAPLACE);
-    if (d_val_lo)  // relative tests: the mesh-motion operator in FP64 (element matrices)
+    if (d_val_lo)  // relative tests: the mesh-motion operator to FP64-class accuracy
         CFD_LAUNCH(k_elem_grad64, branch_grid(E, TB, sv), TB, 0, stream, E, d_elem, d_X, d_Y,
                    (const int*)d_slot_pos, d_k64);
     CFD_CUDA(launch_node_geometry(d_val_lo != nullptr, branch_grid(N, kGeoNodeBlock, sv), stream,
