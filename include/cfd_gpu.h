@@ -350,7 +350,7 @@ int cfd_ctx_download_geometry(cfd_ctx* ctx, double* area, double* dNx, double* d
  * the CSR order of cfd_laplace_pattern (the diagonal first in each row).  The FP64 form
  * assembles it for each step's solve from the mesh before the step moves it, the mixed form
  * for the next step from the moved mesh.  FP64 form: the FP64 values; mixed form: the FP32
- * values, or under the relative BiCG tests the FP64-assembled ones (held as FP32 hi + lo,
+ * values, or under the relative BiCG tests the FP64-class ones (held as FP32 hi + lo,
  * to 2^-47). */
 int cfd_ctx_download_laplace(cfd_ctx* ctx, double* val);
 
